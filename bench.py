@@ -1,0 +1,276 @@
+"""Benchmark of the GB300 collider on the scene-scale closest-hit workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload c1|c0]
+
+Workload c1 (default): the procedural interior (1,239,120 triangles: a
+20x10x20 room of tessellated slabs, 300 boxes, 64 displaced icospheres of
+12,500 triangles), 16,777,216 coherent pinhole rays (4096x4096) plus
+16,777,216 incoherent cosine-hemisphere rays from seeded surface points.
+One step = closest hit (FILL_DISTANCE|TRIANGLE|POINT2D|SIDE) for all
+33,554,432 rays.  Workload c0: one 69,451-triangle displaced icosphere and
+1,048,576 shell rays.
+
+Metric: closest-hit rays per second (Grays/s).  `value` times the kernel on
+device-resident rays (1 GiB of rays, larger than L2, so no flush is needed);
+`e2e` times the C-ABI host call rrg_intersect_host: pinned host rays in,
+host hit records out, copies inside the timed region.
+
+--impl reference times the reference collider's CPU algorithm on this machine's
+host cores: the C oracle (oracle/rr_oracle.c, a restatement of
+IT_BSP_FASTEST's arithmetic over its own BVH; the reference binary itself is
+built for x86-64 only in the container where the reference sources are).
+Multi-GPU: replicas only (each rank traces its own copy of the workload).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_RAY = 48          # 32 B ray in (two float4) + 16 B hit record out
+WORKLOAD_DESC = {
+    "c1": "scene-scale closest hit: 1,239,120-triangle interior, 16,777,216 pinhole (4096x4096) + "
+          "16,777,216 cosine-hemisphere surface rays per step",
+    "c0": "closest hit: 69,451-triangle displaced icosphere, 1,048,576 shell rays per step",
+}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_workload(name: str):
+    from lightsprintsdk_gb300 import scenes
+    if name == "c0":
+        v, t = scenes.icosphere_c0()
+        rays = scenes.shell_rays(1 << 20)
+        return v, t, rays
+    sc = scenes.interior_c1()
+    cam = scenes.camera_rays()
+    sur = scenes.surface_rays(sc.vertices, sc.indices, 4096 * 4096)
+    return sc.vertices, sc.indices, np.concatenate([cam, sur])
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed
+    region (200 ms period)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"rrg_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sms.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+def cpu_baseline(v, t, rays, sample: int):
+    """The oracle port on all host cores over a bounded sample of the rays
+    (every (n/sample)-th ray, so both ray families are represented)."""
+    from oracle import orc
+    step = max(1, len(rays) // sample)
+    sub = np.ascontiguousarray(rays[::step][:sample])
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O = orc.FastestOracle(v, t)
+    build_s = time.perf_counter() - t0
+    O.collide(sub[: min(len(sub), 65536)], threads)     # warm
+    best = 1e30
+    for _ in range(3):
+        t0 = time.perf_counter()
+        O.collide(sub, threads)
+        best = min(best, time.perf_counter() - t0)
+    return {"value": len(sub) / best / 1e9, "unit": "Grays/s", "cores": threads, "kind": "port",
+            "sample": f"{len(sub)} rays (every {step}th of the workload), best of 3, oracle BVH build "
+                      f"{build_s:.2f} s not timed"}
+
+
+def run_reference(args, rank: int):
+    if rank != 0:
+        return
+    v, t, rays = make_workload(args.workload)
+    sample = 2_000_000 if args.workload == "c1" else len(rays)
+    from oracle import orc
+    threads = os.cpu_count() or 1
+    step = max(1, len(rays) // sample)
+    sub = np.ascontiguousarray(rays[::step][:sample])
+    O = orc.FastestOracle(v, t)
+    for _ in range(args.warmup):
+        O.collide(sub[:65536], threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.collide(sub, threads)
+        times.append(time.perf_counter() - t0)
+    sec = sum(times) / len(times)
+    val = len(sub) / sec / 1e9
+    line = {"impl": "reference", "metric": "closest-hit Grays/s", "value": val, "unit": "Grays/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": sec * 1e3 * (len(rays) / len(sub)), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD_DESC[args.workload], "parallelism": "cpu threads"},
+            "cpu_baseline": {"value": val, "unit": "Grays/s", "cores": threads, "kind": "port",
+                             "sample": f"{len(sub)} of {len(rays)} rays per step (every {step}th)"},
+            "e2e": {"value": val, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c0"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from lightsprintsdk_gb300 import collider as col
+
+    v, t, rays = make_workload(args.workload)
+    n = rays.shape[0]
+    c = col.RRCollider.create(v, t, device=local)
+    build_ms = c.build_ms
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    d_rays = torch.from_numpy(rays).to(f"cuda:{local}")
+    d_hits = torch.empty((n, 4), dtype=torch.float32, device=f"cuda:{local}")
+
+    def step():
+        c.intersect_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream=sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        tt = torch.tensor([ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    assert c.status(sp) == 0, "traversal reported an error"
+    hits_total = int((d_hits[:, 1].view(torch.int32) != -1).sum().item())
+
+    # e2e: host buffers through the C ABI (pinned host memory, copies timed)
+    h_rays = torch.from_numpy(rays).pin_memory()
+    h_hits = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    L = col._lib()
+    for _ in range(2):
+        L.rrg_intersect_host(c.handle, h_rays.data_ptr(), n, h_hits.data_ptr(), sp)
+    e2e_steps = max(3, args.steps // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        st = L.rrg_intersect_host(c.handle, h_rays.data_ptr(), n, h_hits.data_ptr(), sp)
+        assert st == 0
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if world > 1:
+        tt = torch.tensor([e2e_s], device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+
+    if rank == 0:
+        peak, peak_src = load_peaks()
+        value = world * n / (ms * 1e-3) / 1e9
+        achieved = BYTES_PER_RAY * n / (ms * 1e-3) / 1e9
+        line = {
+            "metric": "closest-hit Grays/s", "value": value, "unit": "Grays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
+            "config": {"workload": WORKLOAD_DESC[args.workload], "rays_per_step": n, "triangles": int(t.shape[0]),
+                       "parallelism": f"replicas x{world}", "l2": "inputs (32 B/ray) larger than L2, no flush",
+                       "hit_ratio": hits_total / n, "bvh_build_ms": build_ms, "bvh_nodes": c.nodes},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "note": f"algorithmic {BYTES_PER_RAY} B/ray; peak {peak_src}"},
+            "e2e": {"value": world * n / e2e_s / 1e9, "unit": "Grays/s", "h2d_bytes_per_step": 32 * n,
+                    "d2h_bytes_per_step": 16 * n},
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(v, t, rays, 2_000_000 if args.workload == "c1" else n)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,155 @@
+/* rrgpu.h -- C ABI of the GB300 ray-mesh collider (closest hit and any hit).
+ *
+ * This is the drop-in boundary for rr::RRCollider (include/Lightsprint/
+ * RRCollider.h in the reference).  Everything crosses as plain pointers,
+ * sizes and int status codes; no C++ or CUDA types appear in the signatures
+ * (streams are passed as void* = cudaStream_t, NULL = the legacy stream).
+ *
+ * Ray formats
+ *   device rays : float[8] per ray = ox oy oz tmin dx dy dz tmax (two float4,
+ *                 16-byte aligned).  tmin/tmax are RRRay::rayLengthMin/Max.
+ *   hit record  : float[4] per ray = (t, tri_bits, u, v); tri_bits is a
+ *                 uint32 (read it with a bit cast): bits 0..30 = hitTriangle
+ *                 (post-import index), bit 31 = hitFrontSide; 0xFFFFFFFF =
+ *                 no hit.  t = hitDistance, (u, v) = hitPoint2d.
+ *   rr::RRRay   : the reference's 128-byte record (rayOrigin at 0, rayDir at
+ *                 16, rayLengthMin 32, rayLengthMax 36, rayFlags 40,
+ *                 hitDistance 44, hitTriangle 48, hitPoint2d 52, hitPlane 60,
+ *                 hitPoint3d 76, hitFrontSide 88), include/Lightsprint/
+ *                 RRCollider.h:85-137.
+ *
+ * Output semantics follow IT_BSP_FASTEST (RRCollider/IntersectBspFast.cpp):
+ * the hit triangle is the nearest one in [tmin, tmax] by a watertight test
+ * (ties in distance go to the lower triangle index); hitDistance is the
+ * distance to that triangle's plane, hitPoint2d its projected (u, v),
+ * hitPlane its unit plane and hitFrontSide = dot(dir, normal) < 0, each
+ * computed with the reference's own formulas (IntersectBspFast.cpp:130-252).
+ * Triangles whose plane normal is not finite are never hit, as in the
+ * reference (intersectByte 10, IntersectBspFast.cpp:182-186).
+ */
+#ifndef RRGPU_H
+#define RRGPU_H
+#include <stddef.h>
+#include <stdint.h>
+#if defined(_WIN32)
+#define RRG_API __declspec(dllexport)
+#else
+#define RRG_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  RRCollider::create returns nullptr on failure and logs
+ * (RRCollider/RRCollider.cpp:216-239); here every entry point returns one of
+ * these and rrg_status_string() names it. */
+enum {
+	RRG_OK = 0,
+	RRG_ERR_INVALID = 1,   /* bad argument (null pointer, size, alignment) */
+	RRG_ERR_OOM = 2,       /* device or host allocation failed */
+	RRG_ERR_CUDA = 3,      /* a CUDA call failed (rrg_last_cuda_error()) */
+	RRG_ERR_STACK = 4,     /* a traversal stack overflowed (ray left unhit) */
+	RRG_ERR_ABORTED = 5,   /* *aborting was set during create */
+	RRG_ERR_NO_DEVICE = 6, /* no CUDA device, or not an sm_103 device */
+	RRG_ERR_EMPTY = 7,     /* the mesh has no valid triangle */
+	RRG_ERR_TIMEOUT = 8    /* a bounded device wait ran out */
+};
+
+/* RRRay::Flags (include/Lightsprint/RRCollider.h:98-106). */
+enum {
+	RRG_FILL_DISTANCE = 1 << 0,
+	RRG_FILL_POINT3D = 1 << 1,
+	RRG_FILL_POINT2D = 1 << 2,
+	RRG_FILL_PLANE = 1 << 3,
+	RRG_FILL_TRIANGLE = 1 << 4,
+	RRG_FILL_SIDE = 1 << 5
+};
+
+/* Build parameters, a versioned struct like the reference's BuildParams
+ * (RRCollider/bsp.h:50-92), passed where RRCollider::create takes
+ * `void* buildParams` (RRCollider.h:183).  size = sizeof(rrg_build_params);
+ * zero fields take defaults. */
+typedef struct rrg_build_params {
+	uint32_t size;
+	uint32_t max_leaf_size;   /* triangles per leaf, default 4, max 8 */
+	uint32_t sah_bins;        /* bins per axis, default 32 (<= 32) */
+	uint32_t reserved[5];
+} rrg_build_params;
+
+typedef struct rrg_collider rrg_collider;
+
+/* Creates a collider from host arrays: xyz = 3*nv floats, idx = 3*nt uint32
+ * vertex indices (triangle i = idx[3i..3i+2], post-import numbering = i).
+ * The geometry is copied to the device and a BVH is built there.  Replaces
+ * RRCollider::create(mesh, nullptr, technique, aborting, ...)
+ * (RRCollider.h:183, RRCollider.cpp:186-241).  `aborting` may be NULL; when
+ * it becomes nonzero the build stops between levels and RRG_ERR_ABORTED is
+ * returned.  device = CUDA ordinal (usually 0). */
+RRG_API int rrg_collider_create(const float* xyz, uint32_t nv, const uint32_t* idx, uint32_t nt,
+                        const rrg_build_params* params, const volatile int* aborting, int device,
+                        rrg_collider** out);
+
+/* Same, from device arrays (no host copy), enqueued on `stream`. */
+RRG_API int rrg_collider_create_device(const float* xyz_dev, uint32_t nv, const uint32_t* idx_dev, uint32_t nt,
+                               const rrg_build_params* params, const volatile int* aborting, void* stream,
+                               rrg_collider** out);
+
+/* Re-reads vertex positions (same topology) and rebuilds.  RRCollider::update
+ * (RRCollider.h:187-190). */
+RRG_API int rrg_collider_update(rrg_collider* c, const float* xyz_host);
+
+RRG_API void rrg_collider_destroy(rrg_collider* c);
+
+/* RRCollider::getMemoryOccupied (RRCollider.h:259): device bytes held. */
+RRG_API size_t rrg_collider_memory(const rrg_collider* c);
+RRG_API uint32_t rrg_collider_triangles(const rrg_collider* c);
+RRG_API uint32_t rrg_collider_valid_triangles(const rrg_collider* c);
+RRG_API uint32_t rrg_collider_nodes(const rrg_collider* c);
+/* Milliseconds of device time the last build took (CUDA events). */
+RRG_API float rrg_collider_build_ms(const rrg_collider* c);
+
+/* Closest hit for n device rays -> n device hit records (float4 each).
+ * planes_dev (float4 per ray) and points_dev (float[3] per ray) are optional
+ * (NULL = not written; they correspond to FILL_PLANE / FILL_POINT3D).
+ * Asynchronous on `stream`; the status covers launch errors only.  Batch form
+ * of RRCollider::intersect(RRRay&) (RRCollider.h:228). */
+RRG_API int rrg_intersect_device(rrg_collider* c, const float* rays_dev, uint32_t n, float* hits_dev,
+                         float* planes_dev, float* points_dev, void* stream);
+
+/* Any hit (shadow rays): occluded_dev[i] = 1 if any valid triangle is hit in
+ * [tmin, tmax], else 0.  The reference answers shadow rays with intersect()
+ * and a collision handler (RRSolver/gather.cpp:447,
+ * RRStaticSolver/pathtracer.cpp:293); without a handler any hit suffices. */
+RRG_API int rrg_occluded_device(rrg_collider* c, const float* rays_dev, uint32_t n, uint8_t* occluded_dev,
+                        void* stream);
+
+/* Host buffers in, host buffers out: copies the rays to the device, traces,
+ * copies the hit records back and synchronises.  Uses device staging buffers
+ * owned by the collider (grown on demand). */
+RRG_API int rrg_intersect_host(rrg_collider* c, const float* rays_host, uint32_t n, float* hits_host, void* stream);
+
+/* rr::RRRay array on the host (128-byte stride): reads rayOrigin, rayDir,
+ * rayLengthMin/Max and rayFlags, writes the outputs the flags request and
+ * hit_host[i] = the bool RRCollider::intersect would return (hit_host may be
+ * NULL).  The batch form the reference once had as intersectBatch
+ * (doc/doxygen/doc.news:154).  Synchronous. */
+RRG_API int rrg_intersect_rrray(rrg_collider* c, void* rrrays_host, uint32_t n, uint8_t* hit_host, void* stream);
+
+/* Same on a device copy of the RRRay array (asynchronous). */
+RRG_API int rrg_intersect_rrray_device(rrg_collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, void* stream);
+
+/* Status word of the collider's last traces: RRG_OK or RRG_ERR_STACK.
+ * Synchronises the stream first; resets the word. */
+RRG_API int rrg_collider_status(rrg_collider* c, void* stream);
+
+RRG_API const char* rrg_status_string(int status);
+/* Text of the last CUDA error seen by this library (thread-local). */
+RRG_API const char* rrg_last_cuda_error(void);
+/* Library version, (major << 16) | minor. */
+RRG_API uint32_t rrg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

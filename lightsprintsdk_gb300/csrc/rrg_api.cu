@@ -1,0 +1,275 @@
+// C ABI of the collider (include/rrgpu.h): argument checks, device memory,
+// streams and status codes.  The reference equivalents are
+// RRCollider::create / defaultBuilder (RRCollider/RRCollider.cpp:87-241) and
+// the IntersectBspFast members (RRCollider/IntersectBspFast.h:55-74).
+#include "rrg_internal.cuh"
+
+#include <stdio.h>
+#include <string.h>
+#include <new>
+
+namespace rrg {
+
+static thread_local char g_cuda_err[256] = "";
+
+int cuda_fail(cudaError_t e) {
+	snprintf(g_cuda_err, sizeof(g_cuda_err), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+	if (e == cudaErrorMemoryAllocation) return RRG_ERR_OOM;
+	if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorNoKernelImageForDevice)
+		return RRG_ERR_NO_DEVICE;
+	return RRG_ERR_CUDA;
+}
+
+static void free_collider(Collider* c) {
+	if (!c) return;
+	cudaFree(c->d_xyz);
+	cudaFree(c->d_idx);
+	cudaFree(c->d_nodes);
+	cudaFree(c->d_tris);
+	cudaFree(c->d_counter);
+	cudaFree(c->d_stage_in);
+	cudaFree(c->d_stage_out);
+	delete c;
+}
+
+static int init_common(Collider* c, const rrg_build_params* params) {
+	memset(&c->params, 0, sizeof(c->params));
+	if (params) {
+		if (params->size < sizeof(uint32_t) || params->size > sizeof(rrg_build_params)) return RRG_ERR_INVALID;
+		memcpy(&c->params, params, params->size);
+	}
+	c->params.size = sizeof(rrg_build_params);
+	if (c->params.max_leaf_size > (uint32_t)kMaxLeaf) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaGetDevice(&c->device));
+	cudaDeviceProp prop;
+	RRG_CUDA(cudaGetDeviceProperties(&prop, c->device));
+	c->num_sms = prop.multiProcessorCount;
+	RRG_CUDA(cudaMalloc((void**)&c->d_counter, 64));
+	RRG_CUDA(cudaMemset(c->d_counter, 0, 64));
+	return trace_occupancy(c);
+}
+
+static void account(Collider* c) {
+	c->bytes = sizeof(float) * 3 * (size_t)c->nv + sizeof(uint32_t) * 3 * (size_t)c->nt + sizeof(TNode) * (size_t)c->nnodes +
+	           sizeof(float4) * 3 * (size_t)c->nvalid + 64 + c->stage_in_bytes + c->stage_out_bytes;
+}
+
+static int ensure_stage(Collider* c, size_t in_bytes, size_t out_bytes) {
+	if (in_bytes > c->stage_in_bytes) {
+		cudaFree(c->d_stage_in);
+		c->d_stage_in = nullptr;
+		c->stage_in_bytes = 0;
+		RRG_CUDA(cudaMalloc(&c->d_stage_in, in_bytes));
+		c->stage_in_bytes = in_bytes;
+	}
+	if (out_bytes > c->stage_out_bytes) {
+		cudaFree(c->d_stage_out);
+		c->d_stage_out = nullptr;
+		c->stage_out_bytes = 0;
+		RRG_CUDA(cudaMalloc(&c->d_stage_out, out_bytes));
+		c->stage_out_bytes = out_bytes;
+	}
+	account(c);
+	return RRG_OK;
+}
+
+}  // namespace rrg
+
+using namespace rrg;
+
+extern "C" {
+
+uint32_t rrg_version(void) { return (1u << 16) | 0u; }
+
+const char* rrg_last_cuda_error(void) { return g_cuda_err; }
+
+const char* rrg_status_string(int s) {
+	switch (s) {
+		case RRG_OK: return "ok";
+		case RRG_ERR_INVALID: return "invalid argument";
+		case RRG_ERR_OOM: return "out of memory";
+		case RRG_ERR_CUDA: return "CUDA error";
+		case RRG_ERR_STACK: return "traversal stack overflow";
+		case RRG_ERR_ABORTED: return "aborted";
+		case RRG_ERR_NO_DEVICE: return "no usable CUDA device";
+		case RRG_ERR_EMPTY: return "mesh has no valid triangle";
+		case RRG_ERR_TIMEOUT: return "device wait timed out";
+		default: return "unknown status";
+	}
+}
+
+int rrg_collider_create_device(const float* xyz_dev, uint32_t nv, const uint32_t* idx_dev, uint32_t nt,
+                               const rrg_build_params* params, const volatile int* aborting, void* stream,
+                               rrg_collider** out) {
+	if (!out) return RRG_ERR_INVALID;
+	*out = nullptr;
+	if (!xyz_dev || !idx_dev || !nv || !nt) return (nt == 0 && out) ? RRG_ERR_EMPTY : RRG_ERR_INVALID;
+	if ((uint64_t)nt * 3 > 0xFFFFFFFFull || (uint64_t)nv * 3 > 0xFFFFFFFFull) return RRG_ERR_INVALID;
+	Collider* c = new (std::nothrow) Collider();
+	if (!c) return RRG_ERR_OOM;
+	int st = init_common(c, params);
+	if (st) { free_collider(c); return st; }
+	cudaStream_t s = (cudaStream_t)stream;
+	c->nv = nv;
+	c->nt = nt;
+	cudaError_t e = cudaMalloc((void**)&c->d_xyz, sizeof(float) * 3 * (size_t)nv);
+	if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_idx, sizeof(uint32_t) * 3 * (size_t)nt);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_xyz, xyz_dev, sizeof(float) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice, s);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_idx, idx_dev, sizeof(uint32_t) * 3 * (size_t)nt, cudaMemcpyDeviceToDevice, s);
+	if (e != cudaSuccess) { free_collider(c); return cuda_fail(e); }
+	st = build_bvh(c, s, aborting);
+	if (st) { free_collider(c); return st; }
+	account(c);
+	*out = reinterpret_cast<rrg_collider*>(c);
+	return RRG_OK;
+}
+
+int rrg_collider_create(const float* xyz, uint32_t nv, const uint32_t* idx, uint32_t nt,
+                        const rrg_build_params* params, const volatile int* aborting, int device,
+                        rrg_collider** out) {
+	if (!out) return RRG_ERR_INVALID;
+	*out = nullptr;
+	if (nt == 0) return RRG_ERR_EMPTY;
+	if (!xyz || !idx || !nv) return RRG_ERR_INVALID;
+	if ((uint64_t)nt * 3 > 0xFFFFFFFFull || (uint64_t)nv * 3 > 0xFFFFFFFFull) return RRG_ERR_INVALID;
+	int ndev = 0;
+	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return RRG_ERR_NO_DEVICE;
+	if (device < 0 || device >= ndev) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(device));
+	float* dx = nullptr;
+	uint32_t* di = nullptr;
+	cudaError_t e = cudaMalloc((void**)&dx, sizeof(float) * 3 * (size_t)nv);
+	if (e == cudaSuccess) e = cudaMalloc((void**)&di, sizeof(uint32_t) * 3 * (size_t)nt);
+	if (e == cudaSuccess) e = cudaMemcpy(dx, xyz, sizeof(float) * 3 * (size_t)nv, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemcpy(di, idx, sizeof(uint32_t) * 3 * (size_t)nt, cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) {
+		cudaFree(dx);
+		cudaFree(di);
+		return cuda_fail(e);
+	}
+	int st = rrg_collider_create_device(dx, nv, di, nt, params, aborting, nullptr, out);
+	cudaDeviceSynchronize();
+	cudaFree(dx);
+	cudaFree(di);
+	return st;
+}
+
+int rrg_collider_update(rrg_collider* h, const float* xyz_host) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c || !xyz_host) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(c->device));
+	RRG_CUDA(cudaMemcpy(c->d_xyz, xyz_host, sizeof(float) * 3 * (size_t)c->nv, cudaMemcpyHostToDevice));
+	int st = build_bvh(c, nullptr, nullptr);
+	account(c);
+	return st;
+}
+
+void rrg_collider_destroy(rrg_collider* h) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c) return;
+	cudaSetDevice(c->device);
+	cudaDeviceSynchronize();
+	free_collider(c);
+}
+
+size_t rrg_collider_memory(const rrg_collider* h) {
+	const Collider* c = reinterpret_cast<const Collider*>(h);
+	return c ? c->bytes : 0;
+}
+uint32_t rrg_collider_triangles(const rrg_collider* h) {
+	const Collider* c = reinterpret_cast<const Collider*>(h);
+	return c ? c->nt : 0;
+}
+uint32_t rrg_collider_valid_triangles(const rrg_collider* h) {
+	const Collider* c = reinterpret_cast<const Collider*>(h);
+	return c ? c->nvalid : 0;
+}
+uint32_t rrg_collider_nodes(const rrg_collider* h) {
+	const Collider* c = reinterpret_cast<const Collider*>(h);
+	return c ? c->nnodes : 0;
+}
+float rrg_collider_build_ms(const rrg_collider* h) {
+	const Collider* c = reinterpret_cast<const Collider*>(h);
+	return c ? c->build_ms : 0.f;
+}
+
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+int rrg_intersect_device(rrg_collider* h, const float* rays_dev, uint32_t n, float* hits_dev, float* planes_dev,
+                         float* points_dev, void* stream) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c) return RRG_ERR_INVALID;
+	if (n == 0) return RRG_OK;
+	if (!rays_dev || !hits_dev || !aligned16(rays_dev) || !aligned16(hits_dev)) return RRG_ERR_INVALID;
+	if (planes_dev && !aligned16(planes_dev)) return RRG_ERR_INVALID;
+	return launch_closest(c, reinterpret_cast<const float4*>(rays_dev), n, reinterpret_cast<float4*>(hits_dev),
+	                      reinterpret_cast<float4*>(planes_dev), points_dev, (cudaStream_t)stream);
+}
+
+int rrg_occluded_device(rrg_collider* h, const float* rays_dev, uint32_t n, uint8_t* occ_dev, void* stream) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c) return RRG_ERR_INVALID;
+	if (n == 0) return RRG_OK;
+	if (!rays_dev || !occ_dev || !aligned16(rays_dev)) return RRG_ERR_INVALID;
+	return launch_occluded(c, reinterpret_cast<const float4*>(rays_dev), n, occ_dev, (cudaStream_t)stream);
+}
+
+int rrg_intersect_host(rrg_collider* h, const float* rays_host, uint32_t n, float* hits_host, void* stream) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c) return RRG_ERR_INVALID;
+	if (n == 0) return RRG_OK;
+	if (!rays_host || !hits_host) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(c->device));
+	int st = ensure_stage(c, 32 * (size_t)n, 16 * (size_t)n);
+	if (st) return st;
+	cudaStream_t s = (cudaStream_t)stream;
+	RRG_CUDA(cudaMemcpyAsync(c->d_stage_in, rays_host, 32 * (size_t)n, cudaMemcpyHostToDevice, s));
+	st = launch_closest(c, reinterpret_cast<const float4*>(c->d_stage_in), n,
+	                    reinterpret_cast<float4*>(c->d_stage_out), nullptr, nullptr, s);
+	if (st) return st;
+	RRG_CUDA(cudaMemcpyAsync(hits_host, c->d_stage_out, 16 * (size_t)n, cudaMemcpyDeviceToHost, s));
+	RRG_CUDA(cudaStreamSynchronize(s));
+	return RRG_OK;
+}
+
+int rrg_intersect_rrray_device(rrg_collider* h, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, void* stream) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c) return RRG_ERR_INVALID;
+	if (n == 0) return RRG_OK;
+	if (!rrrays_dev || !aligned16(rrrays_dev)) return RRG_ERR_INVALID;
+	return launch_rrray(c, rrrays_dev, n, hit_dev, (cudaStream_t)stream);
+}
+
+int rrg_intersect_rrray(rrg_collider* h, void* rrrays_host, uint32_t n, uint8_t* hit_host, void* stream) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c) return RRG_ERR_INVALID;
+	if (n == 0) return RRG_OK;
+	if (!rrrays_host) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(c->device));
+	int st = ensure_stage(c, 128 * (size_t)n, (size_t)n);
+	if (st) return st;
+	cudaStream_t s = (cudaStream_t)stream;
+	// bytes 0..91 of each record go up (inputs, and the output fields so that
+	// fields the flags do not request come back unchanged); 44..91 come back
+	RRG_CUDA(cudaMemcpy2DAsync(c->d_stage_in, 128, rrrays_host, 128, 92, n, cudaMemcpyHostToDevice, s));
+	st = launch_rrray(c, c->d_stage_in, n, (uint8_t*)c->d_stage_out, s);
+	if (st) return st;
+	RRG_CUDA(cudaMemcpy2DAsync((uint8_t*)rrrays_host + 44, 128, (uint8_t*)c->d_stage_in + 44, 128, 48, n,
+	                           cudaMemcpyDeviceToHost, s));
+	if (hit_host) RRG_CUDA(cudaMemcpyAsync(hit_host, c->d_stage_out, n, cudaMemcpyDeviceToHost, s));
+	RRG_CUDA(cudaStreamSynchronize(s));
+	return RRG_OK;
+}
+
+int rrg_collider_status(rrg_collider* h, void* stream) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c) return RRG_ERR_INVALID;
+	uint32_t w = 0;
+	cudaStream_t s = (cudaStream_t)stream;
+	RRG_CUDA(cudaMemcpyAsync(&w, c->d_counter + 1, 4, cudaMemcpyDeviceToHost, s));
+	RRG_CUDA(cudaStreamSynchronize(s));
+	RRG_CUDA(cudaMemsetAsync(c->d_counter + 1, 0, 4, s));
+	return w ? RRG_ERR_STACK : RRG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,85 @@
+// Internal declarations shared by the collider's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "../../include/rrgpu.h"
+
+namespace rrg {
+
+// ---------------------------------------------------------------- layout
+// Build node (one per BVH node, root = 0).  Leaves: left < 0, prims
+// [begin, begin+count) of the leaf-ordered triangle array.
+struct BNode {
+	float lo[3];
+	float hi[3];
+	int left, right;
+	int begin, count;
+};
+
+// Binary traversal node: both children's boxes in the parent (64 bytes):
+//   a = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   b = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   c = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   d = (ref0, ref1, 0, 0)
+// ref >= 0: inner node index; ref with bit 31 set: leaf, bits 27..30 =
+// count-1, bits 0..26 = first slot; kEmptyRef: no child.
+struct TNode {
+	float4 a, b, c;
+	int4 d;
+};
+
+constexpr int kLeafBit = (int)0x80000000u;
+constexpr int kEmptyRef = (int)0xFFFFFFFFu;   // leaf bit set, count 16: never produced
+constexpr int kMaxLeaf = 8;
+constexpr int kStackSize = 64;
+
+__host__ __device__ inline int leaf_ref(int first, int count) {
+	return kLeafBit | ((count - 1) << 27) | first;
+}
+
+// Triangles in leaf order: 3 x float4 = (v0.xyz, original index bits),
+// (v1.xyz, 0), (v2.xyz, 0); vertices in the mesh's own order.
+
+// -------------------------------------------------------------- collider
+struct Collider {
+	int device = 0;
+	uint32_t nv = 0, nt = 0, nvalid = 0, nnodes = 0;
+	float* d_xyz = nullptr;       // 3*nv
+	uint32_t* d_idx = nullptr;    // 3*nt
+	TNode* d_nodes = nullptr;
+	float4* d_tris = nullptr;     // 3*nvalid
+	uint32_t* d_counter = nullptr;// scratch: [0] ray counter, [1] status word
+	size_t bytes = 0;
+	float build_ms = 0;
+	rrg_build_params params{};
+	// host-call staging (rrg_intersect_host / rrg_intersect_rrray)
+	void* d_stage_in = nullptr;
+	void* d_stage_out = nullptr;
+	size_t stage_in_bytes = 0, stage_out_bytes = 0;
+	int num_sms = 0;
+	int trace_blocks = 0;
+	int occl_blocks = 0;
+};
+
+// build (rrg_build.cu)
+int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting);
+
+// trace (rrg_trace.cu)
+int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
+                   cudaStream_t s);
+int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, cudaStream_t s);
+int launch_rrray(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, cudaStream_t s);
+int trace_occupancy(Collider* c);
+
+// api (rrg_api.cu)
+int cuda_fail(cudaError_t e);
+
+}  // namespace rrg
+
+#define RRG_CUDA(x)                                  \
+	do {                                             \
+		cudaError_t e_ = (x);                        \
+		if (e_ != cudaSuccess) return rrg::cuda_fail(e_); \
+	} while (0)

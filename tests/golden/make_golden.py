@@ -1,0 +1,144 @@
+"""Generates the golden fixtures under tests/golden/ by running the reference
+collider, built from the reference's own sources into oracle/_ref (see
+oracle/ref.mk), on the seeded workloads of lightsprintsdk_gb300.scenes.
+
+    make -f oracle/ref.mk -j8 && python tests/golden/make_golden.py
+
+Each fixture stores md5 hashes of its generated inputs, so the tests also
+check that the generators reproduce the same bytes on the machine they run on,
+and the reference outputs of the rays that hit (ray index, hitTriangle,
+hitDistance, hitPoint2d, hitPlane, hitFrontSide).  Test infrastructure only.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from lightsprintsdk_gb300 import scenes  # noqa: E402
+from oracle import refio  # noqa: E402
+
+
+def md5(*arrays) -> str:
+    h = hashlib.md5()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def compact(h: dict) -> dict:
+    idx = np.nonzero(h["hit"])[0].astype(np.uint32)
+    return {"hit_idx": idx, "tri": h["tri"][idx], "dist": h["dist"][idx], "uv": h["uv"][idx],
+            "plane": h["plane"][idx], "side": h["side"][idx].astype(np.uint8), "n": np.uint32(h["hit"].shape[0])}
+
+
+def save(name: str, **kw):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, **kw)
+    print(f"{name}: {os.path.getsize(path)} bytes")
+
+
+def hello_mesh():
+    """The two-triangle mesh and ray of samples/HelloCollider/HelloCollider.cpp:15-42."""
+    v = np.array([[-1, 0, 0], [1, 0, 0], [0, 1, 0], [1, 0, 0], [-1, 0, 0], [0, 0, 1]], np.float32)
+    t = np.arange(6, dtype=np.uint32).reshape(2, 3)
+    rays = np.array([[0, -1, 0.3, 0, 0, 1, 0, 1000]], np.float32)
+    return v, t, rays
+
+
+def edge_mesh():
+    """Small mesh with the cases the reference handles specially: degenerate
+    triangles (zero area, repeated vertex; RRMesh.cpp:48-52 and
+    IntersectBspFast.cpp:182-186), two coincident triangles (a distance tie),
+    an axis-aligned quad, and a sliver."""
+    v = np.array([
+        [0, 0, 0], [1, 0, 0], [0, 1, 0],          # 0 tri in z=0
+        [1, 1, 0],                                 # 3
+        [0, 0, 1], [1, 0, 1], [0, 1, 1],          # 4..6 tri in z=1
+        [2, 0, 0], [3, 0, 0], [4, 0, 0],          # 7..9 collinear
+        [0, 0, 2], [2, 0, 2], [0, 2, 2], [2, 2, 2],  # 10..13 quad z=2
+        [0.5, 0.5, 3], [0.5 + 1e-7, 0.5, 3], [0.5, 2.5, 3],  # 14..16 sliver
+    ], np.float32)
+    t = np.array([
+        [0, 1, 2],      # 0
+        [1, 3, 2],      # 1
+        [4, 5, 6],      # 2
+        [6, 5, 4],      # 3 coincident with 2, opposite winding: distance tie
+        [7, 8, 9],      # 4 degenerate (collinear)
+        [0, 0, 1],      # 5 degenerate (repeated vertex)
+        [10, 11, 12],   # 6
+        [11, 13, 12],   # 7
+        [14, 15, 16],   # 8 sliver
+    ], np.uint32)
+    rng_rays = []
+    # axis-aligned rays through interiors, edges and vertices
+    for x, y in [(0.25, 0.25), (0.5, 0.5), (0.0, 0.0), (1.0, 0.0), (0.75, 0.75), (1.5, 1.5), (0.3, 0.6),
+                 (0.5, 0.0), (0.0, 0.5), (1.0, 1.0), (2.0, 0.0)]:
+        rng_rays.append([x, y, -5, 0, 0, 0, 1, 100])
+        rng_rays.append([x, y, 10, 0, 0, 0, -1, 100])
+    # rayLengthMin / Max clipping
+    rng_rays.append([0.25, 0.25, -5, 5.5, 0, 0, 1, 100])      # starts past z=0 -> first hit z=1
+    rng_rays.append([0.25, 0.25, -5, 0, 0, 0, 1, 5.5])        # ends before z=1
+    rng_rays.append([0.25, 0.25, -5, 6.0, 0, 0, 1, 6.0])      # exactly at z=1 (t=6)
+    rng_rays.append([0.25, 0.25, -5, 5.0, 0, 0, 1, 5.0])      # exactly at z=0 (t=5)
+    # oblique rays
+    d = np.array([0.3, 0.2, 1.0]); d /= np.linalg.norm(d)
+    rng_rays.append([0.1, 0.1, -3, 0, *d, 100])
+    d2 = np.array([1.0, 1.0, 0.0]); d2 /= np.linalg.norm(d2)
+    rng_rays.append([-1, -1, 0.0, 0, *d2, 100])              # in the plane z=0
+    rng_rays.append([0.6, 1.0, -1, 0, 0, 0, 1, 100])          # sliver region
+    return v, t, np.array(rng_rays, np.float32)
+
+
+def main():
+    assert refio.ref_available(), "build oracle/_ref first: make -f oracle/ref.mk -j8"
+    # 1. HelloCollider known answer
+    v, t, r = hello_mesh()
+    out = {}
+    for tech in ("linear", "bsp_fastest"):
+        _, h = refio.run_ref_collide(v, t, r, tech, 1)
+        out[tech] = h
+    save("hello_kat.npz", v=v, t=t, rays=r,
+         **{f"{k}_{f}": out[k][f] for k in out for f in ("hit", "tri", "dist", "uv", "plane", "point3d", "side")})
+
+    # 2. edge cases
+    v, t, r = edge_mesh()
+    kw = {"v": v, "t": t, "rays": r}
+    for tech in ("linear", "bsp_fastest"):
+        _, h = refio.run_ref_collide(v, t, r, tech, 1)
+        for f in ("hit", "tri", "dist", "uv", "plane", "point3d", "side"):
+            kw[f"{tech}_{f}"] = h[f]
+    save("edge_cases.npz", **kw)
+
+    # 3. config 0: displaced icosphere, 2^18 shell rays, IT_BSP_FASTEST
+    v, t = scenes.icosphere_c0()
+    n0 = 1 << 18
+    r = scenes.shell_rays(n0)
+    tm, h = refio.run_ref_collide(v, t, r, "bsp_fastest", 0)
+    print("c0 fastest", tm)
+    save("c0_fastest.npz", mesh_md5=md5(v, t), rays_md5=md5(r), **compact(h))
+    # IT_LINEAR (exact Moller-Trumbore) on the first 4096 rays
+    tm, h = refio.run_ref_collide(v, t, r[:4096], "linear", 0)
+    print("c0 linear", tm)
+    save("c0_linear.npz", rays_md5=md5(r[:4096]), **compact(h))
+
+    # 4. config 1: interior scene, camera + surface rays (closest) and shadow rays
+    sc = scenes.interior_c1()
+    cam = scenes.camera_rays(cols=[0, 1024, 2048, 3072])          # 16384 rays across the image
+    sur = scenes.surface_rays(sc.vertices, sc.indices, 16384)
+    sha = scenes.shadow_rays(sc.vertices, sc.indices, 16384)
+    rays = np.concatenate([cam, sur, sha])
+    tm, h = refio.run_ref_collide(sc.vertices, sc.indices, rays, "bsp_fastest", 0)
+    print("c1 fastest", tm)
+    save("c1_fastest.npz", mesh_md5=md5(sc.vertices, sc.indices), rays_md5=md5(rays), n_cam=len(cam),
+         n_sur=len(sur), n_sha=len(sha), **compact(h))
+
+
+if __name__ == "__main__":
+    main()

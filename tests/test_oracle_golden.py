@@ -1,0 +1,123 @@
+"""Pins the C oracle (oracle/rr_oracle.c) to the reference collider's own
+outputs (tests/golden/, made by tests/golden/make_golden.py from the reference
+built from its sources).  CPU only."""
+import numpy as np
+import pytest
+
+from lightsprintsdk_gb300 import scenes
+from oracle import orc
+from tests.helpers import classify_mismatches, expand, load_golden, md5
+
+FIELDS = ("hit", "tri", "dist", "uv", "plane", "side")
+
+
+def _ref(g, tech):
+    return {f: g[f"{tech}_{f}"] for f in FIELDS + ("point3d",)}
+
+
+def test_hello_collider_known_answer():
+    """samples/HelloCollider: hit=1 tri=1 dist=1 uv=(0.35,0.30) back side,
+    plane (0,1,0,0), for IT_LINEAR and IT_BSP_FASTEST alike."""
+    g = load_golden("hello_kat.npz")
+    for tech in ("linear", "bsp_fastest"):
+        r = _ref(g, tech)
+        assert r["hit"][0] and r["tri"][0] == 1
+        assert r["dist"][0] == np.float32(1.0)
+        np.testing.assert_array_equal(r["uv"][0], np.array([0.35, 0.3], np.float32))
+        assert not r["side"][0]
+    o = orc.FastestOracle(g["v"], g["t"]).collide(g["rays"], 1)
+    lin = orc.collide_linear(g["v"], g["t"], g["rays"], 1)
+    for got, tech in ((o, "bsp_fastest"), (lin, "linear")):
+        r = _ref(g, tech)
+        for f in FIELDS + ("point3d",):
+            np.testing.assert_array_equal(got[f], r[f].astype(got[f].dtype), err_msg=f"{tech} {f}")
+
+
+@pytest.mark.parametrize("tech", ["linear", "bsp_fastest"])
+def test_edge_cases_bit_exact(tech):
+    """Degenerate triangles, coincident triangles (distance ties), rays along
+    edges and through vertices, rayLengthMin/Max clipping, rays in a triangle's
+    plane: the oracle reproduces the reference bit for bit."""
+    g = load_golden("edge_cases.npz")
+    if tech == "linear":
+        got = orc.collide_linear(g["v"], g["t"], g["rays"], 1)
+    else:
+        got = orc.FastestOracle(g["v"], g["t"]).collide(g["rays"], 1)
+    r = _ref(g, tech)
+    np.testing.assert_array_equal(got["hit"], r["hit"].astype(bool))
+    m = got["hit"]
+    for f in ("tri", "dist", "uv", "plane", "point3d", "side"):
+        np.testing.assert_array_equal(got[f][m], r[f][m].astype(got[f].dtype), err_msg=f)
+
+
+@pytest.fixture(scope="module")
+def c0():
+    v, t = scenes.icosphere_c0()
+    g = load_golden("c0_fastest.npz")
+    assert md5(v, t) == str(g["mesh_md5"]), "mesh generator is not reproducing the fixture's mesh"
+    rays = scenes.shell_rays(int(g["n"]))
+    assert md5(rays) == str(g["rays_md5"]), "ray generator is not reproducing the fixture's rays"
+    return v, t, rays, expand(g)
+
+
+def test_c0_oracle_matches_reference(c0):
+    """Config 0 (69,451 triangles, 2^18 shell rays) against IT_BSP_FASTEST:
+    identical hit set and hitTriangle; hitPlane and hitFrontSide bit-exact;
+    hitDistance and hitPoint2d bit-exact except where the reference took the
+    plane of another triangle of a near-coplanar BSP node (its error against
+    the exact FP64 distance reaches 5e-4 there; the oracle's stays < 2e-5)."""
+    v, t, rays, ref = c0
+    o = orc.FastestOracle(v, t)
+    got = o.collide(rays, 0)
+    np.testing.assert_array_equal(got["hit"], ref["hit"])
+    np.testing.assert_array_equal(got["tri"][ref["hit"]], ref["tri"][ref["hit"]])
+    m = ref["hit"]
+    np.testing.assert_array_equal(got["plane"][m], ref["plane"][m])
+    np.testing.assert_array_equal(got["side"][m], ref["side"][m])
+    diff = m & (got["dist"] != ref["dist"])
+    assert diff.sum() <= 0.02 * m.sum()
+    tri64, d64 = o.exact64(rays, 0)
+    err_ours = np.abs(got["dist"][diff] - d64[diff]) / d64[diff]
+    err_ref = np.abs(ref["dist"][diff] - d64[diff]) / d64[diff]
+    assert err_ours.max() <= err_ref.max()
+    big = err_ref > 1e-5          # the reference's plane-reuse outliers
+    assert np.all(err_ours[big] < err_ref[big])
+    assert np.max(np.abs(got["dist"][m] - d64[m]) / d64[m]) < 2e-5
+
+
+def test_c0_linear_matches_reference():
+    """IT_LINEAR (exhaustive Moller-Trumbore) on 4096 config-0 rays: bit-exact."""
+    v, t = scenes.icosphere_c0()
+    g = load_golden("c0_linear.npz")
+    rays = scenes.shell_rays(4096)
+    assert md5(rays) == str(g["rays_md5"])
+    ref = expand(g)
+    got = orc.collide_linear(v, t, rays, 0)
+    np.testing.assert_array_equal(got["hit"], ref["hit"])
+    m = ref["hit"]
+    for f in ("tri", "dist", "uv", "plane", "side"):
+        np.testing.assert_array_equal(got[f][m], ref[f][m], err_msg=f)
+
+
+def test_c1_oracle_matches_reference():
+    """Config 1 (1.24 M triangles) sample of 16,384 camera, 16,384 surface and
+    16,384 shadow rays.  Every difference is a distance tie (coincident faces
+    of overlapping slabs) or a reference hit that is not an exact
+    intersection (BSP node plane reuse near the ray origin)."""
+    sc = scenes.interior_c1()
+    g = load_golden("c1_fastest.npz")
+    assert md5(sc.vertices, sc.indices) == str(g["mesh_md5"])
+    cam = scenes.camera_rays(cols=[0, 1024, 2048, 3072])
+    sur = scenes.surface_rays(sc.vertices, sc.indices, int(g["n_sur"]))
+    sha = scenes.shadow_rays(sc.vertices, sc.indices, int(g["n_sha"]))
+    rays = np.concatenate([cam, sur, sha])
+    assert md5(rays) == str(g["rays_md5"])
+    ref = expand(g)
+    got = orc.FastestOracle(sc.vertices, sc.indices).collide(rays, 0)
+    cls = classify_mismatches(sc.vertices, sc.indices, rays, ref, got)
+    assert not cls["other"], cls
+    assert len(cls["hit_mismatch"]) <= 2
+    ncam = int(g["n_cam"])
+    assert np.array_equal(got["tri"][:ncam], ref["tri"][:ncam])
+    n_diff = len(cls["tie"]) + len(cls["ref_off"])
+    assert n_diff <= 0.002 * ref["hit"].sum()
