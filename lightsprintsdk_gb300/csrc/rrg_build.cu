@@ -777,14 +777,31 @@ __global__ void __launch_bounds__(kSmallThreads) k_small(const Task* __restrict_
 }
 
 // ------------------------------------------------------------------ emit
+// Child boxes are widened by 2^-20 of each coordinate's magnitude plus
+// 2^-20 of the scene's largest coordinate, so that a ray lying exactly on a
+// box face (an axis-aligned ray with a zero direction component, common in
+// architectural scenes) still enters the box and reaches triangles on its
+// boundary.
+__device__ __forceinline__ void widen(BNode& n, float pad) {
+	for (int k = 0; k < 3; k++) {
+		n.lo[k] = n.lo[k] - (fabsf(n.lo[k]) * 9.5367431640625e-07f + pad);
+		n.hi[k] = n.hi[k] + (fabsf(n.hi[k]) * 9.5367431640625e-07f + pad);
+	}
+}
+
 __global__ void k_emit_nodes(const BNode* __restrict__ bn, int nnodes, TNode* __restrict__ tn) {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= nnodes) return;
 	BNode n = bn[i];
+	const BNode root = bn[0];
+	float mx = 0.f;
+	for (int k = 0; k < 3; k++) mx = fmaxf(mx, fmaxf(fabsf(root.lo[k]), fabsf(root.hi[k])));
+	const float pad = mx * 9.5367431640625e-07f + 1e-30f;
 	TNode o;
 	if (n.left < 0) {
 		if (i != 0) return;   // leaves live in their parent's child refs
 		// a root that is a leaf: wrap it in a one-child inner node
+		widen(n, pad);
 		o.a = make_float4(n.lo[0], n.hi[0], n.lo[1], n.hi[1]);
 		o.b = make_float4(INFINITY, -INFINITY, INFINITY, -INFINITY);
 		o.c = make_float4(n.lo[2], n.hi[2], INFINITY, -INFINITY);
@@ -794,11 +811,14 @@ __global__ void k_emit_nodes(const BNode* __restrict__ bn, int nnodes, TNode* __
 	}
 	if (n.left >= nnodes || n.right >= nnodes) return;
 	BNode l = bn[n.left], r = bn[n.right];
+	const int lleft = l.left, rleft = r.left;
+	widen(l, pad);
+	widen(r, pad);
 	o.a = make_float4(l.lo[0], l.hi[0], l.lo[1], l.hi[1]);
 	o.b = make_float4(r.lo[0], r.hi[0], r.lo[1], r.hi[1]);
 	o.c = make_float4(l.lo[2], l.hi[2], r.lo[2], r.hi[2]);
-	int r0 = l.left < 0 ? leaf_ref(l.begin, l.count) : n.left;
-	int r1 = r.left < 0 ? leaf_ref(r.begin, r.count) : n.right;
+	int r0 = lleft < 0 ? leaf_ref(l.begin, l.count) : n.left;
+	int r1 = rleft < 0 ? leaf_ref(r.begin, r.count) : n.right;
 	o.d = make_int4(r0, r1, 0, 0);
 	tn[i] = o;
 }

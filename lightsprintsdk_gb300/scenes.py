@@ -326,15 +326,18 @@ class Scene:
 def interior_c1(seed: int = 0xC1, cell: float = 0.125, nboxes: int = 300, ninst: int = 64,
                 sphere_freq: int = 25) -> Scene:
     """Collider config 1: room interior x in [-10,10], y in [0,10], z in
-    [-10,10] bounded by six 0.25-thick axis-aligned slabs tessellated at
-    `cell`; `nboxes` seeded boxes (sides 0.2..1.5) inside; `ninst` instances
+    [-10,10] bounded by 0.25-thick axis-aligned slabs tessellated at `cell`
+    (floor, four walls, and a ceiling of four slabs around a 6 x 6 skylight); `nboxes` seeded boxes (sides 0.2..1.5) inside; `ninst` instances
     of one displaced icosphere (frequency 25 = 12,500 triangles, radius 1)
     with seeded rotation, scale 0.35..0.8 and position on an 8x8 grid at
-    heights 1..8 with jitter.  Objects: 6 slabs, then boxes, then spheres."""
+    heights 1..8 with jitter.  Objects: 9 slabs, then boxes, then spheres."""
     th = 0.25
     slabs = [
         ((-10 - th, -th, -10 - th), (10 + th, 0.0, 10 + th)),          # floor
-        ((-10 - th, 10.0, -10 - th), (10 + th, 10 + th, 10 + th)),     # ceiling
+        ((-10 - th, 10.0, -10 - th), (10 + th, 10 + th, -3.0)),        # ceiling, around a
+        ((-10 - th, 10.0, 3.0), (10 + th, 10 + th, 10 + th)),          #   6 x 6 skylight
+        ((-10 - th, 10.0, -3.0), (-3.0, 10 + th, 3.0)),                #   opening over
+        ((3.0, 10.0, -3.0), (10 + th, 10 + th, 3.0)),                  #   the centre
         ((-10 - th, 0.0, -10 - th), (-10.0, 10.0, 10 + th)),           # wall -x
         ((10.0, 0.0, -10 - th), (10 + th, 10.0, 10 + th)),             # wall +x
         ((-10.0, 0.0, -10 - th), (10.0, 10.0, -10.0)),                 # wall -z
@@ -490,3 +493,89 @@ def shadow_rays(scene_v, scene_t, n: int, light=(0.5, 9.0, 0.5), seed: int = 0x5
     r = pack_rays(p.astype(np.float32), d.astype(np.float32), eps, 0.0)
     r[:, 7] = (dist - eps).astype(np.float32)
     return r
+
+
+# ------------------------------------------------------- lightmap gather
+class GatherScene:
+    """Inputs of the lightmap final gather on the interior scene.
+
+    albedo float32 (T,3): per-triangle diffuse reflectance, each channel
+    uniform in [0.2, 0.8]; tri_atlas int32 (T,): atlas of each triangle;
+    uv float32 (T,3,2): lightmap coordinates in [0,1] of the atlas;
+    lights: dict with the directional light (direction = where the light
+    travels, unit; colour) and the point light (position, colour; irradiance
+    colour / (PREVENT_INF + d^2), RRLight.cpp:353-358)."""
+
+    def __init__(self, scene, albedo, tri_atlas, uv, natlas, size, lights):
+        self.scene = scene
+        self.albedo = albedo
+        self.tri_atlas = tri_atlas
+        self.uv = uv
+        self.natlas = natlas
+        self.size = size
+        self.lights = lights
+
+
+def atlas_of_objects(nobj: int, nslab: int, nsphere: int, natlas: int = 256) -> np.ndarray:
+    """Object -> atlas: slabs and spheres get an atlas each; the boxes share
+    the remaining atlases round robin (box i -> atlas (i mod rest))."""
+    a = np.empty(nobj, np.int32)
+    nbox = nobj - nslab - nsphere
+    a[:nslab] = np.arange(nslab)
+    a[nobj - nsphere:] = nslab + np.arange(nsphere)
+    rest = natlas - nslab - nsphere
+    a[nslab:nslab + nbox] = nslab + nsphere + (np.arange(nbox) % rest)
+    return a
+
+
+def grid_unwrap(tri_atlas: np.ndarray, natlas: int) -> np.ndarray:
+    """Per-atlas uniform-grid unwrap: the n triangles of an atlas (in index
+    order) fill a g x g grid of square cells, g = ceil(sqrt(ceil(n/2))), two
+    triangles per cell: even local index -> lower-left half (corner, +u, +v),
+    odd -> upper-right half (opposite corner, -u, -v).  uv in [0,1]."""
+    T = tri_atlas.shape[0]
+    uv = np.zeros((T, 3, 2), np.float64)
+    order = np.argsort(tri_atlas, kind="stable")
+    counts = np.bincount(tri_atlas, minlength=natlas)
+    starts = np.concatenate([[0], np.cumsum(counts)])
+    for a in range(natlas):
+        ids = order[starts[a]:starts[a + 1]]
+        n = ids.shape[0]
+        if n == 0:
+            continue
+        g = int(np.ceil(np.sqrt(np.ceil(n / 2.0))))
+        j = np.arange(n)
+        cell = j // 2
+        cx = (cell % g).astype(np.float64)
+        cy = (cell // g).astype(np.float64)
+        lo = np.stack([cx, cy], -1) / g
+        c = 1.0 / g
+        even = (j % 2) == 0
+        p0 = np.where(even[:, None], lo, lo + c)
+        p1 = np.where(even[:, None], lo + np.array([c, 0.0]), lo + np.array([0.0, c]))
+        p2 = np.where(even[:, None], lo + np.array([0.0, c]), lo + np.array([c, 0.0]))
+        uv[ids, 0] = p0
+        uv[ids, 1] = p1
+        uv[ids, 2] = p2
+    return uv.astype(np.float32)
+
+
+def gather_c2(sc: Scene | None = None, seed: int = 0xC2, natlas: int = 256, size: int = 256) -> GatherScene:
+    """Config 2: the interior scene with per-triangle albedo U[0.2,0.8]^3,
+    256 atlases of 256 x 256 texels (uniform-grid unwrap), one directional
+    light through the skylight and one point light."""
+    if sc is None:
+        sc = interior_c1()
+    T = sc.ntri
+    ids = np.arange(T, dtype=np.uint64)
+    albedo = np.stack([0.2 + 0.6 * uniform01(seed, 50 + k, ids) for k in range(3)], -1).astype(np.float32)
+    nsphere = 0 if sc.instance_object_ids is None else int(sc.instance_object_ids.shape[0])
+    atlas_obj = atlas_of_objects(sc.nobj, 9, nsphere, natlas)
+    tri_atlas = atlas_obj[sc.tri_object]
+    uv = grid_unwrap(tri_atlas, natlas)
+    d = np.array([0.25, -1.0, 0.15])
+    d = d / np.sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])
+    lights = {"dir_direction": d.astype(np.float32), "dir_color": np.array([3.0, 2.9, 2.7], np.float32),
+              "point_position": np.array([-5.0, 8.0, -5.0], np.float32),
+              "point_color": np.array([20.0, 18.0, 15.0], np.float32)}
+    return GatherScene(sc, albedo, tri_atlas, uv, natlas, size, lights)

@@ -549,3 +549,79 @@ void orc_collide_exact64(const orc_bvh* b, const float* rays, uint32_t n, int th
 #endif
 	for (long i = 0; i < (long)n; i++) trace_one(b, rays + 8 * (size_t)i, 2, NULL, i, tri, dist);
 }
+
+/* ------------------------------------------------------------------------
+ * Ray cast with the final-gathering collision handler
+ * (RRStaticSolver/pathtracer.h:117-242) for opaque one-sided diffuse
+ * materials (RRMaterial::reset(false), RRObject/RRMaterial.cpp:154-166):
+ *   - the shooter triangle `skip` is never hit;
+ *   - a triangle with the same three vertices as the shooter is not hit at
+ *     distances below 1000 * tmin (pathtracer.h:138-161);
+ *   - hemisphere rays (shadow = 0) see only front sides (back renderFrom = 0);
+ *   - shadow rays (shadow = 1) are stopped by either side; any hit ends them.
+ * Hits reach the handler nearest first, so the result is the nearest
+ * accepted hit.  Returns its triangle (or 0xFFFFFFFF), FASTEST distance and
+ * plane. */
+static int same_vertices(const orc_bvh* b, uint32_t t, uint32_t s) {
+	for (int i = 0; i < 3; i++) {
+		const float* p = b->xyz + 3 * (size_t)b->idx[3 * t + i];
+		int found = 0;
+		for (int j = 0; j < 3 && !found; j++) {
+			const float* q = b->xyz + 3 * (size_t)b->idx[3 * s + j];
+			found = p[0] == q[0] && p[1] == q[1] && p[2] == q[2];
+		}
+		if (!found) return 0;
+	}
+	return 1;
+}
+
+uint32_t orc_cast(const orc_bvh* b, const float* o, const float* d, float tmin, float tmax, int shadow,
+                  uint32_t skip, float* dist_out, float* plane_out) {
+	float hmin, hmax;
+	if (!b->nnodes) return 0xFFFFFFFFu;
+	if (!orc_box_intersect(b->bmin, b->bmax, o, d, tmin, tmax, &hmin, &hmax)) return 0xFFFFFFFFu;
+	float inv[3] = {1.0f / d[0], 1.0f / d[1], 1.0f / d[2]};
+	uint32_t stack[128];
+	int sp = 0;
+	stack[sp++] = 0;
+	float best = hmax;
+	uint32_t best_tri = 0xFFFFFFFFu;
+	while (sp) {
+		const onode* nd = &b->nodes[stack[--sp]];
+		float slack = 1e-6f * (fabsf(best) + fabsf(hmin)) + b->pad;
+		if (!slab(nd, o, inv, hmin - slack, best + slack)) continue;
+		if (nd->left < 0) {
+			for (uint32_t k = nd->first; k < nd->first + nd->count; k++) {
+				uint32_t t = b->prims[k];
+				const orc_tri* tr = &b->tris[t];
+				float dp = orc_plane_distance(tr, o, d);
+				if (!(dp >= hmin && dp <= best)) continue;
+				float u, v;
+				int fr;
+				if (!orc_tri_fastest(tr, o, d, dp, &u, &v, &fr)) continue;
+				if (t == skip) continue;
+				if (skip != 0xFFFFFFFFu && dp < 1000 * tmin && same_vertices(b, t, skip)) continue;
+				if (!shadow && !fr) continue;
+				if (dp < best || t < best_tri) {
+					best = dp;
+					best_tri = t;
+				}
+				if (shadow) { sp = 0; break; }
+			}
+		} else {
+			const onode* l = &b->nodes[nd->left];
+			const onode* rr = &b->nodes[nd->right];
+			float dl = (l->mn[0] + l->mx[0]) * d[0] + (l->mn[1] + l->mx[1]) * d[1] + (l->mn[2] + l->mx[2]) * d[2];
+			float dr = (rr->mn[0] + rr->mx[0]) * d[0] + (rr->mn[1] + rr->mx[1]) * d[1] + (rr->mn[2] + rr->mx[2]) * d[2];
+			if (sp + 2 > 128) continue;
+			if (dl <= dr) { stack[sp++] = (uint32_t)nd->right; stack[sp++] = (uint32_t)nd->left; }
+			else { stack[sp++] = (uint32_t)nd->left; stack[sp++] = (uint32_t)nd->right; }
+		}
+	}
+	if (best_tri != 0xFFFFFFFFu) {
+		if (dist_out) *dist_out = best;
+		if (plane_out)
+			for (int k = 0; k < 4; k++) plane_out[k] = b->tris[best_tri].n4[k];
+	}
+	return best_tri;
+}

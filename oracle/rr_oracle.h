@@ -84,6 +84,9 @@ void orc_collide_fastest(const orc_bvh* b, const float* rays, uint32_t n, int th
 void orc_collide_exact64(const orc_bvh* b, const float* rays, uint32_t n, int threads,
                          uint32_t* tri, double* dist);
 int orc_max_threads(void);
+/* Ray cast with the final-gathering handler semantics (see rr_oracle.c). */
+uint32_t orc_cast(const orc_bvh* b, const float* o, const float* d, float tmin, float tmax, int shadow,
+                  uint32_t skip, float* dist, float* plane);
 
 #ifdef __cplusplus
 }

@@ -133,7 +133,7 @@ def test_c1_sample_against_reference():
     c, h = gpu_collide(sc.vertices, sc.indices, rays)
     cls = classify_mismatches(sc.vertices, sc.indices, rays, ref, h)
     assert not cls["other"], cls
-    assert len(cls["tie"]) + len(cls["ref_off"]) <= 0.002 * ref["hit"].sum()
+    assert len(cls["tie"]) + len(cls["ref_off"]) <= 0.005 * ref["hit"].sum()
     ncam = int(g["n_cam"])
     assert np.array_equal(h["tri"][:ncam], ref["tri"][:ncam])
 
