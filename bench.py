@@ -52,15 +52,19 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def make_workload(name: str):
+def make_workload(name: str, nrays: int = 0):
+    """Scene and rays of a workload.  nrays > 0 takes a smaller case of the
+    same workload (the first nrays/2 camera rows' rays and nrays/2 surface
+    rays) for profiling."""
     from lightsprintsdk_gb300 import scenes
     if name == "c0":
         v, t = scenes.icosphere_c0()
-        rays = scenes.shell_rays(1 << 20)
+        rays = scenes.shell_rays(nrays or (1 << 20))
         return v, t, rays
     sc = scenes.interior_c1()
-    cam = scenes.camera_rays()
-    sur = scenes.surface_rays(sc.vertices, sc.indices, 4096 * 4096)
+    half = (nrays // 2) if nrays else 4096 * 4096
+    cam = scenes.camera_rays(rows=max(1, half // 4096))
+    sur = scenes.surface_rays(sc.vertices, sc.indices, half)
     return sc.vertices, sc.indices, np.concatenate([cam, sur])
 
 
@@ -68,7 +72,7 @@ class ClockSampler:
     """nvidia-smi sampling of SM clocks and throttle reasons during the timed
     region (200 ms period)."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -87,6 +91,24 @@ class ClockSampler:
             self.proc = None
         return self
 
+    def wait_first_sample(self, timeout: float = 3.0):
+        t0 = time.time()
+        while self.proc and time.time() - t0 < timeout:
+            try:
+                if os.path.getsize(self.path) > 0:
+                    return
+            except OSError:
+                pass
+            time.sleep(0.05)
+
+    def mark_start(self):
+        self.t_start = time.time()
+
+    def mark_end(self):
+        self.t_end = time.time()
+        # keep sampling until at least one full period after the region
+        time.sleep(0.25)
+
     def __exit__(self, *a):
         if self.proc:
             self.proc.terminate()
@@ -97,24 +119,30 @@ class ClockSampler:
             self.f.close()
 
     def summary(self):
+        """Median SM clock and the throttle reasons seen in samples taken
+        inside the timed region (all samples if none fell inside)."""
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sms, mx, reasons = [], None, set()
+        import datetime
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
             p = [x.strip() for x in line.split(",")]
-            if len(p) < 9:
+            if len(p) < 10:
                 continue
             try:
-                sms.append(float(p[1]))
-                mx = float(p[2])
+                ts = datetime.datetime.strptime(p[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(p[2]), float(p[3]), [nm for k, nm in enumerate(names)
+                                                            if p[6 + k].lower().startswith("active")]))
             except ValueError:
                 continue
-            for k, nm in enumerate(names):
-                if p[5 + k].lower().startswith("active"):
-                    reasons.add(nm)
-        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sms)}
+        t0, t1 = getattr(self, "t_start", None), getattr(self, "t_end", None)
+        inside = [r for r in rows if t0 is not None and t0 - 0.25 <= r[0] <= t1 + 0.25]
+        use = inside or rows
+        reasons = sorted({x for r in use for x in r[3]})
+        return {"sm_mhz": statistics.median([r[1] for r in use]) if use else None,
+                "sm_max_mhz": use[-1][2] if use else None, "reasons": reasons, "samples": len(use),
+                "in_timed_region": bool(inside)}
 
 
 def cpu_baseline(v, t, rays, sample: int):
@@ -171,11 +199,12 @@ def run_reference(args, rank: int):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c1", choices=["c1", "c0"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rays", type=int, default=0, help="smaller case of the workload (profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -193,7 +222,7 @@ def main():
         dist.init_process_group("nccl")
     from lightsprintsdk_gb300 import collider as col
 
-    v, t, rays = make_workload(args.workload)
+    v, t, rays = make_workload(args.workload, args.rays)
     n = rays.shape[0]
     c = col.RRCollider.create(v, t, device=local)
     build_ms = c.build_ms
@@ -205,20 +234,24 @@ def main():
     def step():
         c.intersect_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream=sp)
 
+    clk = ClockSampler(local).__enter__()
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
+    clk.wait_first_sample()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        e0.record(stream)
-        for _ in range(args.steps):
-            step()
-        e1.record(stream)
-        torch.cuda.synchronize()
+    clk.mark_start()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk.mark_end()
+    clk.__exit__()
     ms = e0.elapsed_time(e1) / args.steps
     if world > 1:
         tt = torch.tensor([ms], device=f"cuda:{local}")

@@ -1,0 +1,71 @@
+/* rrgpu_gather.h -- C ABI of the GB300 lightmap final gather.
+ *
+ * Replaces, for the plain N-bounce estimator, the reference's
+ * RRSolver::updateLightmaps / updateLightmap (RRSolver/lightmap.cpp:648-1163)
+ * with its texel enumeration (enumerateTexelsPartial, lightmap.cpp:83-404) and
+ * per-texel gather (processTexel, RRSolver/gather.cpp:600-836).  The scene is
+ * the collider's mesh (rrgpu.h); materials are per-triangle diffuse albedo
+ * (RRMaterial::diffuseReflectance, one-sided, RRMaterial.cpp:154-166);
+ * lights are one directional and one point light with REALISTIC falloff
+ * (RRLight.cpp:345-362, 450-455).  Lightmaps are `natlas` square atlases of
+ * size x size texels, float RGBA per texel (RGB = irradiance in the
+ * reference's physical scale, A = 1 where the texel is covered).
+ *
+ * Texel t of atlas a has global id a*size*size + y*size + x; its sample
+ * streams are seeded by that id, so any subset of texels can be gathered and
+ * every result is reproducible.
+ */
+#ifndef RRGPU_GATHER_H
+#define RRGPU_GATHER_H
+#include "rrgpu.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rrg_lightmapper rrg_lightmapper;
+
+/* UpdateParameters / PathTracingParameters subset (RRSolver.h:468-594,
+ * 964-1001).  size = sizeof(rrg_gather_params). */
+typedef struct rrg_gather_params {
+	uint32_t size;
+	uint32_t quality;          /* hemisphere rays per texel (UpdateParameters::quality), 1..256 */
+	uint32_t max_depth;        /* diffuse bounces (PathTracingParameters::stopAtDepth) */
+	uint32_t reserved0;
+	uint64_t seed;             /* sample streams */
+	float ray_length_min;      /* 0 = the solver's minimalSafeDistance of the mesh */
+	float locality;            /* UpdateParameters::locality, 0 = 100000 */
+	float dir_direction[3];    /* directional light: unit direction the light travels */
+	float dir_color[3];
+	float point_position[3];   /* point light */
+	float point_color[3];
+} rrg_gather_params;
+
+/* Enumerates sub-texels on the device.  albedo: 3 floats per triangle;
+ * tri_atlas: atlas of each triangle (-1 = not lightmapped); uv: 3 corners x
+ * (u, v) in [0,1] per triangle, in the triangle's vertex order.  The
+ * collider must outlive the lightmapper. */
+RRG_API int rrg_lightmapper_create(rrg_collider* c, const float* albedo, const int32_t* tri_atlas, const float* uv,
+                                   uint32_t natlas, uint32_t size, rrg_lightmapper** out);
+RRG_API void rrg_lightmapper_destroy(rrg_lightmapper* lm);
+RRG_API uint64_t rrg_lightmapper_subtexels(const rrg_lightmapper* lm);
+/* minimalSafeDistance used when ray_length_min = 0. */
+RRG_API float rrg_lightmapper_ray_length_min(const rrg_lightmapper* lm);
+/* Copies the sub-texel lists: offsets (natlas*size*size + 1 uint32) and
+ * 32-byte records {uint32 triangle; float uv[3][2] in triangle space; float
+ * area in map space} (may be NULL). */
+RRG_API int rrg_lightmapper_copy_subtexels(const rrg_lightmapper* lm, uint32_t* offsets_host, void* subtexels_host);
+
+/* Gathers texels [first_texel, first_texel + ntexels) into out (4 floats per
+ * texel, 16-byte aligned device memory).  Asynchronous on `stream`. */
+RRG_API int rrg_lightmap_gather(rrg_lightmapper* lm, const rrg_gather_params* p, uint64_t first_texel,
+                                uint64_t ntexels, float* out_dev, void* stream);
+/* Same into host memory; synchronous. */
+RRG_API int rrg_lightmap_gather_host(rrg_lightmapper* lm, const rrg_gather_params* p, uint64_t first_texel,
+                                     uint64_t ntexels, float* out_host, void* stream);
+/* RRG_OK, or RRG_ERR_STACK if a traversal overflowed since the last call. */
+RRG_API int rrg_lightmapper_status(rrg_lightmapper* lm, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

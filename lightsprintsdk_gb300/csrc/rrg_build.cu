@@ -103,6 +103,28 @@ __global__ void k_prep(const float* __restrict__ xyz, uint32_t nv, const uint32_
 	phi[t] = make_float4(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)), 0.f);
 }
 
+// AABB of all vertices (RRMesh::getAABB), as ordered ints
+__global__ void k_vertex_aabb(const float* __restrict__ xyz, uint32_t nv, int* __restrict__ rb) {
+	float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x)
+		for (int k = 0; k < 3; k++) {
+			float v = xyz[3 * (size_t)i + k];
+			if (v < lo[k]) lo[k] = v;   // NaN never compares: skipped, as getAABB's comparisons skip it
+			if (v > hi[k]) hi[k] = v;
+		}
+	for (int k = 0; k < 3; k++) {
+		float a = lo[k], b = hi[k];
+		for (int o = 16; o; o >>= 1) {
+			a = fminf(a, __shfl_xor_sync(0xFFFFFFFFu, a, o));
+			b = fmaxf(b, __shfl_xor_sync(0xFFFFFFFFu, b, o));
+		}
+		if ((threadIdx.x & 31) == 0) {
+			atomicMin(&rb[k], f2o(a));
+			atomicMax(&rb[3 + k], f2o(b));
+		}
+	}
+}
+
 // ------------------------------------------------------------ compaction
 constexpr int kScanItems = 1024;   // flags per scan block (256 threads x 4)
 
@@ -931,6 +953,20 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 		for (int k = 0; k < 3; k++) { rb_init[k] = ip; rb_init[3 + k] = in; rb_init[6 + k] = ip; rb_init[9 + k] = in; }
 	}
 	RRG_CUDA(cudaMemcpyAsync(rb, rb_init, sizeof(rb_init), cudaMemcpyHostToDevice, s));
+	{
+		int vgrid = (int)((c->nv + 255) / 256);
+		if (vgrid > 4 * 152) vgrid = 4 * 152;
+		k_vertex_aabb<<<vgrid, 256, 0, s>>>(c->d_xyz, c->nv, rb);
+		int hb[6];
+		RRG_CUDA(cudaMemcpyAsync(hb, rb, sizeof(hb), cudaMemcpyDeviceToHost, s));
+		RRG_CUDA(cudaStreamSynchronize(s));
+		for (int k = 0; k < 3; k++) {
+			int lo = hb[k] >= 0 ? hb[k] : hb[k] ^ 0x7FFFFFFF, hi = hb[3 + k] >= 0 ? hb[3 + k] : hb[3 + k] ^ 0x7FFFFFFF;
+			memcpy(&c->aabb_lo[k], &lo, 4);
+			memcpy(&c->aabb_hi[k], &hi, 4);
+		}
+		RRG_CUDA(cudaMemcpyAsync(rb, rb_init, sizeof(rb_init), cudaMemcpyHostToDevice, s));
+	}
 	int rgrid = (int)((nvalid + 255) / 256);
 	if (rgrid > 4 * 152) rgrid = 4 * 152;
 	k_root_bounds<<<rgrid, 256, 0, s>>>(idsA, nvalid, plo, phi, rb);

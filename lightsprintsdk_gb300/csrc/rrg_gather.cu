@@ -1,0 +1,815 @@
+// Lightmap final gather on the GPU: texel enumeration and the plain N-bounce
+// gather, behind the C ABI of include/rrgpu_gather.h.
+//
+// Reference path: RRSolver::updateLightmaps -> updateLightmap ->
+// enumerateTexelsFull/Partial -> processTexel (RRSolver/lightmap.cpp:83-454,
+// 648-930; RRSolver/gather.cpp:600-836) with
+// PathtracerWorker::getIncidentRadiance (RRStaticSolver/pathtracer.cpp:139-394).
+//
+// 1. enumeration: one warp per triangle; lanes walk the texels of the
+//    triangle's lightmap bounding box, clip each texel square by the
+//    triangle's three edges in triangle space and fan the polygon into
+//    sub-texels (lightmap.cpp:145-330), first counting per texel, then (after
+//    a device-wide scan) writing; each texel's list is then sorted by
+//    (triangle, fan index), the order in which the reference appends them.
+// 2. gather: one warp per texel.  The 64 hemisphere samples of a texel are
+//    the 32 lanes x 2; each lane selects its sub-texel by the reference's
+//    area stepping, takes its point and its HomogenousFiller2 direction (the
+//    filler's accepted points are found cooperatively with a ballot), and
+//    traces an N-bounce path with next-event shadow rays.  Light rounds
+//    (quality/10+1, interleaved as gather.cpp:773-785) add direct light.
+//    Lane 0 sums the samples in the reference's order.
+// Every floating-point step mirrors the C oracle (oracle/rr_gather.c) with
+// one rounding per operation (__f*_rn), so both produce the same values from
+// the same counter-based sample streams.
+#include "rrg_traverse.cuh"
+#include "../../include/rrgpu_gather.h"
+
+#include <vector>
+
+namespace rrg {
+
+// ------------------------------------------------------------------ RNG
+__device__ __forceinline__ uint64_t fmix64(uint64_t k) {
+	k ^= k >> 33;
+	k *= 0xFF51AFD7ED558CCDULL;
+	k ^= k >> 33;
+	k *= 0xC4CEB9FE1A85EC53ULL;
+	k ^= k >> 33;
+	return k;
+}
+__device__ __forceinline__ uint64_t hash64(uint64_t seed, uint64_t stream, uint64_t index) {
+	uint64_t key = seed * 0x9E3779B97F4A7C15ULL + stream * 0xD1B54A32D192ED03ULL;
+	return fmix64(fmix64(index ^ key) + 0x632BE59BD9B4E019ULL);
+}
+__device__ __forceinline__ uint32_t rng24(uint64_t seed, uint64_t stream, uint64_t index) {
+	return (uint32_t)(hash64(seed, stream, index) >> 40);
+}
+__device__ __forceinline__ float rng01(uint64_t seed, uint64_t stream, uint64_t index) {
+	return __fmul_rn((float)rng24(seed, stream, index), 1.0f / 16777216.0f);
+}
+
+enum { S_FILLER = 60, S_PU = 61, S_PV = 62, S_ROULETTE = 63, S_DISKX = 64, S_DISKY = 65 };
+constexpr uint32_t kM24 = 16777215u;
+constexpr int kDiskTries = 32;
+constexpr float kPreventInf = 0.000000000137289f;   // RRLight.cpp:21
+constexpr float kStopAtVisibility = 0.001f;         // PathTracingParameters default
+
+// -------------------------------------------------------------- vectors
+struct V3 {
+	float x, y, z;
+};
+__host__ __device__ __forceinline__ V3 mk(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 add(V3 a, V3 b) { return mk(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)); }
+__device__ __forceinline__ V3 sub(V3 a, V3 b) { return mk(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)); }
+__device__ __forceinline__ V3 mul(V3 a, float f) { return mk(__fmul_rn(a.x, f), __fmul_rn(a.y, f), __fmul_rn(a.z, f)); }
+__device__ __forceinline__ V3 mulv(V3 a, V3 b) { return mk(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y), __fmul_rn(a.z, b.z)); }
+__device__ __forceinline__ V3 divf(V3 a, float f) { return mk(__fdiv_rn(a.x, f), __fdiv_rn(a.y, f), __fdiv_rn(a.z, f)); }
+__device__ __forceinline__ V3 neg(V3 a) { return mk(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float dot(V3 a, V3 b) {
+	return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ float len(V3 a) { return __fsqrt_rn(dot(a, a)); }
+__device__ __forceinline__ V3 normalized(V3 a) { return divf(a, len(a)); }
+__device__ __forceinline__ float avg3(V3 a) { return __fmul_rn(__fadd_rn(__fadd_rn(a.x, a.y), a.z), 0.33333333333333f); }
+__device__ __forceinline__ V3 ortho1(V3 a) { return fabsf(a.x) > fabsf(a.z) ? mk(-a.y, a.x, 0.f) : mk(0.f, -a.z, a.y); }
+__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+	return mk(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)), __fadd_rn(__fmul_rn(-a.x, b.z), __fmul_rn(a.z, b.x)),
+	          __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ float clampf(float a, float lo, float hi) { return a < lo ? lo : (a > hi ? hi : a); }
+
+// ---------------------------------------------------------- enumeration
+struct Sub {            // one sub-texel, 32 bytes (matches orc_subtexel)
+	uint32_t tri;
+	float uv[6];
+	float area;
+};
+
+struct V2 {
+	float x, y;
+};
+
+__device__ __forceinline__ float get_area(V2 v0, V2 v1, V2 v2) {
+	auto l = [](V2 p, V2 q) {
+		float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y);
+		return __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+	};
+	float a = l(v0, v1), b = l(v1, v2), c = l(v2, v0);
+	float s = __fmul_rn(__fadd_rn(__fadd_rn(a, b), c), 0.5f);
+	return __fsqrt_rn(__fmul_rn(__fmul_rn(__fmul_rn(s, __fsub_rn(s, a)), __fsub_rn(s, b)), __fsub_rn(s, c)));
+}
+
+struct Raster {
+	unsigned x0, x1, y0, y1;   // texel bbox [x0,x1) x [y0,y1)
+	float inv[2][3];
+	float tri_area;
+	bool ok;
+};
+
+// bounding box and map -> triangle space matrix (lightmap.cpp:155-205)
+__device__ Raster raster_setup(const float* uvm, unsigned size) {
+	Raster R;
+	R.ok = false;
+	const float W = (float)size, H = (float)size;
+	V2 u0{uvm[0], uvm[1]}, u1{uvm[2], uvm[3]}, u2{uvm[4], uvm[5]};
+	float xmin = __fmul_rn(W, fminf(u0.x, fminf(u1.x, u2.x)));
+	float xmax = __fmul_rn(W, fmaxf(u0.x, fmaxf(u1.x, u2.x)));
+	float ymin = __fmul_rn(H, fminf(u0.y, fminf(u1.y, u2.y)));
+	float ymax = __fmul_rn(H, fmaxf(u0.y, fmaxf(u1.y, u2.y)));
+	R.x0 = (unsigned)(xmin > 0.f ? xmin : 0.f);
+	R.x1 = (unsigned)clampf(__fadd_rn(xmax, 1.f), 0.f, W);
+	R.y0 = (unsigned)(ymin > 0.f ? ymin : 0.f);
+	R.y1 = (unsigned)clampf(__fadd_rn(ymax, 1.f), 0.f, H);
+	if (R.y0 >= R.y1 || R.x0 >= R.x1) return R;
+	float m00 = __fsub_rn(u1.x, u0.x), m01 = __fsub_rn(u2.x, u0.x), m02 = u0.x;
+	float m10 = __fsub_rn(u1.y, u0.y), m11 = __fsub_rn(u2.y, u0.y), m12 = u0.y;
+	const float m20 = 0.f, m21 = 0.f, m22 = 1.f;
+	float det = __fsub_rn(
+	    __fsub_rn(__fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(m00, m11), m22), __fmul_rn(__fmul_rn(m01, m12), m20)),
+	                                  __fmul_rn(__fmul_rn(m02, m10), m21)),
+	                        __fmul_rn(__fmul_rn(m00, m12), m21)),
+	              __fmul_rn(__fmul_rn(m01, m10), m22)),
+	    __fmul_rn(__fmul_rn(m02, m11), m20));
+	if (!(det != 0.f)) return R;
+	float invdet = __fdiv_rn(1.f, det);
+	R.inv[0][0] = __fdiv_rn(__fmul_rn(__fsub_rn(__fmul_rn(m11, m22), __fmul_rn(m12, m21)), invdet), W);
+	R.inv[0][1] = __fdiv_rn(__fmul_rn(__fsub_rn(__fmul_rn(m02, m21), __fmul_rn(m01, m22)), invdet), H);
+	R.inv[0][2] = __fmul_rn(__fsub_rn(__fmul_rn(m01, m12), __fmul_rn(m02, m11)), invdet);
+	R.inv[1][0] = __fdiv_rn(__fmul_rn(__fsub_rn(__fmul_rn(m12, m20), __fmul_rn(m10, m22)), invdet), W);
+	R.inv[1][1] = __fdiv_rn(__fmul_rn(__fsub_rn(__fmul_rn(m00, m22), __fmul_rn(m02, m20)), invdet), H);
+	R.inv[1][2] = __fmul_rn(__fsub_rn(__fmul_rn(m02, m10), __fmul_rn(m00, m12)), invdet);
+	R.tri_area = get_area(u0, u1, u2);
+	R.ok = true;
+	return R;
+}
+
+// clips texel (x, y) by the triangle; returns the polygon size (0..7)
+__device__ int clip_texel(const Raster& R, unsigned x, unsigned y, V2* poly) {
+	auto m2t = [&](unsigned X, unsigned Y) {
+		float fx = (float)X, fy = (float)Y;
+		return V2{__fadd_rn(__fadd_rn(__fmul_rn(fx, R.inv[0][0]), __fmul_rn(fy, R.inv[0][1])), R.inv[0][2]),
+		          __fadd_rn(__fadd_rn(__fmul_rn(fx, R.inv[1][0]), __fmul_rn(fy, R.inv[1][1])), R.inv[1][2])};
+	};
+	unsigned n = 4;
+	poly[0] = m2t(x, y);
+	poly[1] = m2t(x + 1, y);
+	poly[2] = m2t(x + 1, y + 1);
+	poly[3] = m2t(x, y + 1);
+	for (int side = 0; side < 3; side++) {
+		float L0 = side == 0 ? 0.f : (side == 1 ? -1.f : 1.f);
+		float L1 = side == 0 ? 1.f : (side == 1 ? -1.f : 0.f);
+		float L2 = side == 0 ? 0.f : (side == 1 ? 1.f : 0.f);
+		int inside[7];
+		unsigned nin = 0, nout = 0;
+		for (unsigned i = 0; i < n; i++) {
+			float dd = __fadd_rn(__fadd_rn(__fmul_rn(L0, poly[i].x), __fmul_rn(L1, poly[i].y)), L2);
+			if (dd < 0.f) { inside[i] = 2; nout++; }
+			else if (dd > 0.f) { inside[i] = 0; nin++; }
+			else inside[i] = 1;
+		}
+		if (!nout) continue;
+		if (!nin) return 0;
+		unsigned fp = 1;
+		while (inside[(fp - 1) % n] == 0 || inside[fp % n] != 0) fp++;
+		V2 orig[7];
+		for (int i = 0; i < 7; i++) orig[i] = poly[i];
+		unsigned src = fp, dst = 0;
+		while (inside[src % n] == 0 && dst < 7) poly[dst++] = orig[src++ % n];
+		auto isect = [&](V2 A, V2 B) {
+			float dA = __fadd_rn(__fadd_rn(__fmul_rn(L0, A.x), __fmul_rn(L1, A.y)), L2);
+			float den = __fadd_rn(__fmul_rn(L0, __fsub_rn(B.x, A.x)), __fmul_rn(L1, __fsub_rn(B.y, A.y)));
+			return V2{__fsub_rn(A.x, __fdiv_rn(__fmul_rn(__fsub_rn(B.x, A.x), dA), den)),
+			          __fsub_rn(A.y, __fdiv_rn(__fmul_rn(__fsub_rn(B.y, A.y), dA), den))};
+		};
+		if (dst + 2 > 7) return 0;   // cannot happen for a convex quad cut three times
+		poly[dst++] = isect(orig[(src - 1) % n], orig[src % n]);
+		poly[dst++] = isect(orig[(fp - 1) % n], orig[fp % n]);
+		n = dst;
+	}
+	return (int)n;
+}
+
+// One warp per triangle.  COUNT: counts[texel] += sub-texels.  Otherwise
+// writes them at off[texel] + cursor, with the fan index in .tri's top bits
+// replaced later by the sort.
+template <bool COUNT>
+__global__ void k_enumerate(const float* __restrict__ uv, const int32_t* __restrict__ tri_atlas, uint32_t nt,
+                            uint32_t size, uint32_t natlas, uint32_t* __restrict__ counts,
+                            const uint32_t* __restrict__ off, uint32_t* __restrict__ cursor, Sub* __restrict__ out,
+                            uint32_t* __restrict__ fan_out, uint64_t cap, uint32_t* err) {
+	const int lane = threadIdx.x & 31;
+	const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+	for (uint32_t t = warp; t < nt; t += nwarps) {
+		int a = tri_atlas[t];
+		if (a < 0 || (uint32_t)a >= natlas) continue;
+		Raster R = raster_setup(uv + 6 * (size_t)t, size);
+		if (!R.ok) continue;
+		const uint32_t bw = R.x1 - R.x0, bh = R.y1 - R.y0;
+		const uint64_t nb = (uint64_t)bw * bh;
+		const uint64_t abase = (uint64_t)a * size * size;
+		for (uint64_t j = lane; j < nb; j += 32) {
+			unsigned x = R.x0 + (unsigned)(j % bw), y = R.y0 + (unsigned)(j / bw);
+			V2 poly[7];
+			int n = clip_texel(R, x, y, poly);
+			if (n < 3) continue;
+			uint64_t texel = abase + (uint64_t)y * size + x;
+			float areas[5];
+			int valid = 0;
+			for (int i = 0; i + 2 < n; i++) {
+				float ar = __fmul_rn(get_area(poly[0], poly[i + 1], poly[i + 2]), R.tri_area);
+				areas[i] = ar;
+				if (isfinite(ar)) valid++;
+			}
+			if (!valid) continue;
+			if (COUNT) {
+				atomicAdd(&counts[texel], (uint32_t)valid);
+			} else {
+				uint32_t base = off[texel] + atomicAdd(&cursor[texel], (uint32_t)valid);
+				int w = 0;
+				for (int i = 0; i + 2 < n; i++) {
+					if (!isfinite(areas[i])) continue;
+					uint64_t pos = (uint64_t)base + w;
+					if (pos >= cap) { atomicOr(err, 1u); break; }
+					Sub s;
+					s.tri = t;
+					s.uv[0] = poly[0].x; s.uv[1] = poly[0].y;
+					s.uv[2] = poly[i + 1].x; s.uv[3] = poly[i + 1].y;
+					s.uv[4] = poly[i + 2].x; s.uv[5] = poly[i + 2].y;
+					s.area = areas[i];
+					out[pos] = s;
+					fan_out[pos] = (uint32_t)i;
+					w++;
+				}
+			}
+		}
+	}
+}
+
+// per texel: insertion sort of its sub-texels by (triangle, fan)
+__global__ void k_sort_texels(const uint32_t* __restrict__ off, uint64_t ntexels, Sub* __restrict__ st,
+                              uint32_t* __restrict__ fan) {
+	for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ntexels; t += (uint64_t)gridDim.x * blockDim.x) {
+		uint32_t b = off[t], e = off[t + 1];
+		for (uint32_t i = b + 1; i < e; i++) {
+			Sub s = st[i];
+			uint32_t f = fan[i];
+			uint64_t key = ((uint64_t)s.tri << 8) | f;
+			uint32_t j = i;
+			while (j > b && ((((uint64_t)st[j - 1].tri) << 8) | fan[j - 1]) > key) {
+				st[j] = st[j - 1];
+				fan[j] = fan[j - 1];
+				j--;
+			}
+			st[j] = s;
+			fan[j] = f;
+		}
+	}
+}
+
+// exclusive scan of n uint32 (total < 2^32) -> off[0..n]
+constexpr int kScanBT = 256, kScanPer = 4096;
+__global__ void k_scan_sums(const uint32_t* __restrict__ in, uint64_t n, uint32_t* __restrict__ bsum) {
+	__shared__ uint32_t ws[kScanBT / 32];
+	uint64_t base = (uint64_t)blockIdx.x * kScanPer;
+	uint32_t s = 0;
+	for (int k = threadIdx.x; k < kScanPer; k += kScanBT)
+		if (base + k < n) s += in[base + k];
+	for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+	if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		uint32_t t = 0;
+		for (int w = 0; w < kScanBT / 32; w++) t += ws[w];
+		bsum[blockIdx.x] = t;
+	}
+}
+__global__ void k_scan_top(uint32_t* __restrict__ bsum, uint32_t nb) {
+	if (threadIdx.x) return;
+	uint32_t s = 0;
+	for (uint32_t i = 0; i < nb; i++) {
+		uint32_t v = bsum[i];
+		bsum[i] = s;
+		s += v;
+	}
+	bsum[nb] = s;
+}
+__global__ void k_scan_apply(const uint32_t* __restrict__ in, uint64_t n, const uint32_t* __restrict__ bsum,
+                             uint32_t* __restrict__ out) {
+	__shared__ uint32_t ws[kScanBT / 32];
+	__shared__ uint32_t carry;
+	uint64_t base = (uint64_t)blockIdx.x * kScanPer;
+	if (threadIdx.x == 0) carry = bsum[blockIdx.x];
+	__syncthreads();
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+	for (int k0 = 0; k0 < kScanPer; k0 += kScanBT) {
+		uint64_t i = base + k0 + threadIdx.x;
+		uint32_t v = i < n ? in[i] : 0;
+		uint32_t x = v;
+		for (int o = 1; o < 32; o <<= 1) {
+			uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+			if (lane >= o) x += y;
+		}
+		if (lane == 31) ws[w] = x;
+		__syncthreads();
+		uint32_t wo = 0, tot = 0;
+		for (int q = 0; q < kScanBT / 32; q++) {
+			if (q < w) wo += ws[q];
+			tot += ws[q];
+		}
+		if (i < n) out[i] = carry + wo + x - v;
+		__syncthreads();
+		if (threadIdx.x == 0) carry += tot;
+		__syncthreads();
+	}
+	if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = bsum[gridDim.x];
+}
+
+// ---------------------------------------------------------------- gather
+struct GatherScene {
+	const TNode* nodes;
+	const float4* tris;
+	int nnodes, ntris;
+	const float* xyz;
+	const uint32_t* idx;
+	const float* albedo;
+	V3 dir_direction, dir_color, point_position, point_color;
+	float tmin, locality;
+	uint32_t quality, max_depth;
+	uint64_t seed;
+};
+
+__device__ __forceinline__ V3 ld3(const float* p) { return mk(p[0], p[1], p[2]); }
+
+__device__ V3 tri_normal(const GatherScene& g, uint32_t t, V3& v0, V3& s1, V3& s2) {
+	v0 = ld3(g.xyz + 3 * (size_t)g.idx[3 * t]);
+	s1 = sub(ld3(g.xyz + 3 * (size_t)g.idx[3 * t + 1]), v0);
+	s2 = sub(ld3(g.xyz + 3 * (size_t)g.idx[3 * t + 2]), v0);
+	V3 n = cross(s1, s2);
+	float l = len(n);
+	return l != 0.f ? divf(n, l) : mk(1.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ V3 point_irr(const GatherScene& g, V3 p) {
+	V3 d = sub(p, g.point_position);
+	float att = __fdiv_rn(1.f, __fadd_rn(kPreventInf, dot(d, d)));
+	return mul(g.point_color, att);
+}
+
+__device__ __forceinline__ void basis_from_normal(V3 n, V3& t, V3& b) {
+	t = normalized(ortho1(n));
+	b = cross(n, t);
+}
+
+__device__ __forceinline__ void set_ray(RayState& r, V3 o, V3 d, float tmin, float tmax) {
+	r.ox = o.x; r.oy = o.y; r.oz = o.z; r.tmin = tmin;
+	r.dx = d.x; r.dy = d.y; r.dz = d.z; r.tmax = tmax;
+	ray_setup(r);
+}
+
+__device__ GatherFilter make_filter(const GatherScene& g, uint32_t skip, bool front_only) {
+	GatherFilter f;
+	f.skip = skip;
+	f.ident_t = __fmul_rn(1000.f, g.tmin);
+	f.front_only = front_only;
+	const float* a = g.xyz + 3 * (size_t)g.idx[3 * skip];
+	const float* b = g.xyz + 3 * (size_t)g.idx[3 * skip + 1];
+	const float* c = g.xyz + 3 * (size_t)g.idx[3 * skip + 2];
+	f.s0 = make_float4(a[0], a[1], a[2], 0.f);
+	f.s1 = make_float4(b[0], b[1], b[2], 0.f);
+	f.s2 = make_float4(c[0], c[1], c[2], 0.f);
+	return f;
+}
+
+// shadow ray: any accepted hit blocks
+__device__ bool occluded(const GatherScene& g, V3 o, V3 d, float tmin, float tmax, uint32_t skip, bool& overflow) {
+	RayState r;
+	set_ray(r, o, d, tmin, tmax);
+	GatherFilter f = make_filter(g, skip, false);
+	float tb = r.tmax;
+	uint32_t bt = 0xFFFFFFFFu;
+	return traverse<true, true>(g.nodes, g.tris, r, g.nnodes, g.ntris, tb, bt, overflow, &f) >= 0;
+}
+
+// one hemisphere sample: getIncidentRadiance restated iteratively
+__device__ V3 trace_path(const GatherScene& g, V3 eye, V3 dir, uint32_t skip, uint64_t sid, bool& overflow) {
+	V3 T = mk(1.f, 1.f, 1.f), L = mk(0.f, 0.f, 0.f);
+	float tmax = g.locality;
+	for (uint32_t depth = 0;; depth++) {
+		RayState r;
+		set_ray(r, eye, dir, g.tmin, tmax);
+		GatherFilter f = make_filter(g, skip, true);
+		float tb = r.tmax;
+		uint32_t tri = 0xFFFFFFFFu;
+		int slot = traverse<false, true>(g.nodes, g.tris, r, g.nnodes, g.ntris, tb, tri, overflow, &f);
+		if (slot < 0) break;
+		float4 a, b, c;
+		load_tri(g.tris, slot, a, b, c);
+		Fastest fs = fastest_fields(r, a, b, c);
+		V3 p = add(eye, mul(dir, fs.dist));
+		V3 n = mk(fs.n[0], fs.n[1], fs.n[2]);
+		V3 alb = ld3(g.albedo + 3 * (size_t)tri);
+		for (int li = 0; li < 2; li++) {
+			V3 sdir;
+			float smax;
+			if (li == 0) {
+				sdir = neg(g.dir_direction);
+				smax = 1e10f;
+			} else {
+				V3 d = sub(g.point_position, p);
+				sdir = normalized(d);
+				smax = len(d);
+			}
+			if (!(dot(n, sdir) > 0.f)) continue;
+			V3 unob = li == 0 ? g.dir_color : point_irr(g, p);
+			float dif = clampf(-dot(neg(sdir), n), 0.f, 1.f);
+			V3 contrib = mulv(unob, mul(alb, dif));
+			if (contrib.x == 0.f && contrib.y == 0.f && contrib.z == 0.f) continue;
+			if (occluded(g, p, sdir, g.tmin, smax, tri, overflow)) continue;
+			L = add(L, mulv(T, contrib));
+		}
+		tmax = 1e10f;
+		float pdiff = avg3(alb);
+		if (pdiff < 0.f) pdiff = 0.f;
+		float pstop = __fsub_rn(1.f, pdiff);
+		if (pstop < 0.f) pstop = 0.f;
+		float rr = rng01(g.seed, S_ROULETTE, sid * 16 + depth);
+		if (!(rr < pdiff && depth < g.max_depth)) break;
+		float intensity = __fdiv_rn(__fadd_rn(pdiff, pstop), pdiff);
+		float x = 0.f, y = 0.f;
+		for (int j = 0; j < kDiskTries; j++) {
+			uint64_t cc = (sid * 16 + depth) * kDiskTries + j;
+			float ax = __fsub_rn(__fmul_rn(rng01(g.seed, S_DISKX, cc), 2.0f), 1.0f);
+			float by = __fsub_rn(__fmul_rn(rng01(g.seed, S_DISKY, cc), 2.0f), 1.0f);
+			if (__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(by, by)) < 1.0f) { x = ax; y = by; break; }
+		}
+		float cosT = __fsqrt_rn(__fsub_rn(1.0f, __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y))));
+		V3 tg, bt;
+		basis_from_normal(n, tg, bt);
+		V3 s = add(add(mul(n, cosT), mul(tg, x)), mul(bt, y));
+		float pdf = cosT;
+		V3 dirIn = neg(s);
+		float dif = clampf(-dot(dirIn, n), 0.f, 1.f);
+		V3 colorOut = mul(alb, dif);
+		if (!(pdf > 0.f && dot(dirIn, n) < 0.f)) break;
+		V3 rs = mul(colorOut, __fdiv_rn(intensity, pdf));
+		if (!(avg3(rs) > kStopAtVisibility)) break;
+		T = mulv(T, rs);
+		eye = p;
+		dir = s;
+		skip = tri;
+	}
+	return L;
+}
+
+// HomogenousFiller2::GetTrianglePoint (gather.cpp:65-83)
+__device__ __forceinline__ void filler_point(unsigned n, float& a, float& b) {
+	float x = 0.f, y = 0.f, dist = 1.f;
+	while (n) {
+		unsigned q = n & 3;
+		float dx = q == 0 ? 0.f : (q == 1 ? 0.f : (q == 2 ? 0.86602540378444f : -0.86602540378444f));
+		float dy = q == 0 ? 0.f : (q == 1 ? 1.f : -0.5f);
+		float dm = q == 0 ? -0.5f : 0.5f;
+		x = __fadd_rn(x, __fmul_rn(dist, dx));
+		y = __fadd_rn(y, __fmul_rn(dist, dy));
+		dist = __fmul_rn(dist, dm);
+		n >>= 2;
+	}
+	a = x;
+	b = y;
+}
+
+constexpr int kGatherWarps = 4;
+constexpr int kMaxQuality = 256;
+constexpr int kMaxRounds = kMaxQuality / 10 + 1;
+
+struct WarpSmem {
+	float fx[kMaxQuality], fy[kMaxQuality], fd[kMaxQuality];
+	V3 hemi[kMaxQuality];
+	V3 light[kMaxRounds][2];
+	unsigned char lit[kMaxRounds][2];
+};
+
+__global__ void __launch_bounds__(kGatherWarps * 32) k_gather(GatherScene g, const uint32_t* __restrict__ off,
+                                                              const Sub* __restrict__ st, uint64_t first,
+                                                              uint64_t count, float4* __restrict__ out,
+                                                              uint32_t* counter, uint32_t* status) {
+	__shared__ WarpSmem sm_all[kGatherWarps];
+	WarpSmem& sm = sm_all[threadIdx.x >> 5];
+	const int lane = threadIdx.x & 31;
+	const uint32_t Q = g.quality;
+	const uint32_t rounds = Q / 10 + 1;
+	const uint32_t N = Q > rounds ? Q : rounds;
+	bool overflow = false;
+	while (true) {
+		uint64_t ti = 0;
+		if (lane == 0) ti = atomicAdd((unsigned long long*)counter, 1ull);
+		ti = __shfl_sync(0xFFFFFFFFu, ti, 0);
+		if (ti >= count) break;
+		const uint64_t tid = first + ti;
+		const uint32_t b = off[tid], m = off[tid + 1] - b;
+		if (m == 0) {
+			if (lane == 0) out[ti] = make_float4(0.f, 0.f, 0.f, 0.f);
+			continue;
+		}
+		const Sub* S = st + b;
+		for (int q = lane; q < kMaxRounds * 2; q += 32) sm.lit[q >> 1][q & 1] = 0;
+		// HomogenousFiller2 points: candidate num = reset + j, the k-th accepted one
+		// serves hemisphere ray k (gather.cpp:88-93)
+		const unsigned reset = (unsigned)(hash64(g.seed, S_FILLER, tid) & 0xffffu);
+		uint32_t found = 0;
+		for (uint32_t j0 = 0; found < Q; j0 += 32) {
+			float x, y;
+			filler_point(reset + j0 + lane, x, y);
+			float dd = __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y));
+			bool ok = dd < 1.f;
+			unsigned m32 = __ballot_sync(0xFFFFFFFFu, ok);
+			uint32_t slot = found + __popc(m32 & ((1u << lane) - 1));
+			if (ok && slot < Q) { sm.fx[slot] = x; sm.fy[slot] = y; sm.fd[slot] = dd; }
+			found += __popc(m32);
+		}
+		__syncwarp();
+		float areaMax = 0.f;
+		for (uint32_t i = 0; i < m; i++) areaMax = __fadd_rn(areaMax, S[i].area);
+		const float areaStep = __fdiv_rn(areaMax, __fadd_rn((float)N, 0.91f));
+		for (uint32_t k = lane; k < N; k += 32) {
+			// area stepping (gather.cpp:665-688), replayed up to shooter k
+			float areaAccu = -S[0].area;
+			uint32_t it = 0;
+			uint32_t gl = 0, round = 0;
+			bool fires = false;
+			for (uint32_t q = 0; q <= k; q++) {
+				areaAccu = __fadd_rn(areaAccu, areaStep);
+				while (areaAccu > 0.f) {
+					it++;
+					if (it == m) it = 0;
+					areaAccu = __fsub_rn(areaAccu, S[it].area);
+				}
+				bool f = (uint64_t)gl * (N - 1) < (uint64_t)rounds * q || rounds >= Q;
+				if (q == k) { fires = f; round = gl; }
+				if (f) gl++;
+			}
+			const Sub& s = S[it];
+			V3 v0, s1, s2;
+			V3 fn = tri_normal(g, s.tri, v0, s1, s2);
+			float cu = __fmul_rn(__fadd_rn(__fadd_rn(s.uv[0], s.uv[2]), s.uv[4]), 0.333333333f);
+			float cv = __fmul_rn(__fadd_rn(__fadd_rn(s.uv[1], s.uv[3]), s.uv[5]), 0.333333333f);
+			float w = __fsub_rn(__fsub_rn(1.f, cu), cv);
+			V3 nrm = normalized(add(add(mul(fn, w), mul(fn, cu)), mul(fn, cv)));
+			V3 tg, bt;
+			basis_from_normal(nrm, tg, bt);
+			const uint64_t sid = tid * N + k;
+			uint32_t ru = rng24(g.seed, S_PU, sid), rv = rng24(g.seed, S_PV, sid);
+			if (ru + rv > kM24) { ru = kM24 - ru; rv = kM24 - rv; }
+			float fu = __fdiv_rn((float)ru, (float)kM24), fv = __fdiv_rn((float)rv, (float)kM24);
+			float pu = __fadd_rn(__fadd_rn(s.uv[0], __fmul_rn(__fsub_rn(s.uv[2], s.uv[0]), fu)),
+			                     __fmul_rn(__fsub_rn(s.uv[4], s.uv[0]), fv));
+			float pv = __fadd_rn(__fadd_rn(s.uv[1], __fmul_rn(__fsub_rn(s.uv[3], s.uv[1]), fu)),
+			                     __fmul_rn(__fsub_rn(s.uv[5], s.uv[1]), fv));
+			V3 origin = add(add(v0, mul(s1, pu)), mul(s2, pv));
+			if (k < Q) {
+				float cosa = __fsqrt_rn(__fsub_rn(1.f, sm.fd[k]));
+				V3 dir = add(add(mul(nrm, cosa), mul(tg, sm.fx[k])), mul(bt, sm.fy[k]));
+				sm.hemi[k] = trace_path(g, origin, dir, s.tri, sid, overflow);
+			}
+			if (fires && round < (uint32_t)kMaxRounds) {
+				for (int li = 0; li < 2; li++) {
+					sm.lit[round][li] = 0;
+					V3 d = li == 0 ? neg(g.dir_direction) : sub(g.point_position, origin);
+					float dsize = len(d);
+					d = divf(d, dsize);
+					if (li == 0) dsize = __fmul_rn(dsize, g.locality);
+					float ni = dot(d, nrm);
+					if (ni <= 0.f || !isfinite(ni)) continue;
+					if (occluded(g, origin, d, g.tmin, dsize, s.tri, overflow)) continue;
+					V3 irr = li == 0 ? g.dir_color : point_irr(g, origin);
+					sm.light[round][li] = mul(irr, ni);
+					sm.lit[round][li] = 1;
+				}
+			}
+		}
+		__syncwarp();
+		if (lane == 0) {
+			V3 hemi = mk(0.f, 0.f, 0.f), lights = mk(0.f, 0.f, 0.f);
+			for (uint32_t k = 0; k < Q; k++) hemi = add(hemi, sm.hemi[k]);
+			uint32_t shot = rounds < (uint32_t)kMaxRounds ? rounds : (uint32_t)kMaxRounds;
+			for (uint32_t r = 0; r < shot; r++)
+				for (int li = 0; li < 2; li++)
+					if (sm.lit[r][li]) lights = add(lights, sm.light[r][li]);
+			lights = divf(lights, (float)shot);
+			hemi = mul(hemi, __fdiv_rn(1.f, (float)Q));
+			V3 res = add(lights, hemi);
+			out[ti] = make_float4(res.x, res.y, res.z, 1.f);
+		}
+		__syncwarp();
+	}
+	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// ------------------------------------------------------------ lightmapper
+struct Lightmapper {
+	Collider* c = nullptr;
+	uint32_t natlas = 0, size = 0;
+	uint64_t ntexels = 0, nsub = 0;
+	float* d_albedo = nullptr;
+	uint32_t* d_off = nullptr;    // ntexels + 1
+	Sub* d_sub = nullptr;
+	uint64_t* d_counter = nullptr;
+	uint32_t* d_status = nullptr;
+	float* d_stage = nullptr;
+	size_t stage_bytes = 0;
+	float tmin_default = 0.f;
+};
+
+static void free_lm(Lightmapper* L) {
+	if (!L) return;
+	cudaFree(L->d_albedo);
+	cudaFree(L->d_off);
+	cudaFree(L->d_sub);
+	cudaFree(L->d_counter);
+	cudaFree(L->d_status);
+	cudaFree(L->d_stage);
+	delete L;
+}
+
+}  // namespace rrg
+
+using namespace rrg;
+
+extern "C" {
+
+int rrg_lightmapper_create(rrg_collider* ch, const float* albedo, const int32_t* tri_atlas, const float* uv,
+                           uint32_t natlas, uint32_t size, rrg_lightmapper** out) {
+	if (!out) return RRG_ERR_INVALID;
+	*out = nullptr;
+	Collider* c = reinterpret_cast<Collider*>(ch);
+	if (!c || !albedo || !tri_atlas || !uv || !natlas || !size || size > 16384) return RRG_ERR_INVALID;
+	const uint64_t ntexels = (uint64_t)natlas * size * size;
+	if (ntexels >= (1ull << 32)) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(c->device));
+	Lightmapper* L = new Lightmapper();
+	L->c = c;
+	L->natlas = natlas;
+	L->size = size;
+	L->ntexels = ntexels;
+	const uint32_t nt = c->nt;
+	float *d_uv = nullptr;
+	int32_t* d_atlas = nullptr;
+	uint32_t *d_counts = nullptr, *d_cursor = nullptr, *d_bsum = nullptr, *d_err = nullptr, *d_fan = nullptr;
+	auto fail = [&](cudaError_t e) {
+		cudaFree(d_uv); cudaFree(d_atlas); cudaFree(d_counts); cudaFree(d_cursor); cudaFree(d_bsum);
+		cudaFree(d_err); cudaFree(d_fan);
+		free_lm(L);
+		return cuda_fail(e);
+	};
+	cudaError_t e;
+	if ((e = cudaMalloc(&L->d_albedo, sizeof(float) * 3 * (size_t)nt)) != cudaSuccess) return fail(e);
+	if ((e = cudaMemcpy(L->d_albedo, albedo, sizeof(float) * 3 * (size_t)nt, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+	if ((e = cudaMalloc(&d_uv, sizeof(float) * 6 * (size_t)nt)) != cudaSuccess) return fail(e);
+	if ((e = cudaMemcpy(d_uv, uv, sizeof(float) * 6 * (size_t)nt, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+	if ((e = cudaMalloc(&d_atlas, sizeof(int32_t) * (size_t)nt)) != cudaSuccess) return fail(e);
+	if ((e = cudaMemcpy(d_atlas, tri_atlas, sizeof(int32_t) * (size_t)nt, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+	if ((e = cudaMalloc(&d_counts, sizeof(uint32_t) * ntexels)) != cudaSuccess) return fail(e);
+	if ((e = cudaMemset(d_counts, 0, sizeof(uint32_t) * ntexels)) != cudaSuccess) return fail(e);
+	if ((e = cudaMalloc(&d_err, 4)) != cudaSuccess) return fail(e);
+	if ((e = cudaMemset(d_err, 0, 4)) != cudaSuccess) return fail(e);
+	const int grid = c->num_sms * 16;
+	k_enumerate<true><<<grid, 256>>>(d_uv, d_atlas, nt, size, natlas, d_counts, nullptr, nullptr, nullptr, nullptr, 0, d_err);
+	if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+	const uint32_t nb = (uint32_t)((ntexels + kScanPer - 1) / kScanPer);
+	if ((e = cudaMalloc(&d_bsum, sizeof(uint32_t) * (nb + 1))) != cudaSuccess) return fail(e);
+	if ((e = cudaMalloc(&L->d_off, sizeof(uint32_t) * (ntexels + 1))) != cudaSuccess) return fail(e);
+	k_scan_sums<<<nb, kScanBT>>>(d_counts, ntexels, d_bsum);
+	k_scan_top<<<1, 32>>>(d_bsum, nb);
+	k_scan_apply<<<nb, kScanBT>>>(d_counts, ntexels, d_bsum, L->d_off);
+	if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+	uint32_t total = 0;
+	if ((e = cudaMemcpy(&total, L->d_off + ntexels, 4, cudaMemcpyDeviceToHost)) != cudaSuccess) return fail(e);
+	L->nsub = total;
+	if ((e = cudaMalloc(&L->d_sub, sizeof(Sub) * (total ? total : 1))) != cudaSuccess) return fail(e);
+	if ((e = cudaMalloc(&d_fan, sizeof(uint32_t) * (total ? total : 1))) != cudaSuccess) return fail(e);
+	if ((e = cudaMalloc(&d_cursor, sizeof(uint32_t) * ntexels)) != cudaSuccess) return fail(e);
+	if ((e = cudaMemset(d_cursor, 0, sizeof(uint32_t) * ntexels)) != cudaSuccess) return fail(e);
+	k_enumerate<false><<<grid, 256>>>(d_uv, d_atlas, nt, size, natlas, nullptr, L->d_off, d_cursor, L->d_sub, d_fan, total, d_err);
+	k_sort_texels<<<grid, 256>>>(L->d_off, ntexels, L->d_sub, d_fan);
+	if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+	uint32_t herr = 0;
+	if ((e = cudaMemcpy(&herr, d_err, 4, cudaMemcpyDeviceToHost)) != cudaSuccess) return fail(e);
+	cudaFree(d_uv); cudaFree(d_atlas); cudaFree(d_counts); cudaFree(d_cursor); cudaFree(d_bsum); cudaFree(d_err);
+	cudaFree(d_fan);
+	d_uv = nullptr; d_atlas = nullptr; d_counts = d_cursor = d_bsum = d_err = d_fan = nullptr;
+	if (herr) { free_lm(L); return RRG_ERR_INVALID; }
+	if ((e = cudaMalloc(&L->d_counter, 8)) != cudaSuccess) return fail(e);
+	if ((e = cudaMalloc(&L->d_status, 4)) != cudaSuccess) return fail(e);
+	if ((e = cudaMemset(L->d_status, 0, 4)) != cudaSuccess) return fail(e);
+	// minimalSafeDistance = (aabb max - min).avg() * 1e-6 (RRSolver.cpp:329-334)
+	float ex = c->aabb_hi[0] - c->aabb_lo[0], ey = c->aabb_hi[1] - c->aabb_lo[1], ez = c->aabb_hi[2] - c->aabb_lo[2];
+	L->tmin_default = ((ex + ey) + ez) * 0.33333333333333f * 1e-6f;
+	*out = reinterpret_cast<rrg_lightmapper*>(L);
+	return RRG_OK;
+}
+
+void rrg_lightmapper_destroy(rrg_lightmapper* h) {
+	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
+	if (!L) return;
+	cudaSetDevice(L->c->device);
+	cudaDeviceSynchronize();
+	free_lm(L);
+}
+
+uint64_t rrg_lightmapper_subtexels(const rrg_lightmapper* h) {
+	const Lightmapper* L = reinterpret_cast<const Lightmapper*>(h);
+	return L ? L->nsub : 0;
+}
+
+float rrg_lightmapper_ray_length_min(const rrg_lightmapper* h) {
+	const Lightmapper* L = reinterpret_cast<const Lightmapper*>(h);
+	return L ? L->tmin_default : 0.f;
+}
+
+int rrg_lightmapper_copy_subtexels(const rrg_lightmapper* h, uint32_t* offsets_host, void* subtexels_host) {
+	const Lightmapper* L = reinterpret_cast<const Lightmapper*>(h);
+	if (!L || !offsets_host) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaMemcpy(offsets_host, L->d_off, sizeof(uint32_t) * (L->ntexels + 1), cudaMemcpyDeviceToHost));
+	if (subtexels_host && L->nsub)
+		RRG_CUDA(cudaMemcpy(subtexels_host, L->d_sub, sizeof(Sub) * L->nsub, cudaMemcpyDeviceToHost));
+	return RRG_OK;
+}
+
+static int gather_launch(Lightmapper* L, const rrg_gather_params* p, uint64_t first, uint64_t count, float* out_dev,
+                         cudaStream_t s) {
+	if (!p || p->size < sizeof(rrg_gather_params)) return RRG_ERR_INVALID;
+	if (p->quality == 0 || p->quality > (uint32_t)kMaxQuality) return RRG_ERR_INVALID;
+	if (first + count > L->ntexels) return RRG_ERR_INVALID;
+	if (!count) return RRG_OK;
+	Collider* c = L->c;
+	GatherScene g;
+	g.nodes = c->d_nodes;
+	g.tris = c->d_tris;
+	g.nnodes = (int)c->nnodes;
+	g.ntris = (int)c->nvalid;
+	g.xyz = c->d_xyz;
+	g.idx = c->d_idx;
+	g.albedo = L->d_albedo;
+	g.dir_direction = mk(p->dir_direction[0], p->dir_direction[1], p->dir_direction[2]);
+	g.dir_color = mk(p->dir_color[0], p->dir_color[1], p->dir_color[2]);
+	g.point_position = mk(p->point_position[0], p->point_position[1], p->point_position[2]);
+	g.point_color = mk(p->point_color[0], p->point_color[1], p->point_color[2]);
+	g.tmin = p->ray_length_min > 0.f ? p->ray_length_min : L->tmin_default;
+	g.locality = p->locality > 0.f ? p->locality : 100000.f;
+	g.quality = p->quality;
+	g.max_depth = p->max_depth;
+	g.seed = p->seed;
+	RRG_CUDA(cudaMemsetAsync(L->d_counter, 0, 8, s));
+	int per_sm = 0;
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather, kGatherWarps * 32, 0));
+	uint64_t want = (count + kGatherWarps - 1) / kGatherWarps;
+	uint64_t cap = (uint64_t)(per_sm > 0 ? per_sm : 1) * c->num_sms;
+	int grid = (int)(want < cap ? want : cap);
+	k_gather<<<grid, kGatherWarps * 32, 0, s>>>(g, L->d_off, L->d_sub, first, count, reinterpret_cast<float4*>(out_dev),
+	                                            reinterpret_cast<uint32_t*>(L->d_counter), L->d_status);
+	RRG_CUDA(cudaGetLastError());
+	return RRG_OK;
+}
+
+int rrg_lightmap_gather(rrg_lightmapper* h, const rrg_gather_params* p, uint64_t first_texel, uint64_t ntexels,
+                        float* out_dev, void* stream) {
+	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
+	if (!L || !out_dev || ((uintptr_t)out_dev & 15)) return RRG_ERR_INVALID;
+	return gather_launch(L, p, first_texel, ntexels, out_dev, (cudaStream_t)stream);
+}
+
+int rrg_lightmap_gather_host(rrg_lightmapper* h, const rrg_gather_params* p, uint64_t first_texel, uint64_t ntexels,
+                             float* out_host, void* stream) {
+	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
+	if (!L || !out_host) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(L->c->device));
+	size_t bytes = 16 * (size_t)ntexels;
+	if (bytes > L->stage_bytes) {
+		cudaFree(L->d_stage);
+		L->d_stage = nullptr;
+		L->stage_bytes = 0;
+		RRG_CUDA(cudaMalloc(&L->d_stage, bytes));
+		L->stage_bytes = bytes;
+	}
+	cudaStream_t s = (cudaStream_t)stream;
+	int st = gather_launch(L, p, first_texel, ntexels, L->d_stage, s);
+	if (st) return st;
+	RRG_CUDA(cudaMemcpyAsync(out_host, L->d_stage, bytes, cudaMemcpyDeviceToHost, s));
+	RRG_CUDA(cudaStreamSynchronize(s));
+	return RRG_OK;
+}
+
+int rrg_lightmapper_status(rrg_lightmapper* h, void* stream) {
+	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
+	if (!L) return RRG_ERR_INVALID;
+	uint32_t w = 0;
+	cudaStream_t s = (cudaStream_t)stream;
+	RRG_CUDA(cudaMemcpyAsync(&w, L->d_status, 4, cudaMemcpyDeviceToHost, s));
+	RRG_CUDA(cudaStreamSynchronize(s));
+	RRG_CUDA(cudaMemsetAsync(L->d_status, 0, 4, s));
+	return w ? RRG_ERR_STACK : RRG_OK;
+}
+
+}  // extern "C"

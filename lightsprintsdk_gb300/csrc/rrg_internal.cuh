@@ -53,6 +53,7 @@ struct Collider {
 	uint32_t* d_counter = nullptr;// scratch: [0] ray counter, [1] status word
 	size_t bytes = 0;
 	float build_ms = 0;
+	float aabb_lo[3] = {0, 0, 0}, aabb_hi[3] = {0, 0, 0};   // all vertices
 	rrg_build_params params{};
 	// host-call staging (rrg_intersect_host / rrg_intersect_rrray)
 	void* d_stage_in = nullptr;

@@ -1,0 +1,124 @@
+"""Python mirror of the lightmap final gather (include/rrgpu_gather.h).
+
+Mirrors RRSolver::updateLightmaps with UpdateParameters(quality) for the
+plain N-bounce estimator (RRSolver/lightmap.cpp:943-1163,
+RRSolver/gather.cpp:600-836): a lightmapper is bound to a collider and the
+scene's materials and unwrap; texel ranges of its atlases are gathered on the
+GPU.  No CPU fallback: every call goes to the CUDA library or raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import collider as col
+
+SUBTEXEL_DTYPE = np.dtype([("tri", "<u4"), ("uv", "<f4", (3, 2)), ("area", "<f4"), ("pad", "<u4")])
+
+
+class GatherParams(C.Structure):
+    _fields_ = [("size", C.c_uint32), ("quality", C.c_uint32), ("max_depth", C.c_uint32),
+                ("reserved0", C.c_uint32), ("seed", C.c_uint64), ("ray_length_min", C.c_float),
+                ("locality", C.c_float), ("dir_direction", C.c_float * 3), ("dir_color", C.c_float * 3),
+                ("point_position", C.c_float * 3), ("point_color", C.c_float * 3)]
+
+
+_bound = False
+
+
+def _lib():
+    global _bound
+    L = col._lib()
+    if not _bound:
+        P, U = C.c_void_p, C.c_uint32
+        L.rrg_lightmapper_create.argtypes = [P, P, P, P, U, U, C.POINTER(P)]
+        L.rrg_lightmapper_destroy.argtypes = [P]
+        L.rrg_lightmapper_destroy.restype = None
+        L.rrg_lightmapper_subtexels.argtypes = [P]
+        L.rrg_lightmapper_subtexels.restype = C.c_uint64
+        L.rrg_lightmapper_ray_length_min.argtypes = [P]
+        L.rrg_lightmapper_ray_length_min.restype = C.c_float
+        L.rrg_lightmapper_copy_subtexels.argtypes = [P, P, P]
+        L.rrg_lightmap_gather.argtypes = [P, C.POINTER(GatherParams), C.c_uint64, C.c_uint64, P, P]
+        L.rrg_lightmap_gather_host.argtypes = [P, C.POINTER(GatherParams), C.c_uint64, C.c_uint64, P, P]
+        L.rrg_lightmapper_status.argtypes = [P, P]
+        _bound = True
+    return L
+
+
+def make_params(lights: dict, quality: int = 64, max_depth: int = 8, seed: int = 0xC2, ray_length_min: float = 0.0,
+                locality: float = 100000.0) -> GatherParams:
+    return GatherParams(C.sizeof(GatherParams), quality, max_depth, 0, seed, ray_length_min, locality,
+                        (C.c_float * 3)(*lights["dir_direction"]), (C.c_float * 3)(*lights["dir_color"]),
+                        (C.c_float * 3)(*lights["point_position"]), (C.c_float * 3)(*lights["point_color"]))
+
+
+class RRLightmapper:
+    """Sub-texel enumeration and plain gather for the atlases of one scene."""
+
+    def __init__(self, collider: col.RRCollider, albedo, tri_atlas, uv, natlas: int, size: int):
+        self.c = collider
+        self.albedo = np.ascontiguousarray(albedo, np.float32)
+        self.tri_atlas = np.ascontiguousarray(tri_atlas, np.int32)
+        self.uv = np.ascontiguousarray(uv, np.float32)
+        self.natlas, self.size = natlas, size
+        h = C.c_void_p()
+        st = _lib().rrg_lightmapper_create(collider.handle, self.albedo.ctypes.data, self.tri_atlas.ctypes.data,
+                                           self.uv.ctypes.data, natlas, size, C.byref(h))
+        if st:
+            raise col.RRGError(st, "rrg_lightmapper_create")
+        self._h = h
+
+    @classmethod
+    def from_scene(cls, collider, gs) -> "RRLightmapper":
+        return cls(collider, gs.albedo, gs.tri_atlas, gs.uv, gs.natlas, gs.size)
+
+    def __del__(self):
+        self.close()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib().rrg_lightmapper_destroy(self._h)
+            self._h = None
+
+    @property
+    def ntexels(self) -> int:
+        return self.natlas * self.size * self.size
+
+    @property
+    def nsubtexels(self) -> int:
+        return int(_lib().rrg_lightmapper_subtexels(self._h))
+
+    @property
+    def ray_length_min(self) -> float:
+        return float(_lib().rrg_lightmapper_ray_length_min(self._h))
+
+    def subtexels(self):
+        off = np.zeros(self.ntexels + 1, np.uint32)
+        st = np.zeros(self.nsubtexels, SUBTEXEL_DTYPE)
+        r = _lib().rrg_lightmapper_copy_subtexels(self._h, off.ctypes.data, st.ctypes.data if len(st) else None)
+        if r:
+            raise col.RRGError(r, "rrg_lightmapper_copy_subtexels")
+        return off, st
+
+    def gather(self, params: GatherParams, first: int = 0, count: int | None = None) -> np.ndarray:
+        """Texels [first, first+count) -> (count, 4) float32 host array."""
+        if count is None:
+            count = self.ntexels - first
+        out = np.zeros((count, 4), np.float32)
+        r = _lib().rrg_lightmap_gather_host(self._h, C.byref(params), first, count, out.ctypes.data, None)
+        if r:
+            raise col.RRGError(r, "rrg_lightmap_gather_host")
+        self.check()
+        return out
+
+    def gather_device(self, params: GatherParams, first: int, count: int, out_ptr: int, stream: int = 0) -> None:
+        r = _lib().rrg_lightmap_gather(self._h, C.byref(params), first, count, out_ptr, stream or None)
+        if r:
+            raise col.RRGError(r, "rrg_lightmap_gather")
+
+    def check(self, stream: int = 0) -> None:
+        r = _lib().rrg_lightmapper_status(self._h, stream or None)
+        if r:
+            raise col.RRGError(r, "gather")

@@ -11,8 +11,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liborc.so")
-SRC = [os.path.join(HERE, "rr_oracle.c")]
-HDR = os.path.join(HERE, "rr_oracle.h")
+SRC = [os.path.join(HERE, "rr_oracle.c"), os.path.join(HERE, "rr_gather.c")]
+HDRS = [os.path.join(HERE, "rr_oracle.h"), os.path.join(HERE, "rr_gather.h")]
 
 _lib = None
 
@@ -20,7 +20,7 @@ _lib = None
 def build(force: bool = False) -> str:
     """gcc -O2 -ffp-contract=off -fopenmp: one rounding per float operation, as
     in the reference's own x86-64 build, and the same results on aarch64."""
-    newest = max(os.path.getmtime(p) for p in SRC + [HDR])
+    newest = max(os.path.getmtime(p) for p in SRC + HDRS)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         tmp = LIB + ".tmp"
         subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-shared", "-fPIC",
@@ -50,6 +50,11 @@ def lib():
         L.orc_delta_bsp.argtypes = [P, U]
         L.orc_delta_bsp.restype = C.c_float
         L.orc_max_threads.restype = C.c_int
+        L.orc_enumerate.argtypes = [P, P, U, U, P, P, P]
+        L.orc_enumerate.restype = C.c_uint64
+        L.orc_gather.argtypes = [P, C.POINTER(GatherScene), P, U, P, P, C.c_int, C.c_int, P]
+        L.orc_hash.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
+        L.orc_hash.restype = C.c_uint64
         _lib = L
     return _lib
 
@@ -118,3 +123,69 @@ class FastestOracle:
         dist = np.zeros(n, np.float64)
         lib().orc_collide_exact64(self.h, _ptr(rays), n, threads, _ptr(tri), _ptr(dist))
         return tri, dist
+
+
+# ------------------------------------------------------------------ gather
+SUBTEXEL_DTYPE = np.dtype([("tri", "<u4"), ("uv", "<f4", (3, 2)), ("area", "<f4"), ("pad", "<u4")])
+
+
+class GatherScene(C.Structure):
+    _fields_ = [("xyz", C.c_void_p), ("idx", C.c_void_p), ("nt", C.c_uint32), ("albedo", C.c_void_p),
+                ("dir_direction", C.c_float * 3), ("dir_color", C.c_float * 3), ("point_position", C.c_float * 3),
+                ("point_color", C.c_float * 3), ("ray_length_min", C.c_float), ("locality", C.c_float),
+                ("quality", C.c_uint32), ("max_depth", C.c_uint32), ("seed", C.c_uint64)]
+
+
+def hash_u64(seed: int, stream: int, index: int) -> int:
+    return int(lib().orc_hash(seed, stream, index))
+
+
+def enumerate_atlas(uv_map: np.ndarray, tri_ids: np.ndarray, size: int):
+    """Sub-texels of one atlas (lightmap.cpp:145-330 restated).  uv_map: (n,3,2)
+    map-space corners of the atlas' triangles, tri_ids their world indices in
+    visiting order.  Returns (offsets (size*size+1,) uint64, subtexels)."""
+    uv_map = np.ascontiguousarray(uv_map, np.float32)
+    tri_ids = np.ascontiguousarray(tri_ids, np.uint32)
+    n = tri_ids.shape[0]
+    counts = np.zeros(size * size, np.uint32)
+    L = lib()
+    total = L.orc_enumerate(_ptr(uv_map), _ptr(tri_ids), n, size, _ptr(counts), None, None)
+    off = np.zeros(size * size + 1, np.uint64)
+    np.cumsum(counts, out=off[1:])
+    st = np.zeros(int(total), SUBTEXEL_DTYPE)
+    L.orc_enumerate(_ptr(uv_map), _ptr(tri_ids), n, size, _ptr(counts), _ptr(off), _ptr(st) if total else None)
+    return off, st
+
+
+def min_safe_distance(v: np.ndarray) -> float:
+    """RRSolver::setStaticObjects: (aabb max - min).avg() * 1e-6 (RRSolver.cpp:329-334)."""
+    v = np.asarray(v, np.float32)
+    ext = (v.max(0) - v.min(0)).astype(np.float32)
+    return float(np.float32((ext[0] + ext[1] + ext[2]) * np.float32(0.33333333333333)) * np.float32(1e-6))
+
+
+class GatherOracle:
+    """Plain N-bounce lightmap gather on the CPU (rr_gather.c)."""
+
+    def __init__(self, gs, quality: int = 64, max_depth: int = 8, seed: int = 0xC2, locality: float = 100000.0,
+                 bvh: "FastestOracle | None" = None):
+        sc = gs.scene
+        self.fo = bvh or FastestOracle(sc.vertices, sc.indices)
+        self.albedo = np.ascontiguousarray(gs.albedo, np.float32)
+        L = gs.lights
+        self.s = GatherScene(self.fo.v.ctypes.data, self.fo.t.ctypes.data, self.fo.t.shape[0], self.albedo.ctypes.data,
+                             (C.c_float * 3)(*L["dir_direction"]), (C.c_float * 3)(*L["dir_color"]),
+                             (C.c_float * 3)(*L["point_position"]), (C.c_float * 3)(*L["point_color"]),
+                             min_safe_distance(sc.vertices), locality, quality, max_depth, seed)
+
+    def gather(self, texel_ids: np.ndarray, off: np.ndarray, st: np.ndarray, threads: int = 0,
+               fp64: bool = False) -> np.ndarray:
+        """texel_ids (n,) global ids; off (n+1,) offsets into st for these
+        texels.  Returns (n,4) float32."""
+        texel_ids = np.ascontiguousarray(texel_ids, np.uint64)
+        off = np.ascontiguousarray(off, np.uint64)
+        st = np.ascontiguousarray(st)
+        out = np.zeros((texel_ids.shape[0], 4), np.float32)
+        lib().orc_gather(self.fo.h, C.byref(self.s), _ptr(texel_ids), texel_ids.shape[0], _ptr(off),
+                         _ptr(st) if len(st) else None, threads, int(fp64), _ptr(out))
+        return out

@@ -1,0 +1,89 @@
+/* ORACLE: CPU restatement of the reference's lightmap final gather, for the
+ * plain N-bounce estimator.  Test infrastructure only: the parity tests and
+ * the CPU-baseline leg of the benchmark call it as the checker.
+ *
+ * Restated (file:line in the reference project):
+ *   orc_enumerate      enumerateTexelsPartial: texel x triangle clipping in
+ *                      triangle space, fan triangulation into sub-texels
+ *                      (RRSolver/lightmap.cpp:145-330), getArea (:32-40)
+ *   orc_gather         processTexel (RRSolver/gather.cpp:600-836) with
+ *                      GatheredIrradianceHemisphere (:164-343) and
+ *                      GatheredIrradianceLights (:356-586), HomogenousFiller2
+ *                      (:57-111), getRandomEnterDirNormalized (:121-135);
+ *                      PathtracerWorker::getIncidentRadiance
+ *                      (RRStaticSolver/pathtracer.cpp:139-394) with
+ *                      useSolver*SinceDepth = UINT_MAX (no radiosity
+ *                      shortcuts), next-event shadow rays to every light and
+ *                      Russian roulette on the diffuse reflectance;
+ *                      RRMaterial::getResponse diffuse (RRMaterial.cpp:666-675),
+ *                      RRLight::getIrradiance (RRLight.cpp:345-362),
+ *                      buildBasisFromNormal (RRMesh.cpp:70-75).
+ *
+ * Deliberate differences from the reference, shared with the GPU kernel so
+ * both run the same sample streams:
+ *   - libc rand() is replaced by a counter-based hash of (seed, stream,
+ *     index): the sub-texel point (rand() pair), the filler seed
+ *     (rand()&0xffff), the roulette draw (RR_RAND01);
+ *   - the bounce direction is cosine-weighted by Malley's method (a disk
+ *     point by rejection lifted to the hemisphere) instead of the polar
+ *     sin/cos form of sampleHemisphereDiffuse; the distribution is the same,
+ *     and no transcendental function is needed, so CPU and GPU agree bitwise;
+ *   - one shooting series per texel (every ray here is reliable);
+ *   - the path radiance is accumulated iteratively (L += T * contribution)
+ *     rather than by recursion.
+ * With fp64 = 1 the same paths are accumulated in double precision: the
+ * FP64-accumulated reference that states the float accumulation error.
+ */
+#ifndef RR_GATHER_H
+#define RR_GATHER_H
+#include <stdint.h>
+#include "rr_oracle.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_subtexel {
+	uint32_t tri;       /* world triangle index */
+	float uv[3][2];     /* corners in triangle space (barycentric u, v) */
+	float area;         /* area in map space */
+	uint32_t pad;
+} orc_subtexel;
+
+typedef struct orc_gather_scene {
+	const float* xyz;       /* world vertices */
+	const uint32_t* idx;    /* triangles */
+	uint32_t nt;
+	const float* albedo;    /* nt * 3 */
+	float dir_direction[3]; /* directional light: direction the light travels */
+	float dir_color[3];
+	float point_position[3];
+	float point_color[3];
+	float ray_length_min;   /* minimalSafeDistance */
+	float locality;         /* UpdateParameters::locality */
+	uint32_t quality;       /* hemisphere rays per texel */
+	uint32_t max_depth;     /* PathTracingParameters::stopAtDepth */
+	uint64_t seed;
+} orc_gather_scene;
+
+/* Sub-texels of one atlas.  uv: n triangles x 3 corners x 2 in map space
+ * [0,1]; tri: their world indices, in the order the reference visits them.
+ * counts[size*size] receives sub-texels per texel; when out != NULL the
+ * sub-texels are written texel by texel (offsets = exclusive scan of
+ * counts, computed by the caller).  Returns the total. */
+uint64_t orc_enumerate(const float* uv, const uint32_t* tri, uint32_t n, uint32_t size, uint32_t* counts,
+                       const uint64_t* offsets, orc_subtexel* out);
+
+/* Gathers `ntexels` texels: texel i has global id texel_id[i] (seeds its
+ * sample streams) and sub-texels st[off[i] .. off[i+1]).  out: 4 floats per
+ * texel (irradiance RGB, 1 if covered else 0). */
+void orc_gather(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,
+                const uint64_t* off, const orc_subtexel* st, int threads, int fp64, float* out);
+
+/* Counter-based generator shared with the GPU (and with the Python
+ * generators): MurmurHash3 fmix64 of (seed, stream, index). */
+uint64_t orc_hash(uint64_t seed, uint64_t stream, uint64_t index);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,131 @@
+"""Parity of the GPU lightmap gather (through the C ABI) with the C oracle
+(oracle/rr_gather.c) on identical sample streams.
+
+Tolerance (the benchmark spec): plain-gather texels agree within 1e-4 relative.  The
+sub-texel enumeration is compared exactly.  Each texel's error against the
+FP64-accumulated oracle is stated."""
+import numpy as np
+import pytest
+
+from lightsprintsdk_gb300 import collider as col
+from lightsprintsdk_gb300 import lightmap as lm
+from lightsprintsdk_gb300 import scenes
+from oracle import orc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup():
+    gs = scenes.gather_c2()
+    c = col.RRCollider.create(gs.scene.vertices, gs.scene.indices)
+    L = lm.RRLightmapper.from_scene(c, gs)
+    G = orc.GatherOracle(gs)
+    return gs, c, L, G
+
+
+def oracle_lists(gs, atlas):
+    ids = np.nonzero(gs.tri_atlas == atlas)[0]
+    return orc.enumerate_atlas(gs.uv[ids], ids, gs.size)
+
+
+@pytest.mark.parametrize("atlas", [0, 1, 9, 80, 255])
+def test_enumeration_matches_oracle(setup, atlas):
+    gs, c, L, G = setup
+    off, st = L.subtexels()
+    S = gs.size * gs.size
+    o_off, o_st = oracle_lists(gs, atlas)
+    g_off = off[atlas * S:(atlas + 1) * S + 1].astype(np.int64) - int(off[atlas * S])
+    np.testing.assert_array_equal(g_off, o_off.astype(np.int64))
+    g = st[off[atlas * S]:off[(atlas + 1) * S]]
+    np.testing.assert_array_equal(g["tri"], o_st["tri"])
+    np.testing.assert_array_equal(g["uv"], o_st["uv"])
+    np.testing.assert_array_equal(g["area"], o_st["area"])
+
+
+def test_ray_length_min_is_minimal_safe_distance(setup):
+    gs, c, L, G = setup
+    assert L.ray_length_min == np.float32(orc.min_safe_distance(gs.scene.vertices))
+
+
+def pick_texels(L, atlases, per_atlas, seed=3):
+    off, st = L.subtexels()
+    S = L.size * L.size
+    rng = np.random.default_rng(seed)
+    tids = []
+    for a in atlases:
+        cov = np.nonzero(np.diff(off[a * S:(a + 1) * S + 1]) > 0)[0]
+        tids.append(a * S + rng.choice(cov, size=min(per_atlas, len(cov)), replace=False))
+    return np.sort(np.concatenate(tids)), off, st
+
+
+def oracle_gather(G, tids, off, st, fp64=False):
+    cnt = (off[tids + 1] - off[tids]).astype(np.uint64)
+    o2 = np.concatenate([[0], np.cumsum(cnt)]).astype(np.uint64)
+    sts = np.concatenate([st[off[t]:off[t + 1]] for t in tids]).view(orc.SUBTEXEL_DTYPE)
+    return G.gather(tids.astype(np.uint64), o2, sts, 0, fp64=fp64)
+
+
+def gpu_gather(L, params, tids):
+    """Gathers each requested texel (contiguous runs in one call each)."""
+    out = np.zeros((len(tids), 4), np.float32)
+    i = 0
+    while i < len(tids):
+        j = i
+        while j + 1 < len(tids) and tids[j + 1] == tids[j] + 1:
+            j += 1
+        out[i:j + 1] = L.gather(params, int(tids[i]), j - i + 1)
+        i = j + 1
+    return out
+
+
+def test_gather_matches_oracle(setup):
+    gs, c, L, G = setup
+    params = lm.make_params(gs.lights)
+    tids, off, st = pick_texels(L, [0, 1, 2, 9, 40, 75, 200], 48)
+    got = gpu_gather(L, params, tids)
+    ref = oracle_gather(G, tids, off, st)
+    ref64 = oracle_gather(G, tids, off, st, fp64=True)
+    assert np.all(got[:, 3] == 1) and np.all(ref[:, 3] == 1)
+    rel = np.abs(got[:, :3] - ref[:, :3]) / np.maximum(np.abs(ref[:, :3]), 1e-6)
+    exact = np.all(got == ref, axis=1).mean()
+    assert rel.max() <= 1e-4, (rel.max(), exact)
+    assert exact >= 0.95
+    err64 = np.abs(got[:, :3] - ref64[:, :3]) / np.maximum(np.abs(ref64[:, :3]), 1e-6)
+    assert err64.max() <= 1e-4
+
+
+def test_gather_deterministic_and_range_independent(setup):
+    gs, c, L, G = setup
+    params = lm.make_params(gs.lights)
+    S = gs.size * gs.size
+    a = L.gather(params, 9 * S, 4096)
+    b = L.gather(params, 9 * S, 4096)
+    np.testing.assert_array_equal(a, b)
+    c2 = L.gather(params, 9 * S + 1000, 100)
+    np.testing.assert_array_equal(c2, a[1000:1100])
+
+
+def test_uncovered_texels_are_zero(setup):
+    gs, c, L, G = setup
+    off, st = L.subtexels()
+    params = lm.make_params(gs.lights)
+    S = gs.size * gs.size
+    a = 255
+    cnt = np.diff(off[a * S:(a + 1) * S + 1])
+    out = L.gather(params, a * S, S)
+    assert np.all(out[cnt == 0] == 0)
+    assert np.all(out[cnt > 0, 3] == 1)
+    assert np.all(out[cnt > 0, :3] >= 0)
+
+
+def test_skylight_patch_is_brighter(setup):
+    """Physical sanity: floor texels lit by the sun through the skylight
+    receive more irradiance than shadowed floor texels."""
+    gs, c, L, G = setup
+    params = lm.make_params(gs.lights, quality=16)
+    S = gs.size * gs.size
+    out = L.gather(params, 0, S)       # atlas 0 = floor slab
+    lum = out[:, :3].mean(1)
+    cov = out[:, 3] > 0
+    assert lum[cov].max() > 4 * np.median(lum[cov])

@@ -1,0 +1,51 @@
+"""CPU checks of the gather oracle (oracle/rr_gather.c): the sample-stream
+hash matches the Python generators, the enumeration conserves area, and the
+float gather agrees with its FP64-accumulated twin."""
+import numpy as np
+
+from lightsprintsdk_gb300 import scenes
+from oracle import orc
+
+
+def test_hash_matches_python_generators():
+    for seed, stream, idx in [(0, 0, 0), (1, 2, 3), (0xC2, 61, 123456789), (2**40 + 5, 65, 2**50 + 7)]:
+        assert orc.hash_u64(seed, stream, idx) == int(scenes.hash_u64(seed, stream, idx))
+
+
+def test_enumeration_conserves_area():
+    """Sub-texel areas sum to half the triangles' map areas (the reference
+    measures sub-texels in triangle space, where a triangle has area 1/2,
+    and scales by the map-space area: lightmap.cpp:313-318)."""
+    gs = scenes.gather_c2()
+    for a in (9, 100):
+        ids = np.nonzero(gs.tri_atlas == a)[0]
+        off, st = orc.enumerate_atlas(gs.uv[ids], ids, gs.size)
+        uv = gs.uv[ids].astype(np.float64)
+        area = 0.5 * np.abs((uv[:, 1, 0] - uv[:, 0, 0]) * (uv[:, 2, 1] - uv[:, 0, 1])
+                            - (uv[:, 2, 0] - uv[:, 0, 0]) * (uv[:, 1, 1] - uv[:, 0, 1]))
+        assert abs(st["area"].astype(np.float64).sum() - 0.5 * area.sum()) < 1e-3 * area.sum()
+        assert np.all(np.diff(off.astype(np.int64)) >= 0)
+        # each texel's list is in triangle order
+        for t in np.nonzero(np.diff(off) > 1)[0][:200]:
+            tri = st["tri"][off[t]:off[t + 1]]
+            assert np.all(np.diff(tri.astype(np.int64)) >= 0)
+
+
+def test_gather_fp32_vs_fp64_accumulation():
+    gs = scenes.gather_c2()
+    G = orc.GatherOracle(gs, quality=16)
+    a = 9
+    ids = np.nonzero(gs.tri_atlas == a)[0]
+    off, st = orc.enumerate_atlas(gs.uv[ids], ids, gs.size)
+    sel = np.nonzero(np.diff(off) > 0)[0][::97][:64]
+    tid = (a * gs.size * gs.size + sel).astype(np.uint64)
+    cnt = (off[sel + 1] - off[sel]).astype(np.uint64)
+    o2 = np.concatenate([[0], np.cumsum(cnt)]).astype(np.uint64)
+    sts = np.concatenate([st[off[i]:off[i + 1]] for i in sel])
+    f32 = G.gather(tid, o2, sts, 0)
+    f64 = G.gather(tid, o2, sts, 0, fp64=True)
+    rel = np.abs(f32[:, :3] - f64[:, :3]) / np.maximum(np.abs(f64[:, :3]), 1e-9)
+    assert rel.max() < 1e-5
+    assert np.all(f32[:, :3] > 0)
+    again = G.gather(tid, o2, sts, 0)
+    np.testing.assert_array_equal(f32, again)
