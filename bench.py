@@ -196,13 +196,114 @@ def run_reference(args, rank: int):
     print(json.dumps(line), flush=True)
 
 
+def gather_cpu_baseline(gs, L, nsample: int = 4096):
+    """The gather oracle on all host cores over a bounded texel sample (every
+    k-th covered texel of atlas 0..255)."""
+    from oracle import orc
+    off, st = L.subtexels()
+    cov = np.nonzero(np.diff(off) > 0)[0]
+    step = max(1, len(cov) // nsample)
+    tids = cov[::step][:nsample].astype(np.uint64)
+    cnt = (off[tids + 1] - off[tids]).astype(np.uint64)
+    o2 = np.concatenate([[0], np.cumsum(cnt)]).astype(np.uint64)
+    sts = np.concatenate([st[off[t]:off[t + 1]] for t in tids]).view(orc.SUBTEXEL_DTYPE)
+    G = orc.GatherOracle(gs)
+    threads = os.cpu_count() or 1
+    G.gather(tids[:64], o2[:65], sts[:int(o2[64])], threads)
+    t0 = time.perf_counter()
+    G.gather(tids, o2, sts, threads)
+    sec = time.perf_counter() - t0
+    return {"value": len(tids) / sec, "unit": "texels/s", "cores": threads, "kind": "port",
+            "sample": f"{len(tids)} covered texels (every {step}th), quality 64, 8 bounces"}
+
+
+def run_gather(args, world, rank, local):
+    """Config 2: plain 8-bounce lightmap gather, 64 rays per texel, 256 atlases
+    of 256 x 256 texels on the interior scene."""
+    import torch
+    from lightsprintsdk_gb300 import collider as col
+    from lightsprintsdk_gb300 import lightmap as lm
+    from lightsprintsdk_gb300 import scenes
+    gs = scenes.gather_c2()
+    c = col.RRCollider.create(gs.scene.vertices, gs.scene.indices, device=local)
+    t0 = time.perf_counter()
+    L = lm.RRLightmapper.from_scene(c, gs)
+    enum_s = time.perf_counter() - t0
+    params = lm.make_params(gs.lights, quality=64, max_depth=8)
+    S = gs.size * gs.size
+    natl = args.atlases or gs.natlas
+    n = natl * S
+    out = torch.empty((n, 4), dtype=torch.float32, device=f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    learned = args.workload == "c4"
+    extra = {}
+    if learned:
+        from lightsprintsdk_gb300 import cache as rc
+
+        def step():
+            cache = rc.RadianceCache.for_scene(gs.scene.vertices, seed=7)
+            extra.update(rc.bake_learned(L, cache, params, 0, n, out.data_ptr(), stream=sp))
+    else:
+        def step():
+            L.gather_device(params, 0, n, out.data_ptr(), sp)
+    for _ in range(max(1, args.warmup // 3)):
+        if learned:
+            step()
+        else:
+            L.gather_device(params, 0, min(n, 4 * S), out.data_ptr(), sp)
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 3))
+    clk = ClockSampler(local).__enter__()
+    clk.wait_first_sample()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    clk.mark_start()
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk.mark_end()
+    clk.__exit__()
+    L.check(sp)
+    ms = e0.elapsed_time(e1) / steps
+    covered = int((out[:, 3] > 0).sum().item())
+    if learned:
+        # error against the plain 64-sample gather on atlases 0, 9, 100 (same first-bounce streams)
+        errs = {}
+        for a in (0, 9, 100):
+            if a >= natl:
+                continue
+            pl = L.gather(params, a * S, S)
+            le = out[a * S:(a + 1) * S].cpu().numpy()
+            m = pl[:, 3] > 0
+            d = (le[m, :3] - pl[m, :3]).astype(np.float64)
+            errs[str(a)] = float(np.sqrt((d ** 2).sum() / (pl[m, :3].astype(np.float64) ** 2).sum()))
+        extra["rel_rmse_vs_plain64"] = errs
+    if rank == 0:
+        metric = "learned lightmap texels/s" if learned else "plain lightmap texels/s"
+        line = {"metric": metric, "value": world * n / (ms * 1e-3), "unit": "texels/s",
+                "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": ms,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded generators)",
+                "config": {"workload": f"plain gather, quality 64, 8 bounces, {natl} atlases of 256x256 on the "
+                                       f"{gs.scene.ntri}-triangle interior", "texels": n, "covered": covered,
+                           "subtexels": L.nsubtexels, "enumeration_s": enum_s, **extra},
+                "gpu_launches": steps, "clocks": clk.summary()}
+        if not args.no_cpu_baseline and not learned:
+            line["cpu_baseline"] = gather_cpu_baseline(gs, L)
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c1", choices=["c1", "c0"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c2", "c4"])
+    ap.add_argument("--atlases", type=int, default=0, help="c2: gather only the first N atlases")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rays", type=int, default=0, help="smaller case of the workload (profiling)")
     args = ap.parse_args()
@@ -221,6 +322,9 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     from lightsprintsdk_gb300 import collider as col
+    if args.workload in ("c2", "c4"):
+        run_gather(args, world, rank, local)
+        return
 
     v, t, rays = make_workload(args.workload, args.rays)
     n = rays.shape[0]

@@ -18,6 +18,7 @@
 #ifndef RRGPU_GATHER_H
 #define RRGPU_GATHER_H
 #include "rrgpu.h"
+#include "rrgpu_cache.h"
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -62,6 +63,28 @@ RRG_API int rrg_lightmap_gather(rrg_lightmapper* lm, const rrg_gather_params* p,
 /* Same into host memory; synchronous. */
 RRG_API int rrg_lightmap_gather_host(rrg_lightmapper* lm, const rrg_gather_params* p, uint64_t first_texel,
                                      uint64_t ntexels, float* out_host, void* stream);
+/* Number of texels that have sub-texels. */
+RRG_API uint64_t rrg_lightmapper_covered(const rrg_lightmapper* lm);
+
+/* Training records for a radiance cache (rrgpu_cache.h) from the gather's
+ * own paths: from every `stride`-th covered texel, paths_per_texel plain
+ * N-bounce paths; each path vertex gives one record (position, plane
+ * normal, albedo, outgoing radiance toward the previous vertex).  Writes at
+ * most cap records to recs_dev (48 bytes each); *nrec_out = records written. */
+RRG_API int rrg_lightmap_train_samples(rrg_lightmapper* lm, const rrg_gather_params* p, uint32_t stride,
+                                       uint32_t paths_per_texel, void* recs_dev, uint64_t cap, uint64_t* nrec_out,
+                                       void* stream);
+/* Learned gather of texels [first, first + ntexels): the light rounds as in
+ * the plain gather, and for each hemisphere sample one traced segment plus a
+ * cache query at its hit (in place of the remaining bounces).  Texels whose
+ * samples land in cells the cache's error grid marks unreliable more often
+ * than fallback_frac * quality are recomputed by the plain gather;
+ * *nfallback (may be NULL) receives their number.  Synchronises the stream
+ * between chunks of 2^20 texels. */
+RRG_API int rrg_lightmap_gather_learned(rrg_lightmapper* lm, rrg_cache* cache, const rrg_gather_params* p,
+                                        uint64_t first_texel, uint64_t ntexels, float* out_dev, float fallback_frac,
+                                        uint64_t* nfallback, void* stream);
+
 /* RRG_OK, or RRG_ERR_STACK if a traversal overflowed since the last call. */
 RRG_API int rrg_lightmapper_status(rrg_lightmapper* lm, void* stream);
 

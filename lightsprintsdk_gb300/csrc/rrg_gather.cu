@@ -24,6 +24,8 @@
 // the same counter-based sample streams.
 #include "rrg_traverse.cuh"
 #include "../../include/rrgpu_gather.h"
+#include "../../include/rrgpu_cache.h"
+#include "rrg_mlp.cuh"
 
 #include <vector>
 
@@ -326,6 +328,16 @@ __global__ void k_scan_apply(const uint32_t* __restrict__ in, uint64_t n, const 
 	if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = bsum[gridDim.x];
 }
 
+__global__ void k_covered_flags(const uint32_t* __restrict__ off, uint64_t n, uint32_t* __restrict__ flag) {
+	for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x)
+		flag[t] = off[t + 1] > off[t] ? 1u : 0u;
+}
+__global__ void k_covered_scatter(const uint32_t* __restrict__ flag, const uint32_t* __restrict__ pos, uint64_t n,
+                                  uint32_t* __restrict__ list) {
+	for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x)
+		if (flag[t]) list[pos[t]] = (uint32_t)t;
+}
+
 // ---------------------------------------------------------------- gather
 struct GatherScene {
 	const TNode* nodes;
@@ -392,9 +404,20 @@ __device__ bool occluded(const GatherScene& g, V3 o, V3 d, float tmin, float tma
 	return traverse<true, true>(g.nodes, g.tris, r, g.nnodes, g.ntris, tb, bt, overflow, &f) >= 0;
 }
 
+// Per-vertex record of a path, for training the radiance cache.
+constexpr int kMaxVerts = 17;
+struct PathLog {
+	int n;
+	V3 p[kMaxVerts], nrm[kMaxVerts], alb[kMaxVerts], nee[kMaxVerts], rs[kMaxVerts];
+	bool cont[kMaxVerts];
+};
+
 // one hemisphere sample: getIncidentRadiance restated iteratively
-__device__ V3 trace_path(const GatherScene& g, V3 eye, V3 dir, uint32_t skip, uint64_t sid, bool& overflow) {
+template <bool LOG = false>
+__device__ V3 trace_path(const GatherScene& g, V3 eye, V3 dir, uint32_t skip, uint64_t sid, bool& overflow,
+                         PathLog* log = nullptr) {
 	V3 T = mk(1.f, 1.f, 1.f), L = mk(0.f, 0.f, 0.f);
+	if (LOG) log->n = 0;
 	float tmax = g.locality;
 	for (uint32_t depth = 0;; depth++) {
 		RayState r;
@@ -410,6 +433,7 @@ __device__ V3 trace_path(const GatherScene& g, V3 eye, V3 dir, uint32_t skip, ui
 		V3 p = add(eye, mul(dir, fs.dist));
 		V3 n = mk(fs.n[0], fs.n[1], fs.n[2]);
 		V3 alb = ld3(g.albedo + 3 * (size_t)tri);
+		V3 nee = mk(0.f, 0.f, 0.f);
 		for (int li = 0; li < 2; li++) {
 			V3 sdir;
 			float smax;
@@ -428,6 +452,12 @@ __device__ V3 trace_path(const GatherScene& g, V3 eye, V3 dir, uint32_t skip, ui
 			if (contrib.x == 0.f && contrib.y == 0.f && contrib.z == 0.f) continue;
 			if (occluded(g, p, sdir, g.tmin, smax, tri, overflow)) continue;
 			L = add(L, mulv(T, contrib));
+			if (LOG) nee = add(nee, contrib);
+		}
+		const int vi = LOG ? log->n : 0;
+		if (LOG && vi < kMaxVerts) {
+			log->p[vi] = p; log->nrm[vi] = n; log->alb[vi] = alb; log->nee[vi] = nee; log->cont[vi] = false;
+			log->n = vi + 1;
 		}
 		tmax = 1e10f;
 		float pdiff = avg3(alb);
@@ -456,11 +486,38 @@ __device__ V3 trace_path(const GatherScene& g, V3 eye, V3 dir, uint32_t skip, ui
 		V3 rs = mul(colorOut, __fdiv_rn(intensity, pdf));
 		if (!(avg3(rs) > kStopAtVisibility)) break;
 		T = mulv(T, rs);
+		if (LOG && vi < kMaxVerts) { log->rs[vi] = rs; log->cont[vi] = true; }
 		eye = p;
 		dir = s;
 		skip = tri;
 	}
 	return L;
+}
+
+// first segment of a hemisphere sample (learned gather): the hit point,
+// plane and albedo as a cache query record; t[0] = 1 marks a hit
+__device__ CacheRec first_hit(const GatherScene& g, V3 eye, V3 dir, uint32_t skip, bool& overflow) {
+	CacheRec r;
+	RayState rs;
+	set_ray(rs, eye, dir, g.tmin, g.locality);
+	GatherFilter f = make_filter(g, skip, true);
+	float tb = rs.tmax;
+	uint32_t tri = 0xFFFFFFFFu;
+	int slot = traverse<false, true>(g.nodes, g.tris, rs, g.nnodes, g.ntris, tb, tri, overflow, &f);
+	if (slot < 0) {
+		for (int k = 0; k < 3; k++) { r.p[k] = 0.f; r.n[k] = 0.f; r.alb[k] = 0.f; r.t[k] = 0.f; }
+		return r;
+	}
+	float4 a, b, c;
+	load_tri(g.tris, slot, a, b, c);
+	Fastest fs = fastest_fields(rs, a, b, c);
+	V3 p = add(eye, mul(dir, fs.dist));
+	const float* al = g.albedo + 3 * (size_t)tri;
+	r.p[0] = p.x; r.p[1] = p.y; r.p[2] = p.z;
+	r.n[0] = fs.n[0]; r.n[1] = fs.n[1]; r.n[2] = fs.n[2];
+	r.alb[0] = al[0]; r.alb[1] = al[1]; r.alb[2] = al[2];
+	r.t[0] = 1.f; r.t[1] = 0.f; r.t[2] = 0.f;
+	return r;
 }
 
 // HomogenousFiller2::GetTrianglePoint (gather.cpp:65-83)
@@ -491,10 +548,17 @@ struct WarpSmem {
 	unsigned char lit[kMaxRounds][2];
 };
 
+// LEARNED = false: the plain gather, out[tid - out_base] = texel RGBA.
+// LEARNED = true : first segments only; recs[(tid - out_base) * Q + k] get the
+// cache queries and out[tid - out_base] the light rounds' average (the plain
+// texel's first term) with w = 1.  list (may be null) selects texel ids.
+template <bool LEARNED>
 __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(GatherScene g, const uint32_t* __restrict__ off,
                                                               const Sub* __restrict__ st, uint64_t first,
-                                                              uint64_t count, float4* __restrict__ out,
-                                                              uint32_t* counter, uint32_t* status) {
+                                                              uint64_t count, const uint32_t* __restrict__ list,
+                                                              uint64_t out_base, float4* __restrict__ out,
+                                                              CacheRec* __restrict__ recs, uint32_t* counter,
+                                                              uint32_t* status) {
 	__shared__ WarpSmem sm_all[kGatherWarps];
 	WarpSmem& sm = sm_all[threadIdx.x >> 5];
 	const int lane = threadIdx.x & 31;
@@ -507,10 +571,11 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(GatherScene g, con
 		if (lane == 0) ti = atomicAdd((unsigned long long*)counter, 1ull);
 		ti = __shfl_sync(0xFFFFFFFFu, ti, 0);
 		if (ti >= count) break;
-		const uint64_t tid = first + ti;
+		const uint64_t tid = list ? (uint64_t)list[ti] : first + ti;
+		const uint64_t oi = tid - out_base;
 		const uint32_t b = off[tid], m = off[tid + 1] - b;
 		if (m == 0) {
-			if (lane == 0) out[ti] = make_float4(0.f, 0.f, 0.f, 0.f);
+			if (lane == 0) out[oi] = make_float4(0.f, 0.f, 0.f, 0.f);
 			continue;
 		}
 		const Sub* S = st + b;
@@ -571,7 +636,8 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(GatherScene g, con
 			if (k < Q) {
 				float cosa = __fsqrt_rn(__fsub_rn(1.f, sm.fd[k]));
 				V3 dir = add(add(mul(nrm, cosa), mul(tg, sm.fx[k])), mul(bt, sm.fy[k]));
-				sm.hemi[k] = trace_path(g, origin, dir, s.tri, sid, overflow);
+				if (LEARNED) recs[oi * Q + k] = first_hit(g, origin, dir, s.tri, overflow);
+				else sm.hemi[k] = trace_path(g, origin, dir, s.tri, sid, overflow);
 			}
 			if (fires && round < (uint32_t)kMaxRounds) {
 				for (int li = 0; li < 2; li++) {
@@ -592,19 +658,111 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(GatherScene g, con
 		__syncwarp();
 		if (lane == 0) {
 			V3 hemi = mk(0.f, 0.f, 0.f), lights = mk(0.f, 0.f, 0.f);
-			for (uint32_t k = 0; k < Q; k++) hemi = add(hemi, sm.hemi[k]);
+			if (!LEARNED)
+				for (uint32_t k = 0; k < Q; k++) hemi = add(hemi, sm.hemi[k]);
 			uint32_t shot = rounds < (uint32_t)kMaxRounds ? rounds : (uint32_t)kMaxRounds;
 			for (uint32_t r = 0; r < shot; r++)
 				for (int li = 0; li < 2; li++)
 					if (sm.lit[r][li]) lights = add(lights, sm.light[r][li]);
 			lights = divf(lights, (float)shot);
-			hemi = mul(hemi, __fdiv_rn(1.f, (float)Q));
-			V3 res = add(lights, hemi);
-			out[ti] = make_float4(res.x, res.y, res.z, 1.f);
+			if (LEARNED) {
+				out[oi] = make_float4(lights.x, lights.y, lights.z, 1.f);
+			} else {
+				hemi = mul(hemi, __fdiv_rn(1.f, (float)Q));
+				V3 res = add(lights, hemi);
+				out[oi] = make_float4(res.x, res.y, res.z, 1.f);
+			}
 		}
 		__syncwarp();
 	}
 	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// Training paths for the radiance cache: path i starts at covered texel
+// covered[(i / spt) * stride] (spt paths per texel) from a random point of a
+// random sub-texel in a cosine direction, traces the plain N-bounce path and
+// writes one record per vertex: position, plane normal, albedo and the
+// outgoing radiance toward the previous vertex, L_k = nee_k + rs_k * L_{k+1}.
+__global__ void __launch_bounds__(128) k_train_paths(GatherScene g, const uint32_t* __restrict__ off,
+                                                     const Sub* __restrict__ st, const uint32_t* __restrict__ covered,
+                                                     uint32_t ncov, uint32_t stride, uint32_t spt, uint64_t npaths,
+                                                     uint64_t seed, CacheRec* __restrict__ recs, uint64_t cap,
+                                                     unsigned long long* count, uint32_t* status) {
+	bool overflow = false;
+	PathLog log;
+	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < npaths;
+	     i += (uint64_t)gridDim.x * blockDim.x) {
+		uint64_t ci = (i / spt) * stride;
+		if (ci >= ncov) continue;
+		const uint64_t tid = covered[ci];
+		const uint32_t b = off[tid], m = off[tid + 1] - b;
+		if (!m) continue;
+		const Sub& s = st[b + (uint32_t)(hash64(seed, 70, i) % m)];
+		V3 v0, s1, s2;
+		V3 nrm = tri_normal(g, s.tri, v0, s1, s2);
+		uint32_t ru = rng24(seed, 71, i), rv = rng24(seed, 72, i);
+		if (ru + rv > kM24) { ru = kM24 - ru; rv = kM24 - rv; }
+		float fu = __fdiv_rn((float)ru, (float)kM24), fv = __fdiv_rn((float)rv, (float)kM24);
+		float pu = s.uv[0] + (s.uv[2] - s.uv[0]) * fu + (s.uv[4] - s.uv[0]) * fv;
+		float pv = s.uv[1] + (s.uv[3] - s.uv[1]) * fu + (s.uv[5] - s.uv[1]) * fv;
+		V3 origin = add(add(v0, mul(s1, pu)), mul(s2, pv));
+		float x = 0.f, y = 0.f;
+		for (int j = 0; j < kDiskTries; j++) {
+			float ax = rng01(seed, 73, i * kDiskTries + j) * 2.f - 1.f;
+			float by = rng01(seed, 74, i * kDiskTries + j) * 2.f - 1.f;
+			if (ax * ax + by * by < 1.f) { x = ax; y = by; break; }
+		}
+		V3 tg, bt;
+		basis_from_normal(nrm, tg, bt);
+		V3 dir = add(add(mul(nrm, sqrtf(fmaxf(0.f, 1.f - x * x - y * y))), mul(tg, x)), mul(bt, y));
+		trace_path<true>(g, origin, dir, s.tri, (seed << 20) ^ (i + 0x9E37ull), overflow, &log);
+		V3 Lnext = mk(0.f, 0.f, 0.f);
+		for (int k = log.n - 1; k >= 0; k--) {
+			V3 Lk = log.nee[k];
+			if (log.cont[k]) Lk = add(Lk, mulv(log.rs[k], Lnext));
+			Lnext = Lk;
+			unsigned long long slot = atomicAdd(count, 1ull);
+			if (slot >= cap) continue;
+			CacheRec r;
+			r.p[0] = log.p[k].x; r.p[1] = log.p[k].y; r.p[2] = log.p[k].z;
+			r.n[0] = log.nrm[k].x; r.n[1] = log.nrm[k].y; r.n[2] = log.nrm[k].z;
+			r.alb[0] = log.alb[k].x; r.alb[1] = log.alb[k].y; r.alb[2] = log.alb[k].z;
+			r.t[0] = Lk.x; r.t[1] = Lk.y; r.t[2] = Lk.z;
+			recs[slot] = r;
+		}
+	}
+	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// Learned texel = light rounds' average + mean of the cache over the Q
+// hemisphere samples (summed in sample order).  Texels whose samples fall in
+// unreliable cache cells more often than `frac` go to the fallback list.
+__global__ void k_learned_reduce(const uint32_t* __restrict__ off, uint64_t first, uint64_t count, uint32_t Q,
+                                 const CacheRec* __restrict__ recs, const float4* __restrict__ rad,
+                                 float4* __restrict__ out, const uint8_t* __restrict__ reliable, int res,
+                                 float lo0, float lo1, float lo2, float ie0, float ie1, float ie2, float frac,
+                                 uint32_t* __restrict__ fb_list, unsigned int* fb_count) {
+	uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+	if (i >= count) return;
+	const uint64_t tid = first + i;
+	if (off[tid + 1] == off[tid]) return;   // uncovered: the first pass wrote 0
+	V3 hemi = mk(0.f, 0.f, 0.f);
+	uint32_t bad = 0;
+	for (uint32_t k = 0; k < Q; k++) {
+		const float4 r = rad[i * Q + k];
+		hemi = add(hemi, mk(r.x, r.y, r.z));
+		if (reliable && r.w > 0.f) {
+			const CacheRec& c = recs[i * Q + k];
+			int vx = min(res - 1, max(0, (int)((c.p[0] - lo0) * ie0 * res)));
+			int vy = min(res - 1, max(0, (int)((c.p[1] - lo1) * ie1 * res)));
+			int vz = min(res - 1, max(0, (int)((c.p[2] - lo2) * ie2 * res)));
+			if (!reliable[((size_t)vz * res + vy) * res + vx]) bad++;
+		}
+	}
+	hemi = mul(hemi, __fdiv_rn(1.f, (float)Q));
+	float4 l = out[i];
+	out[i] = make_float4(__fadd_rn(l.x, hemi.x), __fadd_rn(l.y, hemi.y), __fadd_rn(l.z, hemi.z), 1.f);
+	if (fb_list && (float)bad > frac * (float)Q) fb_list[atomicAdd(fb_count, 1u)] = (uint32_t)tid;
 }
 
 // ------------------------------------------------------------ lightmapper
@@ -620,6 +778,14 @@ struct Lightmapper {
 	float* d_stage = nullptr;
 	size_t stage_bytes = 0;
 	float tmin_default = 0.f;
+	uint32_t* d_covered = nullptr;   // ids of texels with sub-texels
+	uint64_t ncovered = 0;
+	// learned-gather work buffers (grown on demand)
+	CacheRec* d_recs = nullptr;
+	float4* d_rad = nullptr;
+	uint32_t* d_fb = nullptr;
+	unsigned int* d_fbcount = nullptr;
+	uint64_t lg_cap = 0;             // texels
 };
 
 static void free_lm(Lightmapper* L) {
@@ -630,7 +796,61 @@ static void free_lm(Lightmapper* L) {
 	cudaFree(L->d_counter);
 	cudaFree(L->d_status);
 	cudaFree(L->d_stage);
+	cudaFree(L->d_covered);
+	cudaFree(L->d_recs);
+	cudaFree(L->d_rad);
+	cudaFree(L->d_fb);
+	cudaFree(L->d_fbcount);
 	delete L;
+}
+
+static int make_scene(Lightmapper* L, const rrg_gather_params* p, GatherScene& g) {
+	if (!p || p->size < sizeof(rrg_gather_params)) return RRG_ERR_INVALID;
+	if (p->quality == 0 || p->quality > (uint32_t)kMaxQuality) return RRG_ERR_INVALID;
+	Collider* c = L->c;
+	g.nodes = c->d_nodes;
+	g.tris = c->d_tris;
+	g.nnodes = (int)c->nnodes;
+	g.ntris = (int)c->nvalid;
+	g.xyz = c->d_xyz;
+	g.idx = c->d_idx;
+	g.albedo = L->d_albedo;
+	g.dir_direction = mk(p->dir_direction[0], p->dir_direction[1], p->dir_direction[2]);
+	g.dir_color = mk(p->dir_color[0], p->dir_color[1], p->dir_color[2]);
+	g.point_position = mk(p->point_position[0], p->point_position[1], p->point_position[2]);
+	g.point_color = mk(p->point_color[0], p->point_color[1], p->point_color[2]);
+	g.tmin = p->ray_length_min > 0.f ? p->ray_length_min : L->tmin_default;
+	g.locality = p->locality > 0.f ? p->locality : 100000.f;
+	g.quality = p->quality;
+	g.max_depth = p->max_depth;
+	g.seed = p->seed;
+	return RRG_OK;
+}
+
+template <bool LEARNED>
+static int launch_gather_kernel(Lightmapper* L, const GatherScene& g, uint64_t first, uint64_t count,
+                                const uint32_t* list, uint64_t out_base, float4* out, CacheRec* recs, cudaStream_t s) {
+	if (!count) return RRG_OK;
+	RRG_CUDA(cudaMemsetAsync(L->d_counter, 0, 8, s));
+	int per_sm = 0;
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather<LEARNED>, kGatherWarps * 32, 0));
+	uint64_t want = (count + kGatherWarps - 1) / kGatherWarps;
+	uint64_t cap = (uint64_t)(per_sm > 0 ? per_sm : 1) * L->c->num_sms;
+	int grid = (int)(want < cap ? want : cap);
+	k_gather<LEARNED><<<grid, kGatherWarps * 32, 0, s>>>(g, L->d_off, L->d_sub, first, count, list, out_base, out, recs,
+	                                                     reinterpret_cast<uint32_t*>(L->d_counter), L->d_status);
+	RRG_CUDA(cudaGetLastError());
+	return RRG_OK;
+}
+
+static int gather_launch(Lightmapper* L, const rrg_gather_params* p, uint64_t first, uint64_t count, float* out_dev,
+                         cudaStream_t s) {
+	GatherScene g;
+	int st = make_scene(L, p, g);
+	if (st) return st;
+	if (first + count > L->ntexels) return RRG_ERR_INVALID;
+	return launch_gather_kernel<false>(L, g, first, count, nullptr, first, reinterpret_cast<float4*>(out_dev), nullptr,
+	                                   s);
 }
 
 }  // namespace rrg
@@ -703,6 +923,28 @@ int rrg_lightmapper_create(rrg_collider* ch, const float* albedo, const int32_t*
 	if ((e = cudaMalloc(&L->d_counter, 8)) != cudaSuccess) return fail(e);
 	if ((e = cudaMalloc(&L->d_status, 4)) != cudaSuccess) return fail(e);
 	if ((e = cudaMemset(L->d_status, 0, 4)) != cudaSuccess) return fail(e);
+	{   // covered texel list (deterministic order: flags, scan, scatter)
+		uint32_t *flag = nullptr, *pos = nullptr, *bs = nullptr;
+		if ((e = cudaMalloc(&flag, sizeof(uint32_t) * ntexels)) != cudaSuccess) return fail(e);
+		if ((e = cudaMalloc(&pos, sizeof(uint32_t) * (ntexels + 1))) != cudaSuccess) { cudaFree(flag); return fail(e); }
+		if ((e = cudaMalloc(&bs, sizeof(uint32_t) * (nb + 1))) != cudaSuccess) { cudaFree(flag); cudaFree(pos); return fail(e); }
+		k_covered_flags<<<grid, 256>>>(L->d_off, ntexels, flag);
+		k_scan_sums<<<nb, kScanBT>>>(flag, ntexels, bs);
+		k_scan_top<<<1, 32>>>(bs, nb);
+		k_scan_apply<<<nb, kScanBT>>>(flag, ntexels, bs, pos);
+		uint32_t ncov = 0;
+		e = cudaMemcpy(&ncov, pos + ntexels, 4, cudaMemcpyDeviceToHost);
+		if (e == cudaSuccess) e = cudaMalloc(&L->d_covered, sizeof(uint32_t) * (ncov ? ncov : 1));
+		if (e == cudaSuccess) {
+			k_covered_scatter<<<grid, 256>>>(flag, pos, ntexels, L->d_covered);
+			e = cudaGetLastError();
+		}
+		cudaFree(flag);
+		cudaFree(pos);
+		cudaFree(bs);
+		if (e != cudaSuccess) return fail(e);
+		L->ncovered = ncov;
+	}
 	// minimalSafeDistance = (aabb max - min).avg() * 1e-6 (RRSolver.cpp:329-334)
 	float ex = c->aabb_hi[0] - c->aabb_lo[0], ey = c->aabb_hi[1] - c->aabb_lo[1], ez = c->aabb_hi[2] - c->aabb_lo[2];
 	L->tmin_default = ((ex + ey) + ez) * 0.33333333333333f * 1e-6f;
@@ -737,42 +979,6 @@ int rrg_lightmapper_copy_subtexels(const rrg_lightmapper* h, uint32_t* offsets_h
 	return RRG_OK;
 }
 
-static int gather_launch(Lightmapper* L, const rrg_gather_params* p, uint64_t first, uint64_t count, float* out_dev,
-                         cudaStream_t s) {
-	if (!p || p->size < sizeof(rrg_gather_params)) return RRG_ERR_INVALID;
-	if (p->quality == 0 || p->quality > (uint32_t)kMaxQuality) return RRG_ERR_INVALID;
-	if (first + count > L->ntexels) return RRG_ERR_INVALID;
-	if (!count) return RRG_OK;
-	Collider* c = L->c;
-	GatherScene g;
-	g.nodes = c->d_nodes;
-	g.tris = c->d_tris;
-	g.nnodes = (int)c->nnodes;
-	g.ntris = (int)c->nvalid;
-	g.xyz = c->d_xyz;
-	g.idx = c->d_idx;
-	g.albedo = L->d_albedo;
-	g.dir_direction = mk(p->dir_direction[0], p->dir_direction[1], p->dir_direction[2]);
-	g.dir_color = mk(p->dir_color[0], p->dir_color[1], p->dir_color[2]);
-	g.point_position = mk(p->point_position[0], p->point_position[1], p->point_position[2]);
-	g.point_color = mk(p->point_color[0], p->point_color[1], p->point_color[2]);
-	g.tmin = p->ray_length_min > 0.f ? p->ray_length_min : L->tmin_default;
-	g.locality = p->locality > 0.f ? p->locality : 100000.f;
-	g.quality = p->quality;
-	g.max_depth = p->max_depth;
-	g.seed = p->seed;
-	RRG_CUDA(cudaMemsetAsync(L->d_counter, 0, 8, s));
-	int per_sm = 0;
-	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather, kGatherWarps * 32, 0));
-	uint64_t want = (count + kGatherWarps - 1) / kGatherWarps;
-	uint64_t cap = (uint64_t)(per_sm > 0 ? per_sm : 1) * c->num_sms;
-	int grid = (int)(want < cap ? want : cap);
-	k_gather<<<grid, kGatherWarps * 32, 0, s>>>(g, L->d_off, L->d_sub, first, count, reinterpret_cast<float4*>(out_dev),
-	                                            reinterpret_cast<uint32_t*>(L->d_counter), L->d_status);
-	RRG_CUDA(cudaGetLastError());
-	return RRG_OK;
-}
-
 int rrg_lightmap_gather(rrg_lightmapper* h, const rrg_gather_params* p, uint64_t first_texel, uint64_t ntexels,
                         float* out_dev, void* stream) {
 	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
@@ -798,6 +1004,90 @@ int rrg_lightmap_gather_host(rrg_lightmapper* h, const rrg_gather_params* p, uin
 	if (st) return st;
 	RRG_CUDA(cudaMemcpyAsync(out_host, L->d_stage, bytes, cudaMemcpyDeviceToHost, s));
 	RRG_CUDA(cudaStreamSynchronize(s));
+	return RRG_OK;
+}
+
+uint64_t rrg_lightmapper_covered(const rrg_lightmapper* h) {
+	const Lightmapper* L = reinterpret_cast<const Lightmapper*>(h);
+	return L ? L->ncovered : 0;
+}
+
+int rrg_lightmap_train_samples(rrg_lightmapper* h, const rrg_gather_params* p, uint32_t stride,
+                               uint32_t paths_per_texel, void* recs_dev, uint64_t cap, uint64_t* nrec_out,
+                               void* stream) {
+	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
+	if (!L || !recs_dev || !stride || !paths_per_texel || !cap) return RRG_ERR_INVALID;
+	GatherScene g;
+	int st = make_scene(L, p, g);
+	if (st) return st;
+	cudaStream_t s = (cudaStream_t)stream;
+	const uint64_t npaths = (L->ncovered + stride - 1) / stride * paths_per_texel;
+	RRG_CUDA(cudaMemsetAsync(L->d_counter, 0, 8, s));
+	int grid = L->c->num_sms * 8;
+	k_train_paths<<<grid, 128, 0, s>>>(g, L->d_off, L->d_sub, L->d_covered, (uint32_t)L->ncovered, stride,
+	                                   paths_per_texel, npaths, p->seed ^ 0x7A1Dull, reinterpret_cast<CacheRec*>(recs_dev),
+	                                   cap, reinterpret_cast<unsigned long long*>(L->d_counter), L->d_status);
+	RRG_CUDA(cudaGetLastError());
+	uint64_t n = 0;
+	RRG_CUDA(cudaMemcpyAsync(&n, L->d_counter, 8, cudaMemcpyDeviceToHost, s));
+	RRG_CUDA(cudaStreamSynchronize(s));
+	if (nrec_out) *nrec_out = n < cap ? n : cap;
+	return RRG_OK;
+}
+
+int rrg_lightmap_gather_learned(rrg_lightmapper* h, rrg_cache* cache, const rrg_gather_params* p, uint64_t first,
+                                uint64_t count, float* out_dev, float fallback_frac, uint64_t* nfallback,
+                                void* stream) {
+	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
+	if (!L || !cache || !out_dev || ((uintptr_t)out_dev & 15)) return RRG_ERR_INVALID;
+	GatherScene g;
+	int st = make_scene(L, p, g);
+	if (st) return st;
+	if (first + count > L->ntexels) return RRG_ERR_INVALID;
+	cudaStream_t s = (cudaStream_t)stream;
+	const uint32_t Q = p->quality;
+	const uint64_t chunk = (uint64_t)1 << 20;
+	const uint64_t need = count < chunk ? count : chunk;
+	if (need > L->lg_cap) {
+		cudaFree(L->d_recs); cudaFree(L->d_rad); cudaFree(L->d_fb); cudaFree(L->d_fbcount);
+		L->d_recs = nullptr; L->d_rad = nullptr; L->d_fb = nullptr; L->d_fbcount = nullptr;
+		L->lg_cap = 0;
+		RRG_CUDA(cudaMalloc(&L->d_recs, sizeof(CacheRec) * need * Q));
+		RRG_CUDA(cudaMalloc(&L->d_rad, sizeof(float4) * need * Q));
+		RRG_CUDA(cudaMalloc(&L->d_fb, sizeof(uint32_t) * need));
+		RRG_CUDA(cudaMalloc(&L->d_fbcount, sizeof(unsigned int)));
+		L->lg_cap = need;
+	}
+	const uint8_t* grid = nullptr;
+	int res = 0;
+	float lo[3] = {0, 0, 0}, ie[3] = {0, 0, 0};
+	cache_grid(cache, &grid, &res, lo, ie);
+	uint64_t total_fb = 0;
+	float4* out = reinterpret_cast<float4*>(out_dev);
+	for (uint64_t c0 = first; c0 < first + count; c0 += chunk) {
+		const uint64_t n = (first + count - c0) < chunk ? (first + count - c0) : chunk;
+		float4* oc = out + (c0 - first);
+		st = launch_gather_kernel<true>(L, g, c0, n, nullptr, c0, oc, L->d_recs, s);
+		if (st) return st;
+		st = rrg_cache_infer(cache, L->d_recs, n * Q, reinterpret_cast<float*>(L->d_rad), stream);
+		if (st) return st;
+		RRG_CUDA(cudaMemsetAsync(L->d_fbcount, 0, sizeof(unsigned int), s));
+		k_learned_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+		    L->d_off, c0, n, Q, L->d_recs, L->d_rad, oc, grid, res, lo[0], lo[1], lo[2], ie[0], ie[1], ie[2],
+		    fallback_frac, grid ? L->d_fb : nullptr, L->d_fbcount);
+		RRG_CUDA(cudaGetLastError());
+		unsigned int nf = 0;
+		if (grid) {
+			RRG_CUDA(cudaMemcpyAsync(&nf, L->d_fbcount, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+			RRG_CUDA(cudaStreamSynchronize(s));
+		}
+		if (nf) {
+			st = launch_gather_kernel<false>(L, g, 0, nf, L->d_fb, c0, oc, nullptr, s);
+			if (st) return st;
+		}
+		total_fb += nf;
+	}
+	if (nfallback) *nfallback = total_fb;
 	return RRG_OK;
 }
 

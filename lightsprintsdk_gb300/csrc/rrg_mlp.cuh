@@ -1,0 +1,146 @@
+// Radiance-cache network on BF16 tensor cores (FP32 accumulation).
+//
+// The network and its loss are specified in oracle/rr_mlp.c (the FP64
+// oracle the gradients are checked against):
+//   x(64) -> relu(W1) 64 -> relu(W2) 64 -> relu(W3) 64 -> relu(W4) 64 -> W5 -> 16 (RGB = first 3)
+// Weights live in three forms: FP32 masters (row = input, column = output,
+// layer after layer, 17,408 floats) updated by Adam, and two BF16 copies
+// pre-arranged in the register-fragment order of mma.m16n8k16: W for the
+// forward pass and W^T for back-propagation.  A warp computes 16 samples at
+// a time; a layer's FP32 accumulator fragments become the next layer's BF16
+// A fragments without leaving registers (the C layout of two adjacent
+// n-tiles is the A layout of one k-tile).
+#pragma once
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace rrg {
+
+constexpr int kMlpIn = 64;
+constexpr int kMlpOut = 16;
+constexpr int kMlpParams = 4 * 64 * 64 + 64 * 16;     // 17,408
+constexpr int kMlpFragWords = 4 * (4 * 8 * 32 * 2) + 4 * 2 * 32 * 2;   // 8,704 uint32 (fwd); bwd same
+
+__host__ __device__ constexpr int mlp_layer_off(int l) { return l * 4096; }
+__host__ __device__ constexpr int mlp_layer_out(int l) { return l < 4 ? 64 : 16; }
+// fragment word offset of layer l (forward: K = 64 in, N = out; backward: K = out, N = 64 in)
+__host__ __device__ constexpr int mlp_frag_off(int l) { return l * 2048; }
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+	__nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+	return *reinterpret_cast<uint32_t*>(&v);
+}
+__device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
+
+// D += A(16x16, row) * B(16x8, col); bf16 in, fp32 accumulate
+__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
+	asm volatile(
+	    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+	    "{%0,%1,%2,%3};\n"
+	    : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+	    : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// C fragments of n-tiles 2kt, 2kt+1 (after relu when RELU) -> A fragment of k-tile kt
+template <bool RELU>
+__device__ __forceinline__ void c_to_a(const float* c0, const float* c1, uint32_t* a) {
+	auto f = [](float x) { return RELU ? fmaxf(x, 0.f) : x; };
+	a[0] = pack_bf16(f(c0[0]), f(c0[1]));
+	a[1] = pack_bf16(f(c0[2]), f(c0[3]));
+	a[2] = pack_bf16(f(c1[0]), f(c1[1]));
+	a[3] = pack_bf16(f(c1[2]), f(c1[3]));
+}
+
+// A fragments of a 16 x 64 bf16 row-major tile (row stride in uint32 words)
+__device__ __forceinline__ void load_a(const uint32_t* tile, int stride_words, int kt, uint32_t* a) {
+	const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+	a[0] = tile[g * stride_words + 8 * kt + q];
+	a[1] = tile[(g + 8) * stride_words + 8 * kt + q];
+	a[2] = tile[g * stride_words + 8 * kt + 4 + q];
+	a[3] = tile[(g + 8) * stride_words + 8 * kt + 4 + q];
+}
+
+// One 64-input layer on 4 A k-tiles; NT n-tiles of B fragments at frag.
+template <int NT>
+__device__ __forceinline__ void mlp_layer(const uint32_t (*a)[4], const uint32_t* __restrict__ frag, float (*acc)[4]) {
+	const int lane = threadIdx.x & 31;
+#pragma unroll
+	for (int nt = 0; nt < NT; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+#pragma unroll
+	for (int kt = 0; kt < 4; kt++) {
+#pragma unroll
+		for (int nt = 0; nt < NT; nt++) {
+			const uint2 b = *reinterpret_cast<const uint2*>(frag + ((kt * NT + nt) * 32 + lane) * 2);
+			mma16816(acc[nt], a[kt], b.x, b.y);
+		}
+	}
+}
+
+// Forward of one 16-row tile: x = A fragments of the encoded inputs.
+// Leaves the 16 x 16 output in out (C layout, 2 n-tiles).
+__device__ __forceinline__ void mlp_forward_tile(const uint32_t (*x)[4], const uint32_t* __restrict__ fwd,
+                                                 float (*out)[4]) {
+	uint32_t a[4][4];
+	float acc[8][4];
+#pragma unroll
+	for (int kt = 0; kt < 4; kt++)
+#pragma unroll
+		for (int r = 0; r < 4; r++) a[kt][r] = x[kt][r];
+#pragma unroll
+	for (int l = 0; l < 4; l++) {
+		mlp_layer<8>(a, fwd + mlp_frag_off(l), acc);
+#pragma unroll
+		for (int kt = 0; kt < 4; kt++) c_to_a<true>(acc[2 * kt], acc[2 * kt + 1], a[kt]);
+	}
+	mlp_layer<2>(a, fwd + mlp_frag_off(4), out);
+}
+
+// Encoding of one sample into 64 bf16 features (see oracle/rr_mlp.c);
+// `half` 0 writes words 0..15 (features 0..31), 1 words 16..31.
+__device__ __forceinline__ void mlp_encode_half(const float* p, const float* n, const float* alb, const float* lo,
+                                                const float* inv_ext, int half, uint32_t* row_words) {
+	if (half == 0) {
+#pragma unroll
+		for (int j = 0; j < 2; j++) {
+			float u = fminf(fmaxf((p[j] - lo[j]) * inv_ext[j], 0.f), 1.f);
+#pragma unroll
+			for (int k = 0; k < 8; k++) {
+				float s, c;
+				sincospif((float)(1 << k) * u, &s, &c);
+				row_words[8 * j + k] = pack_bf16(s, c);
+			}
+		}
+	} else {
+		float u = fminf(fmaxf((p[2] - lo[2]) * inv_ext[2], 0.f), 1.f);
+#pragma unroll
+		for (int k = 0; k < 8; k++) {
+			float s, c;
+			sincospif((float)(1 << k) * u, &s, &c);
+			row_words[16 + k] = pack_bf16(s, c);
+		}
+		row_words[24] = pack_bf16(n[0], n[1]);
+		row_words[25] = pack_bf16(n[2], alb[0]);
+		row_words[26] = pack_bf16(alb[1], alb[2]);
+		row_words[27] = pack_bf16(1.f, 0.f);
+		row_words[28] = 0u;
+		row_words[29] = 0u;
+		row_words[30] = 0u;
+		row_words[31] = 0u;
+	}
+}
+
+// Sample record shared by training and inference: position, normal, albedo,
+// and the target (training) or a validity flag in w (inference).
+struct CacheRec {
+	float p[3], n[3], alb[3], t[3];
+};
+
+}  // namespace rrg
+
+typedef struct rrg_cache rrg_cache;
+namespace rrg {
+// The cache's reliability grid (res^3 cells over its box; null if not built).
+void cache_grid(rrg_cache* c, const uint8_t** flags, int* res, float* lo, float* ie);
+
+}  // namespace rrg

@@ -14,7 +14,7 @@ import numpy as np
 
 from . import collider as col
 
-SUBTEXEL_DTYPE = np.dtype([("tri", "<u4"), ("uv", "<f4", (3, 2)), ("area", "<f4"), ("pad", "<u4")])
+SUBTEXEL_DTYPE = np.dtype([("tri", "<u4"), ("uv", "<f4", (3, 2)), ("area", "<f4")])   # 32 bytes
 
 
 class GatherParams(C.Structure):

@@ -11,7 +11,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liborc.so")
-SRC = [os.path.join(HERE, "rr_oracle.c"), os.path.join(HERE, "rr_gather.c")]
+SRC = [os.path.join(HERE, "rr_oracle.c"), os.path.join(HERE, "rr_gather.c"), os.path.join(HERE, "rr_mlp.c")]
 HDRS = [os.path.join(HERE, "rr_oracle.h"), os.path.join(HERE, "rr_gather.h")]
 
 _lib = None
@@ -55,6 +55,10 @@ def lib():
         L.orc_gather.argtypes = [P, C.POINTER(GatherScene), P, U, P, P, C.c_int, C.c_int, P]
         L.orc_hash.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
         L.orc_hash.restype = C.c_uint64
+        L.orc_mlp_encode.argtypes = [P, P, P, P, P, P]
+        L.orc_mlp_grad.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P]
+        L.orc_bf16.argtypes = [C.c_double]
+        L.orc_bf16.restype = C.c_double
         _lib = L
     return _lib
 
@@ -126,7 +130,7 @@ class FastestOracle:
 
 
 # ------------------------------------------------------------------ gather
-SUBTEXEL_DTYPE = np.dtype([("tri", "<u4"), ("uv", "<f4", (3, 2)), ("area", "<f4"), ("pad", "<u4")])
+SUBTEXEL_DTYPE = np.dtype([("tri", "<u4"), ("uv", "<f4", (3, 2)), ("area", "<f4")])   # 32 bytes
 
 
 class GatherScene(C.Structure):
@@ -189,3 +193,31 @@ class GatherOracle:
         lib().orc_gather(self.fo.h, C.byref(self.s), _ptr(texel_ids), texel_ids.shape[0], _ptr(off),
                          _ptr(st) if len(st) else None, threads, int(fp64), _ptr(out))
         return out
+
+
+# --------------------------------------------------------------- network
+def mlp_encode(p, n, alb, lo, hi) -> np.ndarray:
+    """Encoded inputs (B, 64) in double (rr_mlp.c)."""
+    p = np.ascontiguousarray(p, np.float32).reshape(-1, 3)
+    n = np.ascontiguousarray(n, np.float32).reshape(-1, 3)
+    alb = np.ascontiguousarray(alb, np.float32).reshape(-1, 3)
+    lo = np.ascontiguousarray(lo, np.float32)
+    hi = np.ascontiguousarray(hi, np.float32)
+    out = np.zeros((p.shape[0], 64), np.float64)
+    L = lib()
+    for i in range(p.shape[0]):
+        L.orc_mlp_encode(_ptr(p[i]), _ptr(n[i]), _ptr(alb[i]), _ptr(lo), _ptr(hi), out[i].ctypes.data_as(C.c_void_p))
+    return out
+
+
+def mlp_grad(W, X, T, bf16: bool = True):
+    """Mean relative-L2 loss gradient over the batch in double: (dW, loss, Y)."""
+    W = np.ascontiguousarray(W, np.float32)
+    X = np.ascontiguousarray(X, np.float32)
+    T = np.ascontiguousarray(T, np.float32)
+    B = X.shape[0]
+    dW = np.zeros(W.shape[0], np.float64)
+    loss = np.zeros(1, np.float64)
+    Y = np.zeros((B, 3), np.float32)
+    lib().orc_mlp_grad(_ptr(W), _ptr(X), _ptr(T), B, int(bf16), _ptr(dW), _ptr(loss), _ptr(Y))
+    return dW, float(loss[0]), Y

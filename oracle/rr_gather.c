@@ -174,7 +174,6 @@ static void emit_write(void* c, uint32_t texel, uint32_t tri, const v2* uv, floa
 	s->tri = tri;
 	for (int k = 0; k < 3; k++) { s->uv[k][0] = uv[k].x; s->uv[k][1] = uv[k].y; }
 	s->area = area;
-	s->pad = 0;
 	e->total++;
 }
 
@@ -317,6 +316,11 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 		out[0] = out[1] = out[2] = out[3] = 0;
 		return;
 	}
+	for (uint32_t i = 0; i < m; i++)
+		if (S[i].tri >= sc->nt) {   /* malformed input: no answer rather than a wild read */
+			out[0] = out[1] = out[2] = out[3] = NAN;
+			return;
+		}
 	const uint32_t Q = sc->quality ? sc->quality : 1;
 	const uint32_t rounds = Q / 10 + 1;
 	const uint32_t N = Q > rounds ? Q : rounds;

@@ -46,8 +46,7 @@ typedef struct orc_subtexel {
 	uint32_t tri;       /* world triangle index */
 	float uv[3][2];     /* corners in triangle space (barycentric u, v) */
 	float area;         /* area in map space */
-	uint32_t pad;
-} orc_subtexel;
+} orc_subtexel;         /* 32 bytes, the GPU's sub-texel record */
 
 typedef struct orc_gather_scene {
 	const float* xyz;       /* world vertices */

@@ -1,0 +1,137 @@
+"""The radiance cache's BF16 tensor-core training kernels against the FP64
+oracle (oracle/rr_mlp.c), and what the trained cache gains in the lightmap
+gather over the method without it."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from lightsprintsdk_gb300 import cache as rc
+from lightsprintsdk_gb300 import collider as col
+from lightsprintsdk_gb300 import lightmap as lm
+from lightsprintsdk_gb300 import scenes
+from oracle import orc
+
+pytestmark = pytest.mark.gpu
+NP = rc.NPARAMS
+
+
+def layer_slices():
+    return [slice(4096 * l, 4096 * (l + 1)) for l in range(4)] + [slice(16384, NP)]
+
+
+def random_recs(B, seed=0, lo=-1.0, hi=1.0):
+    rng = np.random.default_rng(seed)
+    r = np.zeros(B, rc.REC_DTYPE)
+    r["p"] = rng.uniform(lo, hi, (B, 3))
+    n = rng.normal(size=(B, 3))
+    r["n"] = n / np.linalg.norm(n, axis=1, keepdims=True)
+    r["alb"] = rng.uniform(0.2, 0.8, (B, 3))
+    r["t"] = rng.uniform(0.0, 2.0, (B, 3))
+    return r
+
+
+def test_gradient_matches_fp64_oracle():
+    """GPU forward/backward (BF16 operands, FP32 accumulation) against the
+    oracle with the same BF16 rounding points: per-layer relative error of
+    the weight gradient <= 1e-2; against exact FP64 (no rounding) <= 0.15."""
+    B = 512
+    lo, hi = np.full(3, -1.0, np.float32), np.full(3, 1.0, np.float32)
+    cache = rc.RadianceCache(lo, hi, seed=3)
+    W = cache.get_weights()
+    recs = random_recs(B, seed=1)
+    g, loss, pred = cache.gradient(recs)
+    X = orc.mlp_encode(recs["p"], recs["n"], recs["alb"], lo, hi).astype(np.float32)
+    d16, l16, y16 = orc.mlp_grad(W, X, recs["t"], bf16=True)
+    d64, l64, y64 = orc.mlp_grad(W, X, recs["t"], bf16=False)
+    errs = []
+    for sl in layer_slices():
+        e16 = np.linalg.norm(g[sl] - d16[sl]) / np.linalg.norm(d16[sl])
+        e64 = np.linalg.norm(g[sl] - d64[sl]) / np.linalg.norm(d64[sl])
+        errs.append((e16, e64))
+        assert e16 <= 1e-2, errs
+        assert e64 <= 0.15, errs
+    assert abs(loss - l16) <= 1e-3 * l16
+    np.testing.assert_allclose(pred, y16, rtol=1e-2, atol=1e-3)
+
+
+def test_training_fits_a_smooth_field():
+    """Adam on the GPU drives the relative L2 loss of a smooth target field
+    down by an order of magnitude."""
+    import torch
+    B = 1 << 16
+    lo, hi = np.full(3, -1.0, np.float32), np.full(3, 1.0, np.float32)
+    cache = rc.RadianceCache(lo, hi, seed=5)
+    cache.set_adam(lr=5e-3)
+    recs = random_recs(B, seed=2)
+    p = recs["p"]
+    recs["t"] = np.stack([1 + 0.5 * np.sin(2 * p[:, 0]), 1 + 0.5 * np.cos(3 * p[:, 1]),
+                          0.5 + 0.4 * p[:, 2] * recs["alb"][:, 0]], -1)
+    d = torch.from_numpy(recs.view(np.uint8)).cuda()
+    first = cache.train(d.data_ptr(), B, 4096, 1)
+    last = cache.train(d.data_ptr(), B, 4096, 400)
+    assert cache.steps == 401
+    assert last < 0.1 * first, (first, last)
+
+
+def rel_rmse(a, ref, mask):
+    d = (a[mask, :3] - ref[mask, :3]).astype(np.float64)
+    return float(np.sqrt((d ** 2).sum() / (ref[mask, :3].astype(np.float64) ** 2).sum()))
+
+
+@pytest.fixture(scope="module")
+def gather_setup():
+    gs = scenes.gather_c2()
+    c = col.RRCollider.create(gs.scene.vertices, gs.scene.indices)
+    L = lm.RRLightmapper.from_scene(c, gs)
+    return gs, c, L
+
+
+def test_learned_gather_error_and_gain(gather_setup):
+    """On three atlases (floor, a sphere, a box group): the learned gather
+    (1 traced segment + cache) against a 1024-sample plain reference, beside
+    the plain 64-sample gather and the same pipeline with an untrained
+    cache (the method without the network)."""
+    import torch
+    gs, c, L = gather_setup
+    S = gs.size * gs.size
+    atlases = [0, 9, 100]
+    params64 = lm.make_params(gs.lights, quality=64, max_depth=8, seed=0xC2)
+
+    def plain(q, seed, a):
+        return L.gather(lm.make_params(gs.lights, quality=q, max_depth=8, seed=seed), a * S, S)
+
+    ref = {a: np.mean([plain(256, 100 + k, a) for k in range(4)], axis=0) for a in atlases}
+    p64 = {a: plain(64, 0xC2, a) for a in atlases}
+    cache = rc.RadianceCache.for_scene(gs.scene.vertices, seed=7)
+    out = torch.empty((S, 4), dtype=torch.float32, device="cuda")
+    info = rc.bake_learned(L, cache, params64, atlases[0] * S, S, out.data_ptr(), steps=300)
+    learned = {atlases[0]: out.cpu().numpy()}
+    for a in atlases[1:]:
+        rc.gather_learned(L, cache, params64, a * S, S, out.data_ptr())
+        learned[a] = out.cpu().numpy()
+    untrained = rc.RadianceCache.for_scene(gs.scene.vertices, seed=7)
+    untrained.set_weights(np.zeros(NP, np.float32))
+    base = {}
+    for a in atlases:
+        rc.gather_learned(L, untrained, params64, a * S, S, out.data_ptr(), fallback_frac=2.0)
+        base[a] = out.cpu().numpy()
+    report = {}
+    for a in atlases:
+        m = ref[a][:, 3] > 0
+        report[a] = {"learned": rel_rmse(learned[a], ref[a], m), "plain64": rel_rmse(p64[a], ref[a], m),
+                     "without_cache": rel_rmse(base[a], ref[a], m)}
+    allm = {k: np.concatenate([x for a in atlases for x in [{"l": learned, "p": p64, "b": base}[k][a][ref[a][:, 3] > 0]]])
+            for k in ("l", "p", "b")}
+    refall = np.concatenate([ref[a][ref[a][:, 3] > 0] for a in atlases])
+    ones = np.ones(len(refall), bool)
+    summary = {"per_atlas": report, "learned": rel_rmse(allm["l"], refall, ones),
+               "plain64": rel_rmse(allm["p"], refall, ones), "without_cache": rel_rmse(allm["b"], refall, ones),
+               "train": info}
+    os.makedirs("gpurun_out", exist_ok=True)
+    with open("gpurun_out/learned_gather_error.json", "w") as f:
+        json.dump(summary, f, indent=1, default=float)
+    print(json.dumps(summary, default=float))
+    # the network must gain a lot over the method without it
+    assert summary["learned"] < 0.5 * summary["without_cache"], summary
