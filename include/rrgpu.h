@@ -74,8 +74,16 @@ typedef struct rrg_build_params {
 	uint32_t size;
 	uint32_t max_leaf_size;   /* triangles per leaf, default 4, max 8 */
 	uint32_t sah_bins;        /* bins per axis, default 32 (<= 32) */
-	uint32_t reserved[5];
+	uint32_t traversal;       /* RRG_TRAVERSAL_*, 0 = default */
+	uint32_t reserved[4];
 } rrg_build_params;
+
+/* Traversal kernels (chosen per collider; rrg_collider_set_traversal). */
+enum {
+	RRG_TRAVERSAL_DEFAULT = 0,
+	RRG_TRAVERSAL_IF_IF = 1,       /* warp takes 32 rays, per-thread if-if walk */
+	RRG_TRAVERSAL_WHILE_WHILE = 2  /* persistent while-while, postponed leaves, per-lane refill */
+};
 
 typedef struct rrg_collider rrg_collider;
 
@@ -100,6 +108,9 @@ RRG_API int rrg_collider_create_device(const float* xyz_dev, uint32_t nv, const 
 RRG_API int rrg_collider_update(rrg_collider* c, const float* xyz_host);
 
 RRG_API void rrg_collider_destroy(rrg_collider* c);
+
+/* Selects the traversal kernel of later queries (RRG_TRAVERSAL_*). */
+RRG_API int rrg_collider_set_traversal(rrg_collider* c, uint32_t traversal);
 
 /* RRCollider::getMemoryOccupied (RRCollider.h:259): device bytes held. */
 RRG_API size_t rrg_collider_memory(const rrg_collider* c);

@@ -42,7 +42,9 @@ RRG_API uint64_t rrg_cache_steps(const rrg_cache* c);
 /* Error estimate for the fallback: the cache's mean prediction and the mean
  * target of nrec device records are compared per cell of a res^3 grid over
  * the box; a cell is reliable when it holds >= min_count records and
- * |mean pred - mean target| <= rel_threshold * mean target.  nreliable
+ * |mean pred - mean target| <= max(rel_threshold * mean target, 3 standard
+ * errors of the mean target) (the targets are single-path estimates, so
+ * their noise bounds what the test can resolve).  nreliable
  * (may be NULL) receives the number of reliable cells. */
 RRG_API int rrg_cache_build_error_grid(rrg_cache* c, const void* recs_dev, uint64_t nrec, uint32_t res,
                                        float rel_threshold, uint32_t min_count, uint32_t* nreliable, void* stream);

@@ -56,7 +56,7 @@ _L = None
 
 class _BuildParams(C.Structure):
     _fields_ = [("size", C.c_uint32), ("max_leaf_size", C.c_uint32), ("sah_bins", C.c_uint32),
-                ("reserved", C.c_uint32 * 5)]
+                ("traversal", C.c_uint32), ("reserved", C.c_uint32 * 4)]
 
 
 def _lib():
@@ -85,6 +85,7 @@ def _lib():
         L.rrg_intersect_rrray.argtypes = [P, P, U, P, P]
         L.rrg_intersect_rrray_device.argtypes = [P, P, U, P, P]
         L.rrg_collider_status.argtypes = [P, P]
+        L.rrg_collider_set_traversal.argtypes = [P, U]
         L.rrg_status_string.argtypes = [I]
         L.rrg_status_string.restype = C.c_char_p
         L.rrg_last_cuda_error.restype = C.c_char_p
@@ -136,7 +137,7 @@ class RRCollider:
         bp = None
         if build_params:
             bp = _BuildParams(C.sizeof(_BuildParams), build_params.get("max_leaf_size", 0),
-                              build_params.get("sah_bins", 0))
+                              build_params.get("sah_bins", 0), build_params.get("traversal", 0))
         h = C.c_void_p()
         st = _lib().rrg_collider_create(v.ctypes.data, v.shape[0], t.ctypes.data, t.shape[0],
                                         C.byref(bp) if bp else None,
@@ -150,7 +151,7 @@ class RRCollider:
         bp = None
         if build_params:
             bp = _BuildParams(C.sizeof(_BuildParams), build_params.get("max_leaf_size", 0),
-                              build_params.get("sah_bins", 0))
+                              build_params.get("sah_bins", 0), build_params.get("traversal", 0))
         h = C.c_void_p()
         st = _lib().rrg_collider_create_device(xyz_dev_ptr, nv, idx_dev_ptr, nt, C.byref(bp) if bp else None, None,
                                                stream, C.byref(h))
@@ -172,6 +173,10 @@ class RRCollider:
         self._v = v
 
     # ------------------------------------------------------------ queries
+    def set_traversal(self, traversal: int) -> None:
+        """RRG_TRAVERSAL_IF_IF (1) or RRG_TRAVERSAL_WHILE_WHILE (2, default)."""
+        _check(_lib().rrg_collider_set_traversal(self._h, traversal), "rrg_collider_set_traversal")
+
     def getTechnique(self) -> int:
         return IT_GPU
 

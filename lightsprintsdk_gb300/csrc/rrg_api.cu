@@ -40,6 +40,8 @@ static int init_common(Collider* c, const rrg_build_params* params) {
 	}
 	c->params.size = sizeof(rrg_build_params);
 	if (c->params.max_leaf_size > (uint32_t)kMaxLeaf) return RRG_ERR_INVALID;
+	if (c->params.traversal > RRG_TRAVERSAL_WHILE_WHILE) return RRG_ERR_INVALID;
+	c->traversal = c->params.traversal ? c->params.traversal : RRG_TRAVERSAL_WHILE_WHILE;
 	RRG_CUDA(cudaGetDevice(&c->device));
 	cudaDeviceProp prop;
 	RRG_CUDA(cudaGetDeviceProperties(&prop, c->device));
@@ -170,6 +172,13 @@ void rrg_collider_destroy(rrg_collider* h) {
 	cudaSetDevice(c->device);
 	cudaDeviceSynchronize();
 	free_collider(c);
+}
+
+int rrg_collider_set_traversal(rrg_collider* h, uint32_t traversal) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c || traversal > RRG_TRAVERSAL_WHILE_WHILE) return RRG_ERR_INVALID;
+	c->traversal = traversal ? traversal : RRG_TRAVERSAL_WHILE_WHILE;
+	return RRG_OK;
 }
 
 size_t rrg_collider_memory(const rrg_collider* h) {

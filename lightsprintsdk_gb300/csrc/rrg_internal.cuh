@@ -62,6 +62,8 @@ struct Collider {
 	int num_sms = 0;
 	int trace_blocks = 0;
 	int occl_blocks = 0;
+	int ww_blocks = 0;
+	uint32_t traversal = RRG_TRAVERSAL_WHILE_WHILE;
 };
 
 // build (rrg_build.cu)

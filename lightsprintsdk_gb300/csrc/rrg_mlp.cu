@@ -393,19 +393,31 @@ __global__ void k_grid_accum(const CacheRec* __restrict__ recs, const float4* __
 		int vz = min(res - 1, max(0, (int)((r.p[2] - lo2) * ie2 * res)));
 		size_t c = ((size_t)vz * res + vy) * res + vx;
 		float4 p = pred[i];
-		atomicAdd(&st[c], (r.t[0] + r.t[1] + r.t[2]) * (1.f / 3.f));
+		float tm = (r.t[0] + r.t[1] + r.t[2]) * (1.f / 3.f);
+		atomicAdd(&st[c], tm);
 		atomicAdd(&sp[c], (p.x + p.y + p.z) * (1.f / 3.f));
 		atomicAdd(&cnt[c], 1.f);
+		atomicAdd(&st[c + 3 * (size_t)res * res * res], tm * tm);
 	}
 }
 
+// A cell is reliable when it holds >= min_count records and the mean
+// prediction differs from the mean target by at most max(thr * mean target,
+// 3 standard errors of that mean): the targets are single-path estimates, so
+// their own noise bounds what the test can resolve.
 __global__ void k_grid_flags(const float* __restrict__ st, const float* __restrict__ sp, const float* __restrict__ cnt,
-                             size_t ncell, float thr, float min_count, uint8_t* __restrict__ flags,
-                             unsigned int* __restrict__ nrel) {
+                             const float* __restrict__ st2, size_t ncell, float thr, float min_count,
+                             uint8_t* __restrict__ flags, unsigned int* __restrict__ nrel) {
 	size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
 	if (c >= ncell) return;
 	float n = cnt[c];
-	bool ok = n >= min_count && fabsf(sp[c] - st[c]) <= thr * fmaxf(st[c], 1e-3f * n);
+	bool ok = false;
+	if (n >= min_count) {
+		float mt = st[c] / n, mp = sp[c] / n;
+		float var = fmaxf(st2[c] / n - mt * mt, 0.f);
+		float se = sqrtf(var / n);
+		ok = fabsf(mp - mt) <= fmaxf(thr * fmaxf(mt, 1e-4f), 3.f * se);
+	}
 	flags[c] = ok ? 1 : 0;
 	if (ok) atomicAdd(nrel, 1u);
 }
@@ -436,7 +448,7 @@ int rrg_cache_build_error_grid(rrg_cache* h, const void* recs_dev, uint64_t nrec
 	float* sums = nullptr;
 	unsigned int* nrel = nullptr;
 	RRG_CUDA(cudaMalloc(&pred, sizeof(float4) * nrec));
-	RRG_CUDA(cudaMalloc(&sums, sizeof(float) * 3 * ncell));
+	RRG_CUDA(cudaMalloc(&sums, sizeof(float) * 4 * ncell));
 	RRG_CUDA(cudaMalloc(&nrel, sizeof(unsigned int)));
 	if (C->grid_res != (int)res) {
 		cudaFree(C->grid);
@@ -445,15 +457,16 @@ int rrg_cache_build_error_grid(rrg_cache* h, const void* recs_dev, uint64_t nrec
 		RRG_CUDA(cudaMalloc(&C->grid, ncell));
 		C->grid_res = (int)res;
 	}
-	RRG_CUDA(cudaMemsetAsync(sums, 0, sizeof(float) * 3 * ncell, s));
+	RRG_CUDA(cudaMemsetAsync(sums, 0, sizeof(float) * 4 * ncell, s));
 	RRG_CUDA(cudaMemsetAsync(nrel, 0, sizeof(unsigned int), s));
 	int st = rrg_cache_infer(h, recs_dev, nrec, reinterpret_cast<float*>(pred), stream);
 	if (!st) {
 		k_grid_accum<<<C->num_sms * 8, 256, 0, s>>>(reinterpret_cast<const CacheRec*>(recs_dev), pred, nrec, (int)res,
 		                                             C->lo[0], C->lo[1], C->lo[2], C->ie[0], C->ie[1], C->ie[2], sums,
 		                                             sums + ncell, sums + 2 * ncell);
-		k_grid_flags<<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(sums, sums + ncell, sums + 2 * ncell, ncell,
-		                                                            rel_threshold, (float)min_count, C->grid, nrel);
+		k_grid_flags<<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(sums, sums + ncell, sums + 2 * ncell,
+		                                                            sums + 3 * ncell, ncell, rel_threshold,
+		                                                            (float)min_count, C->grid, nrel);
 		cudaError_t e = cudaGetLastError();
 		if (e != cudaSuccess) st = cuda_fail(e);
 	}

@@ -143,12 +143,161 @@ __global__ void __launch_bounds__(kTraceThreads) k_rrray(const TNode* __restrict
 	}
 }
 
+// ---------------------------------------------------------------------------
+// Persistent while-while traversal with postponed leaves and per-lane refill
+// (after Aila & Laine, "Understanding the efficiency of ray traversal on
+// GPUs", HPG 2009): a lane that finishes its ray takes the next one at the
+// top of the loop while the other lanes keep their traversal state; inner
+// nodes are walked until every active lane holds a leaf, then the leaves are
+// tested; stack entries carry their entry distance and are skipped once a
+// closer hit is known.
+constexpr int kSent = 0x7FFFFFFF;   // no current node
+
+__device__ __forceinline__ int pop_entry(const int2* stack, int& sp, float tbest) {
+	while (sp > 0) {
+		int2 e = stack[--sp];
+		if (__int_as_float(e.y) <= tbest) return e.x;
+	}
+	return kSent;
+}
+
+template <bool ANY>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_ww(const TNode* __restrict__ nodes, int nnodes,
+                                                            const float4* __restrict__ tris, int ntris,
+                                                            const float4* __restrict__ rays, uint32_t n,
+                                                            float4* __restrict__ hits, float4* __restrict__ planes,
+                                                            float* __restrict__ points, uint8_t* __restrict__ occ,
+                                                            uint32_t* counter) {
+	const int lane = threadIdx.x & 31;
+	const unsigned lt = (1u << lane) - 1u;
+	int2 stack[kStackSize];
+	int sp = 0;
+	RayState r;
+	uint32_t ray = 0xFFFFFFFFu;
+	int ref = kSent, leaf = kSent;
+	float tbest = 0.f;
+	uint32_t best_tri = 0xFFFFFFFFu;
+	int best_slot = -1;
+	bool overflow = false;
+	bool exhausted = false;
+	uint32_t steps = 0;
+	while (true) {
+		const bool done = (ref == kSent) && (leaf == kSent);
+		if (done && ray != 0xFFFFFFFFu) {
+			if (ANY) {
+				occ[ray] = best_slot >= 0 ? 1 : 0;
+			} else if (best_slot < 0) {
+				hits[ray] = make_float4(0.f, __int_as_float((int)0xFFFFFFFFu), 0.f, 0.f);
+				if (planes) planes[ray] = make_float4(0.f, 0.f, 0.f, 0.f);
+				if (points) { points[3 * (size_t)ray] = 0.f; points[3 * (size_t)ray + 1] = 0.f; points[3 * (size_t)ray + 2] = 0.f; }
+			} else {
+				float4 a, b, c;
+				load_tri(tris, best_slot, a, b, c);
+				Fastest f = fastest_fields(r, a, b, c);
+				hits[ray] = make_float4(f.dist, __int_as_float((int)(best_tri | (f.front ? 0x80000000u : 0u))), f.u, f.v);
+				if (planes) planes[ray] = make_float4(f.n[0], f.n[1], f.n[2], f.n[3]);
+				if (points) {
+					points[3 * (size_t)ray] = __fadd_rn(r.ox, __fmul_rn(r.dx, f.dist));
+					points[3 * (size_t)ray + 1] = __fadd_rn(r.oy, __fmul_rn(r.dy, f.dist));
+					points[3 * (size_t)ray + 2] = __fadd_rn(r.oz, __fmul_rn(r.dz, f.dist));
+				}
+			}
+			ray = 0xFFFFFFFFu;
+		}
+		const unsigned dmask = __ballot_sync(0xFFFFFFFFu, done);
+		if (dmask && !exhausted) {
+			const int cnt = __popc(dmask);
+			uint32_t base = 0;
+			if (lane == 0) base = atomicAdd(counter, (uint32_t)cnt);
+			base = __shfl_sync(0xFFFFFFFFu, base, 0);
+			if (done) {
+				const uint32_t i = base + __popc(dmask & lt);
+				if (i < n) {
+					ray = i;
+					float4 ra = __ldg(rays + 2 * (size_t)i), rb = __ldg(rays + 2 * (size_t)i + 1);
+					r.ox = ra.x; r.oy = ra.y; r.oz = ra.z; r.tmin = ra.w;
+					r.dx = rb.x; r.dy = rb.y; r.dz = rb.z; r.tmax = rb.w;
+					ray_setup(r);
+					tbest = r.tmax;
+					best_tri = 0xFFFFFFFFu;
+					best_slot = -1;
+					sp = 0;
+					steps = 0;
+					ref = r.tmin <= r.tmax ? 0 : kSent;
+					leaf = kSent;
+				}
+			}
+			if (base + (uint32_t)cnt >= n) exhausted = true;
+		}
+		const bool active = !((ref == kSent) && (leaf == kSent));
+		if (!__any_sync(0xFFFFFFFFu, active)) {
+			if (exhausted) break;
+			continue;
+		}
+		// inner nodes until every active lane holds a postponed leaf
+		while (ref != kSent && ref >= 0) {
+			if (ref >= nnodes || ++steps > kMaxSteps) { overflow = true; ref = kSent; leaf = kSent; break; }
+			const float4* np = reinterpret_cast<const float4*>(nodes + ref);
+			const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
+			const int4 nd = __ldg(reinterpret_cast<const int4*>(np + 3));
+			const float t0 = nd.x != kEmptyRef ? box_enter(r, na.x, na.y, na.z, na.w, nc.x, nc.y, tbest) : INFINITY;
+			const float t1 = nd.y != kEmptyRef ? box_enter(r, nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, tbest) : INFINITY;
+			const bool h0 = t0 != INFINITY, h1 = t1 != INFINITY;
+			if (h0 && h1) {
+				const bool first0 = t0 <= t1;
+				if (sp < kStackSize) stack[sp++] = make_int2(first0 ? nd.y : nd.x, __float_as_int(first0 ? t1 : t0));
+				else overflow = true;
+				ref = first0 ? nd.x : nd.y;
+			} else if (h0) {
+				ref = nd.x;
+			} else if (h1) {
+				ref = nd.y;
+			} else {
+				ref = pop_entry(stack, sp, tbest);
+			}
+			if (ref != kSent && ref < 0 && leaf == kSent) {
+				leaf = ref;
+				ref = pop_entry(stack, sp, tbest);
+			}
+			if (__all_sync(__activemask(), leaf != kSent)) break;
+		}
+		// leaves
+		while (leaf != kSent) {
+			const int first = leaf & 0x07FFFFFF;
+			const int count = ((leaf >> 27) & 15) + 1;
+			leaf = kSent;
+			if (first + count > ntris) { overflow = true; ref = kSent; break; }
+			bool stop = false;
+			for (int k = 0; k < count; k++) {
+				float4 a, b, c;
+				load_tri(tris, first + k, a, b, c);
+				const uint32_t tri = (uint32_t)__float_as_int(a.w);
+				float t;
+				if (tri_test(r, a, b, c, tbest, tri, best_tri, t)) {
+					tbest = t;
+					best_tri = tri;
+					best_slot = first + k;
+					if (ANY) { stop = true; break; }
+				}
+			}
+			if (stop) { ref = kSent; break; }
+			if (ref != kSent && ref < 0) {
+				leaf = ref;
+				ref = pop_entry(stack, sp, tbest);
+			}
+		}
+	}
+	if (overflow) atomicOr(counter + 1, (uint32_t)RRG_ERR_STACK);
+}
+
 int trace_occupancy(Collider* c) {
 	int per_sm = 0;
 	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_closest, kTraceThreads, 0));
 	c->trace_blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
 	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_occluded, kTraceThreads, 0));
 	c->occl_blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_ww<false>, kTraceThreads, 0));
+	c->ww_blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
 	return RRG_OK;
 }
 
@@ -157,6 +306,13 @@ int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, fl
 	if (!n) return RRG_OK;
 	RRG_CUDA(cudaMemsetAsync(c->d_counter, 0, 4, s));
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
+	if (c->traversal != RRG_TRAVERSAL_IF_IF) {
+		int grid = (int)(want < (uint32_t)c->ww_blocks ? want : (uint32_t)c->ww_blocks);
+		k_trace_ww<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays,
+		                                                  n, hits, planes, points, nullptr, c->d_counter);
+		RRG_CUDA(cudaGetLastError());
+		return RRG_OK;
+	}
 	int grid = (int)(want < (uint32_t)c->trace_blocks ? want : (uint32_t)c->trace_blocks);
 	k_closest<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n, hits, planes, points, c->d_counter);
 	RRG_CUDA(cudaGetLastError());
@@ -167,6 +323,13 @@ int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, c
 	if (!n) return RRG_OK;
 	RRG_CUDA(cudaMemsetAsync(c->d_counter, 0, 4, s));
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
+	if (c->traversal != RRG_TRAVERSAL_IF_IF) {
+		int grid = (int)(want < (uint32_t)c->ww_blocks ? want : (uint32_t)c->ww_blocks);
+		k_trace_ww<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays,
+		                                                 n, nullptr, nullptr, nullptr, occ, c->d_counter);
+		RRG_CUDA(cudaGetLastError());
+		return RRG_OK;
+	}
 	int grid = (int)(want < (uint32_t)c->occl_blocks ? want : (uint32_t)c->occl_blocks);
 	k_occluded<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n, occ, c->d_counter);
 	RRG_CUDA(cudaGetLastError());

@@ -106,32 +106,46 @@ def test_learned_gather_error_and_gain(gather_setup):
     p64 = {a: plain(64, 0xC2, a) for a in atlases}
     cache = rc.RadianceCache.for_scene(gs.scene.vertices, seed=7)
     out = torch.empty((S, 4), dtype=torch.float32, device="cuda")
-    info = rc.bake_learned(L, cache, params64, atlases[0] * S, S, out.data_ptr(), steps=300)
+    info = rc.bake_learned(L, cache, params64, atlases[0] * S, S, out.data_ptr(), steps=600)
     learned = {atlases[0]: out.cpu().numpy()}
     for a in atlases[1:]:
         rc.gather_learned(L, cache, params64, a * S, S, out.data_ptr())
         learned[a] = out.cpu().numpy()
+    raw = {}
+    for a in atlases:
+        rc.gather_learned(L, cache, params64, a * S, S, out.data_ptr(), fallback_frac=2.0)
+        raw[a] = out.cpu().numpy()
+    params256 = lm.make_params(gs.lights, quality=256, max_depth=8, seed=0xC3)
+    raw256 = {}
+    for a in atlases:
+        rc.gather_learned(L, cache, params256, a * S, S, out.data_ptr(), fallback_frac=2.0)
+        raw256[a] = out.cpu().numpy()
     untrained = rc.RadianceCache.for_scene(gs.scene.vertices, seed=7)
     untrained.set_weights(np.zeros(NP, np.float32))
     base = {}
     for a in atlases:
         rc.gather_learned(L, untrained, params64, a * S, S, out.data_ptr(), fallback_frac=2.0)
         base[a] = out.cpu().numpy()
+    variants = {"learned": learned, "learned_no_fallback": raw, "learned256_no_fallback": raw256, "plain64": p64,
+                "without_cache": base}
     report = {}
     for a in atlases:
         m = ref[a][:, 3] > 0
-        report[a] = {"learned": rel_rmse(learned[a], ref[a], m), "plain64": rel_rmse(p64[a], ref[a], m),
-                     "without_cache": rel_rmse(base[a], ref[a], m)}
-    allm = {k: np.concatenate([x for a in atlases for x in [{"l": learned, "p": p64, "b": base}[k][a][ref[a][:, 3] > 0]]])
-            for k in ("l", "p", "b")}
+        report[a] = {k: rel_rmse(v[a], ref[a], m) for k, v in variants.items()}
     refall = np.concatenate([ref[a][ref[a][:, 3] > 0] for a in atlases])
     ones = np.ones(len(refall), bool)
-    summary = {"per_atlas": report, "learned": rel_rmse(allm["l"], refall, ones),
-               "plain64": rel_rmse(allm["p"], refall, ones), "without_cache": rel_rmse(allm["b"], refall, ones),
-               "train": info}
+    summary = {"per_atlas": report, "train": info, "reference": "plain gather, 4 x 256 samples per texel"}
+    for k, v in variants.items():
+        allv = np.concatenate([v[a][ref[a][:, 3] > 0] for a in atlases])
+        summary[k] = rel_rmse(allv, refall, ones)
+    # learned against the plain 64-sample gather itself (same first-segment streams)
+    p64all = np.concatenate([p64[a][ref[a][:, 3] > 0] for a in atlases])
+    rawall = np.concatenate([raw[a][ref[a][:, 3] > 0] for a in atlases])
+    summary["learned_no_fallback_vs_plain64"] = rel_rmse(rawall, p64all, ones)
     os.makedirs("gpurun_out", exist_ok=True)
     with open("gpurun_out/learned_gather_error.json", "w") as f:
         json.dump(summary, f, indent=1, default=float)
     print(json.dumps(summary, default=float))
     # the network must gain a lot over the method without it
-    assert summary["learned"] < 0.5 * summary["without_cache"], summary
+    assert summary["learned_no_fallback"] < 0.5 * summary["without_cache"], summary
+    assert summary["learned"] <= summary["plain64"] * 1.05, summary

@@ -231,3 +231,29 @@ def test_out_of_range_index_is_invalid():
     with pytest.raises(col.RRGError) as e:
         col.RRCollider.create(v, t)
     assert e.value.status == 1
+
+
+def test_traversal_variants_agree(c0):
+    """The while-while kernel (default) and the if-if kernel return the same
+    hits (ties broken by triangle index, so bit-identical)."""
+    v, t, rays, _, c = c0
+    c.set_traversal(1)
+    a = c.intersect_batch(rays)
+    c.set_traversal(2)
+    b = c.intersect_batch(rays)
+    for f in ("hit", "tri", "dist", "uv", "side"):
+        np.testing.assert_array_equal(a[f], b[f])
+
+
+def test_autotuner_picks_a_candidate(tmp_path, monkeypatch):
+    from lightsprintsdk_gb300 import autotune
+    monkeypatch.setenv("RRG_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    v, t = scenes.icosphere_c0()
+    rays = scenes.shell_rays(1 << 16)
+    e = autotune.tune(v, t, rays)
+    assert e["max_leaf_size"] in autotune.LEAF_SIZES and e["traversal"] in autotune.TRAVERSALS
+    assert len(e["grays"]) == 6 and all(g > 0 for g in e["grays"].values())
+    c = autotune.create_tuned(v, t, rays)
+    h = c.intersect_batch(rays)
+    ref = col.RRCollider.create(v, t).intersect_batch(rays)
+    np.testing.assert_array_equal(h["tri"], ref["tri"])
