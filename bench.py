@@ -37,10 +37,16 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 BYTES_PER_RAY = 48          # 32 B ray in (two float4) + 16 B hit record out
+C3_SAMPLE_MESHES = (0, 65, 130, 195, 260, 325, 390, 455)   # CPU-baseline sample (both mesh kinds)
+C3_SAMPLE_RAYS = 25_000                                     # rays per sampled mesh
 WORKLOAD_DESC = {
     "c1": "scene-scale closest hit: 1,239,120-triangle interior, 16,777,216 pinhole (4096x4096) + "
           "16,777,216 cosine-hemisphere surface rays per step",
     "c0": "closest hit: 69,451-triangle displaced icosphere, 1,048,576 shell rays per step",
+    "c3": "uneven batching: 512 meshes (displaced icospheres and box clusters, triangles log-uniform in "
+          "1k..500k, 43,285,775 total), rays per mesh log-uniform in 4k..4M (286,319,003 total, half coherent "
+          "pinhole, half incoherent shell rays); one multi-root build, one persistent launch per step "
+          "replayed from a CUDA graph",
 }
 
 
@@ -166,8 +172,68 @@ def cpu_baseline(v, t, rays, sample: int):
                       f"{build_s:.2f} s not timed"}
 
 
+def c3_workload():
+    from lightsprintsdk_gb300 import scenes
+    mb = scenes.batch_meshes_c3()
+    counts = scenes.log_uniform_counts(0xC3, 110, mb.nmesh, 4096, 4194304)
+    return mb, counts
+
+
+def c3_cpu_sample(mb, counts, rays_dev=None, off=None):
+    """(meshes, rays) of the bounded CPU sample: C3_SAMPLE_MESHES, the first
+    C3_SAMPLE_RAYS rays of each (from the device rays when given, else made
+    on the host with the same generator)."""
+    from lightsprintsdk_gb300 import scenes
+    out = []
+    if rays_dev is None:
+        sub = np.zeros_like(counts)
+        for m in C3_SAMPLE_MESHES:
+            sub[m] = counts[m]
+        rays_dev, off = scenes.batch_rays(mb, sub, device="cpu")
+    for m in C3_SAMPLE_MESHES:
+        a = int(off[m])
+        k = min(int(off[m + 1]) - a, C3_SAMPLE_RAYS)
+        out.append((mb.mesh(m), np.ascontiguousarray(rays_dev[a:a + k].cpu().numpy())))
+    return out
+
+
+def c3_cpu_rate(sample, threads: int, repeats: int = 1):
+    """Oracle port over the sample: seconds per repeat (BVH builds untimed)."""
+    from oracle import orc
+    oracles = [(orc.FastestOracle(v, t), r) for (v, t), r in sample]
+    for O, r in oracles:
+        O.collide(r[:4096], threads)
+    times = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        for O, r in oracles:
+            O.collide(r, threads)
+        times.append(time.perf_counter() - t0)
+    return sum(len(r) for _, r in sample), times
+
+
 def run_reference(args, rank: int):
     if rank != 0:
+        return
+    if args.workload == "c3":
+        mb, counts = c3_workload()
+        sample = c3_cpu_sample(mb, counts)
+        threads = os.cpu_count() or 1
+        for _ in range(args.warmup):
+            c3_cpu_rate(sample[:1], threads)
+        nr, times = c3_cpu_rate(sample, threads, args.steps)
+        sec = sum(times) / len(times)
+        val = nr / sec / 1e9
+        line = {"impl": "reference", "metric": "closest-hit Grays/s", "value": val, "unit": "Grays/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": sec * 1e3 * int(counts.sum()) / nr, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD_DESC["c3"], "parallelism": "cpu threads"},
+                "cpu_baseline": {"value": val, "unit": "Grays/s", "cores": threads, "kind": "port",
+                                 "sample": f"{nr} rays per step: the first {C3_SAMPLE_RAYS} rays of meshes "
+                                           f"{list(C3_SAMPLE_MESHES)}"},
+                "e2e": {"value": val, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
         return
     v, t, rays = make_workload(args.workload)
     sample = 2_000_000 if args.workload == "c1" else len(rays)
@@ -296,13 +362,90 @@ def run_gather(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_batch(args, world, rank, local):
+    """Workload c3: all meshes in one batch, all rays per step in one graph
+    launch.  The rays-per-warp knob and the leaf size are autotuned first on
+    the full workload (lightsprintsdk_gb300.autotune.tune_batch)."""
+    import torch
+    from lightsprintsdk_gb300 import autotune
+    from lightsprintsdk_gb300 import batch as rb
+    from lightsprintsdk_gb300 import scenes
+    mb, counts = c3_workload()
+    dev = f"cuda:{local}"
+    rays, off = scenes.batch_rays(mb, counts, device=dev)
+    n = rays.shape[0]
+    off_d = torch.from_numpy(off.astype(np.uint32)).to(dev)
+    hits = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    tuned = autotune.tune_batch(mb, rays, off_d)
+    b = rb.RRColliderBatch.from_meshes(mb, build_params={"max_leaf_size": tuned["max_leaf_size"]})
+    b.set_rays_per_warp(tuned["rays_per_warp"])
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def step():
+        b.intersect_device(rays.data_ptr(), off_d.data_ptr(), n, hits.data_ptr(), stream=sp)
+
+    clk = ClockSampler(local).__enter__()
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clk.wait_first_sample()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    clk.mark_start()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk.mark_end()
+    clk.__exit__()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        tt = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    assert b.status(sp) == 0, "traversal reported an error"
+    hit_ratio = float((hits[:, 1].view(torch.int32) != -1).float().mean().item())
+    if rank == 0:
+        peak, peak_src = load_peaks()
+        achieved = BYTES_PER_RAY * n / (ms * 1e-3) / 1e9
+        line = {
+            "metric": "closest-hit Grays/s", "value": world * n / (ms * 1e-3) / 1e9, "unit": "Grays/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generators; rays made on the device)",
+            "config": {"workload": WORKLOAD_DESC["c3"], "meshes": mb.nmesh, "triangles": int(mb.tri_off[-1]),
+                       "rays_per_step": n, "parallelism": f"replicas x{world}",
+                       "l2": "inputs (32 B/ray, 9.2 GB) larger than L2, no flush", "hit_ratio": hit_ratio,
+                       "bvh_build_ms": b.build_ms, "bvh_nodes": b.nodes, "autotuned": tuned},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "note": f"algorithmic {BYTES_PER_RAY} B/ray; peak {peak_src}"},
+            "e2e": None,
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            nr, times = c3_cpu_rate(c3_cpu_sample(mb, counts, rays, off), threads, 3)
+            line["cpu_baseline"] = {"value": nr / min(times) / 1e9, "unit": "Grays/s", "cores": threads,
+                                    "kind": "port",
+                                    "sample": f"{nr} rays: the first {C3_SAMPLE_RAYS} rays of meshes "
+                                              f"{list(C3_SAMPLE_MESHES)}, best of 3, oracle BVH builds untimed"}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c2", "c4"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c2", "c3", "c4"])
     ap.add_argument("--atlases", type=int, default=0, help="c2: gather only the first N atlases")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rays", type=int, default=0, help="smaller case of the workload (profiling)")
@@ -324,6 +467,12 @@ def main():
     from lightsprintsdk_gb300 import collider as col
     if args.workload in ("c2", "c4"):
         run_gather(args, world, rank, local)
+        return
+    if args.workload == "c3":
+        run_batch(args, world, rank, local)
+        if world > 1:
+            torch.distributed.barrier()
+            torch.distributed.destroy_process_group()
         return
 
     v, t, rays = make_workload(args.workload, args.rays)

@@ -1,0 +1,70 @@
+/* rrgpu_batch.h -- uneven batches of meshes and ray sets on one GPU.
+ *
+ * The reference answers "many meshes, each with its own rays" with one
+ * RRCollider per mesh (RRCollider::create, RRCollider/RRCollider.cpp:186-241;
+ * one BSP build each, bsp.cpp:1192) and a loop of intersect() calls
+ * (RRCollider.h:228), or, for objects of one scene, RRColliderMulti's loop
+ * over per-object colliders (RRCollider/RRColliderMulti.cpp:103-147).  Here
+ * all meshes are built in one multi-root BVH build (mesh m's root is node m;
+ * every level of every mesh's tree goes through the same level loop) and all
+ * rays are answered by one persistent closest-hit launch, replayed from a
+ * CUDA graph.  Per-ray results are those of rrg_intersect_device on a
+ * collider of the ray's own mesh alone (same hit record format, triangle
+ * indices local to the mesh).
+ */
+#ifndef RRGPU_BATCH_H
+#define RRGPU_BATCH_H
+#include "rrgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rrg_batch rrg_batch;
+
+/* Largest number of meshes in one batch. */
+#define RRG_BATCH_MAX_MESHES 8192u
+
+/* Creates a batch of nmesh meshes from host arrays.  vert_off and tri_off
+ * hold nmesh+1 ascending offsets (vert_off[0] = tri_off[0] = 0): mesh m's
+ * vertices are xyz[3*vert_off[m] .. 3*vert_off[m+1]) and its triangles
+ * idx[3*tri_off[m] .. 3*tri_off[m+1]), with vertex indices local to the
+ * mesh (0 .. vert_off[m+1]-vert_off[m]-1).  A mesh may be empty or have no
+ * valid triangle (its rays then miss); an index outside its mesh is
+ * RRG_ERR_INVALID.  params as for rrg_collider_create (max_leaf_size). */
+RRG_API int rrg_batch_create(const float* xyz, const uint32_t* vert_off, const uint32_t* idx,
+                             const uint32_t* tri_off, uint32_t nmesh, const rrg_build_params* params, int device,
+                             rrg_batch** out);
+
+RRG_API void rrg_batch_destroy(rrg_batch* b);
+
+/* Rays fetched by a warp per work-counter atomic: 32, 64, 128 or 256
+ * (default 32).  The autotuner's rays-per-warp knob. */
+RRG_API int rrg_batch_set_rays_per_warp(rrg_batch* b, uint32_t rays_per_warp);
+
+/* Closest hit for n device rays (float[8] each, as rrg_intersect_device);
+ * ray_off_dev = nmesh+1 ascending device offsets, ray_off[nmesh] = n: ray i
+ * belongs to the mesh m with ray_off[m] <= i < ray_off[m+1].  Writes one hit
+ * record (float4) per ray: (hitDistance, hitTriangle local to the mesh |
+ * hitFrontSide << 31, u, v), 0xFFFFFFFF = no hit.  Asynchronous on `stream`:
+ * the counter reset and the persistent kernel are replayed from a CUDA graph,
+ * captured on the first call and again whenever rays, offsets, n, hits or
+ * the rays-per-warp setting change.  Calls on the same batch must not
+ * overlap on the GPU (they share its work counter).  n < 2^31. */
+RRG_API int rrg_batch_intersect_device(rrg_batch* b, const float* rays_dev, const uint32_t* ray_off_dev, uint32_t n,
+                                       float* hits_dev, void* stream);
+
+/* Status word of the batch's traces (RRG_OK or RRG_ERR_STACK); synchronises
+ * the stream and resets the word. */
+RRG_API int rrg_batch_status(rrg_batch* b, void* stream);
+
+RRG_API uint32_t rrg_batch_meshes(const rrg_batch* b);
+RRG_API uint32_t rrg_batch_nodes(const rrg_batch* b);
+RRG_API size_t rrg_batch_memory(const rrg_batch* b);
+/* Milliseconds of device time the batch's build took (CUDA events). */
+RRG_API float rrg_batch_build_ms(const rrg_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -3,7 +3,9 @@ kernel per GPU and mesh-size bucket by timing candidates on a sample of the
 caller's own rays.  Results persist in a JSON file (the package's _lib
 directory, or $RRG_AUTOTUNE_CACHE) keyed by "<gpu name>|<log2 triangles>|<tag>".
 
-Candidates: max_leaf_size in {2, 4, 8} x traversal in {if-if, while-while}.
+Candidates: max_leaf_size in {2, 4, 8} x traversal in {if-if, while-while}
+for single colliders; max_leaf_size in {2, 4, 8} x rays per warp in
+{32, 64, 128} for mesh batches (tune_batch).
 """
 from __future__ import annotations
 
@@ -91,3 +93,43 @@ def create_tuned(vertices, indices, sample_rays: np.ndarray, tag: str = "closest
     c = col.RRCollider.create(vertices, indices, build_params={"max_leaf_size": e["max_leaf_size"],
                                                                "traversal": e["traversal"]})
     return c
+
+
+BATCH_RAYS_PER_WARP = (32, 64, 128)
+
+
+def tune_batch(mb, rays_dev, ray_off_dev, repeats: int = 3, force: bool = False) -> dict:
+    """Leaf size x rays per warp for a mesh batch (scenes.MeshBatch), timed
+    with CUDA events on the caller's device rays (all of them: the tuner
+    sees the real mix of meshes and ray sets).  Remembered per GPU and
+    log2(total triangles) bucket; returns {"max_leaf_size", "rays_per_warp",
+    "grays": {...}}."""
+    import torch
+    from . import batch as rb
+    k = key(int(mb.tri_off[-1]), "batch")
+    db = _load()
+    if k in db and not force:
+        return db[k]
+    n = rays_dev.shape[0]
+    hits = torch.empty((n, 4), dtype=torch.float32, device=rays_dev.device)
+    results = {}
+    for leaf in LEAF_SIZES:
+        b = rb.RRColliderBatch.from_meshes(mb, build_params={"max_leaf_size": leaf})
+        for rpw in BATCH_RAYS_PER_WARP:
+            b.set_rays_per_warp(rpw)
+            b.intersect_device(rays_dev.data_ptr(), ray_off_dev.data_ptr(), n, hits.data_ptr())
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(repeats):
+                b.intersect_device(rays_dev.data_ptr(), ray_off_dev.data_ptr(), n, hits.data_ptr())
+            e1.record()
+            torch.cuda.synchronize()
+            results[f"leaf{leaf}_rpw{rpw}"] = n / (e0.elapsed_time(e1) / repeats * 1e-3) / 1e9
+        b.close()
+    best = max(results, key=results.get)
+    entry = {"max_leaf_size": int(best.split("_")[0][4:]), "rays_per_warp": int(best.split("_")[1][3:]),
+             "grays": results, "rays": int(n)}
+    db[k] = entry
+    _save(db)
+    return entry

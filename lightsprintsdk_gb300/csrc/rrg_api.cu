@@ -20,8 +20,9 @@ int cuda_fail(cudaError_t e) {
 	return RRG_ERR_CUDA;
 }
 
-static void free_collider(Collider* c) {
+void free_collider(Collider* c) {
 	if (!c) return;
+	cudaFree(c->d_tri_off);
 	cudaFree(c->d_xyz);
 	cudaFree(c->d_idx);
 	cudaFree(c->d_nodes);
@@ -32,7 +33,7 @@ static void free_collider(Collider* c) {
 	delete c;
 }
 
-static int init_common(Collider* c, const rrg_build_params* params) {
+int init_collider(Collider* c, const rrg_build_params* params) {
 	memset(&c->params, 0, sizeof(c->params));
 	if (params) {
 		if (params->size < sizeof(uint32_t) || params->size > sizeof(rrg_build_params)) return RRG_ERR_INVALID;
@@ -41,7 +42,7 @@ static int init_common(Collider* c, const rrg_build_params* params) {
 	c->params.size = sizeof(rrg_build_params);
 	if (c->params.max_leaf_size > (uint32_t)kMaxLeaf) return RRG_ERR_INVALID;
 	if (c->params.traversal > RRG_TRAVERSAL_WHILE_WHILE) return RRG_ERR_INVALID;
-	c->traversal = c->params.traversal ? c->params.traversal : RRG_TRAVERSAL_WHILE_WHILE;
+	c->traversal = c->params.traversal ? c->params.traversal : RRG_TRAVERSAL_IF_IF;
 	RRG_CUDA(cudaGetDevice(&c->device));
 	cudaDeviceProp prop;
 	RRG_CUDA(cudaGetDeviceProperties(&prop, c->device));
@@ -51,7 +52,7 @@ static int init_common(Collider* c, const rrg_build_params* params) {
 	return trace_occupancy(c);
 }
 
-static void account(Collider* c) {
+void account_collider(Collider* c) {
 	c->bytes = sizeof(float) * 3 * (size_t)c->nv + sizeof(uint32_t) * 3 * (size_t)c->nt + sizeof(TNode) * (size_t)c->nnodes +
 	           sizeof(float4) * 3 * (size_t)c->nvalid + 64 + c->stage_in_bytes + c->stage_out_bytes;
 }
@@ -71,7 +72,7 @@ static int ensure_stage(Collider* c, size_t in_bytes, size_t out_bytes) {
 		RRG_CUDA(cudaMalloc(&c->d_stage_out, out_bytes));
 		c->stage_out_bytes = out_bytes;
 	}
-	account(c);
+	account_collider(c);
 	return RRG_OK;
 }
 
@@ -109,7 +110,7 @@ int rrg_collider_create_device(const float* xyz_dev, uint32_t nv, const uint32_t
 	if ((uint64_t)nt * 3 > 0xFFFFFFFFull || (uint64_t)nv * 3 > 0xFFFFFFFFull) return RRG_ERR_INVALID;
 	Collider* c = new (std::nothrow) Collider();
 	if (!c) return RRG_ERR_OOM;
-	int st = init_common(c, params);
+	int st = init_collider(c, params);
 	if (st) { free_collider(c); return st; }
 	cudaStream_t s = (cudaStream_t)stream;
 	c->nv = nv;
@@ -121,7 +122,7 @@ int rrg_collider_create_device(const float* xyz_dev, uint32_t nv, const uint32_t
 	if (e != cudaSuccess) { free_collider(c); return cuda_fail(e); }
 	st = build_bvh(c, s, aborting);
 	if (st) { free_collider(c); return st; }
-	account(c);
+	account_collider(c);
 	*out = reinterpret_cast<rrg_collider*>(c);
 	return RRG_OK;
 }
@@ -162,7 +163,7 @@ int rrg_collider_update(rrg_collider* h, const float* xyz_host) {
 	RRG_CUDA(cudaSetDevice(c->device));
 	RRG_CUDA(cudaMemcpy(c->d_xyz, xyz_host, sizeof(float) * 3 * (size_t)c->nv, cudaMemcpyHostToDevice));
 	int st = build_bvh(c, nullptr, nullptr);
-	account(c);
+	account_collider(c);
 	return st;
 }
 
@@ -177,7 +178,7 @@ void rrg_collider_destroy(rrg_collider* h) {
 int rrg_collider_set_traversal(rrg_collider* h, uint32_t traversal) {
 	Collider* c = reinterpret_cast<Collider*>(h);
 	if (!c || traversal > RRG_TRAVERSAL_WHILE_WHILE) return RRG_ERR_INVALID;
-	c->traversal = traversal ? traversal : RRG_TRAVERSAL_WHILE_WHILE;
+	c->traversal = traversal ? traversal : RRG_TRAVERSAL_IF_IF;
 	return RRG_OK;
 }
 

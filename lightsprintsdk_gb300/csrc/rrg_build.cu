@@ -259,6 +259,147 @@ __global__ void k_root_init(const int* __restrict__ rb, uint32_t n, BNode* nodes
 	}
 }
 
+// ------------------------------------------------------ batches of meshes
+// A batch builds one tree per mesh in the same level loop: mesh m's root is
+// node m, its triangles occupy positions [pos[m], pos[m+1]) of the
+// compacted id list (ids ascend, so each mesh's valid triangles are
+// contiguous there), and its subtree never mixes with another mesh's.
+
+// pos[m] = first position in the ascending id list holding a triangle id
+// >= tri_off[m] (m = 0..nroots).
+__global__ void k_mesh_ranges(const int* __restrict__ ids, uint32_t n, const uint32_t* __restrict__ tri_off,
+                              uint32_t nroots, uint32_t* __restrict__ pos) {
+	uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+	if (m > nroots) return;
+	const int key = (int)tri_off[m];
+	uint32_t lo = 0, hi = n;
+	while (lo < hi) {
+		uint32_t mid = (lo + hi) >> 1;
+		if (ids[mid] < key) lo = mid + 1;
+		else hi = mid;
+	}
+	pos[m] = lo;
+}
+
+// rb[12 m ..] = identities of (lo[3] min, hi[3] max, clo[3] min, chi[3] max)
+__global__ void k_fill_root_bounds(int* __restrict__ rb, uint32_t nroots) {
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= 12 * nroots) return;
+	const int k = (int)(i % 12);
+	const bool mx = (k >= 3 && k < 6) || k >= 9;
+	rb[i] = mx ? f2o(-INFINITY) : f2o(INFINITY);
+}
+
+// Per-mesh root bounds and centroid bounds.  A warp covers 32 consecutive
+// positions; when they all belong to one mesh (the usual case) it reduces
+// in registers and issues one atomic per field.
+__global__ void k_root_bounds_multi(const int* __restrict__ ids, uint32_t n, const float4* __restrict__ plo,
+                                    const float4* __restrict__ phi, const uint32_t* __restrict__ pos,
+                                    uint32_t nroots, int* __restrict__ rb) {
+	const int lane = threadIdx.x & 31;
+	const uint32_t stride = gridDim.x * blockDim.x;
+	for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
+		const uint32_t i = base + lane;
+		const bool ok = i < n;
+		float v[12];
+		for (int k = 0; k < 3; k++) {
+			v[k] = INFINITY; v[3 + k] = -INFINITY; v[6 + k] = INFINITY; v[9 + k] = -INFINITY;
+		}
+		int m = -1;
+		if (ok) {
+			m = (int)segment_of(pos, nroots, i);
+			const int t = ids[i];
+			float4 lo = plo[t], hi = phi[t];
+			float l[3] = {lo.x, lo.y, lo.z}, h[3] = {hi.x, hi.y, hi.z};
+			for (int k = 0; k < 3; k++) {
+				float c = 0.5f * (l[k] + h[k]);
+				v[k] = l[k]; v[3 + k] = h[k]; v[6 + k] = c; v[9 + k] = c;
+			}
+		}
+		const int m0 = __shfl_sync(0xFFFFFFFFu, m, 0);
+		const bool uniform = __all_sync(0xFFFFFFFFu, !ok || m == m0);
+		for (int k = 0; k < 12; k++) {
+			const bool mx = (k >= 3 && k < 6) || k >= 9;
+			float x = v[k];
+			if (uniform) {
+				for (int o = 16; o; o >>= 1) {
+					float y = __shfl_xor_sync(0xFFFFFFFFu, x, o);
+					x = mx ? fmaxf(x, y) : fminf(x, y);
+				}
+				if (lane == 0) {
+					if (mx) atomicMax(&rb[12 * m0 + k], f2o(x));
+					else atomicMin(&rb[12 * m0 + k], f2o(x));
+				}
+			} else if (ok) {
+				if (mx) atomicMax(&rb[12 * m + k], f2o(x));
+				else atomicMin(&rb[12 * m + k], f2o(x));
+			}
+		}
+	}
+}
+
+// Root node m and its task (large or small list) for every non-empty mesh.
+__global__ void k_root_init_multi(const int* __restrict__ rb, const uint32_t* __restrict__ pos, uint32_t nroots,
+                                  BNode* nodes, Task* large, Task* small, BuildState* st) {
+	uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+	if (m == 0) st->node_count = (int)nroots;
+	if (m >= nroots) return;
+	const int* b = rb + 12 * m;
+	BNode r;
+	for (int k = 0; k < 3; k++) { r.lo[k] = o2f(b[k]); r.hi[k] = o2f(b[3 + k]); }
+	r.left = r.right = -1;
+	r.begin = (int)pos[m];
+	r.count = (int)(pos[m + 1] - pos[m]);
+	nodes[m] = r;
+	if (r.count == 0) return;
+	Task t;
+	t.node = (int)m; t.begin = r.begin; t.count = r.count; t.depth = 0; t.buf = 0;
+	t.chunk_base = 0; t.nchunks = 0;
+	for (int k = 0; k < 3; k++) { t.cmin[k] = o2f(b[6 + k]); t.cmax[k] = o2f(b[9 + k]); }
+	if (t.count > kSmall) large[atomicAdd(&st->nlarge_next, 1)] = t;
+	else small[atomicAdd(&st->nsmall, 1)] = t;
+}
+
+// Globalises a batch's per-mesh vertex indices: idx of mesh m's triangles
+// += vert_off[m]; an index outside its mesh's vertices becomes 0xFFFFFFFF,
+// which the build reports as invalid input.
+__global__ void k_globalize_indices(uint32_t* __restrict__ idx, uint32_t nt, const uint32_t* __restrict__ tri_off,
+                                    const uint32_t* __restrict__ vert_off, uint32_t nroots) {
+	uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= nt) return;
+	const uint32_t m = segment_of(tri_off, nroots, t);
+	const uint32_t nvm = vert_off[m + 1] - vert_off[m];
+	for (int k = 0; k < 3; k++) {
+		uint32_t v = idx[3 * t + k];
+		idx[3 * t + k] = v < nvm ? v + vert_off[m] : 0xFFFFFFFFu;
+	}
+}
+
+int globalize_batch_indices(Collider* c, const uint32_t* d_vert_off, cudaStream_t s) {
+	k_globalize_indices<<<(c->nt + 255) / 256, 256, 0, s>>>(c->d_idx, c->nt, c->d_tri_off, d_vert_off, c->nroots);
+	RRG_CUDA(cudaGetLastError());
+	return RRG_OK;
+}
+
+// Scene pad of the node boxes: 2^-20 of the largest root coordinate (empty
+// meshes skipped).
+__global__ void k_root_pad(const BNode* __restrict__ bn, uint32_t nroots, float* __restrict__ pad) {
+	__shared__ float red[32];
+	float mx = 0.f;
+	for (uint32_t m = threadIdx.x; m < nroots; m += blockDim.x) {
+		const BNode r = bn[m];
+		if (r.left < 0 && r.count == 0) continue;
+		for (int k = 0; k < 3; k++) mx = fmaxf(mx, fmaxf(fabsf(r.lo[k]), fabsf(r.hi[k])));
+	}
+	for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+	if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		for (int w = 1; w < (int)(blockDim.x >> 5); w++) mx = fmaxf(mx, red[w]);
+		*pad = mx * 9.5367431640625e-07f + 1e-30f;
+	}
+}
+
 // --------------------------------------------------------- shared binning
 __device__ __forceinline__ void bins_clear(int* b, int n_ints) {
 	for (int i = threadIdx.x; i < n_ints; i += blockDim.x) {
@@ -811,24 +952,30 @@ __device__ __forceinline__ void widen(BNode& n, float pad) {
 	}
 }
 
-__global__ void k_emit_nodes(const BNode* __restrict__ bn, int nnodes, TNode* __restrict__ tn) {
+__global__ void k_emit_nodes(const BNode* __restrict__ bn, int nnodes, int nroots, const float* __restrict__ pad_ptr,
+                             TNode* __restrict__ tn) {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= nnodes) return;
 	BNode n = bn[i];
-	const BNode root = bn[0];
-	float mx = 0.f;
-	for (int k = 0; k < 3; k++) mx = fmaxf(mx, fmaxf(fabsf(root.lo[k]), fabsf(root.hi[k])));
-	const float pad = mx * 9.5367431640625e-07f + 1e-30f;
+	const float pad = *pad_ptr;
 	TNode o;
 	if (n.left < 0) {
-		if (i != 0) return;   // leaves live in their parent's child refs
+		if (i >= nroots) return;   // leaves live in their parent's child refs
+		if (n.count == 0) {        // a mesh without valid triangles
+			o.a = make_float4(INFINITY, -INFINITY, INFINITY, -INFINITY);
+			o.b = o.a;
+			o.c = o.a;
+			o.d = make_int4(kEmptyRef, kEmptyRef, 0, 0);
+			tn[i] = o;
+			return;
+		}
 		// a root that is a leaf: wrap it in a one-child inner node
 		widen(n, pad);
 		o.a = make_float4(n.lo[0], n.hi[0], n.lo[1], n.hi[1]);
 		o.b = make_float4(INFINITY, -INFINITY, INFINITY, -INFINITY);
 		o.c = make_float4(n.lo[2], n.hi[2], INFINITY, -INFINITY);
 		o.d = make_int4(leaf_ref(n.begin, n.count), kEmptyRef, 0, 0);
-		tn[0] = o;
+		tn[i] = o;
 		return;
 	}
 	if (n.left >= nnodes || n.right >= nnodes) return;
@@ -919,7 +1066,8 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 	RRG_CUDA(sc.get(&final_ids, nvalid));
 	k_compact<<<nb, kBT, 0, s>>>(valid, nt, bsum, idsA);
 
-	const int max_nodes = 2 * (int)nvalid;
+	const uint32_t nroots = c->d_tri_off ? c->nroots : 1;
+	const int max_nodes = 2 * (int)nvalid + (int)nroots;
 	BNode* bnodes;
 	RRG_CUDA(sc.get(&bnodes, max_nodes));
 	// task lists: large tasks per level <= nvalid / kSmall * 2, small <= nvalid
@@ -969,8 +1117,19 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 	}
 	int rgrid = (int)((nvalid + 255) / 256);
 	if (rgrid > 4 * 152) rgrid = 4 * 152;
-	k_root_bounds<<<rgrid, 256, 0, s>>>(idsA, nvalid, plo, phi, rb);
-	k_root_init<<<1, 1, 0, s>>>(rb, nvalid, bnodes, largeA, small, st);
+	if (c->d_tri_off) {
+		uint32_t* pos;
+		int* rbm;
+		RRG_CUDA(sc.get(&pos, nroots + 1));
+		RRG_CUDA(sc.get(&rbm, 12 * (size_t)nroots));
+		k_mesh_ranges<<<(nroots + 1 + 255) / 256, 256, 0, s>>>(idsA, nvalid, c->d_tri_off, nroots, pos);
+		k_fill_root_bounds<<<(12 * nroots + 255) / 256, 256, 0, s>>>(rbm, nroots);
+		k_root_bounds_multi<<<rgrid, 256, 0, s>>>(idsA, nvalid, plo, phi, pos, nroots, rbm);
+		k_root_init_multi<<<(nroots + 255) / 256, 256, 0, s>>>(rbm, pos, nroots, bnodes, largeA, small, st);
+	} else {
+		k_root_bounds<<<rgrid, 256, 0, s>>>(idsA, nvalid, plo, phi, rb);
+		k_root_init<<<1, 1, 0, s>>>(rb, nvalid, bnodes, largeA, small, st);
+	}
 	RRG_CUDA(cudaGetLastError());
 
 	Task* cur = largeA;
@@ -1018,7 +1177,10 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 	c->d_tris = nullptr;
 	RRG_CUDA(dalloc(&c->d_nodes, nnodes));
 	RRG_CUDA(dalloc(&c->d_tris, 3 * (size_t)nvalid));
-	k_emit_nodes<<<(nnodes + 255) / 256, 256, 0, s>>>(bnodes, nnodes, c->d_nodes);
+	float* pad;
+	RRG_CUDA(sc.get(&pad, 1));
+	k_root_pad<<<1, 256, 0, s>>>(bnodes, nroots, pad);
+	k_emit_nodes<<<(nnodes + 255) / 256, 256, 0, s>>>(bnodes, nnodes, (int)nroots, pad, c->d_nodes);
 	k_emit_tris<<<(nvalid + 255) / 256, 256, 0, s>>>(final_ids, nvalid, c->d_xyz, c->d_idx, c->d_tris);
 	RRG_CUDA(cudaGetLastError());
 	RRG_CUDA(cudaEventRecord(e1, s));

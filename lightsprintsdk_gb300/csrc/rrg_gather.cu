@@ -786,6 +786,7 @@ struct Lightmapper {
 	uint32_t* d_fb = nullptr;
 	unsigned int* d_fbcount = nullptr;
 	uint64_t lg_cap = 0;             // texels
+	uint64_t lg_cap_samples = 0;     // texels x samples per texel
 };
 
 static void free_lm(Lightmapper* L) {
@@ -1048,15 +1049,19 @@ int rrg_lightmap_gather_learned(rrg_lightmapper* h, rrg_cache* cache, const rrg_
 	const uint32_t Q = p->quality;
 	const uint64_t chunk = (uint64_t)1 << 20;
 	const uint64_t need = count < chunk ? count : chunk;
-	if (need > L->lg_cap) {
+	// records and radiances hold Q samples per texel: the capacity check is
+	// on both the texel count and the sample count
+	if (need > L->lg_cap || need * Q > L->lg_cap_samples) {
 		cudaFree(L->d_recs); cudaFree(L->d_rad); cudaFree(L->d_fb); cudaFree(L->d_fbcount);
 		L->d_recs = nullptr; L->d_rad = nullptr; L->d_fb = nullptr; L->d_fbcount = nullptr;
 		L->lg_cap = 0;
+		L->lg_cap_samples = 0;
 		RRG_CUDA(cudaMalloc(&L->d_recs, sizeof(CacheRec) * need * Q));
 		RRG_CUDA(cudaMalloc(&L->d_rad, sizeof(float4) * need * Q));
 		RRG_CUDA(cudaMalloc(&L->d_fb, sizeof(uint32_t) * need));
 		RRG_CUDA(cudaMalloc(&L->d_fbcount, sizeof(unsigned int)));
 		L->lg_cap = need;
+		L->lg_cap_samples = need * Q;
 	}
 	const uint8_t* grid = nullptr;
 	int res = 0;

@@ -39,6 +39,19 @@ __host__ __device__ inline int leaf_ref(int first, int count) {
 	return kLeafBit | ((count - 1) << 27) | first;
 }
 
+// Index m of the segment holding item i, for ascending offsets off[0..n]
+// with off[0] = 0 and i < off[n]: the largest m < n with off[m] <= i (empty
+// segments, whose offsets repeat, are skipped).
+__device__ __forceinline__ uint32_t segment_of(const uint32_t* off, uint32_t n, uint32_t i) {
+	uint32_t lo = 0, hi = n;
+	while (hi - lo > 1) {
+		uint32_t mid = (lo + hi) >> 1;
+		if (off[mid] <= i) lo = mid;
+		else hi = mid;
+	}
+	return lo;
+}
+
 // Triangles in leaf order: 3 x float4 = (v0.xyz, original index bits),
 // (v1.xyz, 0), (v2.xyz, 0); vertices in the mesh's own order.
 
@@ -63,11 +76,16 @@ struct Collider {
 	int trace_blocks = 0;
 	int occl_blocks = 0;
 	int ww_blocks = 0;
-	uint32_t traversal = RRG_TRAVERSAL_WHILE_WHILE;
+	uint32_t traversal = RRG_TRAVERSAL_IF_IF;
+	// batches of meshes (rrg_batch): one BVH root per mesh, nodes 0..nroots-1;
+	// d_tri_off = nroots+1 offsets of each mesh's triangles in d_idx
+	uint32_t nroots = 1;
+	uint32_t* d_tri_off = nullptr;
 };
 
 // build (rrg_build.cu)
 int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting);
+int globalize_batch_indices(Collider* c, const uint32_t* d_vert_off, cudaStream_t s);
 
 // trace (rrg_trace.cu)
 int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
@@ -75,9 +93,17 @@ int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, fl
 int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, cudaStream_t s);
 int launch_rrray(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, cudaStream_t s);
 int trace_occupancy(Collider* c);
+// batches (nmesh roots): ray i belongs to mesh segment_of(ray_off, nmesh, i)
+constexpr uint32_t kBatchMaxMeshes = 8192;
+int batch_trace_blocks(Collider* c, uint32_t nmesh, int* blocks);
+int launch_batch_closest(Collider* c, const float4* rays, uint32_t n, const uint32_t* ray_off, uint32_t nmesh,
+                         int fetch, int blocks, float4* hits, cudaStream_t s);
 
 // api (rrg_api.cu)
 int cuda_fail(cudaError_t e);
+int init_collider(Collider* c, const rrg_build_params* params);
+void free_collider(Collider* c);
+void account_collider(Collider* c);
 
 }  // namespace rrg
 

@@ -95,6 +95,54 @@ __global__ void __launch_bounds__(kTraceThreads) k_occluded(const TNode* __restr
 	}
 }
 
+// Closest hit over a batch of meshes in one persistent launch.  Ray i
+// belongs to mesh m = segment_of(ray_off, nmesh, i) (offsets staged in
+// shared memory) and is traced from that mesh's root, node m; its hit
+// triangle is reported as an index local to mesh m.  A warp takes
+// 32 * fetch consecutive rays per atomic (the rays-per-warp knob).
+__global__ void __launch_bounds__(kTraceThreads) k_batch_closest(const TNode* __restrict__ nodes, int nnodes,
+                                                                 const float4* __restrict__ tris, int ntris,
+                                                                 const float4* __restrict__ rays, uint32_t n,
+                                                                 const uint32_t* __restrict__ ray_off,
+                                                                 const uint32_t* __restrict__ tri_off,
+                                                                 uint32_t nmesh, int fetch,
+                                                                 float4* __restrict__ hits, uint32_t* counter) {
+	extern __shared__ uint32_t s_off[];
+	for (uint32_t k = threadIdx.x; k <= nmesh; k += blockDim.x) s_off[k] = ray_off[k];
+	__syncthreads();
+	const int lane = threadIdx.x & 31;
+	const uint32_t per_fetch = 32u * (uint32_t)fetch;
+	while (true) {
+		uint32_t base = 0;
+		if (lane == 0) base = atomicAdd(counter, per_fetch);
+		base = __shfl_sync(0xFFFFFFFFu, base, 0);
+		if (base >= n) break;
+		for (int j = 0; j < fetch; j++) {
+			const uint32_t i = base + 32u * (uint32_t)j + (uint32_t)lane;
+			if (i >= n) break;
+			const uint32_t m = segment_of(s_off, nmesh, i);
+			RayState r;
+			load_ray(rays, i, r);
+			float tbest = r.tmax;
+			uint32_t best_tri = 0xFFFFFFFFu;
+			bool overflow = false;
+			int slot = -1;
+			if (r.tmin <= r.tmax)
+				slot = traverse<false>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow, nullptr, (int)m);
+			if (overflow) atomicOr(counter + 1, (uint32_t)RRG_ERR_STACK);
+			if (slot < 0) {
+				hits[i] = make_float4(0.f, __int_as_float((int)0xFFFFFFFFu), 0.f, 0.f);
+				continue;
+			}
+			float4 a, b, c;
+			load_tri(tris, slot, a, b, c);
+			Fastest f = fastest_fields(r, a, b, c);
+			const uint32_t bits = (best_tri - __ldg(tri_off + m)) | (f.front ? 0x80000000u : 0u);
+			hits[i] = make_float4(f.dist, __int_as_float((int)bits), f.u, f.v);
+		}
+	}
+}
+
 // rr::RRRay records (128-byte stride) in device memory: offsets of
 // include/Lightsprint/RRCollider.h:85-137 on LP64.
 constexpr int kRRRayStride = 128;
@@ -342,6 +390,30 @@ int launch_rrray(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, cu
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
 	int grid = (int)(want < (uint32_t)c->trace_blocks ? want : (uint32_t)c->trace_blocks);
 	k_rrray<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, (uint8_t*)rrrays_dev, n, hit_dev, c->d_counter);
+	RRG_CUDA(cudaGetLastError());
+	return RRG_OK;
+}
+
+int batch_trace_blocks(Collider* c, uint32_t nmesh, int* blocks) {
+	int per_sm = 0;
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_closest, kTraceThreads,
+	                                                       sizeof(uint32_t) * (nmesh + 1)));
+	*blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
+	return RRG_OK;
+}
+
+// Clears the work counter and launches k_batch_closest on stream s (both
+// stream-ordered, so the pair can be captured in a CUDA graph).
+int launch_batch_closest(Collider* c, const float4* rays, uint32_t n, const uint32_t* ray_off, uint32_t nmesh,
+                         int fetch, int blocks, float4* hits, cudaStream_t s) {
+	if (!n) return RRG_OK;
+	RRG_CUDA(cudaMemsetAsync(c->d_counter, 0, 4, s));
+	const uint32_t per_fetch = 32u * (uint32_t)fetch;
+	const uint32_t want = (uint32_t)(((uint64_t)n + per_fetch - 1) / per_fetch * 32 / kTraceThreads + 1);
+	const int grid = (int)(want < (uint32_t)blocks ? want : (uint32_t)blocks);
+	k_batch_closest<<<grid, kTraceThreads, sizeof(uint32_t) * (nmesh + 1), s>>>(
+	    c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n, ray_off, c->d_tri_off, nmesh, fetch, hits,
+	    c->d_counter);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }

@@ -202,10 +202,10 @@ __device__ __forceinline__ bool front_facing(const RayState& r, float4 a, float4
 template <bool ANY, bool FILTER = false>
 __device__ int traverse(const TNode* __restrict__ nodes, const float4* __restrict__ tris, const RayState& r,
                         int nnodes, int ntris, float& tbest, uint32_t& best_tri, bool& overflow,
-                        const GatherFilter* flt = nullptr) {
+                        const GatherFilter* flt = nullptr, int root = 0) {
 	int stack[kStackSize];
 	int sp = 0;
-	int ref = 0;
+	int ref = root;
 	int best_slot = -1;
 	for (uint32_t steps = 0;; steps++) {
 		if (steps >= kMaxSteps) { overflow = true; break; }

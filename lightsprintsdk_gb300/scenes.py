@@ -579,3 +579,202 @@ def gather_c2(sc: Scene | None = None, seed: int = 0xC2, natlas: int = 256, size
               "point_position": np.array([-5.0, 8.0, -5.0], np.float32),
               "point_color": np.array([20.0, 18.0, 15.0], np.float32)}
     return GatherScene(sc, albedo, tri_atlas, uv, natlas, size, lights)
+
+
+# ------------------------------------------------------- uneven mesh batches
+def geodesic_sphere_grid(freq: int):
+    """The class-I geodesic sphere of geodesic_sphere(freq) (same vertex
+    positions, same 20*freq^2 triangles, outward CCW winding), built with
+    array operations: a grid point's identity is the sorted list of its
+    (corner, weight) pairs with nonzero weight, encoded as one integer, and
+    np.unique merges the copies on shared edges and corners.  Vertex and
+    triangle order differ from geodesic_sphere's (vertices in key order,
+    triangles face by face, upward ones first)."""
+    iv, faces = _icosahedron()
+    f = int(freq)
+    ii, jj = np.meshgrid(np.arange(f + 1), np.arange(f + 1), indexing="ij")
+    inside = ii + jj <= f
+    gi, gj = ii[inside], jj[inside]                      # P grid points per face
+    P = gi.size
+    lut = np.full((f + 1, f + 1), -1, np.int64)
+    lut[gi, gj] = np.arange(P)
+    w = np.stack([f - gi - gj, gi, gj], -1)              # (P, 3) weights of corners a, b, c
+    corners = np.broadcast_to(faces[:, None, :], (20, P, 3))
+    weights = np.broadcast_to(w[None], (20, P, 3))
+    corners = np.where(weights > 0, corners, 12)         # zero weight -> sentinel, sorts last
+    order = np.argsort(corners, axis=-1, kind="stable")
+    cs = np.take_along_axis(corners, order, -1)
+    ws = np.where(cs == 12, 0, np.take_along_axis(weights, order, -1))
+    S = 13 * (f + 1)
+    code = cs * (f + 1) + ws
+    key = ((code[..., 0] * S + code[..., 1]) * S + code[..., 2]).reshape(-1)
+    uniq, first, inv = np.unique(key, return_index=True, return_inverse=True)
+    csf = cs.reshape(-1, 3)[first] % 12
+    wsf = ws.reshape(-1, 3)[first].astype(np.float64)
+    verts = np.zeros((uniq.size, 3), np.float64)
+    for slot in range(3):   # canonical (sorted-corner) order: at most 3 terms
+        verts = verts + wsf[:, slot:slot + 1] * iv[csf[:, slot]]
+    verts = verts / float(f)
+    l = np.sqrt((verts[:, 0] * verts[:, 0] + verts[:, 1] * verts[:, 1]) + verts[:, 2] * verts[:, 2])
+    verts = verts / l[:, None]
+    # triangles of one face in grid-point numbering, then per face
+    ui, uj = np.nonzero(np.add.outer(np.arange(f), np.arange(f)) <= f - 1)
+    up = np.stack([lut[ui, uj], lut[ui + 1, uj], lut[ui, uj + 1]], -1)
+    di, dj = np.nonzero(np.add.outer(np.arange(f), np.arange(f)) <= f - 2)
+    down = np.stack([lut[di + 1, dj], lut[di + 1, dj + 1], lut[di, dj + 1]], -1)
+    local = np.concatenate([up, down])                   # (f^2, 3)
+    tris = (np.arange(20)[:, None, None] * P + local[None]).reshape(-1, 3)
+    return verts, inv.reshape(-1)[tris]
+
+
+def _box_cluster(seed: int, m: int, ntri: int):
+    """4..16 seeded boxes in [-1, 1]^3 (sides 0.1..0.8), tessellated so that
+    the cluster has about `ntri` triangles (truncated to at most ntri)."""
+    nb = 4 + int(hash_u64(seed, 200, m) % np.uint64(13))
+    ids = np.arange(nb, dtype=np.uint64) + np.uint64(m) * np.uint64(64)
+    size = np.stack([0.1 + 0.7 * uniform01(seed, 201 + a, ids) for a in range(3)], -1)
+    ctr = np.stack([-1.0 + (2.0 - size[:, a]) * uniform01(seed, 204 + a, ids) + 0.5 * size[:, a]
+                    for a in range(3)], -1)
+    area = 2.0 * (size[:, 0] * size[:, 1] + size[:, 1] * size[:, 2] + size[:, 2] * size[:, 0])
+    cell = float(np.sqrt(2.0 * area.sum() / max(ntri, 12)))
+    vs, ts, base = [], [], 0
+    for b in range(nb):
+        v, t = _box_tris(ctr[b] - 0.5 * size[b], ctr[b] + 0.5 * size[b], cell)
+        vs.append(v)
+        ts.append(t + base)
+        base += v.shape[0]
+    v = np.concatenate(vs)
+    t = np.concatenate(ts)[:ntri]
+    return v, t
+
+
+class MeshBatch:
+    """Meshes of an uneven batch, concatenated: vertices float32 (V,3),
+    indices uint32 (T,3) local to each mesh, vert_off / tri_off uint32
+    (M+1,) prefix offsets, kind (M,) 0 = displaced icosphere, 1 = box
+    cluster, center float32 (M,3) of each mesh's vertex AABB and radius
+    float32 (M,) = half its largest extent (the mesh's size)."""
+
+    def __init__(self, vertices, indices, vert_off, tri_off, kind, center, radius):
+        self.vertices = vertices
+        self.indices = indices
+        self.vert_off = vert_off
+        self.tri_off = tri_off
+        self.kind = kind
+        self.center = center
+        self.radius = radius
+
+    @property
+    def nmesh(self) -> int:
+        return int(self.tri_off.shape[0] - 1)
+
+    def mesh(self, m: int):
+        v = self.vertices[self.vert_off[m]:self.vert_off[m + 1]]
+        t = self.indices[self.tri_off[m]:self.tri_off[m + 1]]
+        return v, t
+
+
+def log_uniform_counts(seed: int, stream: int, n: int, lo: int, hi: int) -> np.ndarray:
+    """n integers log-uniform in [lo, hi]: round(lo * (hi/lo)^u), u from
+    uniform01 (the power is taken as exp2 of a float64, the only libm call
+    of this module; counts do not need bit reproducibility)."""
+    u = uniform01(seed, stream, np.arange(n, dtype=np.uint64))
+    return np.clip(np.round(lo * np.exp2(u * np.log2(hi / lo))), lo, hi).astype(np.int64)
+
+
+def batch_meshes_c3(seed: int = 0xC3, nmesh: int = 512, tri_lo: int = 1000, tri_hi: int = 500_000) -> MeshBatch:
+    """Uneven-batching workload: `nmesh` meshes with triangle counts
+    log-uniform in [tri_lo, tri_hi]; even-numbered meshes are displaced
+    icospheres (frequency ceil(sqrt(n/20)), truncated to n triangles, value
+    noise of amplitude 0.15), odd-numbered ones clusters of 4..16 boxes;
+    each mesh scaled by 0.5..2 and moved by up to 10 on each axis (its own
+    coordinate frame; meshes are independent)."""
+    counts = log_uniform_counts(seed, 100, nmesh, tri_lo, tri_hi)
+    ids = np.arange(nmesh, dtype=np.uint64)
+    scale = 0.5 + 1.5 * uniform01(seed, 101, ids)
+    shift = np.stack([-10.0 + 20.0 * uniform01(seed, 102 + a, ids) for a in range(3)], -1)
+    vs, ts, kinds = [], [], []
+    cache = {}
+    for m in range(nmesh):
+        n = int(counts[m])
+        if m % 2 == 0:
+            freq = int(np.ceil(np.sqrt(n / 20.0)))
+            if freq not in cache:
+                cache[freq] = geodesic_sphere_grid(freq)
+            sv, st = cache[freq]
+            d = value_noise3(sv, seed + m, 2.5)
+            v = sv * (1.0 + 0.15 * d)[:, None]
+            t = st[:n]
+        else:
+            v, t = _box_cluster(seed, m, n)
+        vs.append((v * scale[m] + shift[m]).astype(np.float32))
+        ts.append(t.astype(np.uint32))
+        kinds.append(m % 2)
+    vert_off = np.zeros(nmesh + 1, np.int64)
+    tri_off = np.zeros(nmesh + 1, np.int64)
+    vert_off[1:] = np.cumsum([v.shape[0] for v in vs])
+    tri_off[1:] = np.cumsum([t.shape[0] for t in ts])
+    lo = np.stack([v.min(0) for v in vs]).astype(np.float64)
+    hi = np.stack([v.max(0) for v in vs]).astype(np.float64)
+    center = 0.5 * (lo + hi)
+    radius = 0.5 * (hi - lo).max(1)
+    return MeshBatch(np.concatenate(vs), np.concatenate(ts), vert_off.astype(np.uint32), tri_off.astype(np.uint32),
+                     np.array(kinds, np.int32), center.astype(np.float32), radius.astype(np.float32))
+
+
+def batch_rays(mb: MeshBatch, counts: np.ndarray, seed: int = 0xC3, device: str = "cuda"):
+    """Rays of an uneven batch, made with torch on `device` (no host copy of
+    the full set): mesh m gets counts[m] rays, the first half coherent
+    (a pinhole camera 3 r from its centre, looking at it through a
+    ceil(sqrt(k)) x ceil(sqrt(k)) image, half-angle tangent 0.4), the rest
+    incoherent (origins uniform in the shell [1.5 r, 3 r] around the centre,
+    directions uniform on the sphere); tmin 0, tmax 10 r.  Seeded with a
+    torch.Generator; reproducible for one torch build and device type.
+    Returns (rays float32 (n, 8), ray_off int64 (M+1,) host array)."""
+    import torch
+    counts = np.asarray(counts, np.int64)
+    M = mb.nmesh
+    off = np.zeros(M + 1, np.int64)
+    off[1:] = np.cumsum(counts)
+    n = int(off[-1])
+    dev = torch.device(device)
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    cnt = torch.from_numpy(counts).to(dev)
+    mesh = torch.repeat_interleave(torch.arange(M, device=dev), cnt)
+    j = torch.arange(n, device=dev) - torch.from_numpy(off[:-1]).to(dev)[mesh]
+    half = (cnt // 2)[mesh]
+    coherent = j < half
+    ctr = torch.from_numpy(mb.center).to(dev)[mesh]
+    rad = torch.from_numpy(mb.radius).to(dev)[mesh]
+    # per-mesh camera
+    fwd = torch.randn((M, 3), generator=g, device=dev)
+    fwd = fwd / fwd.norm(dim=1, keepdim=True)
+    up0 = torch.where(fwd[:, 1:2].abs() < 0.9, torch.tensor([0.0, 1.0, 0.0], device=dev),
+                      torch.tensor([1.0, 0.0, 0.0], device=dev))
+    right = torch.linalg.cross(fwd, up0)
+    right = right / right.norm(dim=1, keepdim=True)
+    up = torch.linalg.cross(right, fwd)
+    w = torch.ceil(torch.sqrt(torch.clamp(cnt // 2, min=1).double())).long()[mesh]
+    px = (j % w).float()
+    py = (j // w).float()
+    sx = (2.0 * (px + 0.5) / w.float() - 1.0) * 0.4
+    sy = (2.0 * (py + 0.5) / w.float() - 1.0) * 0.4
+    dc = fwd[mesh] + sx[:, None] * right[mesh] + sy[:, None] * up[mesh]
+    dc = dc / dc.norm(dim=1, keepdim=True)
+    oc = ctr - 3.0 * rad[:, None] * fwd[mesh]
+    # incoherent: shell origins, uniform directions
+    di = torch.randn((n, 3), generator=g, device=dev)
+    di = di / di.norm(dim=1, keepdim=True).clamp_min(1e-12)
+    u = torch.rand((n,), generator=g, device=dev)
+    rr = torch.pow(1.5 ** 3 + u * (3.0 ** 3 - 1.5 ** 3), 1.0 / 3.0)
+    pdir = torch.randn((n, 3), generator=g, device=dev)
+    pdir = pdir / pdir.norm(dim=1, keepdim=True).clamp_min(1e-12)
+    oi = ctr + (rr * rad)[:, None] * pdir
+    rays = torch.empty((n, 8), dtype=torch.float32, device=dev)
+    c = coherent[:, None]
+    rays[:, 0:3] = torch.where(c, oc, oi)
+    rays[:, 3] = 0.0
+    rays[:, 4:7] = torch.where(c, dc, di)
+    rays[:, 7] = 10.0 * rad
+    return rays, off

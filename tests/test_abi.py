@@ -69,6 +69,25 @@ def test_invalid_arguments_rejected_before_any_device_work():
     assert L.rrg_intersect_host(None, None, 1, None, None) == 1
 
 
+def test_batch_arguments_rejected_before_any_device_work():
+    from lightsprintsdk_gb300 import batch as rb
+    L = rb._lib()
+    out = C.c_void_p()
+    v = np.zeros((6, 3), np.float32)
+    t = np.zeros((2, 3), np.uint32)
+    vo = np.array([0, 3, 6], np.uint32)
+    bad = np.array([0, 2, 1], np.uint32)            # not ascending
+    assert L.rrg_batch_create(v.ctypes.data, vo.ctypes.data, t.ctypes.data, bad.ctypes.data, 2, None, 0,
+                              C.byref(out)) == 1
+    assert L.rrg_batch_create(v.ctypes.data, vo.ctypes.data, t.ctypes.data, vo.ctypes.data, 0, None, 0,
+                              C.byref(out)) == 1
+    z = np.zeros(3, np.uint32)
+    assert L.rrg_batch_create(v.ctypes.data, vo.ctypes.data, t.ctypes.data, z.ctypes.data, 2, None, 0,
+                              C.byref(out)) == 7    # no triangles at all
+    assert L.rrg_batch_intersect_device(None, None, None, 1, None, None) == 1
+    assert L.rrg_batch_set_rays_per_warp(None, 32) == 1
+
+
 def test_decode_hits():
     h = np.zeros((3, 4), np.float32)
     h[0] = [1.5, 0, 0.25, 0.5]

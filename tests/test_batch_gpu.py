@@ -1,0 +1,119 @@
+"""Uneven mesh batches (include/rrgpu_batch.h) on the GPU: the multi-root
+build and the persistent batch launch against per-mesh colliders (bit
+exact) and the C oracle, across rays-per-warp settings and graph replays."""
+import numpy as np
+import pytest
+
+from lightsprintsdk_gb300 import batch as rb
+from lightsprintsdk_gb300 import collider as col
+from lightsprintsdk_gb300 import scenes
+from oracle import orc
+from tests.helpers import classify_mismatches
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def small_batch():
+    """24 meshes (1k..30k triangles), plus a mesh of degenerate triangles
+    only and a mesh that gets no rays; 300..20k rays per mesh."""
+    import torch
+    mb = scenes.batch_meshes_c3(seed=0x5C3, nmesh=24, tri_lo=1000, tri_hi=30000)
+    # mesh 5 -> degenerate triangles only (no valid triangle: its rays miss)
+    t0, t1 = int(mb.tri_off[5]), int(mb.tri_off[6])
+    mb.indices[t0:t1] = 0
+    counts = scenes.log_uniform_counts(0x5C3, 110, mb.nmesh, 300, 20000)
+    counts[7] = 0
+    rays, off = scenes.batch_rays(mb, counts, seed=0x5C3)
+    b = rb.RRColliderBatch.from_meshes(mb)
+    off_d = torch.from_numpy(off.astype(np.uint32)).cuda()
+    return mb, counts, rays, off, off_d, b
+
+
+def run(b, rays, off_d, k=32):
+    import torch
+    hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device="cuda")
+    b.set_rays_per_warp(k)
+    b.intersect_device(rays.data_ptr(), off_d.data_ptr(), rays.shape[0], hits.data_ptr())
+    torch.cuda.synchronize()
+    assert b.status() == 0
+    return hits.cpu().numpy()
+
+
+def test_batch_equals_per_mesh_colliders(small_batch):
+    mb, counts, rays, off, off_d, b = small_batch
+    h = run(b, rays, off_d)
+    r = rays.cpu().numpy()
+    for m in range(mb.nmesh):
+        a, e = int(off[m]), int(off[m + 1])
+        if a == e:
+            continue
+        v, t = mb.mesh(m)
+        if m == 5:
+            assert (h[a:e, 1].view(np.uint32) == 0xFFFFFFFF).all()
+            with pytest.raises(col.RRGError):
+                col.RRCollider.create(v, t)
+            continue
+        c = col.RRCollider.create(v, t)
+        got = col.decode_hits(h[a:e])
+        one = c.intersect_batch(r[a:e])
+        for f in ("hit", "tri", "dist", "uv", "side"):
+            np.testing.assert_array_equal(got[f], one[f], err_msg=f"mesh {m} field {f}")
+        c.close()
+
+
+def test_batch_against_oracle(small_batch):
+    mb, counts, rays, off, off_d, b = small_batch
+    h = run(b, rays, off_d)
+    r = rays.cpu().numpy()
+    checked = 0
+    for m in range(0, mb.nmesh, 3):
+        a, e = int(off[m]), int(off[m + 1])
+        if a == e or m == 5:
+            continue
+        v, t = mb.mesh(m)
+        o = orc.FastestOracle(v, t).collide(r[a:e], 0)
+        got = col.decode_hits(h[a:e])
+        cls = classify_mismatches(v, t, r[a:e], o, got)
+        assert not cls["other"], (m, cls)
+        same = o["hit"] & got["hit"] & (o["tri"] == got["tri"])
+        assert same.sum() >= o["hit"].sum() - 2, m
+        for f in ("dist", "uv", "side"):
+            np.testing.assert_array_equal(got[f][same], o[f][same], err_msg=f"mesh {m} {f}")
+        checked += e - a
+    assert checked > 10000
+
+
+def test_rays_per_warp_and_graph_replay_agree(small_batch):
+    import torch
+    mb, counts, rays, off, off_d, b = small_batch
+    base = run(b, rays, off_d, 32)
+    for k in (64, 128, 256):
+        np.testing.assert_array_equal(run(b, rays, off_d, k).view(np.uint32), base.view(np.uint32), err_msg=str(k))
+    # a recapture for another output buffer, then two replays of that graph
+    b.set_rays_per_warp(32)
+    hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        hits.fill_(7.0)
+        b.intersect_device(rays.data_ptr(), off_d.data_ptr(), rays.shape[0], hits.data_ptr())
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(hits.cpu().numpy().view(np.uint32), base.view(np.uint32))
+
+
+def test_leaf_sizes_agree(small_batch):
+    mb, counts, rays, off, off_d, b = small_batch
+    base = run(b, rays, off_d)
+    for leaf in (1, 2, 8):
+        b2 = rb.RRColliderBatch.from_meshes(mb, build_params={"max_leaf_size": leaf})
+        np.testing.assert_array_equal(run(b2, rays, off_d).view(np.uint32), base.view(np.uint32), err_msg=str(leaf))
+        b2.close()
+
+
+def test_index_outside_its_mesh_is_invalid():
+    mb = scenes.batch_meshes_c3(seed=0x5C4, nmesh=3, tri_lo=1000, tri_hi=2000)
+    bad = mb.indices.copy()
+    # a valid global index, but outside mesh 1's own vertices
+    bad[int(mb.tri_off[1])] = int(mb.vert_off[2] - mb.vert_off[1]) + 3
+    with pytest.raises(col.RRGError) as e:
+        rb.RRColliderBatch.create(mb.vertices, bad, mb.vert_off, mb.tri_off)
+    assert e.value.status == 1
