@@ -53,7 +53,8 @@ enum {
 	RRG_ERR_ABORTED = 5,   /* *aborting was set during create */
 	RRG_ERR_NO_DEVICE = 6, /* no CUDA device, or not an sm_103 device */
 	RRG_ERR_EMPTY = 7,     /* the mesh has no valid triangle */
-	RRG_ERR_TIMEOUT = 8    /* a bounded device wait ran out */
+	RRG_ERR_TIMEOUT = 8,   /* a bounded device wait ran out */
+	RRG_ERR_TOO_LARGE = 9  /* batch above RRG_NOALLOC_MAX_RAYS (rrg_intersect_rrray_noalloc) */
 };
 
 /* RRRay::Flags (include/Lightsprint/RRCollider.h:98-106). */
@@ -149,6 +150,31 @@ RRG_API int rrg_intersect_rrray(rrg_collider* c, void* rrrays_host, uint32_t n, 
 
 /* Same on a device copy of the RRRay array (asynchronous). */
 RRG_API int rrg_intersect_rrray_device(rrg_collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, void* stream);
+
+/* Largest batch of rrg_intersect_rrray_noalloc (its static device scratch is
+ * 256 + 129 * RRG_NOALLOC_MAX_RAYS bytes per device, about 2 MB). */
+#define RRG_NOALLOC_MAX_RAYS 16384u
+
+/* rrg_intersect_rrray without allocating: no counterpart in the reference.
+ * Same arguments, outputs and synchronous behaviour as rrg_intersect_rrray,
+ * but the device scratch (work counter, status word, staging of the records
+ * and hit bytes) is one static array per device instead of buffers that the
+ * collider grows with cudaFree + cudaMalloc.  For callers that must not
+ * allocate device memory: a per-frame loop, where cudaFree's device-wide
+ * synchronisation would stall every stream, and a process whose device memory
+ * is already held (by a caching allocator such as PyTorch's, or by a bake
+ * that sized its buffers to fill the GPU), where cudaMalloc would fail.
+ *   - n > RRG_NOALLOC_MAX_RAYS returns RRG_ERR_TOO_LARGE and does nothing;
+ *   - the first call on a device sets the scratch up (looks up the array's
+ *     device address with that device current); make that first call before
+ *     any stream capture begins;
+ *   - the status of the trace is returned directly (RRG_ERR_STACK on a
+ *     traversal overflow); rrg_collider_status() does not see it;
+ *   - every call on a device shares the one array, whichever collider or
+ *     stream it uses: calls that overlap on the GPU (from two host threads at
+ *     once) race on it and return wrong results.  Serialise them. */
+RRG_API int rrg_intersect_rrray_noalloc(rrg_collider* c, void* rrrays_host, uint32_t n, uint8_t* hit_host,
+                                        void* stream);
 
 /* Status word of the collider's last traces: RRG_OK or RRG_ERR_STACK.
  * Synchronises the stream first; resets the word. */

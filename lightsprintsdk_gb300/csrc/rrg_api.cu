@@ -97,6 +97,7 @@ const char* rrg_status_string(int s) {
 		case RRG_ERR_NO_DEVICE: return "no usable CUDA device";
 		case RRG_ERR_EMPTY: return "mesh has no valid triangle";
 		case RRG_ERR_TIMEOUT: return "device wait timed out";
+		case RRG_ERR_TOO_LARGE: return "batch larger than RRG_NOALLOC_MAX_RAYS (static scratch limit)";
 		default: return "unknown status";
 	}
 }

@@ -92,6 +92,8 @@ int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, fl
                    cudaStream_t s);
 int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, cudaStream_t s);
 int launch_rrray(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, cudaStream_t s);
+int launch_rrray_scratch(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, uint32_t* words,
+                         cudaStream_t s);
 int trace_occupancy(Collider* c);
 // batches (nmesh roots): ray i belongs to mesh segment_of(ray_off, nmesh, i)
 constexpr uint32_t kBatchMaxMeshes = 8192;

@@ -394,6 +394,18 @@ int launch_rrray(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, cu
 	return RRG_OK;
 }
 
+// k_rrray on caller-owned scratch words ([0] work counter, [1] status), which
+// the caller has cleared on stream s.
+int launch_rrray_scratch(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, uint32_t* words,
+                         cudaStream_t s) {
+	if (!n) return RRG_OK;
+	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
+	int grid = (int)(want < (uint32_t)c->trace_blocks ? want : (uint32_t)c->trace_blocks);
+	k_rrray<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, (uint8_t*)rrrays_dev, n, hit_dev, words);
+	RRG_CUDA(cudaGetLastError());
+	return RRG_OK;
+}
+
 int batch_trace_blocks(Collider* c, uint32_t nmesh, int* blocks) {
 	int per_sm = 0;
 	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_closest, kTraceThreads,
