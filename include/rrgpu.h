@@ -76,7 +76,8 @@ typedef struct rrg_build_params {
 	uint32_t max_leaf_size;   /* triangles per leaf, default 4, max 8 */
 	uint32_t sah_bins;        /* bins per axis, default 32 (<= 32) */
 	uint32_t traversal;       /* RRG_TRAVERSAL_*, 0 = default */
-	uint32_t reserved[4];
+	uint32_t bvh_width;       /* 2 (binary) or 8 (compressed 8-wide, leaves <= 4); 0 = default */
+	uint32_t reserved[3];
 } rrg_build_params;
 
 /* Traversal kernels (chosen per collider; rrg_collider_set_traversal). */

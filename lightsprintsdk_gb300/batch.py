@@ -63,7 +63,7 @@ class RRColliderBatch:
         bp = None
         if build_params:
             bp = col._BuildParams(C.sizeof(col._BuildParams), build_params.get("max_leaf_size", 0),
-                                  build_params.get("sah_bins", 0), 0)
+                                  build_params.get("sah_bins", 0), 0, build_params.get("bvh_width", 0))
         h = C.c_void_p()
         st = _lib().rrg_batch_create(v.ctypes.data, vo.ctypes.data, t.ctypes.data, to.ctypes.data, vo.shape[0] - 1,
                                      C.byref(bp) if bp else None, device, C.byref(h))

@@ -56,7 +56,7 @@ _L = None
 
 class _BuildParams(C.Structure):
     _fields_ = [("size", C.c_uint32), ("max_leaf_size", C.c_uint32), ("sah_bins", C.c_uint32),
-                ("traversal", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+                ("traversal", C.c_uint32), ("bvh_width", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
 def _lib():
@@ -137,7 +137,8 @@ class RRCollider:
         bp = None
         if build_params:
             bp = _BuildParams(C.sizeof(_BuildParams), build_params.get("max_leaf_size", 0),
-                              build_params.get("sah_bins", 0), build_params.get("traversal", 0))
+                              build_params.get("sah_bins", 0), build_params.get("traversal", 0),
+                              build_params.get("bvh_width", 0))
         h = C.c_void_p()
         st = _lib().rrg_collider_create(v.ctypes.data, v.shape[0], t.ctypes.data, t.shape[0],
                                         C.byref(bp) if bp else None,
@@ -151,7 +152,8 @@ class RRCollider:
         bp = None
         if build_params:
             bp = _BuildParams(C.sizeof(_BuildParams), build_params.get("max_leaf_size", 0),
-                              build_params.get("sah_bins", 0), build_params.get("traversal", 0))
+                              build_params.get("sah_bins", 0), build_params.get("traversal", 0),
+                              build_params.get("bvh_width", 0))
         h = C.c_void_p()
         st = _lib().rrg_collider_create_device(xyz_dev_ptr, nv, idx_dev_ptr, nt, C.byref(bp) if bp else None, None,
                                                stream, C.byref(h))

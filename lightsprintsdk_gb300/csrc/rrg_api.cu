@@ -23,6 +23,8 @@ int cuda_fail(cudaError_t e) {
 void free_collider(Collider* c) {
 	if (!c) return;
 	cudaFree(c->d_tri_off);
+	cudaFree(c->d_wnodes);
+	cudaFree(c->d_wtris);
 	cudaFree(c->d_xyz);
 	cudaFree(c->d_idx);
 	cudaFree(c->d_nodes);
@@ -42,6 +44,9 @@ int init_collider(Collider* c, const rrg_build_params* params) {
 	c->params.size = sizeof(rrg_build_params);
 	if (c->params.max_leaf_size > (uint32_t)kMaxLeaf) return RRG_ERR_INVALID;
 	if (c->params.traversal > RRG_TRAVERSAL_WHILE_WHILE) return RRG_ERR_INVALID;
+	if (c->params.bvh_width != 0 && c->params.bvh_width != 2 && c->params.bvh_width != 8) return RRG_ERR_INVALID;
+	c->width = c->params.bvh_width ? c->params.bvh_width : 2;
+	if (c->width == 8 && c->params.max_leaf_size > (uint32_t)kWideLeafMax) return RRG_ERR_INVALID;
 	c->traversal = c->params.traversal ? c->params.traversal : RRG_TRAVERSAL_IF_IF;
 	RRG_CUDA(cudaGetDevice(&c->device));
 	cudaDeviceProp prop;
@@ -54,7 +59,8 @@ int init_collider(Collider* c, const rrg_build_params* params) {
 
 void account_collider(Collider* c) {
 	c->bytes = sizeof(float) * 3 * (size_t)c->nv + sizeof(uint32_t) * 3 * (size_t)c->nt + sizeof(TNode) * (size_t)c->nnodes +
-	           sizeof(float4) * 3 * (size_t)c->nvalid + 64 + c->stage_in_bytes + c->stage_out_bytes;
+	           sizeof(float4) * 3 * (size_t)c->nvalid + 64 + c->stage_in_bytes + c->stage_out_bytes +
+	           (c->d_wnodes ? sizeof(uint4) * 5 * (size_t)c->nwnodes + sizeof(float4) * 3 * (size_t)c->nvalid : 0);
 }
 
 static int ensure_stage(Collider* c, size_t in_bytes, size_t out_bytes) {

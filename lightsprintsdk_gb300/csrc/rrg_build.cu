@@ -1183,6 +1183,10 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 	k_emit_nodes<<<(nnodes + 255) / 256, 256, 0, s>>>(bnodes, nnodes, (int)nroots, pad, c->d_nodes);
 	k_emit_tris<<<(nvalid + 255) / 256, 256, 0, s>>>(final_ids, nvalid, c->d_xyz, c->d_idx, c->d_tris);
 	RRG_CUDA(cudaGetLastError());
+	if (c->width == 8) {
+		int wst = build_wide(c, bnodes, nnodes, pad, s);
+		if (wst) return wst;
+	}
 	RRG_CUDA(cudaEventRecord(e1, s));
 	RRG_CUDA(cudaEventSynchronize(e1));
 	float ms = 0;

@@ -35,6 +35,20 @@ constexpr int kEmptyRef = (int)0xFFFFFFFFu;   // leaf bit set, count 16: never p
 constexpr int kMaxLeaf = 8;
 constexpr int kStackSize = 64;
 
+// Compressed 8-wide node (80 bytes = 5 x uint4), built from the binary tree
+// (rrg_wide.cu) for the closest/any-hit kernels:
+//   w[0] = (p.x, p.y, p.z as float bits, e.x | e.y << 8 | e.z << 16 | valid << 24)
+//   w[1] = (child_base, tri_base, meta[0..3], meta[4..7])
+//   w[2] = (qlo.x[0..7], qlo.y[0..7]) bytes, w[3] = (qlo.z, qhi.x), w[4] = (qhi.y, qhi.z)
+// Child slot s spans p + q[s] * 2^(e-127) on each axis (q in 0..255,
+// rounded outward, so the box contains the child's widened box).  meta[s]:
+// internal child 0x80 | k -> node child_base + k; leaf (count-1) << 5 |
+// offset -> triangles tri_base + offset .. + count-1 (count <= 4).  The
+// slots of a node are assigned so that visiting slot i ^ octant(ray) for
+// i = 0..7 goes roughly near to far.
+constexpr int kWideLeafMax = 4;
+constexpr uint32_t kWideMaxNodes = 1u << 24;   // stack entries pack a node index in 24 bits
+
 __host__ __device__ inline int leaf_ref(int first, int count) {
 	return kLeafBit | ((count - 1) << 27) | first;
 }
@@ -76,16 +90,25 @@ struct Collider {
 	int trace_blocks = 0;
 	int occl_blocks = 0;
 	int ww_blocks = 0;
+	int wide_blocks = 0;
 	uint32_t traversal = RRG_TRAVERSAL_IF_IF;
 	// batches of meshes (rrg_batch): one BVH root per mesh, nodes 0..nroots-1;
 	// d_tri_off = nroots+1 offsets of each mesh's triangles in d_idx
 	uint32_t nroots = 1;
 	uint32_t* d_tri_off = nullptr;
+	// 8-wide form (bvh_width 8): nodes 0..nroots-1 are roots; triangles in
+	// wide-leaf order, same 3 x float4 layout as d_tris
+	uint32_t width = 2;
+	uint4* d_wnodes = nullptr;    // 5 per node
+	float4* d_wtris = nullptr;    // 3*nvalid
+	uint32_t nwnodes = 0;
 };
 
 // build (rrg_build.cu)
 int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting);
 int globalize_batch_indices(Collider* c, const uint32_t* d_vert_off, cudaStream_t s);
+// wide (rrg_wide.cu): collapses the binary build nodes into d_wnodes/d_wtris
+int build_wide(Collider* c, const BNode* bnodes, int nnodes, const float* pad, cudaStream_t s);
 
 // trace (rrg_trace.cu)
 int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,

@@ -95,12 +95,76 @@ __global__ void __launch_bounds__(kTraceThreads) k_occluded(const TNode* __restr
 	}
 }
 
+// The same two kernels over the 8-wide tree (traverse_wide).
+__global__ void __launch_bounds__(kTraceThreads) k_closest_w(const uint4* __restrict__ wn, int nwnodes,
+                                                             const float4* __restrict__ tris, int ntris,
+                                                             const float4* __restrict__ rays, uint32_t n,
+                                                             float4* __restrict__ hits, float4* __restrict__ planes,
+                                                             float* __restrict__ points, uint32_t* counter) {
+	const int lane = threadIdx.x & 31;
+	while (true) {
+		uint32_t base = warp_fetch(counter);
+		if (base >= n) break;
+		uint32_t i = base + lane;
+		if (i >= n) continue;
+		RayState r;
+		load_ray(rays, i, r);
+		float tbest = r.tmax;
+		uint32_t best_tri = 0xFFFFFFFFu;
+		bool overflow = false;
+		int slot = -1;
+		if (r.tmin <= r.tmax) slot = traverse_wide<false>(wn, tris, r, nwnodes, ntris, tbest, best_tri, overflow);
+		if (overflow) atomicOr(counter + 1, (uint32_t)RRG_ERR_STACK);
+		if (slot < 0) {
+			hits[i] = make_float4(0.f, __int_as_float((int)0xFFFFFFFFu), 0.f, 0.f);
+			if (planes) planes[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+			if (points) { points[3 * (size_t)i] = 0.f; points[3 * (size_t)i + 1] = 0.f; points[3 * (size_t)i + 2] = 0.f; }
+			continue;
+		}
+		float4 a, b, c;
+		load_tri(tris, slot, a, b, c);
+		Fastest f = fastest_fields(r, a, b, c);
+		uint32_t bits = best_tri | (f.front ? 0x80000000u : 0u);
+		hits[i] = make_float4(f.dist, __int_as_float((int)bits), f.u, f.v);
+		if (planes) planes[i] = make_float4(f.n[0], f.n[1], f.n[2], f.n[3]);
+		if (points) {
+			points[3 * (size_t)i] = __fadd_rn(r.ox, __fmul_rn(r.dx, f.dist));
+			points[3 * (size_t)i + 1] = __fadd_rn(r.oy, __fmul_rn(r.dy, f.dist));
+			points[3 * (size_t)i + 2] = __fadd_rn(r.oz, __fmul_rn(r.dz, f.dist));
+		}
+	}
+}
+
+__global__ void __launch_bounds__(kTraceThreads) k_occluded_w(const uint4* __restrict__ wn, int nwnodes,
+                                                              const float4* __restrict__ tris, int ntris,
+                                                              const float4* __restrict__ rays, uint32_t n,
+                                                              uint8_t* __restrict__ occ, uint32_t* counter) {
+	const int lane = threadIdx.x & 31;
+	while (true) {
+		uint32_t base = warp_fetch(counter);
+		if (base >= n) break;
+		uint32_t i = base + lane;
+		if (i >= n) continue;
+		RayState r;
+		load_ray(rays, i, r);
+		float tbest = r.tmax;
+		uint32_t best_tri = 0xFFFFFFFFu;
+		bool overflow = false;
+		int slot = -1;
+		if (r.tmin <= r.tmax) slot = traverse_wide<true>(wn, tris, r, nwnodes, ntris, tbest, best_tri, overflow);
+		if (overflow) atomicOr(counter + 1, (uint32_t)RRG_ERR_STACK);
+		occ[i] = slot >= 0 ? 1 : 0;
+	}
+}
+
 // Closest hit over a batch of meshes in one persistent launch.  Ray i
 // belongs to mesh m = segment_of(ray_off, nmesh, i) (offsets staged in
 // shared memory) and is traced from that mesh's root, node m; its hit
 // triangle is reported as an index local to mesh m.  A warp takes
 // 32 * fetch consecutive rays per atomic (the rays-per-warp knob).
+template <bool WIDE>
 __global__ void __launch_bounds__(kTraceThreads) k_batch_closest(const TNode* __restrict__ nodes, int nnodes,
+                                                                 const uint4* __restrict__ wn, int nwnodes,
                                                                  const float4* __restrict__ tris, int ntris,
                                                                  const float4* __restrict__ rays, uint32_t n,
                                                                  const uint32_t* __restrict__ ray_off,
@@ -127,8 +191,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_batch_closest(const TNode* __
 			uint32_t best_tri = 0xFFFFFFFFu;
 			bool overflow = false;
 			int slot = -1;
-			if (r.tmin <= r.tmax)
-				slot = traverse<false>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow, nullptr, (int)m);
+			if (r.tmin <= r.tmax) {
+				if (WIDE) slot = traverse_wide<false>(wn, tris, r, nwnodes, ntris, tbest, best_tri, overflow, (int)m);
+				else slot = traverse<false>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow, nullptr, (int)m);
+			}
 			if (overflow) atomicOr(counter + 1, (uint32_t)RRG_ERR_STACK);
 			if (slot < 0) {
 				hits[i] = make_float4(0.f, __int_as_float((int)0xFFFFFFFFu), 0.f, 0.f);
@@ -346,6 +412,8 @@ int trace_occupancy(Collider* c) {
 	c->occl_blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
 	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_ww<false>, kTraceThreads, 0));
 	c->ww_blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_closest_w, kTraceThreads, 0));
+	c->wide_blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
 	return RRG_OK;
 }
 
@@ -354,6 +422,13 @@ int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, fl
 	if (!n) return RRG_OK;
 	RRG_CUDA(cudaMemsetAsync(c->d_counter, 0, 4, s));
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
+	if (c->width == 8 && c->d_wnodes) {
+		int grid = (int)(want < (uint32_t)c->wide_blocks ? want : (uint32_t)c->wide_blocks);
+		k_closest_w<<<grid, kTraceThreads, 0, s>>>(c->d_wnodes, (int)c->nwnodes, c->d_wtris, (int)c->nvalid, rays, n,
+		                                           hits, planes, points, c->d_counter);
+		RRG_CUDA(cudaGetLastError());
+		return RRG_OK;
+	}
 	if (c->traversal != RRG_TRAVERSAL_IF_IF) {
 		int grid = (int)(want < (uint32_t)c->ww_blocks ? want : (uint32_t)c->ww_blocks);
 		k_trace_ww<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays,
@@ -371,6 +446,13 @@ int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, c
 	if (!n) return RRG_OK;
 	RRG_CUDA(cudaMemsetAsync(c->d_counter, 0, 4, s));
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
+	if (c->width == 8 && c->d_wnodes) {
+		int grid = (int)(want < (uint32_t)c->wide_blocks ? want : (uint32_t)c->wide_blocks);
+		k_occluded_w<<<grid, kTraceThreads, 0, s>>>(c->d_wnodes, (int)c->nwnodes, c->d_wtris, (int)c->nvalid, rays,
+		                                            n, occ, c->d_counter);
+		RRG_CUDA(cudaGetLastError());
+		return RRG_OK;
+	}
 	if (c->traversal != RRG_TRAVERSAL_IF_IF) {
 		int grid = (int)(want < (uint32_t)c->ww_blocks ? want : (uint32_t)c->ww_blocks);
 		k_trace_ww<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays,
@@ -408,8 +490,12 @@ int launch_rrray_scratch(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit
 
 int batch_trace_blocks(Collider* c, uint32_t nmesh, int* blocks) {
 	int per_sm = 0;
-	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_closest, kTraceThreads,
-	                                                       sizeof(uint32_t) * (nmesh + 1)));
+	if (c->width == 8)
+		RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_closest<true>, kTraceThreads,
+		                                                       sizeof(uint32_t) * (nmesh + 1)));
+	else
+		RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_closest<false>, kTraceThreads,
+		                                                       sizeof(uint32_t) * (nmesh + 1)));
 	*blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
 	return RRG_OK;
 }
@@ -423,9 +509,15 @@ int launch_batch_closest(Collider* c, const float4* rays, uint32_t n, const uint
 	const uint32_t per_fetch = 32u * (uint32_t)fetch;
 	const uint32_t want = (uint32_t)(((uint64_t)n + per_fetch - 1) / per_fetch * 32 / kTraceThreads + 1);
 	const int grid = (int)(want < (uint32_t)blocks ? want : (uint32_t)blocks);
-	k_batch_closest<<<grid, kTraceThreads, sizeof(uint32_t) * (nmesh + 1), s>>>(
-	    c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n, ray_off, c->d_tri_off, nmesh, fetch, hits,
-	    c->d_counter);
+	const size_t smem = sizeof(uint32_t) * (nmesh + 1);
+	if (c->width == 8 && c->d_wnodes)
+		k_batch_closest<true><<<grid, kTraceThreads, smem, s>>>(c->d_nodes, (int)c->nnodes, c->d_wnodes,
+		                                                       (int)c->nwnodes, c->d_wtris, (int)c->nvalid, rays, n,
+		                                                       ray_off, c->d_tri_off, nmesh, fetch, hits, c->d_counter);
+	else
+		k_batch_closest<false><<<grid, kTraceThreads, smem, s>>>(c->d_nodes, (int)c->nnodes, c->d_wnodes,
+		                                                        (int)c->nwnodes, c->d_tris, (int)c->nvalid, rays, n,
+		                                                        ray_off, c->d_tri_off, nmesh, fetch, hits, c->d_counter);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }

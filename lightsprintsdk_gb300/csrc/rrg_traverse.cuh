@@ -256,4 +256,117 @@ __device__ int traverse(const TNode* __restrict__ nodes, const float4* __restric
 }
 
 
+
+// ------------------------------------------------------------ 8-wide BVH
+// Header of the node being walked: child/triangle bases and the slot codes.
+struct WideHdr {
+	uint32_t child_base, tri_base, meta_lo, meta_hi;
+};
+
+__device__ __forceinline__ uint32_t ray_octant(const RayState& r) {
+	return (r.dx < 0.f ? 1u : 0u) | (r.dy < 0.f ? 2u : 0u) | (r.dz < 0.f ? 4u : 0u);
+}
+
+__device__ __forceinline__ float qbyte(uint32_t lo4, uint32_t hi4, int s) {
+	return (float)(((s < 4 ? lo4 : hi4) >> (8 * (s & 3))) & 0xFFu);
+}
+
+// Tests the ray against the eight child boxes of wide node `node`; returns
+// the hit children as a mask in visiting order (bit i = slot i ^ oct) and
+// the node header.  Each quantised bound is p + q 2^e, so its ray distance
+// is fma(q, 2^e / d, (p - o) / d): one FMA per bound after per-node set-up.
+__device__ __forceinline__ uint32_t wide_visit(const uint4* __restrict__ wn, uint32_t node, const RayState& r,
+                                               uint32_t oct, float tbest, WideHdr& h) {
+	const uint4* np = wn + 5 * (size_t)node;
+	const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+	h.child_base = w1.x;
+	h.tri_base = w1.y;
+	h.meta_lo = w1.z;
+	h.meta_hi = w1.w;
+	const uint32_t ev = w0.w;
+	const float sx = __uint_as_float((ev & 0xFFu) << 23);
+	const float sy = __uint_as_float(((ev >> 8) & 0xFFu) << 23);
+	const float sz = __uint_as_float(((ev >> 16) & 0xFFu) << 23);
+	const uint32_t valid = ev >> 24;
+	const float ax = sx * r.ix, ay = sy * r.iy, az = sz * r.iz;
+	const float bx = fmaf(__uint_as_float(w0.x), r.ix, -r.oix);
+	const float by = fmaf(__uint_as_float(w0.y), r.iy, -r.oiy);
+	const float bz = fmaf(__uint_as_float(w0.z), r.iz, -r.oiz);
+	uint32_t mask = 0;
+#pragma unroll
+	for (int s = 0; s < 8; s++) {
+		const float tx0 = fmaf(qbyte(w2.x, w2.y, s), ax, bx), tx1 = fmaf(qbyte(w3.z, w3.w, s), ax, bx);
+		const float ty0 = fmaf(qbyte(w2.z, w2.w, s), ay, by), ty1 = fmaf(qbyte(w4.x, w4.y, s), ay, by);
+		const float tz0 = fmaf(qbyte(w3.x, w3.y, s), az, bz), tz1 = fmaf(qbyte(w4.z, w4.w, s), az, bz);
+		const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), r.tmin));
+		const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tbest));
+		const bool hit = ((valid >> s) & 1u) && tn <= tf * 1.0000004f;
+		mask |= (hit ? 1u : 0u) << (s ^ oct);
+	}
+	return mask;
+}
+
+// Closest (ANY = any) hit over the 8-wide tree from root node `root`.  The
+// current node's remaining hit children are a mask; when an inner child is
+// entered, the rest of the mask is pushed as one 32-bit entry (24-bit node
+// index, 8-bit mask), so the stack holds at most one entry per level.
+template <bool ANY>
+__device__ int traverse_wide(const uint4* __restrict__ wn, const float4* __restrict__ tris, const RayState& r,
+                             int nwnodes, int ntris, float& tbest, uint32_t& best_tri, bool& overflow, int root = 0) {
+	uint32_t stack[kStackSize];
+	int sp = 0;
+	int best_slot = -1;
+	const uint32_t oct = ray_octant(r);
+	if (root < 0 || root >= nwnodes) { overflow = true; return -1; }
+	uint32_t node = (uint32_t)root;
+	WideHdr h;
+	uint32_t mask = wide_visit(wn, node, r, oct, tbest, h);
+	for (uint32_t steps = 0;; steps++) {
+		if (steps >= kMaxSteps) { overflow = true; break; }
+		if (mask) {
+			const uint32_t i = __ffs(mask) - 1;
+			mask &= mask - 1;
+			const uint32_t slot = i ^ oct;
+			const uint32_t m = ((slot < 4 ? h.meta_lo : h.meta_hi) >> (8 * (slot & 3))) & 0xFFu;
+			if (m & 0x80u) {
+				const uint32_t child = h.child_base + (m & 7u);
+				if (child >= (uint32_t)nwnodes) { overflow = true; break; }
+				if (mask) {
+					if (sp < kStackSize) stack[sp++] = node | (mask << 24);
+					else { overflow = true; break; }
+				}
+				node = child;
+				mask = wide_visit(wn, node, r, oct, tbest, h);
+			} else {
+				const int first = (int)(h.tri_base + (m & 31u));
+				const int count = (int)(m >> 5) + 1;
+				if (first + count > ntris) { overflow = true; break; }
+				for (int k = 0; k < count; k++) {
+					float4 a, b, c;
+					load_tri(tris, first + k, a, b, c);
+					const uint32_t tri = (uint32_t)__float_as_int(a.w);
+					float t;
+					if (tri_test(r, a, b, c, tbest, tri, best_tri, t)) {
+						tbest = t;
+						best_tri = tri;
+						best_slot = first + k;
+						if (ANY) return best_slot;
+					}
+				}
+			}
+			continue;
+		}
+		if (sp == 0) break;
+		const uint32_t e = stack[--sp];
+		node = e & 0xFFFFFFu;
+		mask = e >> 24;
+		const uint4 w1 = __ldg(wn + 5 * (size_t)node + 1);
+		h.child_base = w1.x;
+		h.tri_base = w1.y;
+		h.meta_lo = w1.z;
+		h.meta_hi = w1.w;
+	}
+	return best_slot;
+}
+
 }  // namespace rrg

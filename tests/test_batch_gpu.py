@@ -109,6 +109,15 @@ def test_leaf_sizes_agree(small_batch):
         b2.close()
 
 
+def test_wide_batch_matches_binary(small_batch):
+    mb, counts, rays, off, off_d, b = small_batch
+    base = run(b, rays, off_d)
+    w = rb.RRColliderBatch.from_meshes(mb, build_params={"bvh_width": 8})
+    for k in (32, 128):
+        np.testing.assert_array_equal(run(w, rays, off_d, k).view(np.uint32), base.view(np.uint32), err_msg=str(k))
+    w.close()
+
+
 def test_index_outside_its_mesh_is_invalid():
     mb = scenes.batch_meshes_c3(seed=0x5C4, nmesh=3, tri_lo=1000, tri_hi=2000)
     bad = mb.indices.copy()

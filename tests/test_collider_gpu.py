@@ -245,6 +245,44 @@ def test_traversal_variants_agree(c0):
         np.testing.assert_array_equal(a[f], b[f])
 
 
+def test_wide_bvh_matches_binary():
+    """The compressed 8-wide tree returns bit-identical closest and any hits
+    to the binary tree (leaf sizes 1..4), on config 0 and a config-1 sample."""
+    import torch
+    v0, t0 = scenes.icosphere_c0()
+    sc = scenes.interior_c1()
+    cases = [(v0, t0, scenes.shell_rays(1 << 18)),
+             (sc.vertices, sc.indices, np.concatenate([scenes.camera_rays(rows=16, cols=list(range(0, 4096, 64))),
+                                                      scenes.surface_rays(sc.vertices, sc.indices, 1 << 17),
+                                                      scenes.shadow_rays(sc.vertices, sc.indices, 1 << 16)]))]
+    for v, t, rays in cases:
+        ref = col.RRCollider.create(v, t, build_params={"bvh_width": 2})
+        a = ref.intersect_batch(rays)
+        d = torch.from_numpy(rays).cuda()
+        occ_a = torch.empty(len(rays), dtype=torch.uint8, device="cuda")
+        ref.occluded_device(d.data_ptr(), len(rays), occ_a.data_ptr())
+        for leaf in (1, 2, 4):
+            w = col.RRCollider.create(v, t, build_params={"bvh_width": 8, "max_leaf_size": leaf})
+            b = w.intersect_batch(rays)
+            assert w.status() == 0
+            for f in ("hit", "tri", "dist", "uv", "side"):
+                np.testing.assert_array_equal(a[f], b[f], err_msg=f"leaf {leaf} {f}")
+            occ_b = torch.empty_like(occ_a)
+            w.occluded_device(d.data_ptr(), len(rays), occ_b.data_ptr())
+            torch.cuda.synchronize()
+            assert torch.equal(occ_a, occ_b)
+            np.testing.assert_array_equal(occ_a.cpu().numpy().astype(bool), a["hit"])
+            w.close()
+        ref.close()
+
+
+def test_wide_rejects_large_leaves():
+    v, t = scenes.icosphere_c0()
+    with pytest.raises(col.RRGError) as e:
+        col.RRCollider.create(v, t, build_params={"bvh_width": 8, "max_leaf_size": 8})
+    assert e.value.status == 1
+
+
 def test_autotuner_picks_a_candidate(tmp_path, monkeypatch):
     from lightsprintsdk_gb300 import autotune
     monkeypatch.setenv("RRG_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
