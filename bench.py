@@ -172,9 +172,11 @@ def cpu_baseline(v, t, rays, sample: int):
                       f"{build_s:.2f} s not timed"}
 
 
-def c3_workload():
+def c3_workload(nmesh: int = 512):
+    """The config-3 meshes and per-mesh ray counts; nmesh < 512 takes the
+    first meshes' share of the same generators (a smaller profiling case)."""
     from lightsprintsdk_gb300 import scenes
-    mb = scenes.batch_meshes_c3()
+    mb = scenes.batch_meshes_c3(nmesh=nmesh)
     counts = scenes.log_uniform_counts(0xC3, 110, mb.nmesh, 4096, 4194304)
     return mb, counts
 
@@ -370,14 +372,15 @@ def run_batch(args, world, rank, local):
     from lightsprintsdk_gb300 import autotune
     from lightsprintsdk_gb300 import batch as rb
     from lightsprintsdk_gb300 import scenes
-    mb, counts = c3_workload()
+    mb, counts = c3_workload(args.meshes)
     dev = f"cuda:{local}"
     rays, off = scenes.batch_rays(mb, counts, device=dev)
     n = rays.shape[0]
     off_d = torch.from_numpy(off.astype(np.uint32)).to(dev)
     hits = torch.empty((n, 4), dtype=torch.float32, device=dev)
     tuned = autotune.tune_batch(mb, rays, off_d)
-    b = rb.RRColliderBatch.from_meshes(mb, build_params={"max_leaf_size": tuned["max_leaf_size"]})
+    b = rb.RRColliderBatch.from_meshes(mb, build_params={"max_leaf_size": tuned["max_leaf_size"],
+                                                         "bvh_width": tuned["bvh_width"]})
     b.set_rays_per_warp(tuned["rays_per_warp"])
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
@@ -449,6 +452,8 @@ def main():
     ap.add_argument("--atlases", type=int, default=0, help="c2: gather only the first N atlases")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rays", type=int, default=0, help="smaller case of the workload (profiling)")
+    ap.add_argument("--meshes", type=int, default=512, help="c3: first N meshes only (profiling)")
+    ap.add_argument("--bvh-width", type=int, default=0, choices=[0, 2, 8], help="c0/c1: BVH width (0 = default)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -477,7 +482,7 @@ def main():
 
     v, t, rays = make_workload(args.workload, args.rays)
     n = rays.shape[0]
-    c = col.RRCollider.create(v, t, device=local)
+    c = col.RRCollider.create(v, t, device=local, build_params={"bvh_width": args.bvh_width})
     build_ms = c.build_ms
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
@@ -541,7 +546,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
             "config": {"workload": WORKLOAD_DESC[args.workload], "rays_per_step": n, "triangles": int(t.shape[0]),
                        "parallelism": f"replicas x{world}", "l2": "inputs (32 B/ray) larger than L2, no flush",
-                       "hit_ratio": hits_total / n, "bvh_build_ms": build_ms, "bvh_nodes": c.nodes},
+                       "hit_ratio": hits_total / n, "bvh_build_ms": build_ms, "bvh_nodes": c.nodes,
+                       "bvh_width": args.bvh_width or 2},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None,
                          "note": f"algorithmic {BYTES_PER_RAY} B/ray; peak {peak_src}"},

@@ -139,7 +139,9 @@ RRG_API int rrg_occluded_device(rrg_collider* c, const float* rays_dev, uint32_t
 
 /* Host buffers in, host buffers out: copies the rays to the device, traces,
  * copies the hit records back and synchronises.  Uses device staging buffers
- * owned by the collider (grown on demand). */
+ * owned by the collider (grown on demand).  Batches above 4,194,304 rays go
+ * through in chunks whose copies overlap the tracing of the neighbouring
+ * chunks (the overlap needs page-locked host buffers). */
 RRG_API int rrg_intersect_host(rrg_collider* c, const float* rays_host, uint32_t n, float* hits_host, void* stream);
 
 /* rr::RRRay array on the host (128-byte stride): reads rayOrigin, rayDir,

@@ -95,15 +95,17 @@ def create_tuned(vertices, indices, sample_rays: np.ndarray, tag: str = "closest
     return c
 
 
-BATCH_RAYS_PER_WARP = (32, 64, 128)
+BATCH_RAYS_PER_WARP = (32, 128)
+# (bvh width, leaf size): the 8-wide tree takes leaves of at most 4
+BATCH_TREES = ((2, 2), (2, 4), (2, 8), (8, 2), (8, 4))
 
 
 def tune_batch(mb, rays_dev, ray_off_dev, repeats: int = 3, force: bool = False) -> dict:
-    """Leaf size x rays per warp for a mesh batch (scenes.MeshBatch), timed
+    """BVH width and leaf size x rays per warp for a mesh batch (scenes.MeshBatch), timed
     with CUDA events on the caller's device rays (all of them: the tuner
     sees the real mix of meshes and ray sets).  Remembered per GPU and
-    log2(total triangles) bucket; returns {"max_leaf_size", "rays_per_warp",
-    "grays": {...}}."""
+    log2(total triangles) bucket; returns {"bvh_width", "max_leaf_size",
+    "rays_per_warp", "grays": {...}}."""
     import torch
     from . import batch as rb
     k = key(int(mb.tri_off[-1]), "batch")
@@ -113,8 +115,8 @@ def tune_batch(mb, rays_dev, ray_off_dev, repeats: int = 3, force: bool = False)
     n = rays_dev.shape[0]
     hits = torch.empty((n, 4), dtype=torch.float32, device=rays_dev.device)
     results = {}
-    for leaf in LEAF_SIZES:
-        b = rb.RRColliderBatch.from_meshes(mb, build_params={"max_leaf_size": leaf})
+    for width, leaf in BATCH_TREES:
+        b = rb.RRColliderBatch.from_meshes(mb, build_params={"max_leaf_size": leaf, "bvh_width": width})
         for rpw in BATCH_RAYS_PER_WARP:
             b.set_rays_per_warp(rpw)
             b.intersect_device(rays_dev.data_ptr(), ray_off_dev.data_ptr(), n, hits.data_ptr())
@@ -125,10 +127,11 @@ def tune_batch(mb, rays_dev, ray_off_dev, repeats: int = 3, force: bool = False)
                 b.intersect_device(rays_dev.data_ptr(), ray_off_dev.data_ptr(), n, hits.data_ptr())
             e1.record()
             torch.cuda.synchronize()
-            results[f"leaf{leaf}_rpw{rpw}"] = n / (e0.elapsed_time(e1) / repeats * 1e-3) / 1e9
+            results[f"w{width}_leaf{leaf}_rpw{rpw}"] = n / (e0.elapsed_time(e1) / repeats * 1e-3) / 1e9
         b.close()
     best = max(results, key=results.get)
-    entry = {"max_leaf_size": int(best.split("_")[0][4:]), "rays_per_warp": int(best.split("_")[1][3:]),
+    w, leaf, rpw = best.split("_")
+    entry = {"bvh_width": int(w[1:]), "max_leaf_size": int(leaf[4:]), "rays_per_warp": int(rpw[3:]),
              "grays": results, "rays": int(n)}
     db[k] = entry
     _save(db)

@@ -25,6 +25,14 @@ void free_collider(Collider* c) {
 	cudaFree(c->d_tri_off);
 	cudaFree(c->d_wnodes);
 	cudaFree(c->d_wtris);
+	for (int k = 0; k < 3; k++) {
+		if (c->ev_in[k]) cudaEventDestroy(c->ev_in[k]);
+		if (c->ev_done[k]) cudaEventDestroy(c->ev_done[k]);
+		if (c->ev_out[k]) cudaEventDestroy(c->ev_out[k]);
+	}
+	if (c->ev_start) cudaEventDestroy(c->ev_start);
+	if (c->s_in) cudaStreamDestroy(c->s_in);
+	if (c->s_out) cudaStreamDestroy(c->s_out);
 	cudaFree(c->d_xyz);
 	cudaFree(c->d_idx);
 	cudaFree(c->d_nodes);
@@ -81,6 +89,23 @@ static int ensure_stage(Collider* c, size_t in_bytes, size_t out_bytes) {
 	account_collider(c);
 	return RRG_OK;
 }
+
+static int ensure_pipeline(Collider* c) {
+	if (c->s_in) return RRG_OK;
+	RRG_CUDA(cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking));
+	for (int k = 0; k < 3; k++) {
+		RRG_CUDA(cudaEventCreateWithFlags(&c->ev_in[k], cudaEventDisableTiming));
+		RRG_CUDA(cudaEventCreateWithFlags(&c->ev_done[k], cudaEventDisableTiming));
+		RRG_CUDA(cudaEventCreateWithFlags(&c->ev_out[k], cudaEventDisableTiming));
+	}
+	RRG_CUDA(cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming));
+	RRG_CUDA(cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking));   // last: marks the set complete
+	return RRG_OK;
+}
+
+// Rays per chunk of a pipelined host call (128 MiB of rays in, 64 MiB of
+// hits out per chunk).
+constexpr uint32_t kHostChunk = 1u << 22;
 
 }  // namespace rrg
 
@@ -237,14 +262,45 @@ int rrg_intersect_host(rrg_collider* h, const float* rays_host, uint32_t n, floa
 	if (n == 0) return RRG_OK;
 	if (!rays_host || !hits_host) return RRG_ERR_INVALID;
 	RRG_CUDA(cudaSetDevice(c->device));
-	int st = ensure_stage(c, 32 * (size_t)n, 16 * (size_t)n);
-	if (st) return st;
 	cudaStream_t s = (cudaStream_t)stream;
-	RRG_CUDA(cudaMemcpyAsync(c->d_stage_in, rays_host, 32 * (size_t)n, cudaMemcpyHostToDevice, s));
-	st = launch_closest(c, reinterpret_cast<const float4*>(c->d_stage_in), n,
-	                    reinterpret_cast<float4*>(c->d_stage_out), nullptr, nullptr, s);
+	if (n <= kHostChunk) {
+		int st = ensure_stage(c, 32 * (size_t)n, 16 * (size_t)n);
+		if (st) return st;
+		RRG_CUDA(cudaMemcpyAsync(c->d_stage_in, rays_host, 32 * (size_t)n, cudaMemcpyHostToDevice, s));
+		st = launch_closest(c, reinterpret_cast<const float4*>(c->d_stage_in), n,
+		                    reinterpret_cast<float4*>(c->d_stage_out), nullptr, nullptr, s);
+		if (st) return st;
+		RRG_CUDA(cudaMemcpyAsync(hits_host, c->d_stage_out, 16 * (size_t)n, cudaMemcpyDeviceToHost, s));
+		RRG_CUDA(cudaStreamSynchronize(s));
+		return RRG_OK;
+	}
+	// Large batches: chunks through a ring of three staging slots, rays
+	// copied in on s_in, traced on the caller's stream, hits copied out on
+	// s_out, so the copies of one chunk overlap the tracing of the next.
+	int st = ensure_stage(c, 3 * 32 * (size_t)kHostChunk, 3 * 16 * (size_t)kHostChunk);
+	if (!st) st = ensure_pipeline(c);
 	if (st) return st;
-	RRG_CUDA(cudaMemcpyAsync(hits_host, c->d_stage_out, 16 * (size_t)n, cudaMemcpyDeviceToHost, s));
+	RRG_CUDA(cudaEventRecord(c->ev_start, s));   // after the caller's earlier work on s
+	RRG_CUDA(cudaStreamWaitEvent(c->s_in, c->ev_start, 0));
+	const uint32_t nchunks = (n + kHostChunk - 1) / kHostChunk;
+	for (uint32_t k = 0; k < nchunks; k++) {
+		const int slot = (int)(k % 3);
+		const size_t base = (size_t)k * kHostChunk;
+		const uint32_t m = (uint32_t)((n - base) < kHostChunk ? (n - base) : kHostChunk);
+		float4* in = reinterpret_cast<float4*>(c->d_stage_in) + 2 * (size_t)kHostChunk * slot;
+		float4* out = reinterpret_cast<float4*>(c->d_stage_out) + (size_t)kHostChunk * slot;
+		if (k >= 3) RRG_CUDA(cudaStreamWaitEvent(c->s_in, c->ev_out[slot], 0));   // slot free again
+		RRG_CUDA(cudaMemcpyAsync(in, rays_host + 8 * base, 32 * (size_t)m, cudaMemcpyHostToDevice, c->s_in));
+		RRG_CUDA(cudaEventRecord(c->ev_in[slot], c->s_in));
+		RRG_CUDA(cudaStreamWaitEvent(s, c->ev_in[slot], 0));
+		st = launch_closest(c, in, m, out, nullptr, nullptr, s);
+		if (st) return st;
+		RRG_CUDA(cudaEventRecord(c->ev_done[slot], s));
+		RRG_CUDA(cudaStreamWaitEvent(c->s_out, c->ev_done[slot], 0));
+		RRG_CUDA(cudaMemcpyAsync(hits_host + 4 * base, out, 16 * (size_t)m, cudaMemcpyDeviceToHost, c->s_out));
+		RRG_CUDA(cudaEventRecord(c->ev_out[slot], c->s_out));
+	}
+	RRG_CUDA(cudaStreamSynchronize(c->s_out));
 	RRG_CUDA(cudaStreamSynchronize(s));
 	return RRG_OK;
 }

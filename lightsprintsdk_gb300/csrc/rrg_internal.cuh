@@ -99,6 +99,13 @@ struct Collider {
 	// 8-wide form (bvh_width 8): nodes 0..nroots-1 are roots; triangles in
 	// wide-leaf order, same 3 x float4 layout as d_tris
 	uint32_t width = 2;
+	// pipelined host calls: copy-in and copy-out streams, one event set per
+	// staging slot (created on first use)
+	cudaStream_t s_in = nullptr, s_out = nullptr;
+	cudaEvent_t ev_in[3] = {nullptr, nullptr, nullptr};
+	cudaEvent_t ev_done[3] = {nullptr, nullptr, nullptr};
+	cudaEvent_t ev_out[3] = {nullptr, nullptr, nullptr};
+	cudaEvent_t ev_start = nullptr;
 	uint4* d_wnodes = nullptr;    // 5 per node
 	float4* d_wtris = nullptr;    // 3*nvalid
 	uint32_t nwnodes = 0;

@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_occluded(const TNode* __restr
 }
 
 // The same two kernels over the 8-wide tree (traverse_wide).
-__global__ void __launch_bounds__(kTraceThreads) k_closest_w(const uint4* __restrict__ wn, int nwnodes,
+__global__ void __launch_bounds__(kTraceThreads, 8) k_closest_w(const uint4* __restrict__ wn, int nwnodes,
                                                              const float4* __restrict__ tris, int ntris,
                                                              const float4* __restrict__ rays, uint32_t n,
                                                              float4* __restrict__ hits, float4* __restrict__ planes,
@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_closest_w(const uint4* __rest
 	}
 }
 
-__global__ void __launch_bounds__(kTraceThreads) k_occluded_w(const uint4* __restrict__ wn, int nwnodes,
+__global__ void __launch_bounds__(kTraceThreads, 8) k_occluded_w(const uint4* __restrict__ wn, int nwnodes,
                                                               const float4* __restrict__ tris, int ntris,
                                                               const float4* __restrict__ rays, uint32_t n,
                                                               uint8_t* __restrict__ occ, uint32_t* counter) {

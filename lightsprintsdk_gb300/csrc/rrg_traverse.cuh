@@ -267,8 +267,12 @@ __device__ __forceinline__ uint32_t ray_octant(const RayState& r) {
 	return (r.dx < 0.f ? 1u : 0u) | (r.dy < 0.f ? 2u : 0u) | (r.dz < 0.f ? 4u : 0u);
 }
 
+// Byte s of an 8-byte quantised bound as a float, without an integer to
+// float conversion: one byte permute builds the bits of 2^23 + q, and
+// subtracting 2^23 is exact.
 __device__ __forceinline__ float qbyte(uint32_t lo4, uint32_t hi4, int s) {
-	return (float)(((s < 4 ? lo4 : hi4) >> (8 * (s & 3))) & 0xFFu);
+	const uint32_t bits = __byte_perm(s < 4 ? lo4 : hi4, 0x4B000000u, (uint32_t)(s & 3) | 0x7540u);
+	return __uint_as_float(bits) - 8388608.0f;
 }
 
 // Tests the ray against the eight child boxes of wide node `node`; returns

@@ -245,6 +245,33 @@ def test_traversal_variants_agree(c0):
         np.testing.assert_array_equal(a[f], b[f])
 
 
+def test_host_pipeline_matches_device():
+    """rrg_intersect_host above one 4 Mi-ray chunk (pipelined copies, three
+    staging slots reused) returns what rrg_intersect_device returns."""
+    import torch
+    v, t = scenes.icosphere_c0()
+    c = col.RRCollider.create(v, t)
+    rng = np.random.default_rng(5)
+    n = 3 * (1 << 22) + 12345
+    rays = np.empty((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(-2.5, 2.5, (n, 3))
+    d = rng.normal(size=(n, 3))
+    rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays[:, 3] = 0.0
+    rays[:, 7] = 10.0
+    h_rays = torch.from_numpy(rays).pin_memory()
+    h_hits = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    for _ in range(2):
+        h_hits.fill_(3.0)
+        assert col._lib().rrg_intersect_host(c.handle, h_rays.data_ptr(), n, h_hits.data_ptr(), None) == 0
+        d_rays = h_rays.cuda()
+        d_hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+        c.intersect_device(d_rays.data_ptr(), n, d_hits.data_ptr())
+        torch.cuda.synchronize()
+        assert torch.equal(h_hits.view(torch.int32), d_hits.cpu().view(torch.int32))
+    assert c.status() == 0
+
+
 def test_wide_bvh_matches_binary():
     """The compressed 8-wide tree returns bit-identical closest and any hits
     to the binary tree (leaf sizes 1..4), on config 0 and a config-1 sample."""
