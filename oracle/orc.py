@@ -57,6 +57,8 @@ def lib():
         L.orc_hash.restype = C.c_uint64
         L.orc_mlp_encode.argtypes = [P, P, P, P, P, P]
         L.orc_mlp_grad.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P]
+        L.orc_mlp_encode_hash.argtypes = [P, P, P, P, P, P, P, C.c_uint32, P]
+        L.orc_mlp_grad_hash.argtypes = [P, P, P, C.c_uint32, P, P, P, P, P, P, C.c_int, C.c_int, P, P, P, P]
         L.orc_bf16.argtypes = [C.c_double]
         L.orc_bf16.restype = C.c_double
         _lib = L
@@ -221,3 +223,48 @@ def mlp_grad(W, X, T, bf16: bool = True):
     Y = np.zeros((B, 3), np.float32)
     lib().orc_mlp_grad(_ptr(W), _ptr(X), _ptr(T), B, int(bf16), _ptr(dW), _ptr(loss), _ptr(Y))
     return dW, float(loss[0]), Y
+
+
+def hashgrid_res(levels: int = 16, min_res: float = 16.0, max_res: float = 1024.0) -> np.ndarray:
+    """Per-level grid resolutions of the hash encoding (rr_mlp.c):
+    floor(min_res * b^l), b = (max_res / min_res)^(1 / (levels - 1))."""
+    b = np.exp((np.log(max_res) - np.log(min_res)) / (levels - 1))
+    return np.floor(min_res * b ** np.arange(levels)).astype(np.int32)
+
+
+def mlp_encode_hash(p, n, alb, lo, ie, table, res, T):
+    """Hash-grid encoded inputs (B, 64) in double (rr_mlp.c)."""
+    p = np.ascontiguousarray(p, np.float32).reshape(-1, 3)
+    n = np.ascontiguousarray(n, np.float32).reshape(-1, 3)
+    alb = np.ascontiguousarray(alb, np.float32).reshape(-1, 3)
+    lo = np.ascontiguousarray(lo, np.float32)
+    ie = np.ascontiguousarray(ie, np.float32)
+    table = np.ascontiguousarray(table, np.float32)
+    res = np.ascontiguousarray(res, np.int32)
+    out = np.zeros((p.shape[0], 64), np.float64)
+    L = lib()
+    for i in range(p.shape[0]):
+        L.orc_mlp_encode_hash(_ptr(p[i]), _ptr(n[i]), _ptr(alb[i]), _ptr(lo), _ptr(ie), _ptr(table), _ptr(res), T,
+                              out[i].ctypes.data_as(C.c_void_p))
+    return out
+
+
+def mlp_grad_hash(W, table, res, T, lo, ie, p, n, alb, t, bf16: bool = True):
+    """(dW, dTable, loss, Y) of the hash-grid network (rr_mlp.c)."""
+    W = np.ascontiguousarray(W, np.float32)
+    table = np.ascontiguousarray(table, np.float32)
+    res = np.ascontiguousarray(res, np.int32)
+    lo = np.ascontiguousarray(lo, np.float32)
+    ie = np.ascontiguousarray(ie, np.float32)
+    p = np.ascontiguousarray(p, np.float32)
+    n = np.ascontiguousarray(n, np.float32)
+    alb = np.ascontiguousarray(alb, np.float32)
+    t = np.ascontiguousarray(t, np.float32)
+    B = p.shape[0]
+    dW = np.zeros(W.shape[0], np.float64)
+    dT = np.zeros(table.shape[0], np.float64)
+    loss = np.zeros(1, np.float64)
+    Y = np.zeros((B, 3), np.float32)
+    lib().orc_mlp_grad_hash(_ptr(W), _ptr(table), _ptr(res), T, _ptr(lo), _ptr(ie), _ptr(p), _ptr(n), _ptr(alb),
+                            _ptr(t), B, int(bf16), _ptr(dW), _ptr(dT), _ptr(loss), _ptr(Y))
+    return dW, dT, float(loss[0]), Y
