@@ -17,6 +17,15 @@ from . import lightmap as lm
 REC_DTYPE = np.dtype([("p", "<f4", 3), ("n", "<f4", 3), ("alb", "<f4", 3), ("t", "<f4", 3)])   # 48 bytes
 NPARAMS = 4 * 64 * 64 + 64 * 16
 
+FREQUENCY, HASHGRID = 0, 1      # RRG_CACHE_*
+
+
+class CacheParams(C.Structure):
+    _fields_ = [("size", C.c_uint32), ("encoding", C.c_uint32), ("lo", C.c_float * 3), ("hi", C.c_float * 3),
+                ("seed", C.c_uint64), ("log2_table", C.c_uint32), ("min_res", C.c_float), ("max_res", C.c_float),
+                ("reserved", C.c_uint32 * 4)]
+
+
 _bound = False
 
 
@@ -26,6 +35,13 @@ def _lib():
     if not _bound:
         P, U, U64 = C.c_void_p, C.c_uint32, C.c_uint64
         L.rrg_cache_create.argtypes = [P, P, U64, C.POINTER(P)]
+        L.rrg_cache_create_ex.argtypes = [C.POINTER(CacheParams), C.POINTER(P)]
+        L.rrg_cache_table_floats.argtypes = [P]
+        L.rrg_cache_table_floats.restype = U64
+        L.rrg_cache_get_table.argtypes = [P, P]
+        L.rrg_cache_set_table.argtypes = [P, P]
+        L.rrg_cache_get_resolutions.argtypes = [P, P]
+        L.rrg_cache_gradient_ex.argtypes = [P, P, U, P, P, P, P]
         L.rrg_cache_destroy.argtypes = [P]
         L.rrg_cache_destroy.restype = None
         L.rrg_cache_set_weights.argtypes = [P, P]
@@ -51,20 +67,59 @@ def _check(st, what):
 
 
 class RadianceCache:
-    def __init__(self, lo, hi, seed: int = 1):
+    """encoding: FREQUENCY or HASHGRID (log2_table entries per level, grid
+    resolutions min_res..max_res); see include/rrgpu_cache.h."""
+
+    def __init__(self, lo, hi, seed: int = 1, encoding: int = FREQUENCY, log2_table: int = 19,
+                 min_res: float = 16.0, max_res: float = 1024.0):
         lo = np.ascontiguousarray(lo, np.float32)
         hi = np.ascontiguousarray(hi, np.float32)
+        p = CacheParams()
+        p.size = C.sizeof(CacheParams)
+        p.encoding = encoding
+        for k in range(3):
+            p.lo[k] = float(lo[k])
+            p.hi[k] = float(hi[k])
+        p.seed = seed
+        p.log2_table = log2_table
+        p.min_res = min_res
+        p.max_res = max_res
         h = C.c_void_p()
-        _check(_lib().rrg_cache_create(lo.ctypes.data, hi.ctypes.data, seed, C.byref(h)), "rrg_cache_create")
+        _check(_lib().rrg_cache_create_ex(C.byref(p), C.byref(h)), "rrg_cache_create_ex")
         self._h = h
         self.lo, self.hi = lo, hi
+        self.encoding = encoding
 
     @classmethod
-    def for_scene(cls, vertices, seed: int = 1, pad: float = 1e-3):
+    def for_scene(cls, vertices, seed: int = 1, pad: float = 1e-3, **kw):
         v = np.asarray(vertices, np.float32)
         lo, hi = v.min(0), v.max(0)
         ext = hi - lo
-        return cls(lo - pad * ext, hi + pad * ext, seed)
+        return cls(lo - pad * ext, hi + pad * ext, seed, **kw)
+
+    @property
+    def inv_extent(self) -> np.ndarray:
+        """1 / (hi - lo) in float32, as the library computes it."""
+        return (np.float32(1.0) / (self.hi - self.lo).astype(np.float32)).astype(np.float32)
+
+    @property
+    def table_floats(self) -> int:
+        return int(_lib().rrg_cache_table_floats(self._h))
+
+    def get_table(self) -> np.ndarray:
+        t = np.zeros(self.table_floats, np.float32)
+        _check(_lib().rrg_cache_get_table(self._h, t.ctypes.data), "get_table")
+        return t
+
+    def set_table(self, t) -> None:
+        t = np.ascontiguousarray(t, np.float32)
+        assert t.shape == (self.table_floats,)
+        _check(_lib().rrg_cache_set_table(self._h, t.ctypes.data), "set_table")
+
+    def resolutions(self) -> np.ndarray:
+        r = np.zeros(16, np.float32)
+        _check(_lib().rrg_cache_get_resolutions(self._h, r.ctypes.data), "get_resolutions")
+        return r
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -102,6 +157,18 @@ class RadianceCache:
         _check(_lib().rrg_cache_gradient(self._h, recs.ctypes.data, B, g.ctypes.data, loss.ctypes.data,
                                          pred.ctypes.data), "rrg_cache_gradient")
         return g, float(loss[0]), pred
+
+    def gradient_ex(self, recs: np.ndarray):
+        """gradient() plus the hash table's gradient: (grad, table_grad, loss, pred)."""
+        recs = np.ascontiguousarray(recs, REC_DTYPE)
+        B = recs.shape[0]
+        g = np.zeros(NPARAMS, np.float32)
+        tg = np.zeros(self.table_floats, np.float32)
+        loss = np.zeros(1, np.float32)
+        pred = np.zeros((B, 3), np.float32)
+        _check(_lib().rrg_cache_gradient_ex(self._h, recs.ctypes.data, B, g.ctypes.data, tg.ctypes.data,
+                                            loss.ctypes.data, pred.ctypes.data), "rrg_cache_gradient_ex")
+        return g, tg, float(loss[0]), pred
 
     def train(self, recs_ptr: int, nrec: int, batch: int = 16384, steps: int = 1, stream: int = 0) -> float:
         loss = np.zeros(1, np.float32)

@@ -15,6 +15,8 @@
 // memory, activations in registers from input to output.
 #include "rrg_internal.cuh"
 #include "rrg_mlp.cuh"
+
+#include <math.h>
 #include "../../include/rrgpu_cache.h"
 
 namespace rrg {
@@ -98,7 +100,7 @@ __device__ __forceinline__ uint32_t batch_index(uint64_t seed, uint64_t step, ui
 __global__ void k_mlp_fwd_bwd(const CacheRec* __restrict__ recs, uint32_t nrec, uint32_t B, uint64_t seed, uint64_t step,
                               const uint32_t* __restrict__ order, const uint32_t* __restrict__ fwd,
                               const uint32_t* __restrict__ bwd, MlpBuffers buf, float lo0, float lo1, float lo2,
-                              float ie0, float ie1, float ie2, float* __restrict__ pred) {
+                              float ie0, float ie1, float ie2, float* __restrict__ pred, HashGrid hg) {
 	const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
 	const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const uint32_t ntiles = B / 16;
@@ -109,7 +111,8 @@ __global__ void k_mlp_fwd_bwd(const CacheRec* __restrict__ recs, uint32_t nrec, 
 		int r = lane & 15;
 		uint32_t idx = batch_index(seed, step, row0 + r, nrec, order);
 		const CacheRec rec = recs[idx];
-		mlp_encode_half(rec.p, rec.n, rec.alb, lo, ie, lane >> 4, buf.X + (size_t)(row0 + r) * 32);
+		if (hg.table) mlp_encode_half_hash(rec.p, rec.n, rec.alb, lo, ie, hg, lane >> 4, buf.X + (size_t)(row0 + r) * 32);
+		else mlp_encode_half(rec.p, rec.n, rec.alb, lo, ie, lane >> 4, buf.X + (size_t)(row0 + r) * 32);
 	}
 	__syncwarp();
 	uint32_t a[4][4];
@@ -172,7 +175,28 @@ __global__ void k_mlp_fwd_bwd(const CacheRec* __restrict__ recs, uint32_t nrec, 
 			c_to_a<false>(acc[2 * kt], acc[2 * kt + 1], a[kt]);
 			store_a_rows(buf.dZ[l], row0, a[kt], kt);
 		}
-		if (l == 0) break;
+		if (l == 0) {
+			if (hg.table) {
+				// input gradient of the 32 hash features, dX = dZ_0 W_0^T
+				// (columns 0..31 = n-tiles 0..3), scattered to the table:
+				// n-tile nt holds level 4 nt + q for rows g and g + 8
+#pragma unroll
+				for (int nt = 0; nt < 4; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+#pragma unroll
+				for (int kt = 0; kt < 4; kt++)
+#pragma unroll
+					for (int nt = 0; nt < 4; nt++) {
+						const uint2 b = *reinterpret_cast<const uint2*>(bwd + mlp_frag_off(0) + ((kt * 8 + nt) * 32 + lane) * 2);
+						mma16816(acc[nt], a[kt], b.x, b.y);
+					}
+#pragma unroll
+				for (int nt = 0; nt < 4; nt++) {
+					hash_backward(recs[ia].p, lo, ie, hg, 4 * nt + q, acc[nt][0], acc[nt][1]);
+					hash_backward(recs[ib].p, lo, ie, hg, 4 * nt + q, acc[nt][2], acc[nt][3]);
+				}
+			}
+			break;
+		}
 		// dH_l = dZ_l W_l^T (K = 64)
 #pragma unroll
 		for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
@@ -261,12 +285,37 @@ __global__ void k_mlp_adam(float* __restrict__ w, float* __restrict__ m, float* 
 	w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
+// Hash table: uniform in [-1e-4, 1e-4] (the initialisation of the hash
+// encoding's paper), and Adam with the network's hyper-parameters.
+__global__ void k_table_init(float* __restrict__ t, uint64_t n, uint64_t seed) {
+	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+		uint64_t h = mlp_mix(mlp_mix(i ^ (seed * 0xD1B54A32D192ED03ULL)) + 0x632BE59BD9B4E019ULL);
+		float u = (float)(h >> 40) * (1.0f / 16777216.0f);
+		t[i] = (2.f * u - 1.f) * 1e-4f;
+	}
+}
+
+__global__ void k_table_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                             float* __restrict__ grad, uint64_t n, float lr, float b1, float b2, float eps, float c1,
+                             float c2) {
+	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+		float gr = grad[i];
+		grad[i] = 0.f;
+		if (!isfinite(gr)) continue;
+		float mi = b1 * m[i] + (1.f - b1) * gr;
+		float vi = b2 * v[i] + (1.f - b2) * gr * gr;
+		m[i] = mi;
+		v[i] = vi;
+		w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+	}
+}
+
 // Inference: warp per 16 records.  out[i] = (rgb clamped >= 0, valid flag).
 constexpr int kInferWarps = 8;
 __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_infer(const CacheRec* __restrict__ recs, uint64_t n,
                                                                 const uint32_t* __restrict__ fwd_g, float lo0,
                                                                 float lo1, float lo2, float ie0, float ie1, float ie2,
-                                                                float4* __restrict__ out) {
+                                                                float4* __restrict__ out, HashGrid hg) {
 	extern __shared__ uint32_t smem[];
 	uint32_t* fwd = smem;                                   // kMlpFragWords
 	uint32_t* tiles = smem + kMlpFragWords;                  // kInferWarps x 16 x 32 words
@@ -286,7 +335,8 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_infer(const CacheRec* 
 			else {
 				for (int k = 0; k < 3; k++) { rec.p[k] = lo[k]; rec.n[k] = 0.f; rec.alb[k] = 0.f; rec.t[k] = 0.f; }
 			}
-			mlp_encode_half(rec.p, rec.n, rec.alb, lo, ie, lane >> 4, tile + r * 32);
+			if (hg.table) mlp_encode_half_hash(rec.p, rec.n, rec.alb, lo, ie, hg, lane >> 4, tile + r * 32);
+			else mlp_encode_half(rec.p, rec.n, rec.alb, lo, ie, lane >> 4, tile + r * 32);
 		}
 		__syncwarp();
 		uint32_t x[4][4];
@@ -333,6 +383,13 @@ struct RadianceCache {
 	uint8_t* grid = nullptr;       // reliability per cell
 	int grid_res = 0;
 	float lr = 5e-3f, b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
+	// hash-grid encoding (hg.table == nullptr: frequency encoding)
+	HashGrid hg{};
+	float* table = nullptr;        // kHashLevels x T x 2
+	float* tm = nullptr;
+	float* tv = nullptr;
+	float* tgrad = nullptr;
+	uint64_t table_floats = 0;
 };
 
 static void free_cache(RadianceCache* C) {
@@ -343,6 +400,7 @@ static void free_cache(RadianceCache* C) {
 	for (int i = 0; i < 5; i++) cudaFree(C->buf.dZ[i]);
 	cudaFree(C->buf.grad); cudaFree(C->buf.loss);
 	cudaFree(C->grid);
+	cudaFree(C->table); cudaFree(C->tm); cudaFree(C->tv); cudaFree(C->tgrad);
 	delete C;
 }
 
@@ -376,7 +434,8 @@ static int fwd_bwd(RadianceCache* C, const CacheRec* recs, uint32_t nrec, uint32
 	if (st) return st;
 	const int warps = B / 16;
 	k_mlp_fwd_bwd<<<(warps + 3) / 4, 128, 0, s>>>(recs, nrec, B, seed, C->steps, order, C->fwd, C->bwd, C->buf,
-	                                              C->lo[0], C->lo[1], C->lo[2], C->ie[0], C->ie[1], C->ie[2], pred);
+	                                              C->lo[0], C->lo[1], C->lo[2], C->ie[0], C->ie[1], C->ie[2], pred,
+	                                              C->hg);
 	k_mlp_wgrad<<<5 * (B / kWgRows), 128, 0, s>>>(C->buf, B);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
@@ -483,8 +542,28 @@ int rrg_cache_build_error_grid(rrg_cache* h, const void* recs_dev, uint64_t nrec
 }
 
 int rrg_cache_create(const float* lo, const float* hi, uint64_t seed, rrg_cache** out) {
-	if (!out || !lo || !hi) return RRG_ERR_INVALID;
+	if (!lo || !hi) return RRG_ERR_INVALID;
+	rrg_cache_params p{};
+	p.size = sizeof(p);
+	for (int k = 0; k < 3; k++) { p.lo[k] = lo[k]; p.hi[k] = hi[k]; }
+	p.seed = seed;
+	p.encoding = RRG_CACHE_FREQUENCY;
+	return rrg_cache_create_ex(&p, out);
+}
+
+int rrg_cache_create_ex(const rrg_cache_params* params, rrg_cache** out) {
+	if (!out || !params) return RRG_ERR_INVALID;
 	*out = nullptr;
+	if (params->size < sizeof(rrg_cache_params)) return RRG_ERR_INVALID;
+	if (params->encoding != RRG_CACHE_FREQUENCY && params->encoding != RRG_CACHE_HASHGRID) return RRG_ERR_INVALID;
+	const float* lo = params->lo;
+	const float* hi = params->hi;
+	const uint64_t seed = params->seed;
+	const uint32_t log2T = params->log2_table ? params->log2_table : 19;
+	const float min_res = params->min_res > 0.f ? params->min_res : 16.f;
+	const float max_res = params->max_res > 0.f ? params->max_res : 1024.f;
+	if (params->encoding == RRG_CACHE_HASHGRID && (log2T < 10 || log2T > 24 || !(max_res >= min_res) || min_res < 2.f))
+		return RRG_ERR_INVALID;
 	RadianceCache* C = new RadianceCache();
 	RRG_CUDA(cudaGetDevice(&C->device));
 	cudaDeviceProp prop;
@@ -509,9 +588,62 @@ int rrg_cache_create(const float* lo, const float* hi, uint64_t seed, rrg_cache*
 	if (e == cudaSuccess) e = cudaMemset(C->buf.grad, 0, sizeof(float) * kMlpParams);
 	if (e != cudaSuccess) { free_cache(C); return cuda_fail(e); }
 	k_mlp_init<<<(kMlpParams + 255) / 256, 256>>>(C->w, seed);
+	if (params->encoding == RRG_CACHE_HASHGRID) {
+		const uint32_t T = 1u << log2T;
+		C->table_floats = (uint64_t)kHashLevels * T * 2;
+		const size_t bytes = sizeof(float) * C->table_floats;
+		e = cudaMalloc(&C->table, bytes);
+		if (e == cudaSuccess) e = cudaMalloc(&C->tm, bytes);
+		if (e == cudaSuccess) e = cudaMalloc(&C->tv, bytes);
+		if (e == cudaSuccess) e = cudaMalloc(&C->tgrad, bytes);
+		if (e == cudaSuccess) e = cudaMemset(C->tm, 0, bytes);
+		if (e == cudaSuccess) e = cudaMemset(C->tv, 0, bytes);
+		if (e == cudaSuccess) e = cudaMemset(C->tgrad, 0, bytes);
+		if (e != cudaSuccess) { free_cache(C); return cuda_fail(e); }
+		k_table_init<<<C->num_sms * 8, 256>>>(C->table, C->table_floats, seed);
+		C->hg.table = reinterpret_cast<const float2*>(C->table);
+		C->hg.tgrad = C->tgrad;
+		C->hg.T = T;
+		C->hg.dense = 0;
+		// resolutions floor(min_res b^l), b = (max_res / min_res)^(1/15), as
+		// oracle/rr_mlp.c and oracle/orc.py::hashgrid_res compute them
+		const double b = exp((log((double)max_res) - log((double)min_res)) / (kHashLevels - 1));
+		for (int l = 0; l < kHashLevels; l++) {
+			const double r = floor((double)min_res * pow(b, (double)l));
+			C->hg.res[l] = (float)r;
+			const double n1 = r + 1.0;
+			if (n1 * n1 * n1 <= (double)T) C->hg.dense |= 1u << l;
+		}
+	}
 	int st = pack(C, nullptr);
 	if (st) { free_cache(C); return st; }
 	*out = reinterpret_cast<rrg_cache*>(C);
+	return RRG_OK;
+}
+
+uint64_t rrg_cache_table_floats(const rrg_cache* h) {
+	const RadianceCache* C = reinterpret_cast<const RadianceCache*>(h);
+	return C ? C->table_floats : 0;
+}
+
+int rrg_cache_get_table(rrg_cache* h, float* host) {
+	RadianceCache* C = reinterpret_cast<RadianceCache*>(h);
+	if (!C || !host || !C->table) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaMemcpy(host, C->table, sizeof(float) * C->table_floats, cudaMemcpyDeviceToHost));
+	return RRG_OK;
+}
+
+int rrg_cache_set_table(rrg_cache* h, const float* host) {
+	RadianceCache* C = reinterpret_cast<RadianceCache*>(h);
+	if (!C || !host || !C->table) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaMemcpy(C->table, host, sizeof(float) * C->table_floats, cudaMemcpyHostToDevice));
+	return RRG_OK;
+}
+
+int rrg_cache_get_resolutions(const rrg_cache* h, float* res16) {
+	const RadianceCache* C = reinterpret_cast<const RadianceCache*>(h);
+	if (!C || !res16 || !C->table) return RRG_ERR_INVALID;
+	for (int l = 0; l < kHashLevels; l++) res16[l] = C->hg.res[l];
 	return RRG_OK;
 }
 
@@ -546,8 +678,15 @@ int rrg_cache_set_adam(rrg_cache* h, float lr, float beta1, float beta2, float e
 
 int rrg_cache_gradient(rrg_cache* h, const void* recs_host, uint32_t B, float* grad_host, float* loss_host,
                        float* pred_host) {
+	return rrg_cache_gradient_ex(h, recs_host, B, grad_host, nullptr, loss_host, pred_host);
+}
+
+int rrg_cache_gradient_ex(rrg_cache* h, const void* recs_host, uint32_t B, float* grad_host, float* table_grad_host,
+                          float* loss_host, float* pred_host) {
 	RadianceCache* C = reinterpret_cast<RadianceCache*>(h);
 	if (!C || !recs_host || !grad_host || B == 0 || B % kWgRows) return RRG_ERR_INVALID;
+	if (table_grad_host && !C->table) return RRG_ERR_INVALID;
+	if (C->tgrad) RRG_CUDA(cudaMemset(C->tgrad, 0, sizeof(float) * C->table_floats));
 	CacheRec* d = nullptr;
 	uint32_t* order = nullptr;
 	float* pred = nullptr;
@@ -566,7 +705,10 @@ int rrg_cache_gradient(rrg_cache* h, const void* recs_host, uint32_t B, float* g
 		RRG_CUDA(cudaMemcpy(grad_host, C->buf.grad, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost));
 		if (loss_host) RRG_CUDA(cudaMemcpy(loss_host, C->buf.loss, sizeof(float), cudaMemcpyDeviceToHost));
 		if (pred_host) RRG_CUDA(cudaMemcpy(pred_host, pred, sizeof(float) * 3 * B, cudaMemcpyDeviceToHost));
+		if (table_grad_host)
+			RRG_CUDA(cudaMemcpy(table_grad_host, C->tgrad, sizeof(float) * C->table_floats, cudaMemcpyDeviceToHost));
 		RRG_CUDA(cudaMemset(C->buf.grad, 0, sizeof(float) * kMlpParams));
+		if (C->tgrad) RRG_CUDA(cudaMemset(C->tgrad, 0, sizeof(float) * C->table_floats));
 	}
 	cudaFree(d);
 	cudaFree(order);
@@ -587,6 +729,9 @@ int rrg_cache_train(rrg_cache* h, const void* recs_dev, uint32_t nrec, uint32_t 
 		float c1 = 1.f - powf(C->b1, (float)C->steps), c2 = 1.f - powf(C->b2, (float)C->steps);
 		k_mlp_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(C->w, C->m, C->v, C->buf.grad, C->lr, C->b1, C->b2,
 		                                                    C->eps, c1, c2);
+		if (C->table)
+			k_table_adam<<<C->num_sms * 8, 256, 0, s>>>(C->table, C->tm, C->tv, C->tgrad, C->table_floats, C->lr,
+			                                           C->b1, C->b2, C->eps, c1, c2);
 		st = pack(C, s);
 		if (st) return st;
 	}
@@ -613,7 +758,7 @@ int rrg_cache_infer(rrg_cache* h, const void* recs_dev, uint64_t n, float* out_d
 	uint64_t cap = (uint64_t)C->num_sms * 4;
 	k_mlp_infer<<<(int)(blocks < cap ? blocks : cap), kInferWarps * 32, smem, (cudaStream_t)stream>>>(
 	    reinterpret_cast<const CacheRec*>(recs_dev), n, C->fwd, C->lo[0], C->lo[1], C->lo[2], C->ie[0], C->ie[1],
-	    C->ie[2], reinterpret_cast<float4*>(out_dev));
+	    C->ie[2], reinterpret_cast<float4*>(out_dev), C->hg);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }

@@ -96,7 +96,7 @@ __device__ __forceinline__ void mlp_forward_tile(const uint32_t (*x)[4], const u
 	mlp_layer<2>(a, fwd + mlp_frag_off(4), out);
 }
 
-// Encoding of one sample into 64 bf16 features (see oracle/rr_mlp.c);
+// Frequency encoding of one sample into 64 bf16 features (see oracle/rr_mlp.c);
 // `half` 0 writes words 0..15 (features 0..31), 1 words 16..31.
 __device__ __forceinline__ void mlp_encode_half(const float* p, const float* n, const float* alb, const float* lo,
                                                 const float* inv_ext, int half, uint32_t* row_words) {
@@ -135,6 +135,112 @@ __device__ __forceinline__ void mlp_encode_half(const float* p, const float* n, 
 struct CacheRec {
 	float p[3], n[3], alb[3], t[3];
 };
+
+// ------------------------------------------------------ hash-grid encoding
+// Multiresolution hash encoding (specified in oracle/rr_mlp.c): 16 levels x
+// 2 features from trilinearly interpolated table entries, 4 octaves of
+// frequency encoding, normal, albedo, bias.  table == nullptr selects the
+// frequency encoding above.
+constexpr int kHashLevels = 16;
+
+struct HashGrid {
+	const float2* table;   // kHashLevels x T entries of 2 features
+	float* tgrad;          // same layout, gradient (training only)
+	uint32_t T;            // entries per level (power of two)
+	uint32_t dense;        // bit l: level l indexed densely ((res+1)^3 <= T)
+	float res[kHashLevels];
+};
+
+// Corner c (0..7) of level l: table index (within the level) and weight.
+struct HashCorners {
+	uint32_t x0[3];
+	float w[3];
+};
+
+__device__ __forceinline__ HashCorners hash_cell(const float* p, const float* lo, const float* ie, float res) {
+	HashCorners h;
+	const int n = (int)res;
+#pragma unroll
+	for (int j = 0; j < 3; j++) {
+		float v = __fmul_rn(__fsub_rn(p[j], lo[j]), ie[j]);
+		float u = fminf(fmaxf(v, 0.f), 1.f);
+		float x = __fmul_rn(u, res);
+		int f = (int)floorf(x);
+		f = f < 0 ? 0 : (f > n - 1 ? n - 1 : f);
+		h.x0[j] = (uint32_t)f;
+		h.w[j] = __fsub_rn(x, (float)f);
+	}
+	return h;
+}
+
+__device__ __forceinline__ uint32_t hash_index(const HashGrid& g, int l, uint32_t ix, uint32_t iy, uint32_t iz) {
+	if ((g.dense >> l) & 1u) {
+		const uint32_t n1 = (uint32_t)g.res[l] + 1u;
+		return ix + iy * n1 + iz * n1 * n1;
+	}
+	return (ix ^ (iy * 2654435761u) ^ (iz * 805459861u)) & (g.T - 1u);
+}
+
+__device__ __forceinline__ float hash_weight(const HashCorners& h, int c) {
+	const float wx = (c & 1) ? h.w[0] : __fsub_rn(1.f, h.w[0]);
+	const float wy = (c & 2) ? h.w[1] : __fsub_rn(1.f, h.w[1]);
+	const float wz = (c & 4) ? h.w[2] : __fsub_rn(1.f, h.w[2]);
+	return __fmul_rn(__fmul_rn(wx, wy), wz);
+}
+
+// Encoding with the hash grid; `half` 0 writes words 0..15 (the 16 levels'
+// feature pairs), 1 words 16..31 (frequencies, normal, albedo, bias).
+__device__ __forceinline__ void mlp_encode_half_hash(const float* p, const float* n, const float* alb,
+                                                     const float* lo, const float* ie, const HashGrid& g, int half,
+                                                     uint32_t* row_words) {
+	if (half == 0) {
+		for (int l = 0; l < kHashLevels; l++) {
+			const HashCorners h = hash_cell(p, lo, ie, g.res[l]);
+			const float2* tl = g.table + (size_t)l * g.T;
+			float f0 = 0.f, f1 = 0.f;
+#pragma unroll
+			for (int c = 0; c < 8; c++) {
+				const uint32_t idx = hash_index(g, l, h.x0[0] + (c & 1), h.x0[1] + ((c >> 1) & 1),
+				                                h.x0[2] + ((c >> 2) & 1));
+				const float wc = hash_weight(h, c);
+				const float2 e = __ldg(tl + idx);
+				f0 = fmaf(wc, e.x, f0);
+				f1 = fmaf(wc, e.y, f1);
+			}
+			row_words[l] = pack_bf16(f0, f1);
+		}
+	} else {
+#pragma unroll
+		for (int j = 0; j < 3; j++) {
+			float u = fminf(fmaxf(__fmul_rn(__fsub_rn(p[j], lo[j]), ie[j]), 0.f), 1.f);
+#pragma unroll
+			for (int k = 0; k < 4; k++) {
+				float s, c;
+				sincospif((float)(1 << k) * u, &s, &c);
+				row_words[16 + 4 * j + k] = pack_bf16(s, c);
+			}
+		}
+		row_words[28] = pack_bf16(n[0], n[1]);
+		row_words[29] = pack_bf16(n[2], alb[0]);
+		row_words[30] = pack_bf16(alb[1], alb[2]);
+		row_words[31] = pack_bf16(1.f, 0.f);
+	}
+}
+
+// Scatter of the input gradient of level l's two features for one sample
+// to the 8 corners (atomics; the table gradient is zeroed by the optimiser).
+__device__ __forceinline__ void hash_backward(const float* p, const float* lo, const float* ie, const HashGrid& g,
+                                              int l, float d0, float d1) {
+	const HashCorners h = hash_cell(p, lo, ie, g.res[l]);
+	float* tl = g.tgrad + (size_t)l * g.T * 2;
+#pragma unroll
+	for (int c = 0; c < 8; c++) {
+		const uint32_t idx = hash_index(g, l, h.x0[0] + (c & 1), h.x0[1] + ((c >> 1) & 1), h.x0[2] + ((c >> 2) & 1));
+		const float wc = hash_weight(h, c);
+		atomicAdd(tl + 2 * idx, wc * d0);
+		atomicAdd(tl + 2 * idx + 1, wc * d1);
+	}
+}
 
 }  // namespace rrg
 

@@ -250,7 +250,7 @@ def mlp_encode_hash(p, n, alb, lo, ie, table, res, T):
 
 
 def mlp_grad_hash(W, table, res, T, lo, ie, p, n, alb, t, bf16: bool = True):
-    """(dW, dTable, loss, Y) of the hash-grid network (rr_mlp.c)."""
+    """(dW, dTable, loss, Y) of the hash-grid network (rr_mlp.c); Y in double."""
     W = np.ascontiguousarray(W, np.float32)
     table = np.ascontiguousarray(table, np.float32)
     res = np.ascontiguousarray(res, np.int32)
@@ -264,7 +264,7 @@ def mlp_grad_hash(W, table, res, T, lo, ie, p, n, alb, t, bf16: bool = True):
     dW = np.zeros(W.shape[0], np.float64)
     dT = np.zeros(table.shape[0], np.float64)
     loss = np.zeros(1, np.float64)
-    Y = np.zeros((B, 3), np.float32)
+    Y = np.zeros((B, 3), np.float64)
     lib().orc_mlp_grad_hash(_ptr(W), _ptr(table), _ptr(res), T, _ptr(lo), _ptr(ie), _ptr(p), _ptr(n), _ptr(alb),
                             _ptr(t), B, int(bf16), _ptr(dW), _ptr(dT), _ptr(loss), _ptr(Y))
     return dW, dT, float(loss[0]), Y

@@ -199,11 +199,12 @@ void orc_mlp_encode_hash(const float* p, const float* n, const float* alb, const
 
 /* orc_mlp_grad with the hash-grid encoding computed here from the records
  * (P, N, A: B x 3 floats; T3: B x 3 targets): dW as orc_mlp_grad, and
- * dTable (levels x T x 2 doubles, zeroed here) the table gradient.  With
+ * dTable (levels x T x 2 doubles, zeroed here) the table gradient; Y (B x 3
+ * doubles, may be NULL) the outputs.  With
  * bf16 the encoded inputs, weights and deltas are rounded as on the GPU. */
 void orc_mlp_grad_hash(const float* W, const float* table, const int* res, uint32_t T, const float* lo,
                        const float* ie, const float* P, const float* N, const float* A, const float* T3, int B,
-                       int bf16, double* dW, double* dTable, double* loss, float* Y) {
+                       int bf16, double* dW, double* dTable, double* loss, double* Y) {
 	double* w = (double*)malloc(sizeof(double) * NPARAM);
 	for (int i = 0; i < NPARAM; i++) w[i] = bf16 ? orc_bf16(W[i]) : W[i];
 	memset(dW, 0, sizeof(double) * NPARAM);
@@ -237,7 +238,7 @@ void orc_mlp_grad_hash(const float* W, const float* table, const int* res, uint3
 			double den = y[c] * y[c] + 0.01;
 			L += (y[c] - t) * (y[c] - t) / den / B;
 			dy[c] = 2 * (y[c] - t) / den / B;
-			if (Y) Y[3 * b + c] = (float)y[c];
+			if (Y) Y[3 * b + c] = y[c];
 		}
 		for (int c = 0; c < 16; c++) d[4][c] = bf16 ? orc_bf16(dy[c]) : dy[c];
 		for (int l = 4; l >= 0; l--) {

@@ -64,3 +64,79 @@ def test_bf16_emulation_close_to_exact():
     assert abs(l16 - l64) < 0.02 * l64
     assert orc.lib().orc_bf16(1.0 + 2 ** -9) == 1.0            # ties to even
     assert orc.lib().orc_bf16(1.0 + 3 * 2 ** -9) == 1.0 + 2 ** -7
+
+
+# ------------------------------------------------------------ hash grid
+HT = 1 << 14
+
+
+def hash_problem(B=48, seed=5):
+    rng = np.random.default_rng(seed)
+    W = np.concatenate([rng.uniform(-0.2, 0.2, 4 * 4096), rng.uniform(-0.27, 0.27, 1024)]).astype(np.float32)
+    table = rng.uniform(-0.5, 0.5, 16 * HT * 2).astype(np.float32)
+    p = rng.uniform(-1, 1, (B, 3)).astype(np.float32)
+    n = rng.normal(size=(B, 3)).astype(np.float32)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    alb = rng.uniform(0.2, 0.8, (B, 3)).astype(np.float32)
+    t = rng.uniform(0, 2, (B, 3)).astype(np.float32)
+    lo = np.full(3, -1, np.float32)
+    ie = np.full(3, 0.5, np.float32)
+    return W, table, orc.hashgrid_res(), lo, ie, p, n, alb, t
+
+
+def test_hashgrid_resolutions():
+    r = orc.hashgrid_res()
+    assert r[0] == 16 and r[-1] in (1023, 1024) and np.all(np.diff(r) > 0)
+    b = (1024 / 16) ** (1 / 15)
+    np.testing.assert_array_equal(r, np.floor(16 * b ** np.arange(16)).astype(np.int32))
+
+
+def test_hash_encoding_interpolates_a_linear_table():
+    """On densely indexed levels a table holding (ix, iy) at each lattice
+    point encodes to (u_x N, u_y N): trilinear interpolation is exact on a
+    linear field."""
+    res = orc.hashgrid_res()
+    table = np.zeros(16 * HT * 2, np.float32)
+    dense = [l for l in range(16) if (res[l] + 1) ** 3 <= HT]
+    assert dense == [0, 1]
+    for l in dense:
+        n1 = res[l] + 1
+        iz, iy, ix = np.meshgrid(np.arange(n1), np.arange(n1), np.arange(n1), indexing="ij")
+        idx = (ix + iy * n1 + iz * n1 * n1).ravel()
+        table[(l * HT + idx) * 2] = ix.ravel()
+        table[(l * HT + idx) * 2 + 1] = iy.ravel()
+    rng = np.random.default_rng(2)
+    p = rng.uniform(-1, 1, (20, 3)).astype(np.float32)
+    lo = np.full(3, -1, np.float32)
+    ie = np.full(3, 0.5, np.float32)
+    X = orc.mlp_encode_hash(p, np.zeros((20, 3)), np.zeros((20, 3)), lo, ie, table, res, HT)
+    u = (p - lo) * ie
+    for l in dense:
+        np.testing.assert_allclose(X[:, 2 * l], u[:, 0] * res[l], atol=1e-4)
+        np.testing.assert_allclose(X[:, 2 * l + 1], u[:, 1] * res[l], atol=1e-4)
+    np.testing.assert_allclose(X[:, 62], 1.0)
+    np.testing.assert_allclose(X[:, 32], np.sin(np.pi * u[:, 0].astype(np.float64)), atol=1e-6)
+
+
+def test_hash_table_gradient_matches_finite_differences():
+    W, table, res, lo, ie, p, n, alb, t = hash_problem()
+    dW, dT, loss, Y0 = orc.mlp_grad_hash(W, table, res, HT, lo, ie, p, n, alb, t, bf16=False)
+    B = p.shape[0]
+    den = Y0.astype(np.float64) ** 2 + 0.01
+    touched = np.nonzero(dT)[0]
+    assert touched.size > 1000
+    rng = np.random.default_rng(3)
+    errs = []
+    for i in rng.choice(touched, 12, replace=False):
+        h = 1e-3
+        tp, tm = table.copy(), table.copy()
+        tp[i] += h
+        tm[i] -= h
+        _, _, _, Yp = orc.mlp_grad_hash(W, tp, res, HT, lo, ie, p, n, alb, t, bf16=False)
+        _, _, _, Ym = orc.mlp_grad_hash(W, tm, res, HT, lo, ie, p, n, alb, t, bf16=False)
+        Lp = (((Yp - t) ** 2) / den).sum() / B
+        Lm = (((Ym - t) ** 2) / den).sum() / B
+        fd = (Lp - Lm) / (float(tp[i]) - float(tm[i]))
+        errs.append(abs(fd - dT[i]) / abs(dT[i]))
+    # relu kinks inside +-h can move a few; the bulk agrees to FD precision
+    assert np.median(errs) < 1e-3 and max(errs) < 0.1, errs
