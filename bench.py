@@ -285,6 +285,47 @@ def gather_cpu_baseline(gs, L, nsample: int = 4096):
             "sample": f"{len(tids)} covered texels (every {step}th), quality 64, 8 bounces"}
 
 
+def rel_rmse_blocks(x, ref, size: int, block: int = 1) -> float:
+    """Relative RMSE of RGB over covered texels (ref alpha > 0); block > 1
+    compares sums over block x block texel tiles (noise averages out, bias
+    stays)."""
+    m = ref[:, 3] > 0
+    if block == 1:
+        d = (x[m, :3] - ref[m, :3]).astype(np.float64)
+        return float(np.sqrt((d ** 2).sum() / (ref[m, :3].astype(np.float64) ** 2).sum()))
+    g = size // block
+
+    def tiles(y):
+        y = y[:, :3].astype(np.float64).reshape(size, size, 3) * m.reshape(size, size, 1)
+        return y.reshape(g, block, g, block, 3).sum((1, 3))
+    xb, rb = tiles(x), tiles(ref)
+    return float(np.sqrt(((xb - rb) ** 2).sum() / (rb ** 2).sum()))
+
+
+def learned_errors(L, gs, params, out, natl, stream, sp, atlases=(0, 9, 100), seeds: int = 16):
+    """Errors of the learned bake (in `out`) and of the plain 64-sample
+    gather against a converged plain gather (`seeds` x quality 256 =
+    4,096 samples per texel) on three atlases: per texel and per 8 x 8
+    block."""
+    from lightsprintsdk_gb300 import lightmap as lm
+    S = gs.size * gs.size
+    res = {"reference": f"plain gather, {seeds} x 256 samples per texel", "per_atlas": {}}
+    tot = {"learned": [0.0, 0.0], "plain64": [0.0, 0.0]}
+    for a in atlases:
+        if a >= natl:
+            continue
+        ref = np.zeros((S, 4))
+        for k in range(seeds):
+            ref += L.gather(lm.make_params(gs.lights, quality=256, max_depth=8, seed=1000 + k), a * S, S)
+        ref /= seeds
+        pl = L.gather(params, a * S, S)
+        le = out[a * S:(a + 1) * S].cpu().numpy()
+        res["per_atlas"][str(a)] = {
+            "learned": [rel_rmse_blocks(le, ref, gs.size), rel_rmse_blocks(le, ref, gs.size, 8)],
+            "plain64": [rel_rmse_blocks(pl, ref, gs.size), rel_rmse_blocks(pl, ref, gs.size, 8)]}
+    return {"errors_vs_converged": res}
+
+
 def run_gather(args, world, rank, local):
     """Config 2: plain 8-bounce lightmap gather, 64 rays per texel, 256 atlases
     of 256 x 256 texels on the interior scene."""
@@ -337,25 +378,29 @@ def run_gather(args, world, rank, local):
     L.check(sp)
     ms = e0.elapsed_time(e1) / steps
     covered = int((out[:, 3] > 0).sum().item())
+    if learned and rank == 0:
+        # the plain gather of the same texels, timed the same way, for the ratio
+        plain_out = torch.empty_like(out)
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        L.gather_device(params, 0, n, plain_out.data_ptr(), sp)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        extra["plain_texels_per_s"] = n / (p0.elapsed_time(p1) * 1e-3)
+        extra["speedup_vs_plain"] = (n / (ms * 1e-3)) / extra["plain_texels_per_s"]
+        del plain_out
     if learned:
-        # error against the plain 64-sample gather on atlases 0, 9, 100 (same first-bounce streams)
-        errs = {}
-        for a in (0, 9, 100):
-            if a >= natl:
-                continue
-            pl = L.gather(params, a * S, S)
-            le = out[a * S:(a + 1) * S].cpu().numpy()
-            m = pl[:, 3] > 0
-            d = (le[m, :3] - pl[m, :3]).astype(np.float64)
-            errs[str(a)] = float(np.sqrt((d ** 2).sum() / (pl[m, :3].astype(np.float64) ** 2).sum()))
-        extra["rel_rmse_vs_plain64"] = errs
+        extra.update(learned_errors(L, gs, params, out, natl, stream, sp))
     if rank == 0:
         metric = "learned lightmap texels/s" if learned else "plain lightmap texels/s"
         line = {"metric": metric, "value": world * n / (ms * 1e-3), "unit": "texels/s",
                 "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded generators)",
-                "config": {"workload": f"plain gather, quality 64, 8 bounces, {natl} atlases of 256x256 on the "
+                "config": {"workload": (("learned gather (1 traced segment + radiance cache, fallback to the plain "
+                                         "gather), ") if learned else "plain gather, ") +
+                                       f"quality 64, 8 bounces, {natl} atlases of 256x256 on the "
                                        f"{gs.scene.ntri}-triangle interior", "texels": n, "covered": covered,
                            "subtexels": L.nsubtexels, "enumeration_s": enum_s, **extra},
                 "gpu_launches": steps, "clocks": clk.summary()}

@@ -78,6 +78,13 @@ RRG_API uint64_t rrg_cache_steps(const rrg_cache* c);
  * (may be NULL) receives the number of reliable cells. */
 RRG_API int rrg_cache_build_error_grid(rrg_cache* c, const void* recs_dev, uint64_t nrec, uint32_t res,
                                        float rel_threshold, uint32_t min_count, uint32_t* nreliable, void* stream);
+/* Same, with the tolerance also at least the standard deviation of the
+ * cell's targets over sqrt(plain_samples): a cell whose bias is below the
+ * noise of the plain gather's plain_samples-sample mean is kept, because
+ * falling back would add more error than it removes (0 = off). */
+RRG_API int rrg_cache_build_error_grid_ex(rrg_cache* c, const void* recs_dev, uint64_t nrec, uint32_t res,
+                                          float rel_threshold, uint32_t min_count, float plain_samples,
+                                          uint32_t* nreliable, void* stream);
 
 #ifdef __cplusplus
 }

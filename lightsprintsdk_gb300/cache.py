@@ -53,6 +53,7 @@ def _lib():
         L.rrg_cache_steps.argtypes = [P]
         L.rrg_cache_steps.restype = U64
         L.rrg_cache_build_error_grid.argtypes = [P, P, U64, U, C.c_float, U, P, P]
+        L.rrg_cache_build_error_grid_ex.argtypes = [P, P, U64, U, C.c_float, U, C.c_float, P, P]
         L.rrg_lightmapper_covered.argtypes = [P]
         L.rrg_lightmapper_covered.restype = U64
         L.rrg_lightmap_train_samples.argtypes = [P, C.POINTER(lm.GatherParams), U, U, P, U64, P, P]
@@ -180,10 +181,10 @@ class RadianceCache:
         _check(_lib().rrg_cache_infer(self._h, recs_ptr, n, out_ptr, stream or None), "rrg_cache_infer")
 
     def build_error_grid(self, recs_ptr: int, nrec: int, res: int = 32, rel_threshold: float = 0.25,
-                         min_count: int = 32, stream: int = 0) -> int:
+                         min_count: int = 32, stream: int = 0, plain_samples: float = 0.0) -> int:
         n = np.zeros(1, np.uint32)
-        _check(_lib().rrg_cache_build_error_grid(self._h, recs_ptr, nrec, res, rel_threshold, min_count,
-                                                 n.ctypes.data, stream or None), "build_error_grid")
+        _check(_lib().rrg_cache_build_error_grid_ex(self._h, recs_ptr, nrec, res, rel_threshold, min_count,
+                                                    plain_samples, n.ctypes.data, stream or None), "build_error_grid")
         return int(n[0])
 
 
@@ -211,9 +212,12 @@ def gather_learned(L: lm.RRLightmapper, cache: RadianceCache, params, first: int
 def bake_learned(L: lm.RRLightmapper, cache: RadianceCache, params, first: int, count: int, out_ptr: int,
                  stride: int = 16, paths_per_texel: int = 4, batch: int = 16384, steps: int = 300,
                  grid_res: int = 32, rel_threshold: float = 0.25, min_count: int = 32,
-                 fallback_frac: float = 0.25, stream: int = 0, use_fallback: bool = True):
+                 fallback_frac: float = 0.25, stream: int = 0, use_fallback: bool = True,
+                 noise_aware: bool = True):
     """Online bake: training records from the gather's own paths, `steps`
     Adam steps, the error grid, then the learned gather with fallback.
+    noise_aware: a cell falls back only when the cache's bias there exceeds
+    the noise of the plain gather's quality-sample mean too.
     Returns a dict of counts and the last training loss."""
     import torch
     ncov = covered(L)
@@ -222,7 +226,7 @@ def bake_learned(L: lm.RRLightmapper, cache: RadianceCache, params, first: int, 
     recs = torch.empty(cap * REC_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
     nrec = train_samples(L, params, stride, paths_per_texel, recs.data_ptr(), cap, stream)
     loss = cache.train(recs.data_ptr(), nrec, batch, steps, stream)
-    nrel = cache.build_error_grid(recs.data_ptr(), nrec, grid_res, rel_threshold, min_count, stream) \
-        if use_fallback else 0
+    nrel = cache.build_error_grid(recs.data_ptr(), nrec, grid_res, rel_threshold, min_count, stream,
+                                  float(params.quality) if noise_aware else 0.0) if use_fallback else 0
     nfb = gather_learned(L, cache, params, first, count, out_ptr, fallback_frac if use_fallback else 2.0, stream)
     return {"train_records": nrec, "loss": loss, "reliable_cells": nrel, "fallback_texels": nfb}

@@ -33,6 +33,11 @@ static void free_batch(Batch* b) {
 	delete b;
 }
 
+Collider* batch_collider(rrg_batch* h) {
+	Batch* b = reinterpret_cast<Batch*>(h);
+	return b ? b->c : nullptr;
+}
+
 static bool ascending(const uint32_t* off, uint32_t n) {
 	if (off[0] != 0) return false;
 	for (uint32_t m = 0; m < n; m++)

@@ -6,6 +6,8 @@
 
 #include "../../include/rrgpu.h"
 
+typedef struct rrg_batch rrg_batch;
+
 namespace rrg {
 
 // ---------------------------------------------------------------- layout
@@ -127,6 +129,8 @@ int launch_rrray_scratch(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit
 int trace_occupancy(Collider* c);
 // batches (nmesh roots): ray i belongs to mesh segment_of(ray_off, nmesh, i)
 constexpr uint32_t kBatchMaxMeshes = 8192;
+// the collider holding a batch's meshes (rrg_batch.cu)
+Collider* batch_collider(::rrg_batch* b);
 int batch_trace_blocks(Collider* c, uint32_t nmesh, int* blocks);
 int launch_batch_closest(Collider* c, const float4* rays, uint32_t n, const uint32_t* ray_off, uint32_t nmesh,
                          int fetch, int blocks, float4* hits, cudaStream_t s);

@@ -315,7 +315,8 @@ constexpr int kInferWarps = 8;
 __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_infer(const CacheRec* __restrict__ recs, uint64_t n,
                                                                 const uint32_t* __restrict__ fwd_g, float lo0,
                                                                 float lo1, float lo2, float ie0, float ie1, float ie2,
-                                                                float4* __restrict__ out, HashGrid hg) {
+                                                                float4* __restrict__ out, HashGrid hg,
+                                                                int all_valid) {
 	extern __shared__ uint32_t smem[];
 	uint32_t* fwd = smem;                                   // kMlpFragWords
 	uint32_t* tiles = smem + kMlpFragWords;                  // kInferWarps x 16 x 32 words
@@ -355,7 +356,9 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_infer(const CacheRec* 
 		}
 		__syncwarp();
 		if (lane < 16 && r0 + lane < n) {
-			float valid = recs[r0 + lane].t[0];
+			// queries mark validity in t[0]; training records (the error
+			// grid's input) carry targets there, all of them valid
+			float valid = all_valid ? 1.f : recs[r0 + lane].t[0];
 			float4 o;
 			o.x = valid > 0.f ? fmaxf(ftile[lane * 4 + 0], 0.f) : 0.f;
 			o.y = valid > 0.f ? fmaxf(ftile[lane * 4 + 1], 0.f) : 0.f;
@@ -466,7 +469,7 @@ __global__ void k_grid_accum(const CacheRec* __restrict__ recs, const float4* __
 // their own noise bounds what the test can resolve.
 __global__ void k_grid_flags(const float* __restrict__ st, const float* __restrict__ sp, const float* __restrict__ cnt,
                              const float* __restrict__ st2, size_t ncell, float thr, float min_count,
-                             uint8_t* __restrict__ flags, unsigned int* __restrict__ nrel) {
+                             float plain_samples, uint8_t* __restrict__ flags, unsigned int* __restrict__ nrel) {
 	size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
 	if (c >= ncell) return;
 	float n = cnt[c];
@@ -475,7 +478,11 @@ __global__ void k_grid_flags(const float* __restrict__ st, const float* __restri
 		float mt = st[c] / n, mp = sp[c] / n;
 		float var = fmaxf(st2[c] / n - mt * mt, 0.f);
 		float se = sqrtf(var / n);
-		ok = fabsf(mp - mt) <= fmaxf(thr * fmaxf(mt, 1e-4f), 3.f * se);
+		float tol = fmaxf(thr * fmaxf(mt, 1e-4f), 3.f * se);
+		// a bias below the noise of a plain_samples-sample mean of these
+		// paths costs less than falling back to that mean
+		if (plain_samples > 0.f) tol = fmaxf(tol, sqrtf(var / plain_samples));
+		ok = fabsf(mp - mt) <= tol;
 	}
 	flags[c] = ok ? 1 : 0;
 	if (ok) atomicAdd(nrel, 1u);
@@ -495,12 +502,38 @@ void cache_grid(rrg_cache* h, const uint8_t** flags, int* res, float* lo, float*
 
 using namespace rrg;
 
+static int infer_impl(RadianceCache* C, const void* recs_dev, uint64_t n, float* out_dev, int all_valid,
+                      cudaStream_t stream) {
+	if (!C || !recs_dev || !out_dev || ((uintptr_t)out_dev & 15)) return RRG_ERR_INVALID;
+	if (!n) return RRG_OK;
+	const size_t smem = sizeof(uint32_t) * (kMlpFragWords + kInferWarps * 16 * 32);
+	static bool attr = false;
+	if (!attr) {
+		RRG_CUDA(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+		attr = true;
+	}
+	uint64_t ntiles = (n + 15) / 16;
+	uint64_t blocks = (ntiles + kInferWarps - 1) / kInferWarps;
+	uint64_t cap = (uint64_t)C->num_sms * 4;
+	k_mlp_infer<<<(int)(blocks < cap ? blocks : cap), kInferWarps * 32, smem, (cudaStream_t)stream>>>(
+	    reinterpret_cast<const CacheRec*>(recs_dev), n, C->fwd, C->lo[0], C->lo[1], C->lo[2], C->ie[0], C->ie[1],
+	    C->ie[2], reinterpret_cast<float4*>(out_dev), C->hg, all_valid);
+	RRG_CUDA(cudaGetLastError());
+	return RRG_OK;
+}
+
 extern "C" {
 
 int rrg_cache_build_error_grid(rrg_cache* h, const void* recs_dev, uint64_t nrec, uint32_t res, float rel_threshold,
                                uint32_t min_count, uint32_t* nreliable, void* stream) {
+	return rrg_cache_build_error_grid_ex(h, recs_dev, nrec, res, rel_threshold, min_count, 0.f, nreliable, stream);
+}
+
+int rrg_cache_build_error_grid_ex(rrg_cache* h, const void* recs_dev, uint64_t nrec, uint32_t res,
+                                  float rel_threshold, uint32_t min_count, float plain_samples, uint32_t* nreliable,
+                                  void* stream) {
 	RadianceCache* C = reinterpret_cast<RadianceCache*>(h);
-	if (!C || !recs_dev || !nrec || res < 1 || res > 256) return RRG_ERR_INVALID;
+	if (!C || !recs_dev || !nrec || res < 1 || res > 256 || !(plain_samples >= 0.f)) return RRG_ERR_INVALID;
 	cudaStream_t s = (cudaStream_t)stream;
 	const size_t ncell = (size_t)res * res * res;
 	float4* pred = nullptr;
@@ -518,14 +551,14 @@ int rrg_cache_build_error_grid(rrg_cache* h, const void* recs_dev, uint64_t nrec
 	}
 	RRG_CUDA(cudaMemsetAsync(sums, 0, sizeof(float) * 4 * ncell, s));
 	RRG_CUDA(cudaMemsetAsync(nrel, 0, sizeof(unsigned int), s));
-	int st = rrg_cache_infer(h, recs_dev, nrec, reinterpret_cast<float*>(pred), stream);
+	int st = infer_impl(C, recs_dev, nrec, reinterpret_cast<float*>(pred), 1, s);
 	if (!st) {
 		k_grid_accum<<<C->num_sms * 8, 256, 0, s>>>(reinterpret_cast<const CacheRec*>(recs_dev), pred, nrec, (int)res,
 		                                             C->lo[0], C->lo[1], C->lo[2], C->ie[0], C->ie[1], C->ie[2], sums,
 		                                             sums + ncell, sums + 2 * ncell);
 		k_grid_flags<<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(sums, sums + ncell, sums + 2 * ncell,
 		                                                            sums + 3 * ncell, ncell, rel_threshold,
-		                                                            (float)min_count, C->grid, nrel);
+		                                                            (float)min_count, plain_samples, C->grid, nrel);
 		cudaError_t e = cudaGetLastError();
 		if (e != cudaSuccess) st = cuda_fail(e);
 	}
@@ -744,24 +777,9 @@ int rrg_cache_train(rrg_cache* h, const void* recs_dev, uint32_t nrec, uint32_t 
 }
 
 int rrg_cache_infer(rrg_cache* h, const void* recs_dev, uint64_t n, float* out_dev, void* stream) {
-	RadianceCache* C = reinterpret_cast<RadianceCache*>(h);
-	if (!C || !recs_dev || !out_dev || ((uintptr_t)out_dev & 15)) return RRG_ERR_INVALID;
-	if (!n) return RRG_OK;
-	const size_t smem = sizeof(uint32_t) * (kMlpFragWords + kInferWarps * 16 * 32);
-	static bool attr = false;
-	if (!attr) {
-		RRG_CUDA(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-		attr = true;
-	}
-	uint64_t ntiles = (n + 15) / 16;
-	uint64_t blocks = (ntiles + kInferWarps - 1) / kInferWarps;
-	uint64_t cap = (uint64_t)C->num_sms * 4;
-	k_mlp_infer<<<(int)(blocks < cap ? blocks : cap), kInferWarps * 32, smem, (cudaStream_t)stream>>>(
-	    reinterpret_cast<const CacheRec*>(recs_dev), n, C->fwd, C->lo[0], C->lo[1], C->lo[2], C->ie[0], C->ie[1],
-	    C->ie[2], reinterpret_cast<float4*>(out_dev), C->hg);
-	RRG_CUDA(cudaGetLastError());
-	return RRG_OK;
+	return infer_impl(reinterpret_cast<RadianceCache*>(h), recs_dev, n, out_dev, 0, (cudaStream_t)stream);
 }
+
 
 uint64_t rrg_cache_steps(const rrg_cache* h) {
 	const RadianceCache* C = reinterpret_cast<const RadianceCache*>(h);

@@ -268,3 +268,74 @@ def mlp_grad_hash(W, table, res, T, lo, ie, p, n, alb, t, bf16: bool = True):
     lib().orc_mlp_grad_hash(_ptr(W), _ptr(table), _ptr(res), T, _ptr(lo), _ptr(ie), _ptr(p), _ptr(n), _ptr(alb),
                             _ptr(t), B, int(bf16), _ptr(dW), _ptr(dT), _ptr(loss), _ptr(Y))
     return dW, dT, float(loss[0]), Y
+
+
+# ------------------------------------------------------------------ scenes
+def invert3x4(m: np.ndarray) -> np.ndarray:
+    """RRMatrix3x4::invertedTo (RRMath.cpp:605-628) in float32, same order of
+    operations: cofactors over the float determinant."""
+    m = np.asarray(m, np.float32).reshape(3, 4)
+    f = np.float32
+    det = f(m[0, 0] * f(m[1, 1] * m[2, 2] - m[2, 1] * m[1, 2])) + f(m[0, 1] * f(m[1, 2] * m[2, 0] - m[2, 2] * m[1, 0]))
+    det = f(det + f(m[0, 2] * f(m[1, 0] * m[2, 1] - m[2, 0] * m[1, 1])))
+    d = np.zeros((3, 4), np.float32)
+    d[0, 0] = f(m[2, 2] * m[1, 1] - m[2, 1] * m[1, 2]) / det
+    d[0, 1] = -f(m[2, 2] * m[0, 1] - m[2, 1] * m[0, 2]) / det
+    d[0, 2] = f(m[1, 2] * m[0, 1] - m[1, 1] * m[0, 2]) / det
+    d[1, 0] = -f(m[2, 2] * m[1, 0] - m[2, 0] * m[1, 2]) / det
+    d[1, 1] = f(m[2, 2] * m[0, 0] - m[2, 0] * m[0, 2]) / det
+    d[1, 2] = -f(m[1, 2] * m[0, 0] - m[1, 0] * m[0, 2]) / det
+    d[2, 0] = f(m[2, 1] * m[1, 0] - m[2, 0] * m[1, 1]) / det
+    d[2, 1] = -f(m[2, 1] * m[0, 0] - m[2, 0] * m[0, 1]) / det
+    d[2, 2] = f(m[1, 1] * m[0, 0] - m[1, 0] * m[0, 1]) / det
+    for r in range(3):
+        d[r, 3] = f(f(f(-m[0, 3]) * d[r, 0]) - f(m[1, 3] * d[r, 1])) - f(m[2, 3] * d[r, 2])
+    return d, float(det)
+
+
+def local_rays(rays: np.ndarray, inv: np.ndarray):
+    """Object-space rays of RRColliderMulti::intersect (RRColliderMulti.cpp:121-131)
+    in float32, one rounding per operation: (rays, scale)."""
+    r = np.asarray(rays, np.float32)
+    m = inv
+    o, dd = r[:, 0:3], r[:, 4:7]
+    out = np.empty_like(r)
+    for k in range(3):
+        out[:, k] = ((o[:, 0] * m[k, 0] + o[:, 1] * m[k, 1]) + o[:, 2] * m[k, 2]) + m[k, 3]
+    d = np.stack([(dd[:, 0] * m[k, 0] + dd[:, 1] * m[k, 1]) + dd[:, 2] * m[k, 2] for k in range(3)], -1)
+    scale = np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]).astype(np.float32)
+    out[:, 4:7] = d / scale[:, None]
+    out[:, 3] = r[:, 3] * scale
+    out[:, 7] = r[:, 7] * scale
+    return out, scale
+
+
+def scene_collide(meshes, obj_mesh, world, rays) -> tuple:
+    """Closest hit over objects (meshes[i] = (v, t) local; obj_mesh; world
+    (nobj, 3, 4)) as RRColliderMulti computes it, with the FASTEST oracle per
+    object: the object-space hit of each object, hitDistance / scale, the
+    nearest world distance (ties: the lower object), hitFrontSide flipped for a
+    negative determinant.  Returns (hits dict as FastestOracle.collide, object
+    per ray, 0xFFFFFFFF = none)."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    n = rays.shape[0]
+    oracles = {}
+    best = {"hit": np.zeros(n, bool), "tri": np.full(n, 0xFFFFFFFF, np.uint32),
+            "dist": np.zeros(n, np.float32), "uv": np.zeros((n, 2), np.float32), "side": np.zeros(n, bool)}
+    obj = np.full(n, 0xFFFFFFFF, np.uint32)
+    for o in range(len(obj_mesh)):
+        m = int(obj_mesh[o])
+        if m not in oracles:
+            oracles[m] = FastestOracle(*meshes[m])
+        inv, det = invert3x4(np.asarray(world[o], np.float32))
+        lr, scale = local_rays(rays, inv)
+        h = oracles[m].collide(lr, 0)
+        dw = (h["dist"] / scale).astype(np.float32)
+        take = h["hit"] & (~best["hit"] | (dw < best["dist"]))
+        best["hit"] |= take
+        best["tri"][take] = h["tri"][take]
+        best["dist"][take] = dw[take]
+        best["uv"][take] = h["uv"][take]
+        best["side"][take] = h["side"][take] ^ (det < 0)
+        obj[take] = o
+    return best, obj
