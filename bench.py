@@ -37,6 +37,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 BYTES_PER_RAY = 48          # 32 B ray in (two float4) + 16 B hit record out
+# DRAM bytes per ray of k_closest measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch / its rays): config 1 from a cold-cache
+# capture of 2 Mi rays (profiles/k_closest_binary_vs_wide_c1_2Mrays.md),
+# config 0 from the full 1 Mi-ray launch (profiles/k_closest_c0_1Mrays_dram.md);
+# the bench scales them to its launch
+MEASURED_DRAM_BYTES_PER_RAY = {"c1": 113.5, "c0": 41.2}
 C3_SAMPLE_MESHES = (0, 65, 130, 195, 260, 325, 390, 455)   # CPU-baseline sample (both mesh kinds)
 C3_SAMPLE_RAYS = 25_000                                     # rays per sampled mesh
 WORKLOAD_DESC = {
@@ -594,8 +600,13 @@ def main():
                        "hit_ratio": hits_total / n, "bvh_build_ms": build_ms, "bvh_nodes": c.nodes,
                        "bvh_width": args.bvh_width or 2},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "note": f"algorithmic {BYTES_PER_RAY} B/ray; peak {peak_src}"},
+                         "frac": achieved / peak,
+                         "traffic": (MEASURED_DRAM_BYTES_PER_RAY[args.workload] * n
+                                     if args.workload in MEASURED_DRAM_BYTES_PER_RAY and args.bvh_width != 8
+                                     else None),
+                         "note": f"algorithmic {BYTES_PER_RAY} B/ray; peak {peak_src}; traffic per launch = ncu "
+                                 f"DRAM bytes per ray of the workload's capture x rays (see profiles/); the kernel "
+                                 f"is issue-bound, so the HBM fraction is low by design"},
             "e2e": {"value": world * n / e2e_s / 1e9, "unit": "Grays/s", "h2d_bytes_per_step": 32 * n,
                     "d2h_bytes_per_step": 16 * n},
             "gpu_launches": args.steps,

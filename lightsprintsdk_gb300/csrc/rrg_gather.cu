@@ -546,6 +546,7 @@ struct WarpSmem {
 	V3 hemi[kMaxQuality];
 	V3 light[kMaxRounds][2];
 	unsigned char lit[kMaxRounds][2];
+	unsigned next;   // next unclaimed sample of the texel
 };
 
 // LEARNED = false: the plain gather, out[tid - out_base] = texel RGBA.
@@ -553,7 +554,7 @@ struct WarpSmem {
 // cache queries and out[tid - out_base] the light rounds' average (the plain
 // texel's first term) with w = 1.  list (may be null) selects texel ids.
 template <bool LEARNED>
-__global__ void __launch_bounds__(kGatherWarps * 32) k_gather(GatherScene g, const uint32_t* __restrict__ off,
+__global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, const uint32_t* __restrict__ off,
                                                               const Sub* __restrict__ st, uint64_t first,
                                                               uint64_t count, const uint32_t* __restrict__ list,
                                                               uint64_t out_base, float4* __restrict__ out,
@@ -598,7 +599,12 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(GatherScene g, con
 		float areaMax = 0.f;
 		for (uint32_t i = 0; i < m; i++) areaMax = __fadd_rn(areaMax, S[i].area);
 		const float areaStep = __fdiv_rn(areaMax, __fadd_rn((float)N, 0.91f));
-		for (uint32_t k = lane; k < N; k += 32) {
+		if (lane == 0) sm.next = 32;
+		__syncwarp();
+		// samples are claimed dynamically: a lane whose path ended early takes
+		// the next unclaimed one (results are stored per sample index and
+		// summed in index order, so the texel does not depend on who traced what)
+		for (uint32_t k = lane; k < N; k = atomicAdd(&sm.next, 1u)) {
 			// area stepping (gather.cpp:665-688), replayed up to shooter k
 			float areaAccu = -S[0].area;
 			uint32_t it = 0;
