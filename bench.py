@@ -39,8 +39,7 @@ sys.path.insert(0, ROOT)
 BYTES_PER_RAY = 48          # 32 B ray in (two float4) + 16 B hit record out
 # DRAM bytes per ray of k_closest measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch / its rays): config 1 from a cold-cache
-# capture of 2 Mi rays (profiles/k_closest_binary_vs_wide_c1_2Mrays.md),
-# config 0 from the full 1 Mi-ray launch (profiles/k_closest_c0_1Mrays_dram.md);
+# capture of 2 Mi rays, config 0 from a capture of the full 1 Mi-ray launch;
 # the bench scales them to its launch
 MEASURED_DRAM_BYTES_PER_RAY = {"c1": 113.5, "c0": 41.2}
 C3_SAMPLE_MESHES = (0, 65, 130, 195, 260, 325, 390, 455)   # CPU-baseline sample (both mesh kinds)
@@ -357,8 +356,13 @@ def run_gather(args, world, rank, local):
         from lightsprintsdk_gb300 import cache as rc
 
         def step():
-            cache = rc.RadianceCache.for_scene(gs.scene.vertices, seed=7)
-            extra.update(rc.bake_learned(L, cache, params, 0, n, out.data_ptr(), stream=sp))
+            # hash-grid cache (2^17 entries per level), 1,000 Adam steps on
+            # batches of 65,536 path vertices: of the encodings, table sizes
+            # and step counts measured, the one that kept the fallback rare
+            # with the cache's bias at the plain gather's noise level
+            cache = rc.RadianceCache.for_scene(gs.scene.vertices, seed=7, encoding=rc.HASHGRID, log2_table=17)
+            extra.update(rc.bake_learned(L, cache, params, 0, n, out.data_ptr(), stream=sp, steps=1000,
+                                         batch=65536))
     else:
         def step():
             L.gather_device(params, 0, n, out.data_ptr(), sp)
@@ -404,8 +408,9 @@ def run_gather(args, world, rank, local):
                 "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded generators)",
-                "config": {"workload": (("learned gather (1 traced segment + radiance cache, fallback to the plain "
-                                         "gather), ") if learned else "plain gather, ") +
+                "config": {"workload": (("learned gather (1 traced segment + hash-grid radiance cache trained on "
+                                         "the bake's own paths, fallback to the plain gather), ") if learned
+                                        else "plain gather, ") +
                                        f"quality 64, 8 bounces, {natl} atlases of 256x256 on the "
                                        f"{gs.scene.ntri}-triangle interior", "texels": n, "covered": covered,
                            "subtexels": L.nsubtexels, "enumeration_s": enum_s, **extra},
@@ -605,7 +610,7 @@ def main():
                                      if args.workload in MEASURED_DRAM_BYTES_PER_RAY and args.bvh_width != 8
                                      else None),
                          "note": f"algorithmic {BYTES_PER_RAY} B/ray; peak {peak_src}; traffic per launch = ncu "
-                                 f"DRAM bytes per ray of the workload's capture x rays (see profiles/); the kernel "
+                                 f"DRAM bytes per ray of the workload's ncu capture x rays; the kernel "
                                  f"is issue-bound, so the HBM fraction is low by design"},
             "e2e": {"value": world * n / e2e_s / 1e9, "unit": "Grays/s", "h2d_bytes_per_step": 32 * n,
                     "d2h_bytes_per_step": 16 * n},
