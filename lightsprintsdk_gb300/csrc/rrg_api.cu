@@ -33,6 +33,7 @@ void free_collider(Collider* c) {
 	if (c->ev_start) cudaEventDestroy(c->ev_start);
 	if (c->s_in) cudaStreamDestroy(c->s_in);
 	if (c->s_out) cudaStreamDestroy(c->s_out);
+	if (c->s_comp) cudaStreamDestroy(c->s_comp);
 	cudaFree(c->d_xyz);
 	cudaFree(c->d_idx);
 	cudaFree(c->d_nodes);
@@ -93,6 +94,7 @@ static int ensure_stage(Collider* c, size_t in_bytes, size_t out_bytes) {
 static int ensure_pipeline(Collider* c) {
 	if (c->s_in) return RRG_OK;
 	RRG_CUDA(cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking));
+	RRG_CUDA(cudaStreamCreateWithFlags(&c->s_comp, cudaStreamNonBlocking));
 	for (int k = 0; k < 3; k++) {
 		RRG_CUDA(cudaEventCreateWithFlags(&c->ev_in[k], cudaEventDisableTiming));
 		RRG_CUDA(cudaEventCreateWithFlags(&c->ev_done[k], cudaEventDisableTiming));
@@ -275,13 +277,16 @@ int rrg_intersect_host(rrg_collider* h, const float* rays_host, uint32_t n, floa
 		return RRG_OK;
 	}
 	// Large batches: chunks through a ring of three staging slots, rays
-	// copied in on s_in, traced on the caller's stream, hits copied out on
-	// s_out, so the copies of one chunk overlap the tracing of the next.
+	// copied in on s_in, traced alternately on the caller's stream and s_comp
+	// (each slot with its own work counter, so a chunk's kernel can start in
+	// the previous one's tail), hits copied out on s_out: the copies of one
+	// chunk overlap the tracing of its neighbours.
 	int st = ensure_stage(c, 3 * 32 * (size_t)kHostChunk, 3 * 16 * (size_t)kHostChunk);
 	if (!st) st = ensure_pipeline(c);
 	if (st) return st;
 	RRG_CUDA(cudaEventRecord(c->ev_start, s));   // after the caller's earlier work on s
 	RRG_CUDA(cudaStreamWaitEvent(c->s_in, c->ev_start, 0));
+	RRG_CUDA(cudaStreamWaitEvent(c->s_comp, c->ev_start, 0));
 	const uint32_t nchunks = (n + kHostChunk - 1) / kHostChunk;
 	for (uint32_t k = 0; k < nchunks; k++) {
 		const int slot = (int)(k % 3);
@@ -292,15 +297,17 @@ int rrg_intersect_host(rrg_collider* h, const float* rays_host, uint32_t n, floa
 		if (k >= 3) RRG_CUDA(cudaStreamWaitEvent(c->s_in, c->ev_out[slot], 0));   // slot free again
 		RRG_CUDA(cudaMemcpyAsync(in, rays_host + 8 * base, 32 * (size_t)m, cudaMemcpyHostToDevice, c->s_in));
 		RRG_CUDA(cudaEventRecord(c->ev_in[slot], c->s_in));
-		RRG_CUDA(cudaStreamWaitEvent(s, c->ev_in[slot], 0));
-		st = launch_closest(c, in, m, out, nullptr, nullptr, s);
+		cudaStream_t cs = (k & 1) ? c->s_comp : s;
+		RRG_CUDA(cudaStreamWaitEvent(cs, c->ev_in[slot], 0));
+		st = launch_closest_on(c, in, m, out, nullptr, nullptr, c->d_counter + 4 * slot, cs);
 		if (st) return st;
-		RRG_CUDA(cudaEventRecord(c->ev_done[slot], s));
+		RRG_CUDA(cudaEventRecord(c->ev_done[slot], cs));
 		RRG_CUDA(cudaStreamWaitEvent(c->s_out, c->ev_done[slot], 0));
 		RRG_CUDA(cudaMemcpyAsync(hits_host + 4 * base, out, 16 * (size_t)m, cudaMemcpyDeviceToHost, c->s_out));
 		RRG_CUDA(cudaEventRecord(c->ev_out[slot], c->s_out));
 	}
 	RRG_CUDA(cudaStreamSynchronize(c->s_out));
+	RRG_CUDA(cudaStreamSynchronize(c->s_comp));
 	RRG_CUDA(cudaStreamSynchronize(s));
 	return RRG_OK;
 }
@@ -337,12 +344,13 @@ int rrg_intersect_rrray(rrg_collider* h, void* rrrays_host, uint32_t n, uint8_t*
 int rrg_collider_status(rrg_collider* h, void* stream) {
 	Collider* c = reinterpret_cast<Collider*>(h);
 	if (!c) return RRG_ERR_INVALID;
-	uint32_t w = 0;
+	uint32_t w[12] = {0};
 	cudaStream_t s = (cudaStream_t)stream;
-	RRG_CUDA(cudaMemcpyAsync(&w, c->d_counter + 1, 4, cudaMemcpyDeviceToHost, s));
+	RRG_CUDA(cudaMemcpyAsync(w, c->d_counter, sizeof(w), cudaMemcpyDeviceToHost, s));
 	RRG_CUDA(cudaStreamSynchronize(s));
-	RRG_CUDA(cudaMemsetAsync(c->d_counter + 1, 0, 4, s));
-	return w ? RRG_ERR_STACK : RRG_OK;
+	// status words of the direct launches ([1]) and of the pipelined slots ([5], [9])
+	for (int k = 0; k < 3; k++) RRG_CUDA(cudaMemsetAsync(c->d_counter + 4 * k + 1, 0, 4, s));
+	return (w[1] | w[5] | w[9]) ? RRG_ERR_STACK : RRG_OK;
 }
 
 }  // extern "C"

@@ -79,7 +79,8 @@ struct Collider {
 	uint32_t* d_idx = nullptr;    // 3*nt
 	TNode* d_nodes = nullptr;
 	float4* d_tris = nullptr;     // 3*nvalid
-	uint32_t* d_counter = nullptr;// scratch: [0] ray counter, [1] status word
+	uint32_t* d_counter = nullptr;// scratch (16 words): [0] ray counter, [1] status word; pipelined
+	                              // host calls use [4k], [4k+1] for staging slot k
 	size_t bytes = 0;
 	float build_ms = 0;
 	float aabb_lo[3] = {0, 0, 0}, aabb_hi[3] = {0, 0, 0};   // all vertices
@@ -103,7 +104,7 @@ struct Collider {
 	uint32_t width = 2;
 	// pipelined host calls: copy-in and copy-out streams, one event set per
 	// staging slot (created on first use)
-	cudaStream_t s_in = nullptr, s_out = nullptr;
+	cudaStream_t s_in = nullptr, s_out = nullptr, s_comp = nullptr;
 	cudaEvent_t ev_in[3] = {nullptr, nullptr, nullptr};
 	cudaEvent_t ev_done[3] = {nullptr, nullptr, nullptr};
 	cudaEvent_t ev_out[3] = {nullptr, nullptr, nullptr};
@@ -122,6 +123,8 @@ int build_wide(Collider* c, const BNode* bnodes, int nnodes, const float* pad, c
 // trace (rrg_trace.cu)
 int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
                    cudaStream_t s);
+int launch_closest_on(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
+                      uint32_t* words, cudaStream_t s);
 int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, cudaStream_t s);
 int launch_rrray(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, cudaStream_t s);
 int launch_rrray_scratch(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, uint32_t* words,

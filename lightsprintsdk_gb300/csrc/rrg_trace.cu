@@ -417,29 +417,35 @@ int trace_occupancy(Collider* c) {
 	return RRG_OK;
 }
 
-int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
-                   cudaStream_t s) {
+// words[0] = the launch's work counter (cleared here), words[1] = its status.
+int launch_closest_on(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
+                      uint32_t* words, cudaStream_t s) {
 	if (!n) return RRG_OK;
-	RRG_CUDA(cudaMemsetAsync(c->d_counter, 0, 4, s));
+	RRG_CUDA(cudaMemsetAsync(words, 0, 4, s));
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
 	if (c->width == 8 && c->d_wnodes) {
 		int grid = (int)(want < (uint32_t)c->wide_blocks ? want : (uint32_t)c->wide_blocks);
 		k_closest_w<<<grid, kTraceThreads, 0, s>>>(c->d_wnodes, (int)c->nwnodes, c->d_wtris, (int)c->nvalid, rays, n,
-		                                           hits, planes, points, c->d_counter);
+		                                           hits, planes, points, words);
 		RRG_CUDA(cudaGetLastError());
 		return RRG_OK;
 	}
 	if (c->traversal != RRG_TRAVERSAL_IF_IF) {
 		int grid = (int)(want < (uint32_t)c->ww_blocks ? want : (uint32_t)c->ww_blocks);
 		k_trace_ww<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays,
-		                                                  n, hits, planes, points, nullptr, c->d_counter);
+		                                                  n, hits, planes, points, nullptr, words);
 		RRG_CUDA(cudaGetLastError());
 		return RRG_OK;
 	}
 	int grid = (int)(want < (uint32_t)c->trace_blocks ? want : (uint32_t)c->trace_blocks);
-	k_closest<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n, hits, planes, points, c->d_counter);
+	k_closest<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n, hits, planes, points, words);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
+}
+
+int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
+                   cudaStream_t s) {
+	return launch_closest_on(c, rays, n, hits, planes, points, c->d_counter, s);
 }
 
 int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, cudaStream_t s) {
