@@ -111,6 +111,15 @@ RRG_API int rrg_collider_update(rrg_collider* c, const float* xyz_host);
 
 RRG_API void rrg_collider_destroy(rrg_collider* c);
 
+/* Order in which a batch's rays are traced (results do not depend on it). */
+enum {
+	RRG_RAY_ORDER_DEFAULT = 0,    /* binned for batches of >= 2^22 rays, else as given */
+	RRG_RAY_ORDER_AS_GIVEN = 1,   /* trace ray i by ray i */
+	RRG_RAY_ORDER_BINNED = 2      /* always binned: one counting-sort pass groups rays by origin
+	                                 cell (8^3 over the mesh box) and direction cell (4^3) */
+};
+RRG_API int rrg_collider_set_ray_order(rrg_collider* c, uint32_t order);
+
 /* Selects the traversal kernel of later queries (RRG_TRAVERSAL_*). */
 RRG_API int rrg_collider_set_traversal(rrg_collider* c, uint32_t traversal);
 
@@ -126,7 +135,9 @@ RRG_API float rrg_collider_build_ms(const rrg_collider* c);
  * planes_dev (float4 per ray) and points_dev (float[3] per ray) are optional
  * (NULL = not written; they correspond to FILL_PLANE / FILL_POINT3D).
  * Asynchronous on `stream`; the status covers launch errors only.  Batch form
- * of RRCollider::intersect(RRRay&) (RRCollider.h:228). */
+ * of RRCollider::intersect(RRRay&) (RRCollider.h:228).  Launches on one
+ * collider share its work counter and ray-binning scratch: do not let two of
+ * them overlap on the GPU (issue them on one stream, or synchronise). */
 RRG_API int rrg_intersect_device(rrg_collider* c, const float* rays_dev, uint32_t n, float* hits_dev,
                          float* planes_dev, float* points_dev, void* stream);
 

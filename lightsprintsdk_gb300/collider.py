@@ -22,6 +22,7 @@ from . import build as _build
 # RRRay::Flags (RRCollider.h:98-106)
 FILL_DISTANCE, FILL_POINT3D, FILL_POINT2D, FILL_PLANE, FILL_TRIANGLE, FILL_SIDE = 1, 2, 4, 8, 16, 32
 FILL_ALL = 63
+RAY_ORDER_DEFAULT, RAY_ORDER_AS_GIVEN, RAY_ORDER_BINNED = 0, 1, 2
 
 # RRCollider::IntersectTechnique (RRCollider.h:156-166) plus the GPU technique
 IT_LINEAR, IT_BSP_COMPACT, IT_BSP_FAST, IT_BSP_FASTER, IT_BSP_FASTEST, IT_BVH_COMPACT, IT_BVH_FAST, IT_VERIFICATION = range(8)
@@ -86,6 +87,7 @@ def _lib():
         L.rrg_intersect_rrray_device.argtypes = [P, P, U, P, P]
         L.rrg_collider_status.argtypes = [P, P]
         L.rrg_collider_set_traversal.argtypes = [P, U]
+        L.rrg_collider_set_ray_order.argtypes = [P, U]
         L.rrg_status_string.argtypes = [I]
         L.rrg_status_string.restype = C.c_char_p
         L.rrg_last_cuda_error.restype = C.c_char_p
@@ -176,8 +178,13 @@ class RRCollider:
 
     # ------------------------------------------------------------ queries
     def set_traversal(self, traversal: int) -> None:
-        """RRG_TRAVERSAL_IF_IF (1) or RRG_TRAVERSAL_WHILE_WHILE (2, default)."""
+        """RRG_TRAVERSAL_IF_IF (1, default) or RRG_TRAVERSAL_WHILE_WHILE (2)."""
         _check(_lib().rrg_collider_set_traversal(self._h, traversal), "rrg_collider_set_traversal")
+
+    def set_ray_order(self, order: int) -> None:
+        """RAY_ORDER_DEFAULT (0: binned from 2^22 rays), RAY_ORDER_AS_GIVEN (1)
+        or RAY_ORDER_BINNED (2); results do not depend on it."""
+        _check(_lib().rrg_collider_set_ray_order(self._h, order), "rrg_collider_set_ray_order")
 
     def getTechnique(self) -> int:
         return IT_GPU

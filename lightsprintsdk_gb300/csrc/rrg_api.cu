@@ -41,6 +41,7 @@ void free_collider(Collider* c) {
 	cudaFree(c->d_counter);
 	cudaFree(c->d_stage_in);
 	cudaFree(c->d_stage_out);
+	for (int k = 0; k < 4; k++) cudaFree(c->d_bin[k]);
 	delete c;
 }
 
@@ -69,7 +70,8 @@ int init_collider(Collider* c, const rrg_build_params* params) {
 void account_collider(Collider* c) {
 	c->bytes = sizeof(float) * 3 * (size_t)c->nv + sizeof(uint32_t) * 3 * (size_t)c->nt + sizeof(TNode) * (size_t)c->nnodes +
 	           sizeof(float4) * 3 * (size_t)c->nvalid + 64 + c->stage_in_bytes + c->stage_out_bytes +
-	           (c->d_wnodes ? sizeof(uint4) * 5 * (size_t)c->nwnodes + sizeof(float4) * 3 * (size_t)c->nvalid : 0);
+	           (c->d_wnodes ? sizeof(uint4) * 5 * (size_t)c->nwnodes + sizeof(float4) * 3 * (size_t)c->nvalid : 0) +
+	           c->bin_bytes[0] + c->bin_bytes[1] + c->bin_bytes[2] + c->bin_bytes[3];
 }
 
 static int ensure_stage(Collider* c, size_t in_bytes, size_t out_bytes) {
@@ -209,6 +211,13 @@ void rrg_collider_destroy(rrg_collider* h) {
 	free_collider(c);
 }
 
+int rrg_collider_set_ray_order(rrg_collider* h, uint32_t order) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c || order > RRG_RAY_ORDER_BINNED) return RRG_ERR_INVALID;
+	c->ray_order = order;
+	return RRG_OK;
+}
+
 int rrg_collider_set_traversal(rrg_collider* h, uint32_t traversal) {
 	Collider* c = reinterpret_cast<Collider*>(h);
 	if (!c || traversal > RRG_TRAVERSAL_WHILE_WHILE) return RRG_ERR_INVALID;
@@ -299,7 +308,7 @@ int rrg_intersect_host(rrg_collider* h, const float* rays_host, uint32_t n, floa
 		RRG_CUDA(cudaEventRecord(c->ev_in[slot], c->s_in));
 		cudaStream_t cs = (k & 1) ? c->s_comp : s;
 		RRG_CUDA(cudaStreamWaitEvent(cs, c->ev_in[slot], 0));
-		st = launch_closest_on(c, in, m, out, nullptr, nullptr, c->d_counter + 4 * slot, cs);
+		st = launch_closest_on(c, in, m, out, nullptr, nullptr, c->d_counter + 4 * slot, cs, slot);
 		if (st) return st;
 		RRG_CUDA(cudaEventRecord(c->ev_done[slot], cs));
 		RRG_CUDA(cudaStreamWaitEvent(c->s_out, c->ev_done[slot], 0));

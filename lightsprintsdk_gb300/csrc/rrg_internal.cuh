@@ -109,6 +109,12 @@ struct Collider {
 	cudaEvent_t ev_done[3] = {nullptr, nullptr, nullptr};
 	cudaEvent_t ev_out[3] = {nullptr, nullptr, nullptr};
 	cudaEvent_t ev_start = nullptr;
+	// ray binning scratch, one per concurrently running caller: slots 0..2 for
+	// the pipelined host path's staging slots, 3 for direct launches
+	uint32_t ray_order = RRG_RAY_ORDER_DEFAULT;
+	void* d_bin[4] = {nullptr, nullptr, nullptr, nullptr};
+	size_t bin_bytes[4] = {0, 0, 0, 0};
+	bool bin_attr = false;
 	uint4* d_wnodes = nullptr;    // 5 per node
 	float4* d_wtris = nullptr;    // 3*nvalid
 	uint32_t nwnodes = 0;
@@ -124,7 +130,10 @@ int build_wide(Collider* c, const BNode* bnodes, int nnodes, const float* pad, c
 int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
                    cudaStream_t s);
 int launch_closest_on(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
-                      uint32_t* words, cudaStream_t s);
+                      uint32_t* words, cudaStream_t s, int bin_slot);
+// binning (rrg_binning.cu): permutation of the n rays into binned order in
+// scratch slot bin_slot (0..3) of the collider
+int bin_rays(Collider* c, const float4* rays, uint32_t n, cudaStream_t s, int bin_slot, const uint32_t** perm_out);
 int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, cudaStream_t s);
 int launch_rrray(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, cudaStream_t s);
 int launch_rrray_scratch(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, uint32_t* words,

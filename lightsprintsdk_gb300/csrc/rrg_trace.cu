@@ -34,17 +34,22 @@ __device__ __forceinline__ uint32_t warp_fetch(uint32_t* counter) {
 	return __shfl_sync(0xFFFFFFFFu, base, 0);
 }
 
+// PERM: ray j of the launch is ray perm[j] of the batch (binned order, see
+// rrg_binning.cu); hits are written at the ray's own index.
+template <bool PERM>
 __global__ void __launch_bounds__(kTraceThreads) k_closest(const TNode* __restrict__ nodes, int nnodes,
                                                            const float4* __restrict__ tris, int ntris,
                                                            const float4* __restrict__ rays, uint32_t n,
                                                            float4* __restrict__ hits, float4* __restrict__ planes,
-                                                           float* __restrict__ points, uint32_t* counter) {
+                                                           float* __restrict__ points, uint32_t* counter,
+                                                           const uint32_t* __restrict__ perm) {
 	const int lane = threadIdx.x & 31;
 	while (true) {
 		uint32_t base = warp_fetch(counter);
 		if (base >= n) break;
-		uint32_t i = base + lane;
-		if (i >= n) continue;
+		const uint32_t j = base + lane;
+		if (j >= n) continue;
+		const uint32_t i = PERM ? __ldg(perm + j) : j;
 		RayState r;
 		load_ray(rays, i, r);
 		float tbest = r.tmax;
@@ -73,16 +78,19 @@ __global__ void __launch_bounds__(kTraceThreads) k_closest(const TNode* __restri
 	}
 }
 
+template <bool PERM>
 __global__ void __launch_bounds__(kTraceThreads) k_occluded(const TNode* __restrict__ nodes, int nnodes,
                                                             const float4* __restrict__ tris, int ntris,
                                                             const float4* __restrict__ rays, uint32_t n,
-                                                            uint8_t* __restrict__ occ, uint32_t* counter) {
+                                                            uint8_t* __restrict__ occ, uint32_t* counter,
+                                                            const uint32_t* __restrict__ perm) {
 	const int lane = threadIdx.x & 31;
 	while (true) {
 		uint32_t base = warp_fetch(counter);
 		if (base >= n) break;
-		uint32_t i = base + lane;
-		if (i >= n) continue;
+		const uint32_t j = base + lane;
+		if (j >= n) continue;
+		const uint32_t i = PERM ? __ldg(perm + j) : j;
 		RayState r;
 		load_ray(rays, i, r);
 		float tbest = r.tmax;
@@ -406,9 +414,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_ww(const TNode* __restr
 
 int trace_occupancy(Collider* c) {
 	int per_sm = 0;
-	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_closest, kTraceThreads, 0));
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_closest<false>, kTraceThreads, 0));
 	c->trace_blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
-	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_occluded, kTraceThreads, 0));
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_occluded<false>, kTraceThreads, 0));
 	c->occl_blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
 	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_ww<false>, kTraceThreads, 0));
 	c->ww_blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
@@ -417,9 +425,20 @@ int trace_occupancy(Collider* c) {
 	return RRG_OK;
 }
 
-// words[0] = the launch's work counter (cleared here), words[1] = its status.
+// Batches this large are binned first (rrg_binning.cu) unless the caller
+// asked for the given order.
+constexpr uint32_t kBinMinRays = 1u << 22;
+
+static bool use_binning(const Collider* c, uint32_t n) {
+	if (c->ray_order == RRG_RAY_ORDER_AS_GIVEN) return false;
+	if (c->ray_order == RRG_RAY_ORDER_BINNED) return n >= 1024;
+	return n >= kBinMinRays;
+}
+
+// words[0] = the launch's work counter (cleared here), words[1] = its status;
+// bin_slot selects the binning scratch (one per concurrently running caller).
 int launch_closest_on(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
-                      uint32_t* words, cudaStream_t s) {
+                      uint32_t* words, cudaStream_t s, int bin_slot) {
 	if (!n) return RRG_OK;
 	RRG_CUDA(cudaMemsetAsync(words, 0, 4, s));
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
@@ -438,14 +457,23 @@ int launch_closest_on(Collider* c, const float4* rays, uint32_t n, float4* hits,
 		return RRG_OK;
 	}
 	int grid = (int)(want < (uint32_t)c->trace_blocks ? want : (uint32_t)c->trace_blocks);
-	k_closest<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n, hits, planes, points, words);
+	if (use_binning(c, n)) {
+		const uint32_t* perm = nullptr;
+		int st = bin_rays(c, rays, n, s, bin_slot, &perm);
+		if (st) return st;
+		k_closest<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
+		                                               hits, planes, points, words, perm);
+	} else {
+		k_closest<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
+		                                                hits, planes, points, words, nullptr);
+	}
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }
 
 int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
                    cudaStream_t s) {
-	return launch_closest_on(c, rays, n, hits, planes, points, c->d_counter, s);
+	return launch_closest_on(c, rays, n, hits, planes, points, c->d_counter, s, 3);
 }
 
 int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, cudaStream_t s) {
@@ -467,7 +495,16 @@ int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, c
 		return RRG_OK;
 	}
 	int grid = (int)(want < (uint32_t)c->occl_blocks ? want : (uint32_t)c->occl_blocks);
-	k_occluded<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n, occ, c->d_counter);
+	if (use_binning(c, n)) {
+		const uint32_t* perm = nullptr;
+		int st = bin_rays(c, rays, n, s, 3, &perm);
+		if (st) return st;
+		k_occluded<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
+		                                                occ, c->d_counter, perm);
+	} else {
+		k_occluded<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
+		                                                 occ, c->d_counter, nullptr);
+	}
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }

@@ -245,6 +245,31 @@ def test_traversal_variants_agree(c0):
         np.testing.assert_array_equal(a[f], b[f])
 
 
+def test_ray_orders_agree():
+    """Binned and given ray order give bit-identical closest and any hits
+    (config-1 sample of camera, surface and shadow rays)."""
+    import torch
+    sc = scenes.interior_c1()
+    rays = np.concatenate([scenes.camera_rays(rows=32, cols=list(range(0, 4096, 16))),
+                           scenes.surface_rays(sc.vertices, sc.indices, 1 << 17),
+                           scenes.shadow_rays(sc.vertices, sc.indices, 1 << 17)])
+    c = col.RRCollider.create(sc.vertices, sc.indices)
+    d = torch.from_numpy(rays).cuda()
+    n = len(rays)
+    out = {}
+    for order in (col.RAY_ORDER_AS_GIVEN, col.RAY_ORDER_BINNED):
+        c.set_ray_order(order)
+        h = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+        o = torch.empty(n, dtype=torch.uint8, device="cuda")
+        c.intersect_device(d.data_ptr(), n, h.data_ptr())
+        c.occluded_device(d.data_ptr(), n, o.data_ptr())
+        torch.cuda.synchronize()
+        assert c.status() == 0
+        out[order] = (h.cpu().numpy().view(np.uint32), o.cpu().numpy())
+    np.testing.assert_array_equal(out[1][0], out[2][0])
+    np.testing.assert_array_equal(out[1][1], out[2][1])
+
+
 def test_host_pipeline_matches_device():
     """rrg_intersect_host above one 4 Mi-ray chunk (pipelined copies, three
     staging slots reused) returns what rrg_intersect_device returns."""
