@@ -39,6 +39,13 @@ typedef struct rrg_gather_params {
 	float dir_color[3];
 	float point_position[3];   /* point light */
 	float point_color[3];
+	/* ambient occlusion (UpdateParameters::aoIntensity / aoSize, RRSolver.h:506-510):
+	 * when both are > 0 the hemisphere irradiance is scaled by
+	 * (rays whose first hit is farther than ao_size / rays)^ao_intensity
+	 * (gather.cpp:277,306-309).  A caller built against the struct without
+	 * these two fields (size 80) gets them as 0. */
+	float ao_intensity;
+	float ao_size;
 } rrg_gather_params;
 
 /* Enumerates sub-texels on the device.  albedo: 3 floats per triangle;
@@ -60,6 +67,12 @@ RRG_API int rrg_lightmapper_copy_subtexels(const rrg_lightmapper* lm, uint32_t* 
  * texel, 16-byte aligned device memory).  Asynchronous on `stream`. */
 RRG_API int rrg_lightmap_gather(rrg_lightmapper* lm, const rrg_gather_params* p, uint64_t first_texel,
                                 uint64_t ntexels, float* out_dev, void* stream);
+/* Same, plus the bent normal of each texel when bent_dev != NULL (4 floats
+ * per texel, the reference's LS_BENT_NORMALS encoding: (n + 1) / 2 of the
+ * normalised sum of the lights' and the hemisphere's bent normals, w = 1
+ * where covered; gather.cpp:274,488,811-830). */
+RRG_API int rrg_lightmap_gather_ex(rrg_lightmapper* lm, const rrg_gather_params* p, uint64_t first_texel,
+                                   uint64_t ntexels, float* out_dev, float* bent_dev, void* stream);
 /* Same into host memory; synchronous. */
 RRG_API int rrg_lightmap_gather_host(rrg_lightmapper* lm, const rrg_gather_params* p, uint64_t first_texel,
                                      uint64_t ntexels, float* out_host, void* stream);

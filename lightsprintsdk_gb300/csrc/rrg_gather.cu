@@ -23,6 +23,8 @@
 // one rounding per operation (__f*_rn), so both produce the same values from
 // the same counter-based sample streams.
 #include "rrg_traverse.cuh"
+
+#include <stddef.h>
 #include "../../include/rrgpu_gather.h"
 #include "../../include/rrgpu_cache.h"
 #include "rrg_mlp.cuh"
@@ -350,6 +352,7 @@ struct GatherScene {
 	float tmin, locality;
 	uint32_t quality, max_depth;
 	uint64_t seed;
+	float ao_intensity, ao_size;   // both > 0: ambient occlusion on the hemisphere part
 };
 
 __device__ __forceinline__ V3 ld3(const float* p) { return mk(p[0], p[1], p[2]); }
@@ -415,7 +418,7 @@ struct PathLog {
 // one hemisphere sample: getIncidentRadiance restated iteratively
 template <bool LOG = false>
 __device__ V3 trace_path(const GatherScene& g, V3 eye, V3 dir, uint32_t skip, uint64_t sid, bool& overflow,
-                         PathLog* log = nullptr) {
+                         PathLog* log = nullptr, float* first_t = nullptr) {
 	V3 T = mk(1.f, 1.f, 1.f), L = mk(0.f, 0.f, 0.f);
 	if (LOG) log->n = 0;
 	float tmax = g.locality;
@@ -430,6 +433,7 @@ __device__ V3 trace_path(const GatherScene& g, V3 eye, V3 dir, uint32_t skip, ui
 		float4 a, b, c;
 		load_tri(g.tris, slot, a, b, c);
 		Fastest fs = fastest_fields(r, a, b, c);
+		if (depth == 0 && first_t) *first_t = fs.dist;   // the first hit's distance, for ambient occlusion
 		V3 p = add(eye, mul(dir, fs.dist));
 		V3 n = mk(fs.n[0], fs.n[1], fs.n[2]);
 		V3 alb = ld3(g.albedo + 3 * (size_t)tri);
@@ -545,9 +549,16 @@ struct WarpSmem {
 	float fx[kMaxQuality], fy[kMaxQuality], fd[kMaxQuality];
 	V3 hemi[kMaxQuality];
 	V3 light[kMaxRounds][2];
+	V3 lbent[kMaxRounds][2];          // the light rounds' bent-normal terms
 	unsigned char lit[kMaxRounds][2];
+	unsigned char distant[kMaxQuality];   // first hit farther than ao_size
 	unsigned next;   // next unclaimed sample of the texel
 };
+
+// RRVec3::abs().avg() (RRMath.h:170-171), one rounding per operation
+__device__ __forceinline__ float absavg3(V3 a) {
+	return __fmul_rn(__fadd_rn(__fadd_rn(fabsf(a.x), fabsf(a.y)), fabsf(a.z)), 0.33333333333333f);
+}
 
 // LEARNED = false: the plain gather, out[tid - out_base] = texel RGBA.
 // LEARNED = true : first segments only; recs[(tid - out_base) * Q + k] get the
@@ -559,7 +570,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
                                                               uint64_t count, const uint32_t* __restrict__ list,
                                                               uint64_t out_base, float4* __restrict__ out,
                                                               CacheRec* __restrict__ recs, uint32_t* counter,
-                                                              uint32_t* status) {
+                                                              uint32_t* status, float4* __restrict__ bent_out) {
 	__shared__ WarpSmem sm_all[kGatherWarps];
 	WarpSmem& sm = sm_all[threadIdx.x >> 5];
 	const int lane = threadIdx.x & 31;
@@ -577,6 +588,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 		const uint32_t b = off[tid], m = off[tid + 1] - b;
 		if (m == 0) {
 			if (lane == 0) out[oi] = make_float4(0.f, 0.f, 0.f, 0.f);
+			if (lane == 0 && bent_out) bent_out[oi] = make_float4(0.f, 0.f, 0.f, 0.f);
 			continue;
 		}
 		const Sub* S = st + b;
@@ -642,8 +654,20 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 			if (k < Q) {
 				float cosa = __fsqrt_rn(__fsub_rn(1.f, sm.fd[k]));
 				V3 dir = add(add(mul(nrm, cosa), mul(tg, sm.fx[k])), mul(bt, sm.fy[k]));
-				if (LEARNED) recs[oi * Q + k] = first_hit(g, origin, dir, s.tri, overflow);
-				else sm.hemi[k] = trace_path(g, origin, dir, s.tri, sid, overflow);
+				if (LEARNED) {
+					recs[oi * Q + k] = first_hit(g, origin, dir, s.tri, overflow);
+				} else {
+					float ft = 1e10f;
+					const V3 Lk = trace_path(g, origin, dir, s.tri, sid, overflow, nullptr, &ft);
+					sm.hemi[k] = Lk;
+					sm.distant[k] = ft > g.ao_size ? 1 : 0;
+					// the filler point of sample k is used up: its slots hold the
+					// sample's bent-normal term dir * |L|.avg (gather.cpp:274)
+					const V3 bk = mul(dir, absavg3(Lk));
+					sm.fx[k] = bk.x;
+					sm.fy[k] = bk.y;
+					sm.fd[k] = bk.z;
+				}
 			}
 			if (fires && round < (uint32_t)kMaxRounds) {
 				for (int li = 0; li < 2; li++) {
@@ -657,6 +681,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 					if (occluded(g, origin, d, g.tmin, dsize, s.tri, overflow)) continue;
 					V3 irr = li == 0 ? g.dir_color : point_irr(g, origin);
 					sm.light[round][li] = mul(irr, ni);
+					sm.lbent[round][li] = mul(d, __fmul_rn(absavg3(irr), ni));   // gather.cpp:488
 					sm.lit[round][li] = 1;
 				}
 			}
@@ -674,9 +699,26 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 			if (LEARNED) {
 				out[oi] = make_float4(lights.x, lights.y, lights.z, 1.f);
 			} else {
-				hemi = mul(hemi, __fdiv_rn(1.f, (float)Q));
+				float f = __fdiv_rn(1.f, (float)Q);
+				if (g.ao_intensity > 0.f && g.ao_size > 0.f) {
+					uint32_t nd = 0;
+					for (uint32_t k = 0; k < Q; k++) nd += sm.distant[k];
+					f = __fmul_rn(f, powf(__fdiv_rn((float)nd, (float)Q), g.ao_intensity));
+				}
+				hemi = mul(hemi, f);
 				V3 res = add(lights, hemi);
 				out[oi] = make_float4(res.x, res.y, res.z, 1.f);
+				if (bent_out) {
+					V3 bl = mk(0.f, 0.f, 0.f), bh = mk(0.f, 0.f, 0.f);
+					for (uint32_t r = 0; r < shot; r++)
+						for (int li = 0; li < 2; li++)
+							if (sm.lit[r][li]) bl = add(bl, sm.lbent[r][li]);
+					for (uint32_t k = 0; k < Q; k++) bh = add(bh, mk(sm.fx[k], sm.fy[k], sm.fd[k]));
+					V3 b = add(bl, bh);
+					if (b.x != 0.f || b.y != 0.f || b.z != 0.f) b = divf(b, len(b));
+					bent_out[oi] = make_float4(__fmul_rn(__fadd_rn(b.x, 1.f), 0.5f), __fmul_rn(__fadd_rn(b.y, 1.f), 0.5f),
+					                           __fmul_rn(__fadd_rn(b.z, 1.f), 0.5f), 1.f);
+				}
 			}
 		}
 		__syncwarp();
@@ -812,7 +854,9 @@ static void free_lm(Lightmapper* L) {
 }
 
 static int make_scene(Lightmapper* L, const rrg_gather_params* p, GatherScene& g) {
-	if (!p || p->size < sizeof(rrg_gather_params)) return RRG_ERR_INVALID;
+	// a caller built against the struct without the ambient-occlusion fields
+	// passes the smaller size; those fields then read as 0
+	if (!p || p->size < offsetof(rrg_gather_params, ao_intensity)) return RRG_ERR_INVALID;
 	if (p->quality == 0 || p->quality > (uint32_t)kMaxQuality) return RRG_ERR_INVALID;
 	Collider* c = L->c;
 	g.nodes = c->d_nodes;
@@ -831,12 +875,17 @@ static int make_scene(Lightmapper* L, const rrg_gather_params* p, GatherScene& g
 	g.quality = p->quality;
 	g.max_depth = p->max_depth;
 	g.seed = p->seed;
+	const bool has_ao = p->size >= sizeof(rrg_gather_params);
+	g.ao_intensity = has_ao ? p->ao_intensity : 0.f;
+	g.ao_size = has_ao ? p->ao_size : 0.f;
+	if (!(g.ao_intensity >= 0.f) || !(g.ao_size >= 0.f)) return RRG_ERR_INVALID;
 	return RRG_OK;
 }
 
 template <bool LEARNED>
 static int launch_gather_kernel(Lightmapper* L, const GatherScene& g, uint64_t first, uint64_t count,
-                                const uint32_t* list, uint64_t out_base, float4* out, CacheRec* recs, cudaStream_t s) {
+                                const uint32_t* list, uint64_t out_base, float4* out, CacheRec* recs, cudaStream_t s,
+                                float4* bent = nullptr) {
 	if (!count) return RRG_OK;
 	RRG_CUDA(cudaMemsetAsync(L->d_counter, 0, 8, s));
 	int per_sm = 0;
@@ -845,19 +894,20 @@ static int launch_gather_kernel(Lightmapper* L, const GatherScene& g, uint64_t f
 	uint64_t cap = (uint64_t)(per_sm > 0 ? per_sm : 1) * L->c->num_sms;
 	int grid = (int)(want < cap ? want : cap);
 	k_gather<LEARNED><<<grid, kGatherWarps * 32, 0, s>>>(g, L->d_off, L->d_sub, first, count, list, out_base, out, recs,
-	                                                     reinterpret_cast<uint32_t*>(L->d_counter), L->d_status);
+	                                                     reinterpret_cast<uint32_t*>(L->d_counter), L->d_status,
+	                                                     LEARNED ? nullptr : bent);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }
 
 static int gather_launch(Lightmapper* L, const rrg_gather_params* p, uint64_t first, uint64_t count, float* out_dev,
-                         cudaStream_t s) {
+                         cudaStream_t s, float* bent_dev = nullptr) {
 	GatherScene g;
 	int st = make_scene(L, p, g);
 	if (st) return st;
 	if (first + count > L->ntexels) return RRG_ERR_INVALID;
 	return launch_gather_kernel<false>(L, g, first, count, nullptr, first, reinterpret_cast<float4*>(out_dev), nullptr,
-	                                   s);
+	                                   s, reinterpret_cast<float4*>(bent_dev));
 }
 
 }  // namespace rrg
@@ -991,6 +1041,13 @@ int rrg_lightmap_gather(rrg_lightmapper* h, const rrg_gather_params* p, uint64_t
 	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
 	if (!L || !out_dev || ((uintptr_t)out_dev & 15)) return RRG_ERR_INVALID;
 	return gather_launch(L, p, first_texel, ntexels, out_dev, (cudaStream_t)stream);
+}
+
+int rrg_lightmap_gather_ex(rrg_lightmapper* h, const rrg_gather_params* p, uint64_t first_texel, uint64_t ntexels,
+                           float* out_dev, float* bent_dev, void* stream) {
+	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
+	if (!L || !out_dev || ((uintptr_t)out_dev & 15) || ((uintptr_t)bent_dev & 15)) return RRG_ERR_INVALID;
+	return gather_launch(L, p, first_texel, ntexels, out_dev, (cudaStream_t)stream, bent_dev);
 }
 
 int rrg_lightmap_gather_host(rrg_lightmapper* h, const rrg_gather_params* p, uint64_t first_texel, uint64_t ntexels,

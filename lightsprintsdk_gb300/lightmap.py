@@ -21,7 +21,8 @@ class GatherParams(C.Structure):
     _fields_ = [("size", C.c_uint32), ("quality", C.c_uint32), ("max_depth", C.c_uint32),
                 ("reserved0", C.c_uint32), ("seed", C.c_uint64), ("ray_length_min", C.c_float),
                 ("locality", C.c_float), ("dir_direction", C.c_float * 3), ("dir_color", C.c_float * 3),
-                ("point_position", C.c_float * 3), ("point_color", C.c_float * 3)]
+                ("point_position", C.c_float * 3), ("point_color", C.c_float * 3), ("ao_intensity", C.c_float),
+                ("ao_size", C.c_float)]
 
 
 _bound = False
@@ -42,16 +43,18 @@ def _lib():
         L.rrg_lightmapper_copy_subtexels.argtypes = [P, P, P]
         L.rrg_lightmap_gather.argtypes = [P, C.POINTER(GatherParams), C.c_uint64, C.c_uint64, P, P]
         L.rrg_lightmap_gather_host.argtypes = [P, C.POINTER(GatherParams), C.c_uint64, C.c_uint64, P, P]
+        L.rrg_lightmap_gather_ex.argtypes = [P, C.POINTER(GatherParams), C.c_uint64, C.c_uint64, P, P, P]
         L.rrg_lightmapper_status.argtypes = [P, P]
         _bound = True
     return L
 
 
 def make_params(lights: dict, quality: int = 64, max_depth: int = 8, seed: int = 0xC2, ray_length_min: float = 0.0,
-                locality: float = 100000.0) -> GatherParams:
+                locality: float = 100000.0, ao_intensity: float = 0.0, ao_size: float = 0.0) -> GatherParams:
     return GatherParams(C.sizeof(GatherParams), quality, max_depth, 0, seed, ray_length_min, locality,
                         (C.c_float * 3)(*lights["dir_direction"]), (C.c_float * 3)(*lights["dir_color"]),
-                        (C.c_float * 3)(*lights["point_position"]), (C.c_float * 3)(*lights["point_color"]))
+                        (C.c_float * 3)(*lights["point_position"]), (C.c_float * 3)(*lights["point_color"]),
+                        ao_intensity, ao_size)
 
 
 class RRLightmapper:
@@ -113,10 +116,29 @@ class RRLightmapper:
         self.check()
         return out
 
-    def gather_device(self, params: GatherParams, first: int, count: int, out_ptr: int, stream: int = 0) -> None:
-        r = _lib().rrg_lightmap_gather(self._h, C.byref(params), first, count, out_ptr, stream or None)
+    def gather_device(self, params: GatherParams, first: int, count: int, out_ptr: int, stream: int = 0,
+                      bent_ptr: int = 0) -> None:
+        """Device form; bent_ptr (16-byte aligned, 4 floats per texel) also receives the bent normals."""
+        if bent_ptr:
+            r = _lib().rrg_lightmap_gather_ex(self._h, C.byref(params), first, count, out_ptr, bent_ptr,
+                                              stream or None)
+        else:
+            r = _lib().rrg_lightmap_gather(self._h, C.byref(params), first, count, out_ptr, stream or None)
         if r:
             raise col.RRGError(r, "rrg_lightmap_gather")
+
+    def gather_bent(self, params: GatherParams, first: int = 0, count: int | None = None):
+        """Texels [first, first+count) -> ((count, 4) irradiance, (count, 4) bent normals) host arrays,
+        the bent normals in the reference's LS_BENT_NORMALS encoding (RRSolver/gather.cpp:811-830)."""
+        import torch
+        if count is None:
+            count = self.ntexels - first
+        out = torch.empty((max(count, 1), 4), dtype=torch.float32, device="cuda")
+        bent = torch.empty((max(count, 1), 4), dtype=torch.float32, device="cuda")
+        self.gather_device(params, first, count, out.data_ptr(), torch.cuda.current_stream().cuda_stream,
+                           bent.data_ptr())
+        self.check(torch.cuda.current_stream().cuda_stream)
+        return out[:count].cpu().numpy(), bent[:count].cpu().numpy()
 
     def check(self, stream: int = 0) -> None:
         r = _lib().rrg_lightmapper_status(self._h, stream or None)

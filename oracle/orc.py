@@ -53,6 +53,7 @@ def lib():
         L.orc_enumerate.argtypes = [P, P, U, U, P, P, P]
         L.orc_enumerate.restype = C.c_uint64
         L.orc_gather.argtypes = [P, C.POINTER(GatherScene), P, U, P, P, C.c_int, C.c_int, P]
+        L.orc_gather_ex.argtypes = [P, C.POINTER(GatherScene), P, U, P, P, C.c_int, C.c_int, P, P]
         L.orc_hash.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
         L.orc_hash.restype = C.c_uint64
         L.orc_mlp_encode.argtypes = [P, P, P, P, P, P]
@@ -139,7 +140,8 @@ class GatherScene(C.Structure):
     _fields_ = [("xyz", C.c_void_p), ("idx", C.c_void_p), ("nt", C.c_uint32), ("albedo", C.c_void_p),
                 ("dir_direction", C.c_float * 3), ("dir_color", C.c_float * 3), ("point_position", C.c_float * 3),
                 ("point_color", C.c_float * 3), ("ray_length_min", C.c_float), ("locality", C.c_float),
-                ("quality", C.c_uint32), ("max_depth", C.c_uint32), ("seed", C.c_uint64)]
+                ("quality", C.c_uint32), ("max_depth", C.c_uint32), ("seed", C.c_uint64),
+                ("ao_intensity", C.c_float), ("ao_size", C.c_float)]
 
 
 def hash_u64(seed: int, stream: int, index: int) -> int:
@@ -174,7 +176,7 @@ class GatherOracle:
     """Plain N-bounce lightmap gather on the CPU (rr_gather.c)."""
 
     def __init__(self, gs, quality: int = 64, max_depth: int = 8, seed: int = 0xC2, locality: float = 100000.0,
-                 bvh: "FastestOracle | None" = None):
+                 bvh: "FastestOracle | None" = None, ao_intensity: float = 0.0, ao_size: float = 0.0):
         sc = gs.scene
         self.fo = bvh or FastestOracle(sc.vertices, sc.indices)
         self.albedo = np.ascontiguousarray(gs.albedo, np.float32)
@@ -182,19 +184,22 @@ class GatherOracle:
         self.s = GatherScene(self.fo.v.ctypes.data, self.fo.t.ctypes.data, self.fo.t.shape[0], self.albedo.ctypes.data,
                              (C.c_float * 3)(*L["dir_direction"]), (C.c_float * 3)(*L["dir_color"]),
                              (C.c_float * 3)(*L["point_position"]), (C.c_float * 3)(*L["point_color"]),
-                             min_safe_distance(sc.vertices), locality, quality, max_depth, seed)
+                             min_safe_distance(sc.vertices), locality, quality, max_depth, seed, ao_intensity,
+                             ao_size)
 
     def gather(self, texel_ids: np.ndarray, off: np.ndarray, st: np.ndarray, threads: int = 0,
-               fp64: bool = False) -> np.ndarray:
+               fp64: bool = False, bent: bool = False):
         """texel_ids (n,) global ids; off (n+1,) offsets into st for these
-        texels.  Returns (n,4) float32."""
+        texels.  Returns (n,4) float32, or (that, bent normals (n,4)) with bent."""
         texel_ids = np.ascontiguousarray(texel_ids, np.uint64)
         off = np.ascontiguousarray(off, np.uint64)
         st = np.ascontiguousarray(st)
         out = np.zeros((texel_ids.shape[0], 4), np.float32)
-        lib().orc_gather(self.fo.h, C.byref(self.s), _ptr(texel_ids), texel_ids.shape[0], _ptr(off),
-                         _ptr(st) if len(st) else None, threads, int(fp64), _ptr(out))
-        return out
+        bn = np.zeros((texel_ids.shape[0], 4), np.float32) if bent else None
+        lib().orc_gather_ex(self.fo.h, C.byref(self.s), _ptr(texel_ids), texel_ids.shape[0], _ptr(off),
+                            _ptr(st) if len(st) else None, threads, int(fp64), _ptr(out),
+                            _ptr(bn) if bent else None)
+        return (out, bn) if bent else out
 
 
 # --------------------------------------------------------------- network

@@ -232,7 +232,7 @@ static v3 tri_normal(const orc_gather_scene* sc, uint32_t t, v3* v0, v3* s1, v3*
 
 /* one hemisphere sample: getIncidentRadiance restated iteratively */
 static void path(const orc_bvh* bvh, const orc_gather_scene* sc, v3 eye, v3 dir, uint32_t skip, uint64_t sid,
-                 int fp64, v3* Lf, d3* Ld) {
+                 int fp64, v3* Lf, d3* Ld, float* first_t) {
 	v3 T = mk(1, 1, 1);
 	d3 Td = {1, 1, 1};
 	v3 L = mk(0, 0, 0);
@@ -243,6 +243,7 @@ static void path(const orc_bvh* bvh, const orc_gather_scene* sc, v3 eye, v3 dir,
 		float dist, plane[4];
 		uint32_t tri = orc_cast(bvh, &eye.x, &dir.x, tmin, tmax, 0, skip, &dist, plane);
 		if (tri == 0xFFFFFFFFu) break;
+		if (depth == 0) *first_t = dist;
 		v3 p = add(eye, mul(dir, dist));
 		v3 n = mk(plane[0], plane[1], plane[2]);
 		v3 alb = ld3(sc->albedo + 3 * (size_t)tri);
@@ -310,8 +311,12 @@ static void path(const orc_bvh* bvh, const orc_gather_scene* sc, v3 eye, v3 dir,
 	*Ld = LD;
 }
 
+/* RRVec3::abs().avg() (RRMath.h:170-171) */
+static float absavg(v3 v) { return (fabsf(v.x) + fabsf(v.y) + fabsf(v.z)) * 0.33333333333333f; }
+
 static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_t tid, const orc_subtexel* S,
-                         uint32_t m, int fp64, float* out) {
+                         uint32_t m, int fp64, float* out, float* bent) {
+	if (bent) bent[0] = bent[1] = bent[2] = bent[3] = 0;
 	if (!m) {
 		out[0] = out[1] = out[2] = out[3] = 0;
 		return;
@@ -321,6 +326,8 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 			out[0] = out[1] = out[2] = out[3] = NAN;
 			return;
 		}
+	v3 bentH = mk(0, 0, 0), bentL = mk(0, 0, 0);
+	uint32_t distant = 0;
 	const uint32_t Q = sc->quality ? sc->quality : 1;
 	const uint32_t rounds = Q / 10 + 1;
 	const uint32_t N = Q > rounds ? Q : rounds;
@@ -369,7 +376,10 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 			v3 dir = add(add(mul(nrm, cosa), mul(tg, x)), mul(bt, y));
 			v3 L;
 			d3 LD;
-			path(bvh, sc, origin, dir, st->tri, sid, fp64, &L, &LD);
+			float first_t = 1e10f;
+			path(bvh, sc, origin, dir, st->tri, sid, fp64, &L, &LD, &first_t);
+			if (first_t > sc->ao_size) distant++;
+			bentH = add(bentH, mul(dir, absavg(L)));
 			hemi = add(hemi, L);
 			hemiD.x += LD.x;
 			hemiD.y += LD.y;
@@ -386,6 +396,7 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 				if (ni <= 0 || !isfinite(ni)) continue;
 				if (orc_cast(bvh, &origin.x, &d.x, tmin, dsize, 1, st->tri, NULL, NULL) != 0xFFFFFFFFu) continue;
 				v3 irr = li == 0 ? ld3(sc->dir_color) : point_irradiance(sc, origin);
+				bentL = add(bentL, mul(d, absavg(irr) * ni));
 				lights = add(lights, mul(irr, ni));
 				lightsD.x += (double)irr.x * ni;
 				lightsD.y += (double)irr.y * ni;
@@ -394,13 +405,16 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 			shotRounds++;
 		}
 	}
+	const int ao = sc->ao_intensity > 0 && sc->ao_size > 0;
+	const float aof = ao ? powf((float)distant / (float)Q, sc->ao_intensity) : 1.0f;
 	if (fp64) {
-		double f = 1.0 / (double)Q;
+		double f = 1.0 / (double)Q * aof;
 		out[0] = (float)(lightsD.x / shotRounds + hemiD.x * f);
 		out[1] = (float)(lightsD.y / shotRounds + hemiD.y * f);
 		out[2] = (float)(lightsD.z / shotRounds + hemiD.z * f);
 	} else {
 		float f = 1 / (float)Q;
+		if (ao) f = f * aof;
 		lights = divf(lights, (float)shotRounds);
 		hemi = mul(hemi, f);
 		v3 r = add(lights, hemi);
@@ -409,14 +423,28 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 		out[2] = r.z;
 	}
 	out[3] = 1;
+	if (bent) {
+		v3 b = add(bentL, bentH);
+		if (b.x != 0 || b.y != 0 || b.z != 0) b = divf(b, len(b));
+		bent[0] = (b.x + 1) * 0.5f;
+		bent[1] = (b.y + 1) * 0.5f;
+		bent[2] = (b.z + 1) * 0.5f;
+		bent[3] = 1;
+	}
 }
 
-void orc_gather(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,
-                const uint64_t* off, const orc_subtexel* st, int threads, int fp64, float* out) {
+void orc_gather_ex(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,
+                   const uint64_t* off, const orc_subtexel* st, int threads, int fp64, float* out, float* bent) {
 #ifdef _OPENMP
 	if (threads > 0) omp_set_num_threads(threads);
 #pragma omp parallel for schedule(dynamic, 16)
 #endif
 	for (long i = 0; i < (long)ntexels; i++)
-		gather_texel(bvh, sc, texel_id[i], st + off[i], (uint32_t)(off[i + 1] - off[i]), fp64, out + 4 * (size_t)i);
+		gather_texel(bvh, sc, texel_id[i], st + off[i], (uint32_t)(off[i + 1] - off[i]), fp64, out + 4 * (size_t)i,
+		             bent ? bent + 4 * (size_t)i : NULL);
+}
+
+void orc_gather(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,
+                const uint64_t* off, const orc_subtexel* st, int threads, int fp64, float* out) {
+	orc_gather_ex(bvh, sc, texel_id, ntexels, off, st, threads, fp64, out, NULL);
 }

@@ -31,6 +31,10 @@
  *   - one shooting series per texel (every ray here is reliable);
  *   - the path radiance is accumulated iteratively (L += T * contribution)
  *     rather than by recursion.
+ * Ambient occlusion (aoIntensity, aoSize: the hemisphere irradiance scaled
+ * by (rays whose first hit is farther than aoSize / rays)^aoIntensity,
+ * gather.cpp:277,306-309; the first hit's distance, pathtracer.cpp:145-177)
+ * and bent normals (gather.cpp:274,488,811-830) follow the reference.
  * With fp64 = 1 the same paths are accumulated in double precision: the
  * FP64-accumulated reference that states the float accumulation error.
  */
@@ -62,6 +66,8 @@ typedef struct orc_gather_scene {
 	uint32_t quality;       /* hemisphere rays per texel */
 	uint32_t max_depth;     /* PathTracingParameters::stopAtDepth */
 	uint64_t seed;
+	float ao_intensity;     /* UpdateParameters::aoIntensity (used when both are > 0) */
+	float ao_size;          /* UpdateParameters::aoSize */
 } orc_gather_scene;
 
 /* Sub-texels of one atlas.  uv: n triangles x 3 corners x 2 in map space
@@ -77,6 +83,12 @@ uint64_t orc_enumerate(const float* uv, const uint32_t* tri, uint32_t n, uint32_
  * texel (irradiance RGB, 1 if covered else 0). */
 void orc_gather(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,
                 const uint64_t* off, const orc_subtexel* st, int threads, int fp64, float* out);
+
+/* Same, plus the bent normal of each texel when bent != NULL (4 floats:
+ * (n + 1) / 2 of the normalised sum of the lights' and the hemisphere's
+ * bent normals, 1 if covered; gather.cpp:274,488,811-830). */
+void orc_gather_ex(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,
+                   const uint64_t* off, const orc_subtexel* st, int threads, int fp64, float* out, float* bent);
 
 /* Counter-based generator shared with the GPU (and with the Python
  * generators): MurmurHash3 fmix64 of (seed, stream, index). */

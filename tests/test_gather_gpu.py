@@ -129,3 +129,46 @@ def test_skylight_patch_is_brighter(setup):
     lum = out[:, :3].mean(1)
     cov = out[:, 3] > 0
     assert lum[cov].max() > 4 * np.median(lum[cov])
+
+
+def gpu_gather_bent(L, params, tids):
+    out = np.zeros((len(tids), 4), np.float32)
+    bent = np.zeros((len(tids), 4), np.float32)
+    i = 0
+    while i < len(tids):
+        j = i
+        while j + 1 < len(tids) and tids[j + 1] == tids[j] + 1:
+            j += 1
+        out[i:j + 1], bent[i:j + 1] = L.gather_bent(params, int(tids[i]), j - i + 1)
+        i = j + 1
+    return out, bent
+
+
+def test_ambient_occlusion_and_bent_normals_match_oracle(setup):
+    """AO factor (RRSolver/gather.cpp:306-309) and bent normals (gather.cpp:274,
+    488, 811-830) against the oracle on the same sample streams.  Tolerance:
+    irradiance within 1e-4 relative like the plain gather; bent normals (unit
+    vectors encoded to [0, 1]) within 1e-4 absolute."""
+    gs, c, L, _ = setup
+    ext = gs.scene.vertices.max(0) - gs.scene.vertices.min(0)
+    ao_size = float(ext.mean() * 0.05)
+    G = orc.GatherOracle(gs, bvh=setup[3].fo, ao_intensity=1.0, ao_size=ao_size)
+    params = lm.make_params(gs.lights, ao_intensity=1.0, ao_size=ao_size)
+    tids, off, st = pick_texels(L, [0, 1, 9, 75], 32)
+    got, gb = gpu_gather_bent(L, params, tids)
+    cnt = (off[tids + 1] - off[tids]).astype(np.uint64)
+    o2 = np.concatenate([[0], np.cumsum(cnt)]).astype(np.uint64)
+    sts = np.concatenate([st[off[t]:off[t + 1]] for t in tids]).view(orc.SUBTEXEL_DTYPE)
+    ref, rb = G.gather(tids.astype(np.uint64), o2, sts, 0, bent=True)
+    rel = np.abs(got[:, :3] - ref[:, :3]) / np.maximum(np.abs(ref[:, :3]), 1e-6)
+    assert rel.max() <= 1e-4, rel.max()
+    assert np.abs(gb - rb).max() <= 1e-4, np.abs(gb - rb).max()
+    assert np.all(gb[:, 3] == 1)
+    # unit vectors, except texels that no light reaches: their sum is zero and,
+    # as in the reference (gather.cpp:817-821), stays unnormalised
+    nrm = np.linalg.norm(gb[:, :3] * 2 - 1, axis=1)
+    assert np.all((np.abs(nrm - 1) < 1e-3) | (nrm == 0))
+    assert (nrm > 0).mean() > 0.5
+    plain = gpu_gather(L, lm.make_params(gs.lights), tids)
+    assert np.all(got[:, :3] <= plain[:, :3] * (1 + 1e-6) + 1e-9)
+    assert (got[:, :3].sum(1) < plain[:, :3].sum(1) * 0.999).mean() > 0.2
