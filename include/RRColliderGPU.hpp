@@ -81,12 +81,14 @@ public:
 		return new RRColliderGPU(h, nv);
 	}
 
-	// One ray; a blocking round trip to the device.  Use intersectBatch for
-	// throughput.
+	// One ray; a blocking round trip to the device.  Thread-safe: calls from
+	// many host threads at once are traced together as one batch.  Use
+	// intersectBatch for throughput from one thread.
 	bool intersect(RRRay& ray) const {
 		uint8_t hit = 0;
-		last_status_ = rrg_intersect_rrray(h_, &ray, 1, &hit, nullptr);
-		return last_status_ == RRG_OK && hit;
+		const int st = rrg_intersect_rrray_one(h_, &ray, &hit);
+		last_status_ = st;
+		return st == RRG_OK && hit;
 	}
 
 	// n rays in place; hit[i] (optional) = what intersect() would return.

@@ -150,7 +150,8 @@ RRG_API int rrg_occluded_device(rrg_collider* c, const float* rays_dev, uint32_t
 
 /* Host buffers in, host buffers out: copies the rays to the device, traces,
  * copies the hit records back and synchronises.  Uses device staging buffers
- * owned by the collider (grown on demand).  Batches above 4,194,304 rays go
+ * owned by the collider (grown on demand); host threads that call this or
+ * rrg_intersect_rrray on one collider at once take turns.  Batches above 4,194,304 rays go
  * through in chunks whose copies overlap the tracing of the neighbouring
  * chunks (the overlap needs page-locked host buffers). */
 RRG_API int rrg_intersect_host(rrg_collider* c, const float* rays_host, uint32_t n, float* hits_host, void* stream);
@@ -161,6 +162,22 @@ RRG_API int rrg_intersect_host(rrg_collider* c, const float* rays_host, uint32_t
  * NULL).  The batch form the reference once had as intersectBatch
  * (doc/doxygen/doc.news:154).  Synchronous. */
 RRG_API int rrg_intersect_rrray(rrg_collider* c, void* rrrays_host, uint32_t n, uint8_t* hit_host, void* stream);
+
+/* One rr::RRRay on the host, from any number of host threads at once: the
+ * contract of RRCollider::intersect(RRRay&), thread-safe and stateless
+ * (RRCollider.h:145,217-228), whose callers run it from OpenMP loops
+ * (RRSolver/gather.cpp:917, RRSolver/lightmap.cpp:368).  Calls that arrive
+ * while the collider's four combining slots are busy are combined into one
+ * batch, traced on a slot's own stream and buffers, so throughput grows with
+ * the number of calling threads.  Reads and writes the same fields as
+ * rrg_intersect_rrray; *hit_host (may be NULL) = what intersect() returns.
+ * Synchronous; does not race with the other entry points of the collider.
+ * RRG_ERR_STACK if a traversal stack overflowed anywhere in the batch the ray
+ * went with (that ray may then be left unhit). */
+RRG_API int rrg_intersect_rrray_one(rrg_collider* c, void* rrray_host, uint8_t* hit_host);
+
+/* Batches traced by rrg_intersect_rrray_one so far and the rays in them. */
+RRG_API int rrg_collider_combined(const rrg_collider* c, uint64_t* batches, uint64_t* rays);
 
 /* Same on a device copy of the RRRay array (asynchronous). */
 RRG_API int rrg_intersect_rrray_device(rrg_collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, void* stream);

@@ -15,7 +15,10 @@
 // reference changes.  Semantics:
 //   * the mesh is flattened once (getVertex/getTriangle, RRMesh.h:151,172)
 //     and copied to the device; post-import triangle numbers are kept;
-//   * intersect(RRRay&) without a collision handler is one device query;
+//   * intersect(RRRay&) without a collision handler is one device query,
+//     thread-safe like the reference's (RRCollider.h:145): calls from many
+//     host threads at once are combined into one batch
+//     (rrg_intersect_rrray_one);
 //   * with a collision handler, hits are offered to collides() nearest first
 //     (the IT_BSP contract, RRCollider.h:52-55): after a rejection the query
 //     repeats beyond the rejected distance, up to kMaxHandlerRounds times;
@@ -64,7 +67,7 @@ public:
 		rr::RRCollisionHandler* handler = ray.collisionHandler;
 		if (!handler) {
 			uint8_t hit = 0;
-			return rrg_intersect_rrray(h_, &ray, 1, &hit, nullptr) == RRG_OK && hit;
+			return rrg_intersect_rrray_one(h_, &ray, &hit) == RRG_OK && hit;
 		}
 		handler->init(ray);
 		const float lenMin = ray.rayLengthMin;
@@ -73,7 +76,7 @@ public:
 		for (unsigned round = 0; round < kMaxHandlerRounds; round++) {
 			uint8_t hit = 0;
 			ray.collisionHandler = nullptr;
-			int st = rrg_intersect_rrray(h_, &ray, 1, &hit, nullptr);
+			int st = rrg_intersect_rrray_one(h_, &ray, &hit);
 			ray.collisionHandler = handler;
 			if (st != RRG_OK || !hit) break;
 			if (handler->collides(ray)) break;

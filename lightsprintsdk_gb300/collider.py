@@ -85,6 +85,8 @@ def _lib():
         L.rrg_intersect_host.argtypes = [P, P, U, P, P]
         L.rrg_intersect_rrray.argtypes = [P, P, U, P, P]
         L.rrg_intersect_rrray_device.argtypes = [P, P, U, P, P]
+        L.rrg_intersect_rrray_one.argtypes = [P, P, P]
+        L.rrg_collider_combined.argtypes = [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.rrg_collider_status.argtypes = [P, P]
         L.rrg_collider_set_traversal.argtypes = [P, U]
         L.rrg_collider_set_ray_order.argtypes = [P, U]
@@ -243,10 +245,22 @@ class RRCollider:
         _check(self.status(), "trace")
         return hit.astype(bool)
 
-    def intersect(self, ray: np.ndarray) -> bool:
-        """RRCollider::intersect(RRRay&) for one RRRay record (a 1-element
-        RRRAY_DTYPE array, modified in place)."""
-        return bool(self.intersect_rrrays(ray.reshape(1))[0])
+    def intersect(self, ray: np.ndarray, index: int = 0) -> bool:
+        """RRCollider::intersect(RRRay&) for record `index` of an RRRAY_DTYPE
+        array (modified in place).  Thread-safe: Python threads calling it at
+        once (ctypes releases the GIL) are traced together as one device batch
+        (rrg_intersect_rrray_one)."""
+        assert ray.dtype == RRRAY_DTYPE and ray.flags.c_contiguous and 0 <= index < ray.shape[0]
+        hit = C.c_uint8(0)
+        _check(_lib().rrg_intersect_rrray_one(self._h, ray.ctypes.data + RRRAY_DTYPE.itemsize * index,
+                                              C.byref(hit)), "rrg_intersect_rrray_one")
+        return bool(hit.value)
+
+    def combined(self) -> tuple[int, int]:
+        """(batches, rays) traced so far by the combined single-ray path."""
+        b, r = C.c_uint64(0), C.c_uint64(0)
+        _check(_lib().rrg_collider_combined(self._h, C.byref(b), C.byref(r)), "rrg_collider_combined")
+        return b.value, r.value
 
 
 def make_rrrays(rays: np.ndarray, flags: int = FILL_ALL) -> np.ndarray:

@@ -42,6 +42,7 @@ void free_collider(Collider* c) {
 	cudaFree(c->d_stage_in);
 	cudaFree(c->d_stage_out);
 	for (int k = 0; k < 4; k++) cudaFree(c->d_bin[k]);
+	combiner_free(c->comb);
 	delete c;
 }
 
@@ -64,6 +65,8 @@ int init_collider(Collider* c, const rrg_build_params* params) {
 	c->num_sms = prop.multiProcessorCount;
 	RRG_CUDA(cudaMalloc((void**)&c->d_counter, 64));
 	RRG_CUDA(cudaMemset(c->d_counter, 0, 64));
+	c->comb = combiner_new();
+	if (!c->comb) return RRG_ERR_OOM;
 	return trace_occupancy(c);
 }
 
@@ -272,6 +275,7 @@ int rrg_intersect_host(rrg_collider* h, const float* rays_host, uint32_t n, floa
 	if (!c) return RRG_ERR_INVALID;
 	if (n == 0) return RRG_OK;
 	if (!rays_host || !hits_host) return RRG_ERR_INVALID;
+	std::lock_guard<std::mutex> lk(c->host_mu);
 	RRG_CUDA(cudaSetDevice(c->device));
 	cudaStream_t s = (cudaStream_t)stream;
 	if (n <= kHostChunk) {
@@ -334,6 +338,7 @@ int rrg_intersect_rrray(rrg_collider* h, void* rrrays_host, uint32_t n, uint8_t*
 	if (!c) return RRG_ERR_INVALID;
 	if (n == 0) return RRG_OK;
 	if (!rrrays_host) return RRG_ERR_INVALID;
+	std::lock_guard<std::mutex> lk(c->host_mu);
 	RRG_CUDA(cudaSetDevice(c->device));
 	int st = ensure_stage(c, 128 * (size_t)n, (size_t)n);
 	if (st) return st;

@@ -4,6 +4,8 @@
 #include <stdint.h>
 #include <stddef.h>
 
+#include <mutex>
+
 #include "../../include/rrgpu.h"
 
 typedef struct rrg_batch rrg_batch;
@@ -72,6 +74,8 @@ __device__ __forceinline__ uint32_t segment_of(const uint32_t* off, uint32_t n, 
 // (v1.xyz, 0), (v2.xyz, 0); vertices in the mesh's own order.
 
 // -------------------------------------------------------------- collider
+struct Combiner;
+
 struct Collider {
 	int device = 0;
 	uint32_t nv = 0, nt = 0, nvalid = 0, nnodes = 0;
@@ -118,6 +122,11 @@ struct Collider {
 	uint4* d_wnodes = nullptr;    // 5 per node
 	float4* d_wtris = nullptr;    // 3*nvalid
 	uint32_t nwnodes = 0;
+	// host threads calling the staging entry points (rrg_intersect_host,
+	// rrg_intersect_rrray) take turns on this lock
+	std::mutex host_mu;
+	// single-ray queries combined across host threads (rrg_combine.cu)
+	Combiner* comb = nullptr;
 };
 
 // build (rrg_build.cu)
@@ -146,6 +155,10 @@ Collider* batch_collider(::rrg_batch* b);
 int batch_trace_blocks(Collider* c, uint32_t nmesh, int* blocks);
 int launch_batch_closest(Collider* c, const float4* rays, uint32_t n, const uint32_t* ray_off, uint32_t nmesh,
                          int fetch, int blocks, float4* hits, cudaStream_t s);
+
+// combined single-ray queries (rrg_combine.cu)
+Combiner* combiner_new();
+void combiner_free(Combiner* k);
 
 // api (rrg_api.cu)
 int cuda_fail(cudaError_t e);

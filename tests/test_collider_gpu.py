@@ -347,3 +347,98 @@ def test_autotuner_picks_a_candidate(tmp_path, monkeypatch):
     h = c.intersect_batch(rays)
     ref = col.RRCollider.create(v, t).intersect_batch(rays)
     np.testing.assert_array_equal(h["tri"], ref["tri"])
+
+
+def test_single_ray_calls_from_many_threads_are_combined():
+    """RRCollider::intersect(RRRay&) is thread-safe in the reference
+    (RRCollider.h:145,217-228) and its callers use it from OpenMP loops
+    (RRSolver/gather.cpp:917).  16 Python threads (ctypes releases the GIL)
+    each trace their share of 6,000 rays one call at a time while another
+    thread runs batch calls on the same collider: every record must be
+    byte-identical to a batch trace of the same rays."""
+    import threading
+    import time
+    room = scenes.interior_c1()
+    c = col.RRCollider.create(room.vertices, room.indices)
+    rays = scenes.surface_rays(room.vertices, room.indices, 6000)
+    want = col.make_rrrays(rays)
+    want_hit = c.intersect_rrrays(want)
+    got = col.make_rrrays(rays)
+    got_hit = np.zeros(len(got), bool)
+    other_rays = scenes.surface_rays(room.vertices, room.indices, 20000)
+    other_want = col.make_rrrays(other_rays)
+    c.intersect_rrrays(other_want)
+    errors = []
+    stop = threading.Event()
+
+    def single(t):
+        try:
+            for i in range(t, len(got), 16):
+                got_hit[i] = c.intersect(got, i)
+        except Exception as e:   # reported below
+            errors.append(e)
+
+    def batches():
+        try:
+            while not stop.is_set():
+                o = col.make_rrrays(other_rays)
+                c.intersect_rrrays(o)
+                if o.tobytes() != other_want.tobytes():
+                    errors.append(AssertionError("batch call disturbed"))
+        except Exception as e:
+            errors.append(e)
+
+    bt = threading.Thread(target=batches)
+    bt.start()
+    threads = [threading.Thread(target=single, args=(t,)) for t in range(16)]
+    t0 = time.perf_counter()
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    dt = time.perf_counter() - t0
+    stop.set()
+    bt.join()
+    assert not errors, errors[0]
+    np.testing.assert_array_equal(got_hit, want_hit)
+    assert got.tobytes() == want.tobytes()
+    nb, nr = c.combined()
+    assert nr == len(got)
+    assert 0 < nb <= nr, (nb, nr)
+    print(f"combined single-ray calls: {nr} rays in {nb} batches, {nr / dt:.0f} rays/s on 16 threads")
+    c.close()
+
+
+@pytest.mark.parametrize("threads", [1, 32])
+def test_native_threads_single_ray_calls(tmp_path, threads):
+    """The same from native host threads (tests/cpp/combine_threads.cpp, one
+    std::thread per OpenMP-like worker): records byte-identical to a batch
+    trace, and the rate printed for the record."""
+    import os
+    import subprocess
+    from lightsprintsdk_gb300 import build as B
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lib = B.build()
+    exe = tmp_path / "combine_threads"
+    subprocess.run(["g++", "-std=c++17", "-O2", f"-I{root}/include",
+                    os.path.join(root, "tests", "cpp", "combine_threads.cpp"), "-o", str(exe), lib,
+                    f"-Wl,-rpath,{os.path.dirname(lib)}", "-lpthread"], check=True, capture_output=True, text=True)
+    room = scenes.interior_c1()
+    rays = scenes.surface_rays(room.vertices, room.indices, 40000)
+    np.ascontiguousarray(room.vertices, np.float32).tofile(tmp_path / "xyz.f32")
+    np.ascontiguousarray(room.indices, np.uint32).tofile(tmp_path / "idx.u32")
+    col.make_rrrays(rays).tofile(tmp_path / "rays.rrray")
+    out = subprocess.run([str(exe), str(tmp_path), str(threads)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    traced, batches, secs = out.stdout.split()
+    c = col.RRCollider.create(room.vertices, room.indices)
+    want = col.make_rrrays(rays)
+    want_hit = c.intersect_rrrays(want)
+    c.close()
+    got = np.fromfile(tmp_path / "out.rrray", col.RRRAY_DTYPE)
+    got_hit = np.fromfile(tmp_path / "hit.u8", np.uint8).astype(bool)
+    np.testing.assert_array_equal(got_hit, want_hit)
+    assert got.tobytes() == want.tobytes()
+    assert int(traced) == len(rays)
+    print(f"native single-ray calls, {threads} threads: {len(rays) / float(secs):.0f} rays/s, "
+          f"{int(batches)} batches")
