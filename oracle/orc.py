@@ -11,7 +11,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liborc.so")
-SRC = [os.path.join(HERE, "rr_oracle.c"), os.path.join(HERE, "rr_gather.c"), os.path.join(HERE, "rr_mlp.c")]
+SRC = [os.path.join(HERE, "rr_oracle.c"), os.path.join(HERE, "rr_gather.c"), os.path.join(HERE, "rr_mlp.c"),
+       os.path.join(HERE, "rr_filter.c")]
 HDRS = [os.path.join(HERE, "rr_oracle.h"), os.path.join(HERE, "rr_gather.h")]
 
 _lib = None
@@ -52,6 +53,13 @@ def lib():
         L.orc_max_threads.restype = C.c_int
         L.orc_enumerate.argtypes = [P, P, U, U, P, P, P]
         L.orc_enumerate.restype = C.c_uint64
+        L.orc_texel_flags.argtypes = [P, U, U, P]
+        L.orc_unwrap_seams.argtypes = [P, P, U, P, U]
+        L.orc_unwrap_seams.restype = U
+        L.orc_lightmap_smooth.argtypes = [P, U, U, C.c_float, C.c_int, P, U]
+        L.orc_lightmap_grow_bilinear.argtypes = [P, U, U, C.c_int]
+        L.orc_lightmap_grow.argtypes = [P, U, U, U, C.c_int]
+        L.orc_lightmap_fill_background.argtypes = [P, U, U, P]
         L.orc_gather.argtypes = [P, C.POINTER(GatherScene), P, U, P, P, C.c_int, C.c_int, P]
         L.orc_gather_ex.argtypes = [P, C.POINTER(GatherScene), P, U, P, P, C.c_int, C.c_int, P, P]
         L.orc_hash.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
@@ -141,7 +149,7 @@ class GatherScene(C.Structure):
                 ("dir_direction", C.c_float * 3), ("dir_color", C.c_float * 3), ("point_position", C.c_float * 3),
                 ("point_color", C.c_float * 3), ("ray_length_min", C.c_float), ("locality", C.c_float),
                 ("quality", C.c_uint32), ("max_depth", C.c_uint32), ("seed", C.c_uint64),
-                ("ao_intensity", C.c_float), ("ao_size", C.c_float)]
+                ("ao_intensity", C.c_float), ("ao_size", C.c_float), ("flags", C.c_void_p)]
 
 
 def hash_u64(seed: int, stream: int, index: int) -> int:
@@ -165,6 +173,62 @@ def enumerate_atlas(uv_map: np.ndarray, tri_ids: np.ndarray, size: int):
     return off, st
 
 
+def texel_flags(uv_map: np.ndarray, size: int) -> np.ndarray:
+    """TexelFlags of one atlas (lightmap.cpp:283-314 restated): (size*size,)
+    uint8 from the atlas' triangles' map-space corners (n,3,2)."""
+    uv_map = np.ascontiguousarray(uv_map, np.float32)
+    flags = np.zeros(size * size, np.uint8)
+    lib().orc_texel_flags(_ptr(uv_map), uv_map.shape[0], size, _ptr(flags))
+    return flags
+
+
+def gather_flags(gs, atlases) -> np.ndarray:
+    """TexelFlags by global texel id for the given atlases of a gather scene
+    (other atlases 0)."""
+    S = gs.size * gs.size
+    flags = np.zeros(gs.natlas * S, np.uint8)
+    for a in atlases:
+        ids = np.nonzero(gs.tri_atlas == a)[0]
+        flags[a * S:(a + 1) * S] = texel_flags(gs.uv[ids], gs.size)
+    return flags
+
+
+def unwrap_seams(idx: np.ndarray, uv_map: np.ndarray) -> np.ndarray:
+    """UnwrapSeams (RRBuffer.cpp:534-628 restated, vertices shared by index)
+    of one object: idx (n,3) vertex indices, uv_map (n,3,2) in the object's
+    triangle order -> (m, 8) float32 (edge1 from, edge1 to, edge2 from, edge2 to)."""
+    idx = np.ascontiguousarray(idx, np.uint32)
+    uv_map = np.ascontiguousarray(uv_map, np.float32)
+    n = idx.shape[0]
+    m = lib().orc_unwrap_seams(_ptr(idx), _ptr(uv_map), n, None, 0)
+    out = np.zeros((max(m, 1), 8), np.float32)
+    lib().orc_unwrap_seams(_ptr(idx), _ptr(uv_map), n, _ptr(out), m)
+    return out[:m]
+
+
+FILTER_SMOOTH, FILTER_GROW_BILINEAR, FILTER_GROW, FILTER_FILL_BACKGROUND = 1, 2, 4, 8
+
+
+def lightmap_filter(rgba: np.ndarray, smoothing: float = 1.0, spread: int = 1000, background=(0, 0, 0, 0),
+                    wrap: bool = False, seams: np.ndarray | None = None, stages: int = 15) -> np.ndarray:
+    """The post-filters of updateLightmap (lightmap.cpp:865-874) in order on one
+    lightmap (h, w, 4) float32; returns the filtered copy."""
+    out = np.ascontiguousarray(rgba, np.float32).copy()
+    h, w = out.shape[0], out.shape[1]
+    L = lib()
+    sm = np.ascontiguousarray(seams if seams is not None else np.zeros((0, 8)), np.float32)
+    if stages & FILTER_SMOOTH:
+        L.orc_lightmap_smooth(_ptr(out), w, h, smoothing, int(wrap), _ptr(sm) if len(sm) else None, len(sm))
+    if stages & FILTER_GROW_BILINEAR:
+        L.orc_lightmap_grow_bilinear(_ptr(out), w, h, int(wrap))
+    if stages & FILTER_GROW:
+        L.orc_lightmap_grow(_ptr(out), w, h, spread, int(wrap))
+    if stages & FILTER_FILL_BACKGROUND:
+        bg = np.asarray(background, np.float32)
+        L.orc_lightmap_fill_background(_ptr(out), w, h, _ptr(bg))
+    return out
+
+
 def min_safe_distance(v: np.ndarray) -> float:
     """RRSolver::setStaticObjects: (aabb max - min).avg() * 1e-6 (RRSolver.cpp:329-334)."""
     v = np.asarray(v, np.float32)
@@ -176,8 +240,11 @@ class GatherOracle:
     """Plain N-bounce lightmap gather on the CPU (rr_gather.c)."""
 
     def __init__(self, gs, quality: int = 64, max_depth: int = 8, seed: int = 0xC2, locality: float = 100000.0,
-                 bvh: "FastestOracle | None" = None, ao_intensity: float = 0.0, ao_size: float = 0.0):
+                 bvh: "FastestOracle | None" = None, ao_intensity: float = 0.0, ao_size: float = 0.0,
+                 flags: np.ndarray | None = None):
+        """flags: TexelFlags by global texel id (alpha = flags/255); None: alpha 1."""
         sc = gs.scene
+        self.flags = None if flags is None else np.ascontiguousarray(flags, np.uint8)
         self.fo = bvh or FastestOracle(sc.vertices, sc.indices)
         self.albedo = np.ascontiguousarray(gs.albedo, np.float32)
         L = gs.lights
@@ -185,7 +252,7 @@ class GatherOracle:
                              (C.c_float * 3)(*L["dir_direction"]), (C.c_float * 3)(*L["dir_color"]),
                              (C.c_float * 3)(*L["point_position"]), (C.c_float * 3)(*L["point_color"]),
                              min_safe_distance(sc.vertices), locality, quality, max_depth, seed, ao_intensity,
-                             ao_size)
+                             ao_size, None if self.flags is None else self.flags.ctypes.data)
 
     def gather(self, texel_ids: np.ndarray, off: np.ndarray, st: np.ndarray, threads: int = 0,
                fp64: bool = False, bent: bool = False):

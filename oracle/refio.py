@@ -78,3 +78,71 @@ def run_ref_collide(v, t, rays, technique: str = "bsp_fastest", threads: int = 0
         timing = json.loads(res.stdout.strip().splitlines()[-1])
         hits = read_hits(hp) if want_hits else None
     return timing, hits
+
+
+# LIGHTMAP "RGL1": u32 width, u32 height, f32 rgba[width*height*4]
+# UNWRAP   "RGU1": u32 nv, u32 nt, f32 xyz[3nv], f32 normal[3nv], u32 idx[3nt], f32 uv[6nt]
+def write_lightmap(path: str, rgba: np.ndarray) -> None:
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    h, w = rgba.shape[0], rgba.shape[1]
+    with open(path, "wb") as f:
+        f.write(b"RGL1")
+        f.write(np.array([w, h], np.uint32).tobytes())
+        f.write(rgba.tobytes())
+
+
+def read_lightmap(path: str) -> np.ndarray:
+    b = open(path, "rb").read()
+    assert b[:4] == b"RGL1"
+    w, h = np.frombuffer(b, np.uint32, 2, 4)
+    return np.frombuffer(b, np.float32, int(w) * int(h) * 4, 12).reshape(int(h), int(w), 4).copy()
+
+
+def write_unwrap(path: str, v, normals, t, uv) -> None:
+    v = np.ascontiguousarray(v, np.float32)
+    with open(path, "wb") as f:
+        f.write(b"RGU1")
+        f.write(np.array([v.shape[0], len(t)], np.uint32).tobytes())
+        f.write(v.tobytes())
+        f.write(np.ascontiguousarray(normals, np.float32).tobytes())
+        f.write(np.ascontiguousarray(t, np.uint32).tobytes())
+        f.write(np.ascontiguousarray(uv, np.float32).tobytes())
+
+
+def run_ref_filter(rgba, sigma: float = 1.0, wrap: bool = False, spread: int = 1000, stages: int = 15,
+                   mesh=None) -> np.ndarray:
+    """The reference's lightmap filters (RRBuffer::lightmapSmooth, ...Grow...,
+    lightmapFillBackground) on one (h, w, 4) lightmap; mesh = (v, normals, t,
+    uv) gives lightmapSmooth an object, so it also smooths unwrap seams."""
+    exe = os.path.join(REF_DIR, "ref_filter")
+    with tempfile.TemporaryDirectory() as d:
+        ip, op, mp = os.path.join(d, "i"), os.path.join(d, "o"), os.path.join(d, "m")
+        write_lightmap(ip, rgba)
+        args = [exe, ip, op, repr(float(sigma)), str(int(wrap)), str(spread), str(stages)]
+        if mesh is not None:
+            write_unwrap(mp, *mesh)
+            args.append(mp)
+        subprocess.run(args, capture_output=True, text=True, check=True)
+        return read_lightmap(op)
+
+
+def run_ref_enumerate(v, normals, t, uv, size: int):
+    """The reference's texel enumeration (enumerateTexelsPartial) of one
+    unwrapped mesh into a size x size map: returns (flags (size*size,) uint8,
+    offsets (size*size+1,) uint64, sub-texels as (tri, uv (3,2), area))."""
+    exe = os.path.join(REF_DIR, "ref_enumerate")
+    with tempfile.TemporaryDirectory() as d:
+        mp, op = os.path.join(d, "m"), os.path.join(d, "o")
+        write_unwrap(mp, v, normals, t, uv)
+        subprocess.run([exe, mp, str(size), op], capture_output=True, text=True, check=True)
+        b = open(op, "rb").read()
+    assert b[:4] == b"RGE1"
+    sz, total = (int(x) for x in np.frombuffer(b, np.uint32, 2, 4))
+    S = sz * sz
+    flags = np.frombuffer(b, np.uint8, S, 12).copy()
+    counts = np.frombuffer(b, np.uint32, S, 12 + S).astype(np.uint64)
+    off = np.zeros(S + 1, np.uint64)
+    np.cumsum(counts, out=off[1:])
+    rec = np.dtype([("tri", "<u4"), ("uv", "<f4", (3, 2)), ("area", "<f4")])
+    st = np.frombuffer(b, rec, total, 12 + 5 * S).copy()
+    return flags, off, st

@@ -74,7 +74,44 @@ static float clampf_(float a, float lo, float hi) { return a < lo ? lo : (a > hi
  * sub-texel in texel order, fan order. */
 typedef void (*emit_fn)(void* ctx, uint32_t texel, uint32_t tri, const v2* uv, float area);
 
-static void raster_triangle(const float* uvm, uint32_t tri, uint32_t size, emit_fn emit, void* ctx) {
+/* Texel flags of one clipped polygon (lightmap.cpp:283-314): its vertices in
+ * texel space (texel centre at 0, the texel spans -0.5..0.5) mark the texel
+ * edges they reach and the quadrants they fall in. */
+enum { Q_X0Y0 = 1, Q_X1Y0 = 2, Q_X0Y1 = 4, Q_X1Y1 = 8, E_X0 = 16, E_X1 = 32, E_Y0 = 64, E_Y1 = 128 };
+
+static unsigned polygon_flags(const float m[3][3], const v2* poly, unsigned n, unsigned x, unsigned y, float W,
+                              float H) {
+	const float err = 0.03f;   /* ERROR_IN_TEXELS */
+	unsigned f = 0;
+	v2 old = mk2(0, 0);
+	for (unsigned k = 0; k <= n; k++) {
+		v2 p = poly[(k + n - 1) % n];   /* k = 0: the last vertex, the "old" one of vertex 0 */
+		v2 map = mk2(p.x * m[0][0] + p.y * m[0][1] + m[0][2], p.x * m[1][0] + p.y * m[1][1] + m[1][2]);
+		v2 t = mk2(map.x * W - (float)x - 0.5f, map.y * H - (float)y - 0.5f);
+		if (k) {
+			if (t.x < -0.5f + err) f |= E_X0;
+			if (t.x > 0.5f - err) f |= E_X1;
+			if (t.y < -0.5f + err) f |= E_Y0;
+			if (t.y > 0.5f - err) f |= E_Y1;
+			if (t.x < 0 && t.y < 0) f |= Q_X0Y0;
+			if (t.x > 0 && t.y < 0) f |= Q_X1Y0;
+			if (t.x < 0 && t.y > 0) f |= Q_X0Y1;
+			if (t.x > 0 && t.y > 0) f |= Q_X1Y1;
+			/* an edge crossing both axes passes a quadrant without a vertex */
+			if ((old.x < 0) != (t.x < 0) && (old.y < 0) != (t.y < 0)) {
+				float a = (t.y - old.y) / (t.x - old.x);
+				float b = t.y - a * t.x;
+				f |= (b < 0) ? (Q_X0Y0 | Q_X1Y0) : (Q_X0Y1 | Q_X1Y1);
+				f |= (-b / a < 0) ? (Q_X0Y0 | Q_X0Y1) : (Q_X1Y0 | Q_X1Y1);
+			}
+		}
+		old = t;
+	}
+	return f;
+}
+
+static void raster_triangle(const float* uvm, uint32_t tri, uint32_t size, emit_fn emit, void* ctx,
+                            uint8_t* flags) {
 	const float W = (float)size, H = (float)size;
 	v2 u0 = mk2(uvm[0], uvm[1]), u1 = mk2(uvm[2], uvm[3]), u2 = mk2(uvm[4], uvm[5]);
 	float xmin = W * fminf(u0.x, fminf(u1.x, u2.x));
@@ -140,7 +177,8 @@ static void raster_triangle(const float* uvm, uint32_t tri, uint32_t size, emit_
 #undef ISECT
 				polySize = dst;
 			}
-			if (polySize) {
+			if (polySize && flags) flags[y * size + x] |= (uint8_t)polygon_flags(m, poly, polySize, x, y, W, H);
+			if (polySize && emit) {
 				v2 st[3];
 				st[0] = poly[0];
 				for (unsigned i = 0; i + 2 < polySize; i++) {
@@ -182,13 +220,18 @@ uint64_t orc_enumerate(const float* uv, const uint32_t* tri, uint32_t n, uint32_
 	enum_ctx e = {counts, offsets, NULL, out, 0};
 	if (!out) {
 		memset(counts, 0, sizeof(uint32_t) * (size_t)size * size);
-		for (uint32_t i = 0; i < n; i++) raster_triangle(uv + 6 * (size_t)i, tri[i], size, emit_count, &e);
+		for (uint32_t i = 0; i < n; i++) raster_triangle(uv + 6 * (size_t)i, tri[i], size, emit_count, &e, NULL);
 		return e.total;
 	}
 	e.cursor = (uint32_t*)calloc((size_t)size * size, sizeof(uint32_t));
-	for (uint32_t i = 0; i < n; i++) raster_triangle(uv + 6 * (size_t)i, tri[i], size, emit_write, &e);
+	for (uint32_t i = 0; i < n; i++) raster_triangle(uv + 6 * (size_t)i, tri[i], size, emit_write, &e, NULL);
 	free(e.cursor);
 	return e.total;
+}
+
+void orc_texel_flags(const float* uv, uint32_t n, uint32_t size, uint8_t* flags) {
+	memset(flags, 0, (size_t)size * size);
+	for (uint32_t i = 0; i < n; i++) raster_triangle(uv + 6 * (size_t)i, i, size, NULL, NULL, flags);
 }
 
 /* -------------------------------------------------------------- gather */
@@ -422,14 +465,14 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 		out[1] = r.y;
 		out[2] = r.z;
 	}
-	out[3] = 1;
+	out[3] = sc->flags ? (float)sc->flags[tid] / 255.f : 1.f;
 	if (bent) {
 		v3 b = add(bentL, bentH);
 		if (b.x != 0 || b.y != 0 || b.z != 0) b = divf(b, len(b));
 		bent[0] = (b.x + 1) * 0.5f;
 		bent[1] = (b.y + 1) * 0.5f;
 		bent[2] = (b.z + 1) * 0.5f;
-		bent[3] = 1;
+		bent[3] = out[3];
 	}
 }
 

@@ -68,6 +68,7 @@ typedef struct orc_gather_scene {
 	uint64_t seed;
 	float ao_intensity;     /* UpdateParameters::aoIntensity (used when both are > 0) */
 	float ao_size;          /* UpdateParameters::aoSize */
+	const uint8_t* flags;   /* TexelFlags by texel id (alpha = flags/255, gather.cpp:801); NULL: alpha 1 */
 } orc_gather_scene;
 
 /* Sub-texels of one atlas.  uv: n triangles x 3 corners x 2 in map space
@@ -77,6 +78,10 @@ typedef struct orc_gather_scene {
  * counts, computed by the caller).  Returns the total. */
 uint64_t orc_enumerate(const float* uv, const uint32_t* tri, uint32_t n, uint32_t size, uint32_t* counts,
                        const uint64_t* offsets, orc_subtexel* out);
+/* Texel flags of one atlas (TexelFlags, RRSolver/gather.h:68-80, set in
+ * lightmap.cpp:283-314): flags[size*size], OR over every clipped polygon of
+ * every triangle in the texel.  uv as for orc_enumerate. */
+void orc_texel_flags(const float* uv, uint32_t n, uint32_t size, uint8_t* flags);
 
 /* Gathers `ntexels` texels: texel i has global id texel_id[i] (seeds its
  * sample streams) and sub-texels st[off[i] .. off[i+1]).  out: 4 floats per
@@ -93,6 +98,15 @@ void orc_gather_ex(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_
 /* Counter-based generator shared with the GPU (and with the Python
  * generators): MurmurHash3 fmix64 of (seed, stream, index). */
 uint64_t orc_hash(uint64_t seed, uint64_t stream, uint64_t index);
+
+/* Lightmap post-filters (rr_filter.c).  rgba: width*height RGBA floats,
+ * alpha = TexelFlags/255 where covered; seams: 8 floats per unwrap seam. */
+uint32_t orc_unwrap_seams(const uint32_t* idx, const float* uv, uint32_t n, float* seams, uint32_t cap);
+int orc_lightmap_smooth(float* rgba, uint32_t width, uint32_t height, float sigma, int wrap, const float* seams,
+                        uint32_t nseams);
+int orc_lightmap_grow_bilinear(float* rgba, uint32_t width, uint32_t height, int wrap);
+int orc_lightmap_grow(float* rgba, uint32_t width, uint32_t height, uint32_t steps, int wrap);
+void orc_lightmap_fill_background(float* rgba, uint32_t width, uint32_t height, const float* background);
 
 #ifdef __cplusplus
 }

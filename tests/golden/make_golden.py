@@ -7,7 +7,10 @@ oracle/ref.mk), on the seeded workloads of lightsprintsdk_gb300.scenes.
 Each fixture stores md5 hashes of its generated inputs, so the tests also
 check that the generators reproduce the same bytes on the machine they run on,
 and the reference outputs of the rays that hit (ray index, hitTriangle,
-hitDistance, hitPoint2d, hitPlane, hitFrontSide).  Test infrastructure only.
+hitDistance, hitPoint2d, hitPlane, hitFrontSide).  The lightmap fixture
+holds the reference's texel enumeration (TexelFlags, sub-texel counts and a
+hash of the sub-texels) and hashes of its post-filter outputs.  Test
+infrastructure only.
 """
 from __future__ import annotations
 
@@ -96,6 +99,57 @@ def edge_mesh():
     return v, t, np.array(rng_rays, np.float32)
 
 
+# lightmap cases: (geodesic frequency, atlas size)
+LIGHTMAP_CASES = ((4, 48), (3, 17))
+# filter runs on the first case: (stages, wrap, seams); stages as RRG_FILTER_*
+FILTER_RUNS = ((1, 0, 0), (1, 1, 0), (1, 0, 1), (2, 0, 0), (2, 1, 0), (4, 0, 0), (4, 1, 0), (8, 0, 0),
+               (15, 0, 0), (15, 0, 1), (15, 1, 1))
+
+
+def lightmap_case(freq: int, size: int):
+    """A geodesic sphere (one vertex per position, unit normals = positions)
+    with the uniform-grid unwrap into one size x size atlas."""
+    v, t = scenes.geodesic_sphere_grid(freq)
+    v = np.asarray(v, np.float32)
+    t = np.asarray(t, np.uint32)
+    nrm = (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+    uv = scenes.grid_unwrap(np.zeros(len(t), np.int32), 1)
+    return v, nrm, t, uv
+
+
+def lightmap_image(flags: np.ndarray, size: int, seed: int = 7) -> np.ndarray:
+    """A lightmap as the gather leaves it: covered texels (flags != 0) random
+    RGB in [0.1, 2) with alpha = flags/255, the rest 0."""
+    rng = np.random.default_rng(seed)
+    img = np.zeros((size * size, 4), np.float32)
+    cov = flags > 0
+    img[cov, :3] = rng.uniform(0.1, 2.0, (int(cov.sum()), 3)).astype(np.float32)
+    img[:, 3] = flags.astype(np.float32) / np.float32(255)
+    return img.reshape(size, size, 4)
+
+
+def lightmaps():
+    """Reference texel enumeration (flags, sub-texels) and post-filters."""
+    kw = {}
+    for k, (freq, size) in enumerate(LIGHTMAP_CASES):
+        v, nrm, t, uv = lightmap_case(freq, size)
+        flags, off, st = refio.run_ref_enumerate(v, nrm, t, uv, size)
+        kw[f"case{k}_mesh_md5"] = md5(v, nrm, t, uv)
+        kw[f"case{k}_flags"] = flags
+        kw[f"case{k}_counts"] = np.diff(off).astype(np.uint32)
+        kw[f"case{k}_st_md5"] = md5(st["tri"], st["uv"], st["area"])
+        if k == 0:
+            img = lightmap_image(flags, size)
+            kw["img_md5"] = md5(img)
+            for stages, wrap, seams in FILTER_RUNS:
+                out = refio.run_ref_filter(img, 1.0, bool(wrap), 1000, stages,
+                                           mesh=(v, nrm, t, uv) if seams else None)
+                kw[f"filter_{stages}_{wrap}_{seams}_md5"] = md5(out)
+                if (stages, wrap, seams) == (15, 0, 1):
+                    kw["filter_all_seams"] = out
+    save("lightmap_ref.npz", **kw)
+
+
 def main():
     assert refio.ref_available(), "build oracle/_ref first: make -f oracle/ref.mk -j8"
     # 1. HelloCollider known answer
@@ -139,6 +193,12 @@ def main():
     save("c1_fastest.npz", mesh_md5=md5(sc.vertices, sc.indices), rays_md5=md5(rays), n_cam=len(cam),
          n_sur=len(sur), n_sha=len(sha), **compact(h))
 
+    # 5. lightmaps: texel enumeration and flags, post-filters
+    lightmaps()
+
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "lightmaps":
+        lightmaps()
+    else:
+        main()
