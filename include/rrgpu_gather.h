@@ -78,6 +78,48 @@ RRG_API int rrg_lightmap_gather_host(rrg_lightmapper* lm, const rrg_gather_param
                                      uint64_t ntexels, float* out_host, void* stream);
 /* Number of texels that have sub-texels. */
 RRG_API uint64_t rrg_lightmapper_covered(const rrg_lightmapper* lm);
+/* TexelFlags of every texel (natlas*size*size bytes; RRSolver/gather.h:68-80,
+ * set by the enumeration as lightmap.cpp:283-314 does).  A gathered texel's
+ * alpha is its flags / 255 (gather.cpp:801), which the filters read. */
+RRG_API int rrg_lightmapper_copy_flags(const rrg_lightmapper* lm, uint8_t* flags_host);
+
+/* Post-filters that RRSolver::updateLightmap applies to each gathered
+ * lightmap, in this order (RRSolver/lightmap.cpp:865-874). */
+enum {
+	RRG_FILTER_SMOOTH = 1,          /* RRBuffer::lightmapSmooth (RRBuffer.cpp:630-802) */
+	RRG_FILTER_GROW_BILINEAR = 2,   /* lightmapGrowForBilinearInterpolation (RRBuffer.cpp:804-863) */
+	RRG_FILTER_GROW = 4,            /* lightmapGrow (RRBuffer.cpp:865-962) */
+	RRG_FILTER_FILL_BACKGROUND = 8, /* lightmapFillBackground (RRBuffer.cpp:964-983) */
+	RRG_FILTER_ALL = 15
+};
+
+/* RRSolver::FilteringParameters (include/Lightsprint/RRSolver.h:596-621);
+ * rrg_filter_defaults() fills its defaults. */
+typedef struct rrg_filter_params {
+	uint32_t size;               /* sizeof(rrg_filter_params) */
+	uint32_t stages;             /* RRG_FILTER_* bits, run in the order above */
+	float smoothing_amount;      /* smoothingAmount (default 1; 0 = off; capped at 10) */
+	uint32_t spread_foreground;  /* spreadForegroundColor, in texels (default 1000) */
+	float background[4];         /* backgroundColor (default 0) */
+	uint32_t wrap;               /* wrap (default 0) */
+	uint32_t seams;              /* 1: lightmapSmooth also averages across unwrap seams, as it
+	                                does when given the object (default 1) */
+} rrg_filter_params;
+RRG_API void rrg_filter_defaults(rrg_filter_params* p);
+
+/* Filters atlases [first_atlas, first_atlas + natlas) of `lightmaps_dev`
+ * in place: the lightmapper's layout (atlas a, texel (x, y) at float4 index
+ * (a * size + y) * size + x), RGBA with alpha as the gather writes it.
+ * Asynchronous on `stream` (the grow stage synchronises it every 8 steps to
+ * stop early).  Scratch (two float4 and one byte per texel of the atlases
+ * filtered) is owned by the lightmapper and grown on demand; the unwrap
+ * seams are found on the first call that asks for them: edges shared by two
+ * triangles of an atlas (by vertex index) whose unwrap differs (UnwrapSeams,
+ * RRBuffer.cpp:534-628). */
+RRG_API int rrg_lightmap_filter(rrg_lightmapper* lm, const rrg_filter_params* p, uint32_t first_atlas,
+                                uint32_t natlas, float* lightmaps_dev, void* stream);
+/* Number of unwrap seams found (0 before the first filter call with seams). */
+RRG_API uint64_t rrg_lightmapper_seams(const rrg_lightmapper* lm);
 
 /* Training records for a radiance cache (rrgpu_cache.h) from the gather's
  * own paths: from every `stride`-th covered texel, paths_per_texel plain

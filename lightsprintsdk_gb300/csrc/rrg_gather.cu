@@ -106,6 +106,7 @@ __device__ __forceinline__ float get_area(V2 v0, V2 v1, V2 v2) {
 
 struct Raster {
 	unsigned x0, x1, y0, y1;   // texel bbox [x0,x1) x [y0,y1)
+	float m[2][3];             // triangle space -> map space
 	float inv[2][3];
 	float tri_area;
 	bool ok;
@@ -143,6 +144,8 @@ __device__ Raster raster_setup(const float* uvm, unsigned size) {
 	R.inv[1][0] = __fdiv_rn(__fmul_rn(__fsub_rn(__fmul_rn(m12, m20), __fmul_rn(m10, m22)), invdet), W);
 	R.inv[1][1] = __fdiv_rn(__fmul_rn(__fsub_rn(__fmul_rn(m00, m22), __fmul_rn(m02, m20)), invdet), H);
 	R.inv[1][2] = __fmul_rn(__fsub_rn(__fmul_rn(m02, m10), __fmul_rn(m00, m12)), invdet);
+	R.m[0][0] = m00; R.m[0][1] = m01; R.m[0][2] = m02;
+	R.m[1][0] = m10; R.m[1][1] = m11; R.m[1][2] = m12;
 	R.tri_area = get_area(u0, u1, u2);
 	R.ok = true;
 	return R;
@@ -194,14 +197,54 @@ __device__ int clip_texel(const Raster& R, unsigned x, unsigned y, V2* poly) {
 	return (int)n;
 }
 
-// One warp per triangle.  COUNT: counts[texel] += sub-texels.  Otherwise
+// TexelFlags (RRSolver/gather.h:68-80) of one clipped polygon, set as in
+// lightmap.cpp:283-314: its vertices in texel space (texel centre at 0,
+// spanning -0.5..0.5) mark the texel edges they reach (within 0.03 texel)
+// and the quadrants they fall in; an edge that crosses both axes also marks
+// the quadrants it passes without a vertex.
+constexpr unsigned kQ00 = 1, kQ10 = 2, kQ01 = 4, kQ11 = 8, kEX0 = 16, kEX1 = 32, kEY0 = 64, kEY1 = 128;
+
+__device__ unsigned polygon_flags(const Raster& R, const V2* poly, int n, unsigned x, unsigned y, float W, float H) {
+	const float lo = __fadd_rn(-0.5f, 0.03f), hi = __fsub_rn(0.5f, 0.03f);
+	unsigned f = 0;
+	V2 old{0.f, 0.f};
+	for (int k = 0; k <= n; k++) {
+		const V2 p = poly[(k + n - 1) % n];   // k = 0: the last vertex, "old" of vertex 0
+		const float mx = __fadd_rn(__fadd_rn(__fmul_rn(p.x, R.m[0][0]), __fmul_rn(p.y, R.m[0][1])), R.m[0][2]);
+		const float my = __fadd_rn(__fadd_rn(__fmul_rn(p.x, R.m[1][0]), __fmul_rn(p.y, R.m[1][1])), R.m[1][2]);
+		const V2 t{__fsub_rn(__fsub_rn(__fmul_rn(mx, W), (float)x), 0.5f),
+		           __fsub_rn(__fsub_rn(__fmul_rn(my, H), (float)y), 0.5f)};
+		if (k) {
+			if (t.x < lo) f |= kEX0;
+			if (t.x > hi) f |= kEX1;
+			if (t.y < lo) f |= kEY0;
+			if (t.y > hi) f |= kEY1;
+			if (t.x < 0.f && t.y < 0.f) f |= kQ00;
+			if (t.x > 0.f && t.y < 0.f) f |= kQ10;
+			if (t.x < 0.f && t.y > 0.f) f |= kQ01;
+			if (t.x > 0.f && t.y > 0.f) f |= kQ11;
+			if ((old.x < 0.f) != (t.x < 0.f) && (old.y < 0.f) != (t.y < 0.f)) {
+				const float a = __fdiv_rn(__fsub_rn(t.y, old.y), __fsub_rn(t.x, old.x));
+				const float b = __fsub_rn(t.y, __fmul_rn(a, t.x));
+				f |= (b < 0.f) ? (kQ00 | kQ10) : (kQ01 | kQ11);
+				f |= (__fdiv_rn(-b, a) < 0.f) ? (kQ00 | kQ01) : (kQ10 | kQ11);
+			}
+		}
+		old = t;
+	}
+	return f;
+}
+
+// One warp per triangle.  COUNT: counts[texel] += sub-texels and the texel's
+// flags (4 per word) |= the polygon's.  Otherwise
 // writes them at off[texel] + cursor, with the fan index in .tri's top bits
 // replaced later by the sort.
 template <bool COUNT>
 __global__ void k_enumerate(const float* __restrict__ uv, const int32_t* __restrict__ tri_atlas, uint32_t nt,
                             uint32_t size, uint32_t natlas, uint32_t* __restrict__ counts,
                             const uint32_t* __restrict__ off, uint32_t* __restrict__ cursor, Sub* __restrict__ out,
-                            uint32_t* __restrict__ fan_out, uint64_t cap, uint32_t* err) {
+                            uint32_t* __restrict__ fan_out, uint64_t cap, uint32_t* err,
+                            uint32_t* __restrict__ flags) {
 	const int lane = threadIdx.x & 31;
 	const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -219,6 +262,10 @@ __global__ void k_enumerate(const float* __restrict__ uv, const int32_t* __restr
 			int n = clip_texel(R, x, y, poly);
 			if (n < 3) continue;
 			uint64_t texel = abase + (uint64_t)y * size + x;
+			if (COUNT && flags) {
+				const unsigned f = polygon_flags(R, poly, n, x, y, (float)size, (float)size);
+				if (f) atomicOr(&flags[texel >> 2], f << (8 * (unsigned)(texel & 3)));
+			}
 			float areas[5];
 			int valid = 0;
 			for (int i = 0; i + 2 < n; i++) {
@@ -353,7 +400,14 @@ struct GatherScene {
 	uint32_t quality, max_depth;
 	uint64_t seed;
 	float ao_intensity, ao_size;   // both > 0: ambient occlusion on the hemisphere part
+	const uint8_t* flags;          // TexelFlags per texel
 };
+
+// Alpha of a gathered texel: its TexelFlags / 255 (TEXELFLAGS_TO_FLOAT,
+// gather.cpp:801,814), which the lightmap filters read back.
+__device__ __forceinline__ float texel_alpha(const GatherScene& g, uint64_t tid) {
+	return __fdiv_rn((float)g.flags[tid], 255.f);
+}
 
 __device__ __forceinline__ V3 ld3(const float* p) { return mk(p[0], p[1], p[2]); }
 
@@ -697,7 +751,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 					if (sm.lit[r][li]) lights = add(lights, sm.light[r][li]);
 			lights = divf(lights, (float)shot);
 			if (LEARNED) {
-				out[oi] = make_float4(lights.x, lights.y, lights.z, 1.f);
+				out[oi] = make_float4(lights.x, lights.y, lights.z, texel_alpha(g, tid));
 			} else {
 				float f = __fdiv_rn(1.f, (float)Q);
 				if (g.ao_intensity > 0.f && g.ao_size > 0.f) {
@@ -707,7 +761,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 				}
 				hemi = mul(hemi, f);
 				V3 res = add(lights, hemi);
-				out[oi] = make_float4(res.x, res.y, res.z, 1.f);
+				out[oi] = make_float4(res.x, res.y, res.z, texel_alpha(g, tid));
 				if (bent_out) {
 					V3 bl = mk(0.f, 0.f, 0.f), bh = mk(0.f, 0.f, 0.f);
 					for (uint32_t r = 0; r < shot; r++)
@@ -717,7 +771,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 					V3 b = add(bl, bh);
 					if (b.x != 0.f || b.y != 0.f || b.z != 0.f) b = divf(b, len(b));
 					bent_out[oi] = make_float4(__fmul_rn(__fadd_rn(b.x, 1.f), 0.5f), __fmul_rn(__fadd_rn(b.y, 1.f), 0.5f),
-					                           __fmul_rn(__fadd_rn(b.z, 1.f), 0.5f), 1.f);
+					                           __fmul_rn(__fadd_rn(b.z, 1.f), 0.5f), texel_alpha(g, tid));
 				}
 			}
 		}
@@ -809,7 +863,7 @@ __global__ void k_learned_reduce(const uint32_t* __restrict__ off, uint64_t firs
 	}
 	hemi = mul(hemi, __fdiv_rn(1.f, (float)Q));
 	float4 l = out[i];
-	out[i] = make_float4(__fadd_rn(l.x, hemi.x), __fadd_rn(l.y, hemi.y), __fadd_rn(l.z, hemi.z), 1.f);
+	out[i] = make_float4(__fadd_rn(l.x, hemi.x), __fadd_rn(l.y, hemi.y), __fadd_rn(l.z, hemi.z), l.w);
 	if (fb_list && (float)bad > frac * (float)Q) fb_list[atomicAdd(fb_count, 1u)] = (uint32_t)tid;
 }
 
@@ -827,6 +881,11 @@ struct Lightmapper {
 	size_t stage_bytes = 0;
 	float tmin_default = 0.f;
 	uint32_t* d_covered = nullptr;   // ids of texels with sub-texels
+	uint8_t* d_flags = nullptr;      // TexelFlags per texel (ntexels rounded up to 4)
+	// host copies of the unwrap (for the lightmap filters' seam search)
+	std::vector<float> h_uv;
+	std::vector<int32_t> h_atlas;
+	LightmapFilter* filter = nullptr;   // filter scratch and seams (rrg_filter.cu)
 	uint64_t ncovered = 0;
 	// learned-gather work buffers (grown on demand)
 	CacheRec* d_recs = nullptr;
@@ -839,7 +898,9 @@ struct Lightmapper {
 
 static void free_lm(Lightmapper* L) {
 	if (!L) return;
+	filter_free(L->filter);
 	cudaFree(L->d_albedo);
+	cudaFree(L->d_flags);
 	cudaFree(L->d_off);
 	cudaFree(L->d_sub);
 	cudaFree(L->d_counter);
@@ -866,6 +927,7 @@ static int make_scene(Lightmapper* L, const rrg_gather_params* p, GatherScene& g
 	g.xyz = c->d_xyz;
 	g.idx = c->d_idx;
 	g.albedo = L->d_albedo;
+	g.flags = L->d_flags;
 	g.dir_direction = mk(p->dir_direction[0], p->dir_direction[1], p->dir_direction[2]);
 	g.dir_color = mk(p->dir_color[0], p->dir_color[1], p->dir_color[2]);
 	g.point_position = mk(p->point_position[0], p->point_position[1], p->point_position[2]);
@@ -914,6 +976,20 @@ static int gather_launch(Lightmapper* L, const rrg_gather_params* p, uint64_t fi
 
 using namespace rrg;
 
+LightmapView rrg::lightmapper_view(::rrg_lightmapper* h) {
+	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
+	LightmapView v{};
+	if (!L) return v;
+	v.c = L->c;
+	v.natlas = L->natlas;
+	v.size = L->size;
+	v.nt = L->c->nt;
+	v.uv = L->h_uv.data();
+	v.atlas = L->h_atlas.data();
+	v.filter = &L->filter;
+	return v;
+}
+
 extern "C" {
 
 int rrg_lightmapper_create(rrg_collider* ch, const float* albedo, const int32_t* tri_atlas, const float* uv,
@@ -931,6 +1007,8 @@ int rrg_lightmapper_create(rrg_collider* ch, const float* albedo, const int32_t*
 	L->size = size;
 	L->ntexels = ntexels;
 	const uint32_t nt = c->nt;
+	L->h_uv.assign(uv, uv + 6 * (size_t)nt);
+	L->h_atlas.assign(tri_atlas, tri_atlas + nt);
 	float *d_uv = nullptr;
 	int32_t* d_atlas = nullptr;
 	uint32_t *d_counts = nullptr, *d_cursor = nullptr, *d_bsum = nullptr, *d_err = nullptr, *d_fan = nullptr;
@@ -952,7 +1030,10 @@ int rrg_lightmapper_create(rrg_collider* ch, const float* albedo, const int32_t*
 	if ((e = cudaMalloc(&d_err, 4)) != cudaSuccess) return fail(e);
 	if ((e = cudaMemset(d_err, 0, 4)) != cudaSuccess) return fail(e);
 	const int grid = c->num_sms * 16;
-	k_enumerate<true><<<grid, 256>>>(d_uv, d_atlas, nt, size, natlas, d_counts, nullptr, nullptr, nullptr, nullptr, 0, d_err);
+	if ((e = cudaMalloc(&L->d_flags, (ntexels + 3) / 4 * 4)) != cudaSuccess) return fail(e);
+	if ((e = cudaMemset(L->d_flags, 0, (ntexels + 3) / 4 * 4)) != cudaSuccess) return fail(e);
+	k_enumerate<true><<<grid, 256>>>(d_uv, d_atlas, nt, size, natlas, d_counts, nullptr, nullptr, nullptr, nullptr, 0, d_err,
+	                                 reinterpret_cast<uint32_t*>(L->d_flags));
 	if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
 	const uint32_t nb = (uint32_t)((ntexels + kScanPer - 1) / kScanPer);
 	if ((e = cudaMalloc(&d_bsum, sizeof(uint32_t) * (nb + 1))) != cudaSuccess) return fail(e);
@@ -968,7 +1049,8 @@ int rrg_lightmapper_create(rrg_collider* ch, const float* albedo, const int32_t*
 	if ((e = cudaMalloc(&d_fan, sizeof(uint32_t) * (total ? total : 1))) != cudaSuccess) return fail(e);
 	if ((e = cudaMalloc(&d_cursor, sizeof(uint32_t) * ntexels)) != cudaSuccess) return fail(e);
 	if ((e = cudaMemset(d_cursor, 0, sizeof(uint32_t) * ntexels)) != cudaSuccess) return fail(e);
-	k_enumerate<false><<<grid, 256>>>(d_uv, d_atlas, nt, size, natlas, nullptr, L->d_off, d_cursor, L->d_sub, d_fan, total, d_err);
+	k_enumerate<false><<<grid, 256>>>(d_uv, d_atlas, nt, size, natlas, nullptr, L->d_off, d_cursor, L->d_sub, d_fan, total, d_err,
+	                                  nullptr);
 	k_sort_texels<<<grid, 256>>>(L->d_off, ntexels, L->d_sub, d_fan);
 	if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
 	uint32_t herr = 0;
@@ -1033,6 +1115,13 @@ int rrg_lightmapper_copy_subtexels(const rrg_lightmapper* h, uint32_t* offsets_h
 	RRG_CUDA(cudaMemcpy(offsets_host, L->d_off, sizeof(uint32_t) * (L->ntexels + 1), cudaMemcpyDeviceToHost));
 	if (subtexels_host && L->nsub)
 		RRG_CUDA(cudaMemcpy(subtexels_host, L->d_sub, sizeof(Sub) * L->nsub, cudaMemcpyDeviceToHost));
+	return RRG_OK;
+}
+
+int rrg_lightmapper_copy_flags(const rrg_lightmapper* h, uint8_t* flags_host) {
+	const Lightmapper* L = reinterpret_cast<const Lightmapper*>(h);
+	if (!L || !flags_host) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaMemcpy(flags_host, L->d_flags, L->ntexels, cudaMemcpyDeviceToHost));
 	return RRG_OK;
 }
 

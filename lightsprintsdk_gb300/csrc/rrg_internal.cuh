@@ -9,6 +9,7 @@
 #include "../../include/rrgpu.h"
 
 typedef struct rrg_batch rrg_batch;
+typedef struct rrg_lightmapper rrg_lightmapper;
 
 namespace rrg {
 
@@ -159,6 +160,18 @@ int launch_batch_closest(Collider* c, const float4* rays, uint32_t n, const uint
 // combined single-ray queries (rrg_combine.cu)
 Combiner* combiner_new();
 void combiner_free(Combiner* k);
+
+// lightmaps (rrg_gather.cu, rrg_filter.cu)
+struct LightmapFilter;
+void filter_free(LightmapFilter* f);
+struct LightmapView {
+	Collider* c;
+	uint32_t natlas, size, nt;
+	const float* uv;          // host, 6 per triangle
+	const int32_t* atlas;     // host, per triangle
+	LightmapFilter** filter;  // the lightmapper's filter state
+};
+LightmapView lightmapper_view(::rrg_lightmapper* lm);
 
 // api (rrg_api.cu)
 int cuda_fail(cudaError_t e);

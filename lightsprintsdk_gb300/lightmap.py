@@ -25,6 +25,15 @@ class GatherParams(C.Structure):
                 ("ao_size", C.c_float)]
 
 
+class FilterParams(C.Structure):
+    """rrg_filter_params: RRSolver::FilteringParameters plus the stage mask."""
+    _fields_ = [("size", C.c_uint32), ("stages", C.c_uint32), ("smoothing_amount", C.c_float),
+                ("spread_foreground", C.c_uint32), ("background", C.c_float * 4), ("wrap", C.c_uint32),
+                ("seams", C.c_uint32)]
+
+
+FILTER_SMOOTH, FILTER_GROW_BILINEAR, FILTER_GROW, FILTER_FILL_BACKGROUND, FILTER_ALL = 1, 2, 4, 8, 15
+
 _bound = False
 
 
@@ -45,6 +54,12 @@ def _lib():
         L.rrg_lightmap_gather_host.argtypes = [P, C.POINTER(GatherParams), C.c_uint64, C.c_uint64, P, P]
         L.rrg_lightmap_gather_ex.argtypes = [P, C.POINTER(GatherParams), C.c_uint64, C.c_uint64, P, P, P]
         L.rrg_lightmapper_status.argtypes = [P, P]
+        L.rrg_lightmapper_copy_flags.argtypes = [P, P]
+        L.rrg_lightmap_filter.argtypes = [P, C.POINTER(FilterParams), C.c_uint32, C.c_uint32, P, P]
+        L.rrg_lightmapper_seams.argtypes = [P]
+        L.rrg_lightmapper_seams.restype = C.c_uint64
+        L.rrg_filter_defaults.argtypes = [C.POINTER(FilterParams)]
+        L.rrg_filter_defaults.restype = None
         _bound = True
     return L
 
@@ -55,6 +70,13 @@ def make_params(lights: dict, quality: int = 64, max_depth: int = 8, seed: int =
                         (C.c_float * 3)(*lights["dir_direction"]), (C.c_float * 3)(*lights["dir_color"]),
                         (C.c_float * 3)(*lights["point_position"]), (C.c_float * 3)(*lights["point_color"]),
                         ao_intensity, ao_size)
+
+
+def filter_params(smoothing: float = 1.0, spread: int = 1000, background=(0.0, 0.0, 0.0, 0.0), wrap: bool = False,
+                  seams: bool = True, stages: int = FILTER_ALL) -> FilterParams:
+    """FilteringParameters (RRSolver.h:596-621); the defaults are the reference's."""
+    return FilterParams(C.sizeof(FilterParams), stages, smoothing, spread, (C.c_float * 4)(*background), int(wrap),
+                        int(seams))
 
 
 class RRLightmapper:
@@ -139,6 +161,26 @@ class RRLightmapper:
                            bent.data_ptr())
         self.check(torch.cuda.current_stream().cuda_stream)
         return out[:count].cpu().numpy(), bent[:count].cpu().numpy()
+
+    def flags(self) -> np.ndarray:
+        """TexelFlags of every texel (ntexels,) uint8."""
+        out = np.zeros(self.ntexels, np.uint8)
+        r = _lib().rrg_lightmapper_copy_flags(self._h, out.ctypes.data)
+        if r:
+            raise col.RRGError(r, "rrg_lightmapper_copy_flags")
+        return out
+
+    def filter_device(self, params: FilterParams, first_atlas: int, natlas: int, lightmaps_ptr: int,
+                      stream: int = 0) -> None:
+        """Post-filters atlases [first_atlas, first_atlas+natlas) of a device lightmap array laid out as the
+        gather writes it (float4 per texel, all atlases), in place (rrg_lightmap_filter)."""
+        r = _lib().rrg_lightmap_filter(self._h, C.byref(params), first_atlas, natlas, lightmaps_ptr, stream or None)
+        if r:
+            raise col.RRGError(r, "rrg_lightmap_filter")
+
+    @property
+    def nseams(self) -> int:
+        return int(_lib().rrg_lightmapper_seams(self._h))
 
     def check(self, stream: int = 0) -> None:
         r = _lib().rrg_lightmapper_status(self._h, stream or None)

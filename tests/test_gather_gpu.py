@@ -20,7 +20,7 @@ def setup():
     gs = scenes.gather_c2()
     c = col.RRCollider.create(gs.scene.vertices, gs.scene.indices)
     L = lm.RRLightmapper.from_scene(c, gs)
-    G = orc.GatherOracle(gs)
+    G = orc.GatherOracle(gs, flags=orc.gather_flags(gs, range(gs.natlas)))
     return gs, c, L, G
 
 
@@ -41,6 +41,8 @@ def test_enumeration_matches_oracle(setup, atlas):
     np.testing.assert_array_equal(g["tri"], o_st["tri"])
     np.testing.assert_array_equal(g["uv"], o_st["uv"])
     np.testing.assert_array_equal(g["area"], o_st["area"])
+    # TexelFlags of the atlas (lightmap.cpp:283-314), OR over all its polygons
+    np.testing.assert_array_equal(L.flags()[atlas * S:(atlas + 1) * S], G.flags[atlas * S:(atlas + 1) * S])
 
 
 def test_ray_length_min_is_minimal_safe_distance(setup):
@@ -86,7 +88,9 @@ def test_gather_matches_oracle(setup):
     got = gpu_gather(L, params, tids)
     ref = oracle_gather(G, tids, off, st)
     ref64 = oracle_gather(G, tids, off, st, fp64=True)
-    assert np.all(got[:, 3] == 1) and np.all(ref[:, 3] == 1)
+    # alpha = TexelFlags / 255 (gather.cpp:801), the same on both sides
+    np.testing.assert_array_equal(got[:, 3], ref[:, 3])
+    assert np.all(got[:, 3] > 0)
     rel = np.abs(got[:, :3] - ref[:, :3]) / np.maximum(np.abs(ref[:, :3]), 1e-6)
     exact = np.all(got == ref, axis=1).mean()
     assert rel.max() <= 1e-4, (rel.max(), exact)
@@ -115,7 +119,8 @@ def test_uncovered_texels_are_zero(setup):
     cnt = np.diff(off[a * S:(a + 1) * S + 1])
     out = L.gather(params, a * S, S)
     assert np.all(out[cnt == 0] == 0)
-    assert np.all(out[cnt > 0, 3] == 1)
+    fl = L.flags()[a * S:(a + 1) * S]
+    np.testing.assert_array_equal(out[:, 3], (fl.astype(np.float32) / np.float32(255)) * (cnt > 0))
     assert np.all(out[cnt > 0, :3] >= 0)
 
 
@@ -152,7 +157,7 @@ def test_ambient_occlusion_and_bent_normals_match_oracle(setup):
     gs, c, L, _ = setup
     ext = gs.scene.vertices.max(0) - gs.scene.vertices.min(0)
     ao_size = float(ext.mean() * 0.05)
-    G = orc.GatherOracle(gs, bvh=setup[3].fo, ao_intensity=1.0, ao_size=ao_size)
+    G = orc.GatherOracle(gs, bvh=setup[3].fo, ao_intensity=1.0, ao_size=ao_size, flags=setup[3].flags)
     params = lm.make_params(gs.lights, ao_intensity=1.0, ao_size=ao_size)
     tids, off, st = pick_texels(L, [0, 1, 9, 75], 32)
     got, gb = gpu_gather_bent(L, params, tids)
@@ -163,7 +168,7 @@ def test_ambient_occlusion_and_bent_normals_match_oracle(setup):
     rel = np.abs(got[:, :3] - ref[:, :3]) / np.maximum(np.abs(ref[:, :3]), 1e-6)
     assert rel.max() <= 1e-4, rel.max()
     assert np.abs(gb - rb).max() <= 1e-4, np.abs(gb - rb).max()
-    assert np.all(gb[:, 3] == 1)
+    np.testing.assert_array_equal(gb[:, 3], got[:, 3])
     # unit vectors, except texels that no light reaches: their sum is zero and,
     # as in the reference (gather.cpp:817-821), stays unnormalised
     nrm = np.linalg.norm(gb[:, :3] * 2 - 1, axis=1)
