@@ -331,6 +331,46 @@ def learned_errors(L, gs, params, out, natl, stream, sp, atlases=(0, 9, 100), se
     return {"errors_vs_converged": res}
 
 
+def filter_timing(L, out, natl, stream, sp, gs, cpu: bool) -> dict:
+    """The post-filters of updateLightmap with the reference's default
+    FilteringParameters (smoothing 1 with unwrap seams, spread 1000, background
+    0) on the gathered atlases: the first call also finds the seams on the
+    host; the second, on a fresh copy of the gathered lightmaps, is timed with
+    CUDA events.  With cpu, the oracle's filters on 4 atlases for comparison."""
+    import torch
+    from lightsprintsdk_gb300 import lightmap as lm
+    fp = lm.filter_params()
+    work = out.clone()
+    t0 = time.perf_counter()
+    L.filter_device(fp, 0, natl, work.data_ptr(), sp)
+    torch.cuda.synchronize()
+    first_s = time.perf_counter() - t0
+    work.copy_(out)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    L.filter_device(fp, 0, natl, work.data_ptr(), sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    res = {"params": "smoothing 1, seams, spread 1000, background 0", "atlases": natl,
+           "ms": e0.elapsed_time(e1), "first_call_s_with_seam_search": first_s, "seams": L.nseams,
+           "seam_runs": L.seam_runs}
+    if cpu:
+        from oracle import orc
+        S = gs.size * gs.size
+        host = out[:4 * S].cpu().numpy()
+        idx = np.asarray(gs.scene.indices, np.uint32)
+        t0 = time.perf_counter()
+        for a in range(4):
+            ids = np.nonzero(gs.tri_atlas == a)[0]
+            orc.lightmap_filter(host[a * S:(a + 1) * S].reshape(gs.size, gs.size, 4), 1.0, 1000, (0, 0, 0, 0),
+                                False, orc.unwrap_seams(idx[ids], gs.uv[ids]), 15)
+        res["cpu_port_ms_per_atlas"] = (time.perf_counter() - t0) * 1e3 / 4
+        res["cpu_sample"] = "oracle filters (1 core) on atlases 0..3, seams included"
+    del work
+    return res
+
+
 def run_gather(args, world, rank, local):
     """Config 2: plain 8-bounce lightmap gather, 64 rays per texel, 256 atlases
     of 256 x 256 texels on the interior scene."""
@@ -402,6 +442,8 @@ def run_gather(args, world, rank, local):
         del plain_out
     if learned:
         extra.update(learned_errors(L, gs, params, out, natl, stream, sp))
+    elif rank == 0:
+        extra["filters"] = filter_timing(L, out, natl, stream, sp, gs, not args.no_cpu_baseline)
     if rank == 0:
         metric = "learned lightmap texels/s" if learned else "plain lightmap texels/s"
         line = {"metric": metric, "value": world * n / (ms * 1e-3), "unit": "texels/s",

@@ -54,7 +54,7 @@ enum {
 	RRG_ERR_NO_DEVICE = 6, /* no CUDA device, or not an sm_103 device */
 	RRG_ERR_EMPTY = 7,     /* the mesh has no valid triangle */
 	RRG_ERR_TIMEOUT = 8,   /* a bounded device wait ran out */
-	RRG_ERR_TOO_LARGE = 9  /* batch above RRG_NOALLOC_MAX_RAYS (rrg_intersect_rrray_noalloc) */
+	RRG_ERR_TOO_LARGE = 9  /* batch above RRG_NOALLOC_MAX_RAYS (rrg_intersect_rrray_noalloc); 2^32 or more unwrap-seam runs (rrg_lightmap_filter) */
 };
 
 /* RRRay::Flags (include/Lightsprint/RRCollider.h:98-106). */

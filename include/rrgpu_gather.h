@@ -120,6 +120,9 @@ RRG_API int rrg_lightmap_filter(rrg_lightmapper* lm, const rrg_filter_params* p,
                                 uint32_t natlas, float* lightmaps_dev, void* stream);
 /* Number of unwrap seams found (0 before the first filter call with seams). */
 RRG_API uint64_t rrg_lightmapper_seams(const rrg_lightmapper* lm);
+/* Runs of samples over all seams (a run: consecutive samples of a seam that
+ * fall in the same pair of texels); 0 before the first filter call with seams. */
+RRG_API uint64_t rrg_lightmapper_seam_runs(const rrg_lightmapper* lm);
 
 /* Training records for a radiance cache (rrgpu_cache.h) from the gather's
  * own paths: from every `stride`-th covered texel, paths_per_texel plain

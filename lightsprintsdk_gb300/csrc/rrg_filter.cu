@@ -14,11 +14,14 @@
 // Every per-texel filter is one thread per texel over all atlases of the
 // call (HBM-bound stencils).  The seam pass is sequential by nature: the
 // reference walks each seam's 1,001 samples in order, overwriting a texel
-// whenever a run of samples leaves it, and later samples read what earlier
-// runs wrote.  It runs as one warp per atlas: the 32 lanes place 32 samples
-// at a time, runs of samples in the same texel pair are found with ballots,
-// and lanes 0..7 each carry one float component of the two accumulators, so
-// the sums are the reference's sequential float sums, bit for bit.
+// whenever a run of samples leaves it, and later seams read what earlier
+// ones wrote (on the finely tessellated atlases nearly every seam depends on
+// the one before).  So it runs as one warp per atlas over the atlas's seams,
+// and each seam is made cheap: its runs of samples in one texel pair are
+// found once, from the geometry; the used flags of the atlas sit in shared
+// memory; a seam's texel values are loaded in one round trip; lanes 0..7
+// each carry one float component of the two accumulators, adding in the
+// reference's order, so the sums are its sequential float sums, bit for bit.
 #include "rrg_internal.cuh"
 
 #include <algorithm>
@@ -45,9 +48,10 @@ struct LightmapFilter {
 	uint32_t* h_any = nullptr;        // page-locked copy of the "any atlas changed" word
 	uint32_t chg_cap = 0;
 	bool seams_built = false;
-	Seam* d_seams = nullptr;
-	uint32_t* d_seam_off = nullptr;   // natlas + 1
-	uint64_t nseams = 0;
+	uint32_t* d_seam_off = nullptr;   // natlas + 1: each atlas's seams
+	uint32_t* d_run_off = nullptr;    // nseams + 1: each seam's runs
+	uint32_t* d_runs = nullptr;       // 3 words per run
+	uint64_t nseams = 0, nruns = 0;
 };
 
 void filter_free(LightmapFilter* f) {
@@ -57,8 +61,9 @@ void filter_free(LightmapFilter* f) {
 	cudaFree(f->d_bits);
 	cudaFree(f->d_chg);
 	cudaFreeHost(f->h_any);
-	cudaFree(f->d_seams);
 	cudaFree(f->d_seam_off);
+	cudaFree(f->d_run_off);
+	cudaFree(f->d_runs);
 	delete f;
 }
 
@@ -138,91 +143,211 @@ __global__ void k_smooth_pass(const float4* __restrict__ src, float4* __restrict
 	}
 }
 
-// Seam averaging of one pass (RRBuffer.cpp:744-786), one warp per atlas,
-// seams in order.  Lane l < 8 carries component (l & 3) of accumulator
-// (l >> 2) (acc1, acc2 of the reference).  Texels with alpha 0 are never
-// written and written texels get alpha 1, so whether a sample counts (both
-// its texels have alpha != 0) does not change during the pass and is read
-// up front, 32 samples at a time.
-__global__ void __launch_bounds__(32) k_smooth_seams(float4* __restrict__ work, const Seam* __restrict__ seams,
+// Texels of sample si (0..1000) of a seam's two edges, with the reference's
+// float arithmetic (RRBuffer.cpp:752-760); false where either lies outside
+// the map.
+__device__ __forceinline__ bool seam_sample(const Seam& e, int si, float fs, uint32_t size, uint32_t& i1,
+                                            uint32_t& i2) {
+	if (si < 0 || si > 1000) return false;
+	const float b = __fmul_rn((float)si, 0.001f), am = __fsub_rn(1.f, b);
+	const float u1x = __fadd_rn(__fmul_rn(e.e1.x, am), __fmul_rn(e.e1.z, b));
+	const float u1y = __fadd_rn(__fmul_rn(e.e1.y, am), __fmul_rn(e.e1.w, b));
+	const float u2x = __fadd_rn(__fmul_rn(e.e2.x, am), __fmul_rn(e.e2.z, b));
+	const float u2y = __fadd_rn(__fmul_rn(e.e2.y, am), __fmul_rn(e.e2.w, b));
+	if (!(u1x >= 0.f && u1x < 1.f && u1y >= 0.f && u1y < 1.f && u2x >= 0.f && u2x < 1.f && u2y >= 0.f && u2y < 1.f))
+		return false;
+	i1 = (unsigned)__fmul_rn(u1x, fs) + (unsigned)__fmul_rn(u1y, fs) * size;
+	i2 = (unsigned)__fmul_rn(u2x, fs) + (unsigned)__fmul_rn(u2y, fs) * size;
+	return true;
+}
+
+constexpr uint32_t kNoTexel = 0xFFFFFFFFu;
+
+// The runs of each seam's samples: maximal runs of consecutive samples inside
+// the map whose two texels stay the same, as (texel on edge 1, texel on
+// edge 2, samples), in sample order.  They depend on the geometry only, so
+// they are found once.  One warp per seam; a lane ends a run where the next
+// sample leaves it.  COUNT: counts[s]; else the runs at 3 * off[s].
+template <bool COUNT>
+__global__ void k_seam_runs(const Seam* __restrict__ seams, uint64_t nseams, uint32_t size,
+                            uint32_t* __restrict__ counts, const uint32_t* __restrict__ off,
+                            uint32_t* __restrict__ runs) {
+	const int lane = threadIdx.x & 31;
+	const unsigned kFull = 0xFFFFFFFFu;
+	const unsigned le = (2u << lane) - 1u;   // lanes <= this one (lane 31: all)
+	const unsigned lt = (1u << lane) - 1u;
+	const float fs = (float)size;
+	for (uint64_t s = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; s < nseams;
+	     s += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+		const Seam e = seams[s];
+		uint32_t n = 0;
+		int last_start = 0;   // start of the run open at the end of the previous chunk
+		for (int c0 = 0; c0 <= 1000; c0 += 32) {
+			const int si = c0 + lane;
+			uint32_t a1 = 0, a2 = 0, b1 = 0, b2 = 0, c1 = 0, c2 = 0;
+			const bool in = seam_sample(e, si, fs, size, b1, b2);
+			const bool in_prev = seam_sample(e, si - 1, fs, size, a1, a2);
+			const bool in_next = seam_sample(e, si + 1, fs, size, c1, c2);
+			const bool start = in && !(in_prev && a1 == b1 && a2 == b2);
+			const bool end = in && !(in_next && c1 == b1 && c2 == b2);
+			const unsigned S = __ballot_sync(kFull, start), E = __ballot_sync(kFull, end);
+			const unsigned my_starts = S & le;
+			const int st = my_starts ? c0 + 31 - __clz(my_starts) : last_start;
+			if (!COUNT && end) {
+				uint32_t* r = runs + 3 * ((uint64_t)off[s] + n + __popc(E & lt));
+				r[0] = b1;
+				r[1] = b2;
+				r[2] = (uint32_t)(si - st + 1);
+			}
+			n += __popc(E);
+			if (S) last_start = c0 + 31 - __clz(S);
+		}
+		if (COUNT && lane == 0) counts[s] = n;
+	}
+}
+
+// Seam averaging of one pass (RRBuffer.cpp:744-786): one warp per atlas, its
+// seams in order (each seam reads what the earlier ones wrote, so an atlas's
+// seams are sequential).  Per seam, the lanes take 32 runs at a time: whether
+// a run counts (both its texels used, alpha != 0; texels with alpha 0 are
+// never written and written texels keep alpha 1, so this does not change
+// during the pass) and the runs' texel values, loaded together.  Then the
+// reference's walk over the runs, with lanes 0..7 each carrying one float
+// component of its two accumulators (lane l: component l & 3 of accumulator
+// l >> 2): where a texel's run ends, the texel gets its accumulator's
+// average; a run of c samples adds its texels' sum c times, in the
+// reference's order, so every value is the reference's sequential float
+// result, bit for bit.  A texel this seam wrote and reads
+// again is taken from a log of its writes.
+constexpr int kSeamLog = 2048;                 // >= the writes of one seam (2 per run)
+constexpr uint32_t kUsedSmemMax = 128 * 1024;  // used flags of atlases up to 362^2 texels in shared memory
+
+struct SeamLog {
+	uint32_t key[kSeamLog];
+	float4 val[kSeamLog];
+};
+
+// Latest value this seam wrote to `key`, if any (the last of the log's n
+// entries that matches).
+__device__ __forceinline__ bool seam_log_find(const SeamLog& lg, unsigned n, uint32_t key, int lane, float4& out) {
+	const unsigned kFull = 0xFFFFFFFFu;
+	int found = -1;
+	for (unsigned j0 = 0; j0 < n; j0 += 32) {
+		const unsigned j = j0 + (unsigned)lane;
+		const unsigned m = __ballot_sync(kFull, j < n && lg.key[j] == key);
+		if (m) found = (int)(j0 + 31 - __clz(m));
+	}
+	if (found < 0) return false;
+	out = lg.val[found];
+	return true;
+}
+
+__device__ __forceinline__ float4 shfl4(float4 x, int k) {
+	const unsigned kFull = 0xFFFFFFFFu;
+	return make_float4(__shfl_sync(kFull, x.x, k), __shfl_sync(kFull, x.y, k), __shfl_sync(kFull, x.z, k),
+	                   __shfl_sync(kFull, x.w, k));
+}
+
+__device__ __forceinline__ float comp4(const float4& x, int c) {
+	return c == 0 ? x.x : (c == 1 ? x.y : (c == 2 ? x.z : x.w));
+}
+
+__global__ void __launch_bounds__(32) k_smooth_seams(float4* __restrict__ work, const uint32_t* __restrict__ runs,
+                                                     const uint32_t* __restrict__ run_off,
                                                      const uint32_t* __restrict__ seam_off, uint32_t first_atlas,
-                                                     uint32_t size) {
+                                                     uint32_t size, int used_in_smem) {
+	extern __shared__ __align__(16) unsigned char seam_smem[];
+	SeamLog& lg = *reinterpret_cast<SeamLog*>(seam_smem);
+	uint8_t* used = seam_smem + sizeof(SeamLog);
 	const uint32_t t = blockIdx.x;   // atlas of this call
 	const uint32_t a = first_atlas + t;
 	const int lane = threadIdx.x;
 	const unsigned kFull = 0xFFFFFFFFu;
-	const uint32_t kNone = 0xFFFFFFFFu;
-	float4* img = work + (uint64_t)t * size * size;
+	const uint64_t S = (uint64_t)size * size;
+	float4* img = work + (uint64_t)t * S;
 	float* imgf = reinterpret_cast<float*>(img);
 	const int comp = lane & 3;
 	const bool carrier = lane < 8;
 	const bool first_acc = lane < 4;
-	const float fs = (float)size;
+	if (used_in_smem)
+		for (uint64_t k = lane; k < S; k += 32) used[k] = img[k].w != 0.f;
+	__syncwarp();
 	for (uint32_t s = seam_off[a]; s < seam_off[a + 1]; s++) {
-		const Seam sm = seams[s];
-		uint32_t last1 = kNone, last2 = kNone;
+		const uint64_t r0 = run_off[s];
+		const uint32_t m = (uint32_t)(run_off[s + 1] - r0);
+		uint32_t last1 = kNoTexel, last2 = kNoTexel;
+		unsigned nlog = 0;   // the same in every lane
 		float acc = 0.f, v = 0.f;
-		for (unsigned c0 = 0; c0 <= 1000; c0 += 32) {
-			const unsigned si = c0 + (unsigned)lane;
+		for (uint32_t c0 = 0; c0 < m; c0 += 32) {
+			const uint32_t j = c0 + (uint32_t)lane;
 			bool ok = false;
-			uint32_t i1 = 0, i2 = 0;
-			if (si <= 1000) {
-				const float b = __fmul_rn((float)si, 0.001f), am = __fsub_rn(1.f, b);
-				const float u1x = __fadd_rn(__fmul_rn(sm.e1.x, am), __fmul_rn(sm.e1.z, b));
-				const float u1y = __fadd_rn(__fmul_rn(sm.e1.y, am), __fmul_rn(sm.e1.w, b));
-				const float u2x = __fadd_rn(__fmul_rn(sm.e2.x, am), __fmul_rn(sm.e2.z, b));
-				const float u2y = __fadd_rn(__fmul_rn(sm.e2.y, am), __fmul_rn(sm.e2.w, b));
-				if (u1x >= 0.f && u1x < 1.f && u1y >= 0.f && u1y < 1.f && u2x >= 0.f && u2x < 1.f && u2y >= 0.f &&
-				    u2y < 1.f) {
-					i1 = (unsigned)__fmul_rn(u1x, fs) + (unsigned)__fmul_rn(u1y, fs) * size;
-					i2 = (unsigned)__fmul_rn(u2x, fs) + (unsigned)__fmul_rn(u2y, fs) * size;
-					ok = img[i1].w != 0.f && img[i2].w != 0.f;
+			uint32_t i1 = 0, i2 = 0, cnt = 0;
+			float4 x1 = make_float4(0.f, 0.f, 0.f, 0.f), x2 = x1;
+			if (j < m) {
+				const uint32_t* r = runs + 3 * (r0 + j);
+				i1 = r[0];
+				i2 = r[1];
+				cnt = r[2];
+				ok = used_in_smem ? (used[i1] && used[i2]) : (img[i1].w != 0.f && img[i2].w != 0.f);
+				if (ok) {
+					x1 = img[i1];
+					x2 = img[i2];
 				}
 			}
-			const unsigned M = __ballot_sync(kFull, ok);
-			if (!M) continue;
-			// previous counted sample: the nearest lower lane in M, or the
-			// state carried from the earlier chunks
-			const unsigned below = M & ((1u << lane) - 1u);
-			const int p = below ? 31 - __clz(below) : lane;
-			const uint32_t q1 = __shfl_sync(kFull, i1, p), q2 = __shfl_sync(kFull, i2, p);
-			const uint32_t p1 = below ? q1 : last1, p2 = below ? q2 : last2;
-			const unsigned starts = __ballot_sync(kFull, ok && (i1 != p1 || i2 != p2));
-			// samples before the first run start continue the carried run
-			const unsigned pre = starts ? (starts & (0u - starts)) - 1u : kFull;
-			unsigned n = __popc(M & pre);
-			if (carrier)
-				for (unsigned r = 0; r < n; r++) acc = __fadd_rn(acc, v);
-			unsigned rest = starts;
-			while (rest) {
-				const int k = __ffs(rest) - 1;
-				rest &= rest - 1u;
+			unsigned M = __ballot_sync(kFull, ok);
+			while (M) {
+				const int k = __ffs(M) - 1;
+				M &= M - 1u;
 				const uint32_t k1 = __shfl_sync(kFull, i1, k), k2 = __shfl_sync(kFull, i2, k);
+				const uint32_t kc = __shfl_sync(kFull, cnt, k);
+				const float4 y1 = shfl4(x1, k), y2 = shfl4(x2, k);
 				const float w1 = __shfl_sync(kFull, acc, 3), w2 = __shfl_sync(kFull, acc, 7);
+				bool changed = false;
 				if (k1 != last1) {
-					if (last1 != kNone && first_acc) imgf[4 * (size_t)last1 + comp] = __fdiv_rn(acc, w1);
+					if (last1 != kNoTexel) {
+						if (first_acc) {
+							const float q = __fdiv_rn(acc, w1);
+							imgf[4 * (size_t)last1 + comp] = q;
+							reinterpret_cast<float*>(&lg.val[nlog])[comp] = q;
+						}
+						if (lane == 0) lg.key[nlog] = last1;
+						nlog++;
+					}
 					last1 = k1;
 					if (first_acc) acc = 0.f;
+					changed = true;
 				}
 				__syncwarp();
 				if (k2 != last2) {
-					if (last2 != kNone && carrier && !first_acc) imgf[4 * (size_t)last2 + comp] = __fdiv_rn(acc, w2);
+					if (last2 != kNoTexel) {
+						if (carrier && !first_acc) {
+							const float q = __fdiv_rn(acc, w2);
+							imgf[4 * (size_t)last2 + comp] = q;
+							reinterpret_cast<float*>(&lg.val[nlog])[comp] = q;
+						}
+						if (lane == 0) lg.key[nlog] = last2;
+						nlog++;
+					}
 					last2 = k2;
 					if (carrier && !first_acc) acc = 0.f;
+					changed = true;
 				}
 				__syncwarp();
-				if (carrier) v = __fadd_rn(imgf[4 * (size_t)k1 + comp], imgf[4 * (size_t)k2 + comp]);
-				// this run's samples in the chunk: from k up to the next start
-				const unsigned upto = rest ? (rest & (0u - rest)) - 1u : kFull;
-				n = __popc(M & upto & ~((1u << k) - 1u));
+				if (changed) {
+					// the pair's values: this seam's writes, else as loaded
+					float4 z1 = y1, z2 = y2, l;
+					if (seam_log_find(lg, nlog, k1, lane, l)) z1 = l;
+					if (seam_log_find(lg, nlog, k2, lane, l)) z2 = l;
+					v = __fadd_rn(comp4(z1, comp), comp4(z2, comp));
+				}
 				if (carrier)
-					for (unsigned r = 0; r < n; r++) acc = __fadd_rn(acc, v);
+					for (uint32_t q = 0; q < kc; q++) acc = __fadd_rn(acc, v);
 			}
 		}
 		const float w1 = __shfl_sync(kFull, acc, 3), w2 = __shfl_sync(kFull, acc, 7);
-		if (last1 != kNone && first_acc) imgf[4 * (size_t)last1 + comp] = __fdiv_rn(acc, w1);
+		if (last1 != kNoTexel && first_acc) imgf[4 * (size_t)last1 + comp] = __fdiv_rn(acc, w1);
 		__syncwarp();
-		if (last2 != kNone && carrier && !first_acc) imgf[4 * (size_t)last2 + comp] = __fdiv_rn(acc, w2);
+		if (last2 != kNoTexel && carrier && !first_acc) imgf[4 * (size_t)last2 + comp] = __fdiv_rn(acc, w2);
 		__syncwarp();
 	}
 }
@@ -342,7 +467,40 @@ __global__ void k_fill_background(float4* __restrict__ lm, uint64_t n, float4 bg
 // the edge differs.  Vertices are shared by index (the reference first
 // stitches equal positions whose normals differ by at most 1 degree, which a
 // mesh with one vertex per position already is).  Host code, run once per
-// lightmapper: it is mesh preprocessing, O(triangles).
+// lightmapper: it is mesh preprocessing, O(triangles); the runs of each
+// seam's samples then come from the GPU (k_seam_runs).
+// Runs of all seams (k_seam_runs): offsets and runs, on the device.
+static int seam_runs(LightmapFilter* F, const std::vector<Seam>& seams, uint32_t size, int num_sms) {
+	struct Dev {
+		void* p = nullptr;
+		~Dev() { cudaFree(p); }
+	} dseams, cnt;
+	const uint64_t ns = seams.size();
+	RRG_CUDA(cudaMalloc(&dseams.p, sizeof(Seam) * ns));
+	RRG_CUDA(cudaMemcpy(dseams.p, seams.data(), sizeof(Seam) * ns, cudaMemcpyHostToDevice));
+	RRG_CUDA(cudaMalloc(&cnt.p, sizeof(uint32_t) * ns));
+	const int grid = (int)std::min<uint64_t>((ns * 32 + 255) / 256, (uint64_t)num_sms * 16);
+	k_seam_runs<true><<<grid, 256>>>((const Seam*)dseams.p, ns, size, (uint32_t*)cnt.p, nullptr, nullptr);
+	RRG_CUDA(cudaGetLastError());
+	std::vector<uint32_t> counts(ns);
+	RRG_CUDA(cudaMemcpy(counts.data(), cnt.p, sizeof(uint32_t) * ns, cudaMemcpyDeviceToHost));
+	std::vector<uint32_t> off(ns + 1, 0);
+	uint64_t total = 0;
+	for (uint64_t k = 0; k < ns; k++) {
+		total += counts[k];
+		if (total >= (1ull << 32)) return RRG_ERR_TOO_LARGE;   // run offsets are 32-bit
+		off[k + 1] = (uint32_t)total;
+	}
+	F->nruns = total;
+	RRG_CUDA(cudaMalloc(&F->d_run_off, sizeof(uint32_t) * (ns + 1)));
+	RRG_CUDA(cudaMemcpy(F->d_run_off, off.data(), sizeof(uint32_t) * (ns + 1), cudaMemcpyHostToDevice));
+	RRG_CUDA(cudaMalloc(&F->d_runs, sizeof(uint32_t) * 3 * (off[ns] ? off[ns] : 1)));
+	k_seam_runs<false><<<grid, 256>>>((const Seam*)dseams.p, ns, size, nullptr, F->d_run_off, F->d_runs);
+	RRG_CUDA(cudaGetLastError());
+	RRG_CUDA(cudaDeviceSynchronize());
+	return RRG_OK;
+}
+
 static int build_seams(const LightmapView& v, LightmapFilter* F) {
 	const uint32_t nt = v.nt, natlas = v.natlas;
 	std::vector<uint32_t> idx(3 * (size_t)nt);
@@ -413,12 +571,13 @@ static int build_seams(const LightmapView& v, LightmapFilter* F) {
 		for (uint32_t vi : touched) cnt[vi] = fill[vi] = 0;
 		soff[a + 1] = (uint32_t)seams.size();
 	}
+	F->nseams = seams.size();
 	RRG_CUDA(cudaMalloc(&F->d_seam_off, sizeof(uint32_t) * (natlas + 1)));
 	RRG_CUDA(cudaMemcpy(F->d_seam_off, soff.data(), sizeof(uint32_t) * (natlas + 1), cudaMemcpyHostToDevice));
-	RRG_CUDA(cudaMalloc(&F->d_seams, sizeof(Seam) * (seams.size() ? seams.size() : 1)));
-	if (!seams.empty())
-		RRG_CUDA(cudaMemcpy(F->d_seams, seams.data(), sizeof(Seam) * seams.size(), cudaMemcpyHostToDevice));
-	F->nseams = seams.size();
+	if (!seams.empty()) {
+		int st = seam_runs(F, seams, v.size, v.c->num_sms);
+		if (st) return st;
+	}
 	F->seams_built = true;
 	return RRG_OK;
 }
@@ -494,6 +653,11 @@ int rrg_lightmap_filter(rrg_lightmapper* h, const rrg_filter_params* p, uint32_t
 			if (st) return st;
 		}
 		const bool seams = p->seams && F->nseams;
+		const int used_in_smem = S <= kUsedSmemMax ? 1 : 0;
+		const size_t seam_smem = sizeof(SeamLog) + (used_in_smem ? (size_t)S : 0);
+		if (seams)
+			RRG_CUDA(cudaFuncSetAttribute(k_smooth_seams, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                              (int)seam_smem));
 		k_smooth_prep<<<grid, threads, 0, s>>>(lm, F->d_a, F->d_bits, v.size, n, wrap);
 		if (sigma > 10.f) sigma = 10.f;
 		float sum = sigma * sigma;
@@ -505,7 +669,9 @@ int rrg_lightmap_filter(rrg_lightmapper* h, const rrg_filter_params* p, uint32_t
 			const float k1 = expf(-0.5f / s2), k2 = expf(-1.f / s2);
 			sum -= s2;
 			k_smooth_pass<<<grid, threads, 0, s>>>(src, dst, F->d_bits, v.size, n, k1, k2);
-			if (seams) k_smooth_seams<<<natlas, 32, 0, s>>>(dst, F->d_seams, F->d_seam_off, first_atlas, v.size);
+			if (seams)
+				k_smooth_seams<<<natlas, 32, seam_smem, s>>>(dst, F->d_runs, F->d_run_off, F->d_seam_off, first_atlas,
+				                                             v.size, used_in_smem);
 			std::swap(src, dst);
 		}
 		k_smooth_store<<<grid, threads, 0, s>>>(lm, src, n);
@@ -548,6 +714,11 @@ int rrg_lightmap_filter(rrg_lightmapper* h, const rrg_filter_params* p, uint32_t
 uint64_t rrg_lightmapper_seams(const rrg_lightmapper* h) {
 	LightmapView v = lightmapper_view(const_cast<rrg_lightmapper*>(h));
 	return (v.filter && *v.filter) ? (*v.filter)->nseams : 0;
+}
+
+uint64_t rrg_lightmapper_seam_runs(const rrg_lightmapper* h) {
+	LightmapView v = lightmapper_view(const_cast<rrg_lightmapper*>(h));
+	return (v.filter && *v.filter) ? (*v.filter)->nruns : 0;
 }
 
 }  // extern "C"

@@ -58,6 +58,8 @@ def _lib():
         L.rrg_lightmap_filter.argtypes = [P, C.POINTER(FilterParams), C.c_uint32, C.c_uint32, P, P]
         L.rrg_lightmapper_seams.argtypes = [P]
         L.rrg_lightmapper_seams.restype = C.c_uint64
+        L.rrg_lightmapper_seam_runs.argtypes = [P]
+        L.rrg_lightmapper_seam_runs.restype = C.c_uint64
         L.rrg_filter_defaults.argtypes = [C.POINTER(FilterParams)]
         L.rrg_filter_defaults.restype = None
         _bound = True
@@ -181,6 +183,10 @@ class RRLightmapper:
     @property
     def nseams(self) -> int:
         return int(_lib().rrg_lightmapper_seams(self._h))
+
+    @property
+    def seam_runs(self) -> int:
+        return int(_lib().rrg_lightmapper_seam_runs(self._h))
 
     def check(self, stream: int = 0) -> None:
         r = _lib().rrg_lightmapper_status(self._h, stream or None)
