@@ -9,7 +9,8 @@
  * lights are one directional and one point light with REALISTIC falloff
  * (RRLight.cpp:345-362, 450-455).  Lightmaps are `natlas` square atlases of
  * size x size texels, float RGBA per texel (RGB = irradiance in the
- * reference's physical scale, A = 1 where the texel is covered).
+ * reference's physical scale, A = the texel's TexelFlags / 255 where it is
+ * covered, 0 elsewhere, as the reference stores it, gather.cpp:801).
  *
  * Texel t of atlas a has global id a*size*size + y*size + x; its sample
  * streams are seeded by that id, so any subset of texels can be gathered and
@@ -69,8 +70,8 @@ RRG_API int rrg_lightmap_gather(rrg_lightmapper* lm, const rrg_gather_params* p,
                                 uint64_t ntexels, float* out_dev, void* stream);
 /* Same, plus the bent normal of each texel when bent_dev != NULL (4 floats
  * per texel, the reference's LS_BENT_NORMALS encoding: (n + 1) / 2 of the
- * normalised sum of the lights' and the hemisphere's bent normals, w = 1
- * where covered; gather.cpp:274,488,811-830). */
+ * normalised sum of the lights' and the hemisphere's bent normals, w = the
+ * texel's alpha; gather.cpp:274,488,811-830). */
 RRG_API int rrg_lightmap_gather_ex(rrg_lightmapper* lm, const rrg_gather_params* p, uint64_t first_texel,
                                    uint64_t ntexels, float* out_dev, float* bent_dev, void* stream);
 /* Same into host memory; synchronous. */
