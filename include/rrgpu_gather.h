@@ -77,6 +77,18 @@ RRG_API int rrg_lightmap_gather_ex(rrg_lightmapper* lm, const rrg_gather_params*
 /* Same into host memory; synchronous. */
 RRG_API int rrg_lightmap_gather_host(rrg_lightmapper* lm, const rrg_gather_params* p, uint64_t first_texel,
                                      uint64_t ntexels, float* out_host, void* stream);
+/* Directional lightmaps (LS_DIRECTION1..3, "compatible with Unreal Engine
+ * 3", gather.cpp:43-49): when any of dir1..3 is non-NULL the gather runs in
+ * the reference's directional mode (gatherAllDirections, lightmap.cpp:820):
+ * each hemisphere sample and light is weighted by its cosine to each of the
+ * four directions of the texel's tangent basis (gather.cpp:255-272,
+ * 468-486), and out (LS_LIGHTMAP) is computed that way too, as the
+ * reference does when directional buffers are requested.  Each non-NULL
+ * buffer: 4 floats per texel, 16-byte aligned device memory; bent_dev may
+ * be NULL.  Asynchronous on `stream`. */
+RRG_API int rrg_lightmap_gather_directional(rrg_lightmapper* lm, const rrg_gather_params* p, uint64_t first_texel,
+                                            uint64_t ntexels, float* out_dev, float* dir1_dev, float* dir2_dev,
+                                            float* dir3_dev, float* bent_dev, void* stream);
 /* Number of texels that have sub-texels. */
 RRG_API uint64_t rrg_lightmapper_covered(const rrg_lightmapper* lm);
 /* TexelFlags of every texel (natlas*size*size bytes; RRSolver/gather.h:68-80,

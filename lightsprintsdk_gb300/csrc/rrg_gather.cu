@@ -29,6 +29,7 @@
 #include "../../include/rrgpu_cache.h"
 #include "rrg_mlp.cuh"
 
+#include <type_traits>
 #include <vector>
 
 namespace rrg {
@@ -401,6 +402,12 @@ struct GatherScene {
 	uint64_t seed;
 	float ao_intensity, ao_size;   // both > 0: ambient occlusion on the hemisphere part
 	const uint8_t* flags;          // TexelFlags per texel
+	float ldir[4][3];              // LS_LIGHTMAP, LS_DIRECTION1..3 in tangent space (gather.cpp:43-49)
+};
+
+// Outputs of the directional mode (LS_DIRECTION1..3, each may be null).
+struct DirOut {
+	float4* d[3];
 };
 
 // Alpha of a gathered texel: its TexelFlags / 255 (TEXELFLAGS_TO_FLOAT,
@@ -609,6 +616,17 @@ struct WarpSmem {
 	unsigned next;   // next unclaimed sample of the texel
 };
 
+// Directional mode (gatherAllDirections, lightmap.cpp:820): each hemisphere
+// sample's weights for the four lightmap directions (its cosine to the
+// direction over its cosine to the normal; < 0: not added,
+// gather.cpp:255-272), and each light's irradiance and cosines to the
+// directions (gather.cpp:468-486).
+struct WarpSmemDir {
+	float wgt[kMaxQuality][4];
+	V3 lirr[kMaxRounds][2];
+	float lw[kMaxRounds][2][4];
+};
+
 // RRVec3::abs().avg() (RRMath.h:170-171), one rounding per operation
 __device__ __forceinline__ float absavg3(V3 a) {
 	return __fmul_rn(__fadd_rn(__fadd_rn(fabsf(a.x), fabsf(a.y)), fabsf(a.z)), 0.33333333333333f);
@@ -618,15 +636,18 @@ __device__ __forceinline__ float absavg3(V3 a) {
 // LEARNED = true : first segments only; recs[(tid - out_base) * Q + k] get the
 // cache queries and out[tid - out_base] the light rounds' average (the plain
 // texel's first term) with w = 1.  list (may be null) selects texel ids.
-template <bool LEARNED>
+template <bool LEARNED, bool DIR = false>
 __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, const uint32_t* __restrict__ off,
                                                               const Sub* __restrict__ st, uint64_t first,
                                                               uint64_t count, const uint32_t* __restrict__ list,
                                                               uint64_t out_base, float4* __restrict__ out,
                                                               CacheRec* __restrict__ recs, uint32_t* counter,
-                                                              uint32_t* status, float4* __restrict__ bent_out) {
+                                                              uint32_t* status, float4* __restrict__ bent_out,
+                                                              DirOut dout = DirOut{}) {
 	__shared__ WarpSmem sm_all[kGatherWarps];
 	WarpSmem& sm = sm_all[threadIdx.x >> 5];
+	__shared__ typename std::conditional<DIR, WarpSmemDir, char>::type smd_all[kGatherWarps];
+	auto& smd = smd_all[threadIdx.x >> 5];
 	const int lane = threadIdx.x & 31;
 	const uint32_t Q = g.quality;
 	const uint32_t rounds = Q / 10 + 1;
@@ -643,6 +664,9 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 		if (m == 0) {
 			if (lane == 0) out[oi] = make_float4(0.f, 0.f, 0.f, 0.f);
 			if (lane == 0 && bent_out) bent_out[oi] = make_float4(0.f, 0.f, 0.f, 0.f);
+			if (DIR && lane == 0)
+				for (int i = 0; i < 3; i++)
+					if (dout.d[i]) dout.d[i][oi] = make_float4(0.f, 0.f, 0.f, 0.f);
 			continue;
 		}
 		const Sub* S = st + b;
@@ -696,6 +720,18 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 			V3 nrm = normalized(add(add(mul(fn, w), mul(fn, cu)), mul(fn, cv)));
 			V3 tg, bt;
 			basis_from_normal(nrm, tg, bt);
+			// directional mode: the skewed basis (gather.cpp:725-730; the vertices'
+			// bases are the plane normal's, RRMesh.cpp:77-91) and the four
+			// lightmap directions in it
+			V3 ldir[4];
+			if (DIR) {
+				V3 ft, fb;
+				basis_from_normal(fn, ft, fb);
+				const V3 ts = normalized(add(add(mul(ft, w), mul(ft, cu)), mul(ft, cv)));
+				const V3 bs = normalized(add(add(mul(fb, w), mul(fb, cu)), mul(fb, cv)));
+				for (int i = 0; i < 4; i++)
+					ldir[i] = normalized(add(add(mul(ts, g.ldir[i][0]), mul(bs, g.ldir[i][1])), mul(nrm, g.ldir[i][2])));
+			}
 			const uint64_t sid = tid * N + k;
 			uint32_t ru = rng24(g.seed, S_PU, sid), rv = rng24(g.seed, S_PV, sid);
 			if (ru + rv > kM24) { ru = kM24 - ru; rv = kM24 - rv; }
@@ -721,6 +757,14 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 					sm.fx[k] = bk.x;
 					sm.fy[k] = bk.y;
 					sm.fd[k] = bk.z;
+					if constexpr (DIR) {
+						const float ni1 = dot(dir, nrm);
+						const float inv = ni1 > 0.f ? __fdiv_rn(1.f, ni1) : 0.f;
+						for (int i = 0; i < 4; i++) {
+							const float ni2 = dot(dir, ldir[i]);
+							smd.wgt[k][i] = (ni1 > 0.f && ni2 > 0.f) ? __fmul_rn(ni2, inv) : -1.f;
+						}
+					}
 				}
 			}
 			if (fires && round < (uint32_t)kMaxRounds) {
@@ -736,6 +780,13 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 					V3 irr = li == 0 ? g.dir_color : point_irr(g, origin);
 					sm.light[round][li] = mul(irr, ni);
 					sm.lbent[round][li] = mul(d, __fmul_rn(absavg3(irr), ni));   // gather.cpp:488
+					if constexpr (DIR) {
+						smd.lirr[round][li] = irr;
+						for (int i = 0; i < 4; i++) {
+							const float ni2 = dot(d, ldir[i]);
+							smd.lw[round][li][i] = ni2 > 0.f ? ni2 : -1.f;
+						}
+					}
 					sm.lit[round][li] = 1;
 				}
 			}
@@ -761,6 +812,22 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 				}
 				hemi = mul(hemi, f);
 				V3 res = add(lights, hemi);
+				if constexpr (DIR) {
+					// every output weighted by its direction, summed in sample order
+					for (int i = 0; i < 4; i++) {
+						V3 hi = mk(0.f, 0.f, 0.f), li_ = mk(0.f, 0.f, 0.f);
+						for (uint32_t k = 0; k < Q; k++)
+							if (smd.wgt[k][i] >= 0.f) hi = add(hi, mul(sm.hemi[k], smd.wgt[k][i]));
+						for (uint32_t r = 0; r < shot; r++)
+							for (int l = 0; l < 2; l++)
+								if (sm.lit[r][l] && smd.lw[r][l][i] >= 0.f) li_ = add(li_, mul(smd.lirr[r][l], smd.lw[r][l][i]));
+						const V3 ri = add(divf(li_, (float)shot), mul(hi, f));
+						if (i == 0)
+							res = ri;
+						else if (dout.d[i - 1])
+							dout.d[i - 1][oi] = make_float4(ri.x, ri.y, ri.z, texel_alpha(g, tid));
+					}
+				}
 				out[oi] = make_float4(res.x, res.y, res.z, texel_alpha(g, tid));
 				if (bent_out) {
 					V3 bl = mk(0.f, 0.f, 0.f), bh = mk(0.f, 0.f, 0.f);
@@ -928,6 +995,11 @@ static int make_scene(Lightmapper* L, const rrg_gather_params* p, GatherScene& g
 	g.idx = c->d_idx;
 	g.albedo = L->d_albedo;
 	g.flags = L->d_flags;
+	{   // UE3 lightmap directions, gather.cpp:43-49 (host sqrtf, as the reference's static table)
+		const float s6 = sqrtf(6.0f), s3 = sqrtf(3.0f), s2 = sqrtf(2.0f);
+		const float D[4][3] = {{0.f, 0.f, 1.f}, {0.f, s6 / 3, 1 / s3}, {-1 / s2, -1 / s6, 1 / s3}, {1 / s2, -1 / s6, 1 / s3}};
+		memcpy(g.ldir, D, sizeof(D));
+	}
 	g.dir_direction = mk(p->dir_direction[0], p->dir_direction[1], p->dir_direction[2]);
 	g.dir_color = mk(p->dir_color[0], p->dir_color[1], p->dir_color[2]);
 	g.point_position = mk(p->point_position[0], p->point_position[1], p->point_position[2]);
@@ -944,30 +1016,33 @@ static int make_scene(Lightmapper* L, const rrg_gather_params* p, GatherScene& g
 	return RRG_OK;
 }
 
-template <bool LEARNED>
+template <bool LEARNED, bool DIR = false>
 static int launch_gather_kernel(Lightmapper* L, const GatherScene& g, uint64_t first, uint64_t count,
                                 const uint32_t* list, uint64_t out_base, float4* out, CacheRec* recs, cudaStream_t s,
-                                float4* bent = nullptr) {
+                                float4* bent = nullptr, DirOut dout = DirOut{}) {
 	if (!count) return RRG_OK;
 	RRG_CUDA(cudaMemsetAsync(L->d_counter, 0, 8, s));
 	int per_sm = 0;
-	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather<LEARNED>, kGatherWarps * 32, 0));
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather<LEARNED, DIR>, kGatherWarps * 32, 0));
 	uint64_t want = (count + kGatherWarps - 1) / kGatherWarps;
 	uint64_t cap = (uint64_t)(per_sm > 0 ? per_sm : 1) * L->c->num_sms;
 	int grid = (int)(want < cap ? want : cap);
-	k_gather<LEARNED><<<grid, kGatherWarps * 32, 0, s>>>(g, L->d_off, L->d_sub, first, count, list, out_base, out, recs,
-	                                                     reinterpret_cast<uint32_t*>(L->d_counter), L->d_status,
-	                                                     LEARNED ? nullptr : bent);
+	k_gather<LEARNED, DIR><<<grid, kGatherWarps * 32, 0, s>>>(g, L->d_off, L->d_sub, first, count, list, out_base, out,
+	                                                          recs, reinterpret_cast<uint32_t*>(L->d_counter), L->d_status,
+	                                                          LEARNED ? nullptr : bent, dout);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }
 
 static int gather_launch(Lightmapper* L, const rrg_gather_params* p, uint64_t first, uint64_t count, float* out_dev,
-                         cudaStream_t s, float* bent_dev = nullptr) {
+                         cudaStream_t s, float* bent_dev = nullptr, const DirOut* dirs = nullptr) {
 	GatherScene g;
 	int st = make_scene(L, p, g);
 	if (st) return st;
 	if (first + count > L->ntexels) return RRG_ERR_INVALID;
+	if (dirs && (dirs->d[0] || dirs->d[1] || dirs->d[2]))
+		return launch_gather_kernel<false, true>(L, g, first, count, nullptr, first, reinterpret_cast<float4*>(out_dev),
+		                                         nullptr, s, reinterpret_cast<float4*>(bent_dev), *dirs);
 	return launch_gather_kernel<false>(L, g, first, count, nullptr, first, reinterpret_cast<float4*>(out_dev), nullptr,
 	                                   s, reinterpret_cast<float4*>(bent_dev));
 }
@@ -1137,6 +1212,18 @@ int rrg_lightmap_gather_ex(rrg_lightmapper* h, const rrg_gather_params* p, uint6
 	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
 	if (!L || !out_dev || ((uintptr_t)out_dev & 15) || ((uintptr_t)bent_dev & 15)) return RRG_ERR_INVALID;
 	return gather_launch(L, p, first_texel, ntexels, out_dev, (cudaStream_t)stream, bent_dev);
+}
+
+int rrg_lightmap_gather_directional(rrg_lightmapper* h, const rrg_gather_params* p, uint64_t first_texel,
+                                    uint64_t ntexels, float* out_dev, float* dir1_dev, float* dir2_dev, float* dir3_dev,
+                                    float* bent_dev, void* stream) {
+	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
+	if (!L || !out_dev || ((uintptr_t)out_dev & 15) || ((uintptr_t)bent_dev & 15) || ((uintptr_t)dir1_dev & 15) ||
+	    ((uintptr_t)dir2_dev & 15) || ((uintptr_t)dir3_dev & 15))
+		return RRG_ERR_INVALID;
+	const DirOut d{{reinterpret_cast<float4*>(dir1_dev), reinterpret_cast<float4*>(dir2_dev),
+	                reinterpret_cast<float4*>(dir3_dev)}};
+	return gather_launch(L, p, first_texel, ntexels, out_dev, (cudaStream_t)stream, bent_dev, &d);
 }
 
 int rrg_lightmap_gather_host(rrg_lightmapper* h, const rrg_gather_params* p, uint64_t first_texel, uint64_t ntexels,

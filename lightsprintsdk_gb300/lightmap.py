@@ -53,6 +53,8 @@ def _lib():
         L.rrg_lightmap_gather.argtypes = [P, C.POINTER(GatherParams), C.c_uint64, C.c_uint64, P, P]
         L.rrg_lightmap_gather_host.argtypes = [P, C.POINTER(GatherParams), C.c_uint64, C.c_uint64, P, P]
         L.rrg_lightmap_gather_ex.argtypes = [P, C.POINTER(GatherParams), C.c_uint64, C.c_uint64, P, P, P]
+        L.rrg_lightmap_gather_directional.argtypes = [P, C.POINTER(GatherParams), C.c_uint64, C.c_uint64, P, P, P, P,
+                                                      P, P]
         L.rrg_lightmapper_status.argtypes = [P, P]
         L.rrg_lightmapper_copy_flags.argtypes = [P, P]
         L.rrg_lightmap_filter.argtypes = [P, C.POINTER(FilterParams), C.c_uint32, C.c_uint32, P, P]
@@ -150,6 +152,23 @@ class RRLightmapper:
             r = _lib().rrg_lightmap_gather(self._h, C.byref(params), first, count, out_ptr, stream or None)
         if r:
             raise col.RRGError(r, "rrg_lightmap_gather")
+
+    def gather_directional(self, params: GatherParams, first: int = 0, count: int | None = None):
+        """Directional mode (rrg_lightmap_gather_directional): host arrays (LS_LIGHTMAP (count,4),
+        LS_DIRECTION1..3 (count,3,4), bent normals (count,4))."""
+        import torch
+        if count is None:
+            count = self.ntexels - first
+        n = max(count, 1)
+        bufs = [torch.empty((n, 4), dtype=torch.float32, device="cuda") for _ in range(5)]
+        sp = torch.cuda.current_stream().cuda_stream
+        r = _lib().rrg_lightmap_gather_directional(self._h, C.byref(params), first, count,
+                                                   *[b.data_ptr() for b in bufs], sp)
+        if r:
+            raise col.RRGError(r, "rrg_lightmap_gather_directional")
+        self.check(sp)
+        host = [b[:count].cpu().numpy() for b in bufs]
+        return host[0], np.stack(host[1:4], axis=1), host[4]
 
     def gather_bent(self, params: GatherParams, first: int = 0, count: int | None = None):
         """Texels [first, first+count) -> ((count, 4) irradiance, (count, 4) bent normals) host arrays,

@@ -62,6 +62,7 @@ def lib():
         L.orc_lightmap_fill_background.argtypes = [P, U, U, P]
         L.orc_gather.argtypes = [P, C.POINTER(GatherScene), P, U, P, P, C.c_int, C.c_int, P]
         L.orc_gather_ex.argtypes = [P, C.POINTER(GatherScene), P, U, P, P, C.c_int, C.c_int, P, P]
+        L.orc_gather_dir.argtypes = [P, C.POINTER(GatherScene), P, U, P, P, C.c_int, C.c_int, P, P, P]
         L.orc_hash.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
         L.orc_hash.restype = C.c_uint64
         L.orc_mlp_encode.argtypes = [P, P, P, P, P, P]
@@ -267,6 +268,19 @@ class GatherOracle:
                             _ptr(st) if len(st) else None, threads, int(fp64), _ptr(out),
                             _ptr(bn) if bent else None)
         return (out, bn) if bent else out
+
+    def gather_directional(self, texel_ids: np.ndarray, off: np.ndarray, st: np.ndarray, threads: int = 0):
+        """Directional mode: (LS_LIGHTMAP (n,4), LS_DIRECTION1..3 (n,3,4), bent normals (n,4))."""
+        texel_ids = np.ascontiguousarray(texel_ids, np.uint64)
+        off = np.ascontiguousarray(off, np.uint64)
+        st = np.ascontiguousarray(st)
+        n = texel_ids.shape[0]
+        out = np.zeros((n, 4), np.float32)
+        bn = np.zeros((n, 4), np.float32)
+        dirs = np.zeros((n, 3, 4), np.float32)
+        lib().orc_gather_dir(self.fo.h, C.byref(self.s), _ptr(texel_ids), n, _ptr(off), _ptr(st) if len(st) else None,
+                             threads, 0, _ptr(out), _ptr(bn), _ptr(dirs))
+        return out, dirs, bn
 
 
 # --------------------------------------------------------------- network

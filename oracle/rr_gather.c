@@ -357,9 +357,21 @@ static void path(const orc_bvh* bvh, const orc_gather_scene* sc, v3 eye, v3 dir,
 /* RRVec3::abs().avg() (RRMath.h:170-171) */
 static float absavg(v3 v) { return (fabsf(v.x) + fabsf(v.y) + fabsf(v.z)) * 0.33333333333333f; }
 
+/* Directional lightmaps, compatible with Unreal Engine 3 (gather.cpp:43-49):
+ * LS_LIGHTMAP and LS_DIRECTION1..3 in tangent space. */
+static void lightmap_directions(float D[4][3]) {
+	const float s6 = sqrtf(6.0f), s3 = sqrtf(3.0f), s2 = sqrtf(2.0f);
+	D[0][0] = 0; D[0][1] = 0; D[0][2] = 1;
+	D[1][0] = 0; D[1][1] = s6 / 3; D[1][2] = 1 / s3;
+	D[2][0] = -1 / s2; D[2][1] = -1 / s6; D[2][2] = 1 / s3;
+	D[3][0] = 1 / s2; D[3][1] = -1 / s6; D[3][2] = 1 / s3;
+}
+
 static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_t tid, const orc_subtexel* S,
-                         uint32_t m, int fp64, float* out, float* bent) {
+                         uint32_t m, int fp64, float* out, float* bent, float* dirs) {
 	if (bent) bent[0] = bent[1] = bent[2] = bent[3] = 0;
+	if (dirs)
+		for (int i = 0; i < 12; i++) dirs[i] = 0;
 	if (!m) {
 		out[0] = out[1] = out[2] = out[3] = 0;
 		return;
@@ -382,6 +394,12 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 	unsigned num = (unsigned)(orc_hash(sc->seed, S_FILLER, tid) & 0xffff);
 	v3 hemi = mk(0, 0, 0), lights = mk(0, 0, 0);
 	d3 hemiD = {0, 0, 0}, lightsD = {0, 0, 0};
+	/* directional mode (gatherAllDirections, lightmap.cpp:820): all four
+	 * outputs weighted by the UE3 basis (gather.cpp:255-272, 468-486) */
+	float D[4][3];
+	lightmap_directions(D);
+	v3 hemiI[4], lightsI[4];
+	for (int i = 0; i < 4; i++) hemiI[i] = lightsI[i] = mk(0, 0, 0);
 	uint32_t gl = 0, shotRounds = 0;
 	const float tmin = sc->ray_length_min;
 	for (uint32_t k = 0; k < N; k++) {
@@ -401,6 +419,18 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 		v3 nrm = normalized(add(add(mul(fn, w), mul(fn, cu)), mul(fn, cv)));
 		v3 tg, bt;
 		basis_from_normal(nrm, &tg, &bt);
+		/* the skewed basis (gather.cpp:725-730): the vertices' bases (each the
+		 * plane normal's, RRMesh.cpp:77-91) interpolated and normalised, and the
+		 * four lightmap directions in it */
+		v3 ldir[4];
+		if (dirs) {
+			v3 ft, fb;
+			basis_from_normal(fn, &ft, &fb);
+			v3 ts = normalized(add(add(mul(ft, w), mul(ft, cu)), mul(ft, cv)));
+			v3 bs = normalized(add(add(mul(fb, w), mul(fb, cu)), mul(fb, cv)));
+			for (int i = 0; i < 4; i++)
+				ldir[i] = normalized(add(add(mul(ts, D[i][0]), mul(bs, D[i][1])), mul(nrm, D[i][2])));
+		}
 		/* random point in the sub-texel (gather.cpp:742-752) */
 		uint64_t sid = tid * N + k;
 		uint32_t ru = rng24(sc->seed, S_PU, sid), rv = rng24(sc->seed, S_PV, sid);
@@ -424,6 +454,16 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 			if (first_t > sc->ao_size) distant++;
 			bentH = add(bentH, mul(dir, absavg(L)));
 			hemi = add(hemi, L);
+			if (dirs) {
+				float ni1 = dot(dir, nrm);
+				if (ni1 > 0) {
+					float inv = 1 / ni1;
+					for (int i = 0; i < 4; i++) {
+						float ni2 = dot(dir, ldir[i]);
+						if (ni2 > 0) hemiI[i] = add(hemiI[i], mul(L, ni2 * inv));
+					}
+				}
+			}
 			hemiD.x += LD.x;
 			hemiD.y += LD.y;
 			hemiD.z += LD.z;
@@ -441,6 +481,11 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 				v3 irr = li == 0 ? ld3(sc->dir_color) : point_irradiance(sc, origin);
 				bentL = add(bentL, mul(d, absavg(irr) * ni));
 				lights = add(lights, mul(irr, ni));
+				if (dirs)
+					for (int i = 0; i < 4; i++) {
+						float ni2 = dot(d, ldir[i]);
+						if (ni2 > 0) lightsI[i] = add(lightsI[i], mul(irr, ni2));
+					}
 				lightsD.x += (double)irr.x * ni;
 				lightsD.y += (double)irr.y * ni;
 				lightsD.z += (double)irr.z * ni;
@@ -466,6 +511,18 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 		out[2] = r.z;
 	}
 	out[3] = sc->flags ? (float)sc->flags[tid] / 255.f : 1.f;
+	if (dirs) {
+		float f = 1 / (float)Q;
+		if (ao) f = f * aof;
+		for (int i = 0; i < 4; i++) {
+			v3 r = add(divf(lightsI[i], (float)shotRounds), mul(hemiI[i], f));
+			float* o = i == 0 ? out : dirs + 4 * (i - 1);
+			o[0] = r.x;
+			o[1] = r.y;
+			o[2] = r.z;
+			o[3] = out[3];
+		}
+	}
 	if (bent) {
 		v3 b = add(bentL, bentH);
 		if (b.x != 0 || b.y != 0 || b.z != 0) b = divf(b, len(b));
@@ -476,15 +533,21 @@ static void gather_texel(const orc_bvh* bvh, const orc_gather_scene* sc, uint64_
 	}
 }
 
-void orc_gather_ex(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,
-                   const uint64_t* off, const orc_subtexel* st, int threads, int fp64, float* out, float* bent) {
+void orc_gather_dir(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,
+                    const uint64_t* off, const orc_subtexel* st, int threads, int fp64, float* out, float* bent,
+                    float* dirs) {
 #ifdef _OPENMP
 	if (threads > 0) omp_set_num_threads(threads);
 #pragma omp parallel for schedule(dynamic, 16)
 #endif
 	for (long i = 0; i < (long)ntexels; i++)
 		gather_texel(bvh, sc, texel_id[i], st + off[i], (uint32_t)(off[i + 1] - off[i]), fp64, out + 4 * (size_t)i,
-		             bent ? bent + 4 * (size_t)i : NULL);
+		             bent ? bent + 4 * (size_t)i : NULL, dirs ? dirs + 12 * (size_t)i : NULL);
+}
+
+void orc_gather_ex(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,
+                   const uint64_t* off, const orc_subtexel* st, int threads, int fp64, float* out, float* bent) {
+	orc_gather_dir(bvh, sc, texel_id, ntexels, off, st, threads, fp64, out, bent, NULL);
 }
 
 void orc_gather(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,

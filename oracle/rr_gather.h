@@ -95,6 +95,15 @@ void orc_gather(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* 
 void orc_gather_ex(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,
                    const uint64_t* off, const orc_subtexel* st, int threads, int fp64, float* out, float* bent);
 
+/* Same in directional mode when dirs != NULL (gatherAllDirections,
+ * gather.cpp:255-272,468-486; lightmap.cpp:820): out is LS_LIGHTMAP and dirs
+ * 12 floats per texel, LS_DIRECTION1..3 RGBA, every output weighted by the
+ * UE3 basis directions (gather.cpp:43-49) in the texel's skewed tangent
+ * basis.  fp32 accumulation only. */
+void orc_gather_dir(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,
+                    const uint64_t* off, const orc_subtexel* st, int threads, int fp64, float* out, float* bent,
+                    float* dirs);
+
 /* Counter-based generator shared with the GPU (and with the Python
  * generators): MurmurHash3 fmix64 of (seed, stream, index). */
 uint64_t orc_hash(uint64_t seed, uint64_t stream, uint64_t index);

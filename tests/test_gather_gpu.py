@@ -177,3 +177,35 @@ def test_ambient_occlusion_and_bent_normals_match_oracle(setup):
     plain = gpu_gather(L, lm.make_params(gs.lights), tids)
     assert np.all(got[:, :3] <= plain[:, :3] * (1 + 1e-6) + 1e-9)
     assert (got[:, :3].sum(1) < plain[:, :3].sum(1) * 0.999).mean() > 0.2
+
+
+def test_directional_lightmaps_match_oracle(setup):
+    """Directional mode (LS_DIRECTION1..3, gather.cpp:43-49,255-272,468-486)
+    against the oracle on the same sample streams: LS_LIGHTMAP and the three
+    directions within 1e-4 relative like the plain gather, bent normals within
+    1e-4; LS_LIGHTMAP matches the plain mode's to float rounding."""
+    gs, c, L, G = setup
+    params = lm.make_params(gs.lights)
+    tids, off, st = pick_texels(L, [0, 9, 75], 24)
+    got = np.zeros((len(tids), 4), np.float32)
+    gdir = np.zeros((len(tids), 3, 4), np.float32)
+    gb = np.zeros((len(tids), 4), np.float32)
+    i = 0
+    while i < len(tids):
+        j = i
+        while j + 1 < len(tids) and tids[j + 1] == tids[j] + 1:
+            j += 1
+        got[i:j + 1], gdir[i:j + 1], gb[i:j + 1] = L.gather_directional(params, int(tids[i]), j - i + 1)
+        i = j + 1
+    cnt = (off[tids + 1] - off[tids]).astype(np.uint64)
+    o2 = np.concatenate([[0], np.cumsum(cnt)]).astype(np.uint64)
+    sts = np.concatenate([st[off[t]:off[t + 1]] for t in tids]).view(orc.SUBTEXEL_DTYPE)
+    ref, rdir, rb = G.gather_directional(tids.astype(np.uint64), o2, sts, 0)
+    for g_, r_ in ((got, ref), (gdir.reshape(-1, 4), rdir.reshape(-1, 4))):
+        rel = np.abs(g_[:, :3] - r_[:, :3]) / np.maximum(np.abs(r_[:, :3]), 1e-6)
+        assert rel.max() <= 1e-4, rel.max()
+        np.testing.assert_array_equal(g_[:, 3], r_[:, 3])
+    assert np.abs(gb - rb).max() <= 1e-4
+    plain = gpu_gather(L, params, tids)
+    np.testing.assert_allclose(got[:, :3], plain[:, :3], rtol=1e-5, atol=1e-7)
+    assert np.all(gdir[..., :3] >= 0) and gdir[..., :3].sum() > 0

@@ -49,3 +49,29 @@ def test_gather_fp32_vs_fp64_accumulation():
     assert np.all(f32[:, :3] > 0)
     again = G.gather(tid, o2, sts, 0)
     np.testing.assert_array_equal(f32, again)
+
+
+def test_directional_mode_properties():
+    """Directional mode (gather.cpp:255-272, 468-486): the four outputs are
+    the same samples weighted by the UE3 basis directions (gather.cpp:43-49).
+    LS_LIGHTMAP's weight for a sample is its cosine to the re-normalised
+    normal over its cosine to the normal, so it matches the plain mode's
+    value to float rounding; the three directions are non-negative, bent
+    normals are unchanged, and the weights are lower on average than 1."""
+    gs = scenes.gather_c2()
+    G = orc.GatherOracle(gs, quality=16)
+    a = 9
+    ids = np.nonzero(gs.tri_atlas == a)[0]
+    off, st = orc.enumerate_atlas(gs.uv[ids], ids, gs.size)
+    sel = np.nonzero(np.diff(off) > 0)[0][::131][:48]
+    tid = (a * gs.size * gs.size + sel).astype(np.uint64)
+    cnt = (off[sel + 1] - off[sel]).astype(np.uint64)
+    o2 = np.concatenate([[0], np.cumsum(cnt)]).astype(np.uint64)
+    sts = np.concatenate([st[off[i]:off[i + 1]] for i in sel])
+    plain, bent = G.gather(tid, o2, sts, 0, bent=True)
+    lm, dirs, bent_d = G.gather_directional(tid, o2, sts, 0)
+    np.testing.assert_allclose(lm[:, :3], plain[:, :3], rtol=1e-5, atol=1e-7)
+    np.testing.assert_array_equal(bent_d, bent)
+    assert np.all(dirs[..., :3] >= 0) and np.all(dirs[..., 3] == lm[:, None, 3])
+    assert dirs[..., :3].sum() > 0
+    assert dirs[..., :3].mean() < lm[:, :3].mean()
