@@ -104,6 +104,9 @@ LIGHTMAP_CASES = ((4, 48), (3, 17))
 # filter runs on the first case: (stages, wrap, seams); stages as RRG_FILTER_*
 FILTER_RUNS = ((1, 0, 0), (1, 1, 0), (1, 0, 1), (2, 0, 0), (2, 1, 0), (4, 0, 0), (4, 1, 0), (8, 0, 0),
                (15, 0, 0), (15, 0, 1), (15, 1, 1))
+# and on the second (17 x 17: growing with wrap indexes modulo 289 texels in
+# unsigned arithmetic, which is not a wrap-around at the map's edges)
+FILTER_RUNS_ODD = ((4, 1, 0), (15, 1, 1), (15, 0, 1))
 
 
 def lightmap_case(freq: int, size: int):
@@ -138,15 +141,13 @@ def lightmaps():
         kw[f"case{k}_flags"] = flags
         kw[f"case{k}_counts"] = np.diff(off).astype(np.uint32)
         kw[f"case{k}_st_md5"] = md5(st["tri"], st["uv"], st["area"])
-        if k == 0:
-            img = lightmap_image(flags, size)
-            kw["img_md5"] = md5(img)
-            for stages, wrap, seams in FILTER_RUNS:
-                out = refio.run_ref_filter(img, 1.0, bool(wrap), 1000, stages,
-                                           mesh=(v, nrm, t, uv) if seams else None)
-                kw[f"filter_{stages}_{wrap}_{seams}_md5"] = md5(out)
-                if (stages, wrap, seams) == (15, 0, 1):
-                    kw["filter_all_seams"] = out
+        img = lightmap_image(flags, size)
+        kw[f"case{k}_img_md5"] = md5(img)
+        for stages, wrap, seams in (FILTER_RUNS if k == 0 else FILTER_RUNS_ODD):
+            out = refio.run_ref_filter(img, 1.0, bool(wrap), 1000, stages, mesh=(v, nrm, t, uv) if seams else None)
+            kw[f"case{k}_filter_{stages}_{wrap}_{seams}_md5"] = md5(out)
+            if k == 0 and (stages, wrap, seams) == (15, 0, 1):
+                kw["filter_all_seams"] = out
     save("lightmap_ref.npz", **kw)
 
 

@@ -22,35 +22,41 @@ pytestmark = pytest.mark.gpu
 FIX = np.load(__file__.replace("test_filter_gpu.py", "golden/lightmap_ref.npz"))
 
 
-@pytest.fixture(scope="module")
-def sphere():
-    freq, size = G.LIGHTMAP_CASES[0]
-    v, nrm, t, uv = G.lightmap_case(freq, size)
-    c = col.RRCollider.create(v, t)
-    L = lm.RRLightmapper(c, np.full((len(t), 3), 0.5, np.float32), np.zeros(len(t), np.int32), uv, 1, size)
-    return c, L, size
+_SPHERES = {}
 
 
-def test_sphere_flags_match_reference(sphere):
-    c, L, size = sphere
-    np.testing.assert_array_equal(L.flags(), FIX["case0_flags"])
+def sphere(k):
+    """Collider and lightmapper of golden case k (built once per module)."""
+    if k not in _SPHERES:
+        freq, size = G.LIGHTMAP_CASES[k]
+        v, nrm, t, uv = G.lightmap_case(freq, size)
+        c = col.RRCollider.create(v, t)
+        L = lm.RRLightmapper(c, np.full((len(t), 3), 0.5, np.float32), np.zeros(len(t), np.int32), uv, 1, size)
+        _SPHERES[k] = (c, L, size, len(t))
+    return _SPHERES[k]
 
 
-@pytest.mark.parametrize("run", G.FILTER_RUNS)
-def test_sphere_filters_match_reference(sphere, run):
+@pytest.mark.parametrize("k", range(len(G.LIGHTMAP_CASES)))
+def test_sphere_flags_match_reference(k):
+    c, L, size, nt = sphere(k)
+    np.testing.assert_array_equal(L.flags(), FIX[f"case{k}_flags"])
+
+
+@pytest.mark.parametrize("k,run", [(0, r) for r in G.FILTER_RUNS] + [(1, r) for r in G.FILTER_RUNS_ODD])
+def test_sphere_filters_match_reference(k, run):
     import torch
-    c, L, size = sphere
+    c, L, size, nt = sphere(k)
     stages, wrap, seams = run
-    img = G.lightmap_image(FIX["case0_flags"], size)
+    img = G.lightmap_image(FIX[f"case{k}_flags"], size)
     d = torch.from_numpy(img.reshape(-1, 4).copy()).cuda()
     L.filter_device(lm.filter_params(wrap=bool(wrap), seams=bool(seams), stages=stages), 0, 1, d.data_ptr())
     torch.cuda.synchronize()
     out = d.cpu().numpy().reshape(size, size, 4)
-    if run == (15, 0, 1):
+    if (k, run) == (0, (15, 0, 1)):
         np.testing.assert_array_equal(out, FIX["filter_all_seams"])
-    assert md5(out) == str(FIX[f"filter_{stages}_{wrap}_{seams}_md5"]), run
+    assert md5(out) == str(FIX[f"case{k}_filter_{stages}_{wrap}_{seams}_md5"]), run
     if seams:
-        assert L.nseams == 480
+        assert L.nseams == nt * 3 // 2
 
 
 @pytest.fixture(scope="module")

@@ -26,18 +26,21 @@ def test_enumeration_and_flags_match_reference(k):
     assert md5(st["tri"], st["uv"], st["area"]) == str(FIX[f"case{k}_st_md5"])
 
 
-@pytest.mark.parametrize("run", G.FILTER_RUNS)
-def test_filters_match_reference(run):
+RUNS = [(0, r) for r in G.FILTER_RUNS] + [(1, r) for r in G.FILTER_RUNS_ODD]
+
+
+@pytest.mark.parametrize("k,run", RUNS)
+def test_filters_match_reference(k, run):
     stages, wrap, seams = run
-    freq, size = G.LIGHTMAP_CASES[0]
+    freq, size = G.LIGHTMAP_CASES[k]
     v, nrm, t, uv = G.lightmap_case(freq, size)
-    img = G.lightmap_image(FIX["case0_flags"], size)
-    assert md5(img) == str(FIX["img_md5"])
+    img = G.lightmap_image(FIX[f"case{k}_flags"], size)
+    assert md5(img) == str(FIX[f"case{k}_img_md5"])
     sm = orc.unwrap_seams(t, uv) if seams else None
     out = orc.lightmap_filter(img, 1.0, 1000, (0, 0, 0, 0), bool(wrap), sm, stages)
-    if run == (15, 0, 1):
+    if (k, run) == (0, (15, 0, 1)):
         np.testing.assert_array_equal(out, FIX["filter_all_seams"])
-    assert md5(out) == str(FIX[f"filter_{stages}_{wrap}_{seams}_md5"]), run
+    assert md5(out) == str(FIX[f"case{k}_filter_{stages}_{wrap}_{seams}_md5"]), run
 
 
 def test_unwrap_seams_small_cases():
