@@ -28,7 +28,14 @@
  *     point by rejection lifted to the hemisphere) instead of the polar
  *     sin/cos form of sampleHemisphereDiffuse; the distribution is the same,
  *     and no transcendental function is needed, so CPU and GPU agree bitwise;
- *   - one shooting series per texel (every ray here is reliable);
+ *   - one shooting series per texel (every ray here is reliable).  The
+ *     reference's reliability bookkeeping changes no value under its
+ *     defaults: a light ray that meets a back face (hitsInside) or a hit
+ *     nearer than rugDistance adds nothing, as a shadowed one does; the
+ *     inside-object rejection needs hitsInside > rays * insideObjectsThreshold
+ *     (default 1), which cannot happen; hemisphere rays always count as
+ *     reliable (gather.cpp:283-319, 490-558, UpdateParameters defaults
+ *     RRSolver.h:546-556);
  *   - the path radiance is accumulated iteratively (L += T * contribution)
  *     rather than by recursion.
  * Ambient occlusion (aoIntensity, aoSize: the hemisphere irradiance scaled
