@@ -219,8 +219,58 @@ def c3_cpu_rate(sample, threads: int, repeats: int = 1):
     return sum(len(r) for _, r in sample), times
 
 
+def reference_gather_line(args) -> dict:
+    """Reference arm of the lightmap workloads: the gather oracle (the port of
+    the reference's plain gather) on all host cores, on a bounded sample of
+    config 2's texels; its own CPU enumeration, no GPU code.  The reference has
+    no learned cache, so its plain gather also stands for config 4."""
+    from lightsprintsdk_gb300 import scenes
+    from oracle import orc
+    gs = scenes.gather_c2()
+    S = gs.size * gs.size
+    tids, offs, sts = [], [0], []
+    for a in range(0, gs.natlas, 16):   # 16 atlases, every k-th covered texel of each
+        ids = np.nonzero(gs.tri_atlas == a)[0]
+        if not len(ids):
+            continue
+        off, st = orc.enumerate_atlas(gs.uv[ids], ids, gs.size)
+        cov = np.nonzero(np.diff(off) > 0)[0]
+        for t in cov[::max(1, len(cov) // 256)][:256]:
+            tids.append(a * S + int(t))
+            sts.append(st[off[t]:off[t + 1]])
+            offs.append(offs[-1] + int(off[t + 1] - off[t]))
+    tids = np.asarray(tids, np.uint64)
+    o2 = np.asarray(offs, np.uint64)
+    sts = np.concatenate(sts).view(orc.SUBTEXEL_DTYPE)
+    G = orc.GatherOracle(gs)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        G.gather(tids[:32], o2[:33], sts[:int(o2[32])], threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        G.gather(tids, o2, sts, threads)
+        times.append(time.perf_counter() - t0)
+    sec = sum(times) / len(times)
+    val = len(tids) / sec
+    metric = "learned lightmap texels/s" if args.workload == "c4" else "plain lightmap texels/s"
+    return {"impl": "reference", "metric": metric, "value": val, "unit": "texels/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3 * (gs.natlas * S) / len(tids),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "plain gather, quality 64, 8 bounces, 256 atlases of 256x256 on the interior "
+                                   "(the reference's plain gather; it has no learned cache)",
+                       "parallelism": "cpu threads"},
+            "cpu_baseline": {"value": val, "unit": "texels/s", "cores": threads, "kind": "port",
+                             "sample": f"{len(tids)} covered texels of 16 atlases (every 16th), quality 64"},
+            "e2e": {"value": val, "unit": "texels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def run_reference(args, rank: int):
     if rank != 0:
+        return
+    if args.workload in ("c2", "c4"):
+        print(json.dumps(reference_gather_line(args)), flush=True)
         return
     if args.workload == "c3":
         mb, counts = c3_workload()
