@@ -26,13 +26,21 @@ extern "C" {
 
 typedef struct rrg_lightmapper rrg_lightmapper;
 
+/* Scheduling of the plain gather.  Every texel's value is the same bit for
+ * bit whichever runs. */
+enum {
+	RRG_GATHER_AUTO = 0,        /* wavefront for calls of >= 16,384 texels, else warp per texel */
+	RRG_GATHER_WARP = 1,        /* one warp per texel, lanes follow whole hemisphere paths */
+	RRG_GATHER_WAVEFRONT = 2    /* paths of a batch of texels advance bounce by bounce, one thread per path */
+};
+
 /* UpdateParameters / PathTracingParameters subset (RRSolver.h:468-594,
  * 964-1001).  size = sizeof(rrg_gather_params). */
 typedef struct rrg_gather_params {
 	uint32_t size;
 	uint32_t quality;          /* hemisphere rays per texel (UpdateParameters::quality), 1..256 */
 	uint32_t max_depth;        /* diffuse bounces (PathTracingParameters::stopAtDepth) */
-	uint32_t reserved0;
+	uint32_t mode;             /* RRG_GATHER_*: how the plain gather is scheduled (results do not depend on it) */
 	uint64_t seed;             /* sample streams */
 	float ray_length_min;      /* 0 = the solver's minimalSafeDistance of the mesh */
 	float locality;            /* UpdateParameters::locality, 0 = 100000 */

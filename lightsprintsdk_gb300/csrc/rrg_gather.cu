@@ -29,6 +29,7 @@
 #include "../../include/rrgpu_cache.h"
 #include "rrg_mlp.cuh"
 
+#include <algorithm>
 #include <type_traits>
 #include <vector>
 
@@ -616,6 +617,34 @@ struct WarpSmem {
 	unsigned next;   // next unclaimed sample of the texel
 };
 
+// ---------------------------------------------------------------- wavefront
+// The plain gather as a wavefront: the hemisphere paths of a batch of texels
+// advance bounce by bounce, one thread per live path, instead of one warp per
+// texel following its lanes' paths to the end (where the warp waits for its
+// longest path: about 5 of 32 lanes busy).  Each bounce is trace_path's loop
+// body split in two: k_wf_closest (the closest hit and its fields) and
+// k_wf_shade (next event estimation, roulette, next direction), with the same
+// arithmetic in the same order, so every path's radiance is bit-identical to
+// trace_path's; k_wf_reduce sums each texel's samples in the order the
+// warp-per-texel kernel does.  Path state is structure-of-arrays in HBM.
+struct WfState {
+	float4* eye;           // eye.xyz, skip triangle (bits)
+	float4* dir;           // dir.xyz, depth (bits)
+	float4* T;             // throughput.xyz, first hit distance
+	float4* L;             // radiance.xyz
+	float4* dir0;          // first direction.xyz (bent normals)
+	float4* hitp;          // hit point.xyz, hit triangle (bits)
+	float4* hitn;          // hit plane normal.xyz
+	float4* slot_lights;   // per texel of the batch: the light rounds' average (xyz)
+	float4* slot_bl;       // per texel of the batch: the light rounds' bent-normal sum (xyz)
+	uint64_t* slot_tid;    // per texel of the batch: texel id (~0: uncovered)
+	uint32_t* live;        // 2 x cap: live path lists, ping-pong
+	uint32_t* hits;        // cap: paths that hit in this bounce
+	uint32_t* counts;      // [0], [1]: live counts (ping-pong), [2]: hits
+	uint32_t cap;          // paths
+	uint32_t Q, N;
+};
+
 // Directional mode (gatherAllDirections, lightmap.cpp:820): each hemisphere
 // sample's weights for the four lightmap directions (its cosine to the
 // direction over its cosine to the normal; < 0: not added,
@@ -636,14 +665,17 @@ __device__ __forceinline__ float absavg3(V3 a) {
 // LEARNED = true : first segments only; recs[(tid - out_base) * Q + k] get the
 // cache queries and out[tid - out_base] the light rounds' average (the plain
 // texel's first term) with w = 1.  list (may be null) selects texel ids.
-template <bool LEARNED, bool DIR = false>
+// WF = true: the set-up of the wavefront gather (k_wf_*): texel ti of the
+// launch writes its Q paths' first rays (path ti * Q + k) and its light
+// rounds' sums instead of tracing the paths.
+template <bool LEARNED, bool DIR = false, bool WF = false>
 __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, const uint32_t* __restrict__ off,
                                                               const Sub* __restrict__ st, uint64_t first,
                                                               uint64_t count, const uint32_t* __restrict__ list,
                                                               uint64_t out_base, float4* __restrict__ out,
                                                               CacheRec* __restrict__ recs, uint32_t* counter,
                                                               uint32_t* status, float4* __restrict__ bent_out,
-                                                              DirOut dout = DirOut{}) {
+                                                              DirOut dout = DirOut{}, WfState wf = WfState{}) {
 	__shared__ WarpSmem sm_all[kGatherWarps];
 	WarpSmem& sm = sm_all[threadIdx.x >> 5];
 	__shared__ typename std::conditional<DIR, WarpSmemDir, char>::type smd_all[kGatherWarps];
@@ -662,6 +694,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 		const uint64_t oi = tid - out_base;
 		const uint32_t b = off[tid], m = off[tid + 1] - b;
 		if (m == 0) {
+			if (WF && lane == 0) wf.slot_tid[ti] = ~0ull;
 			if (lane == 0) out[oi] = make_float4(0.f, 0.f, 0.f, 0.f);
 			if (lane == 0 && bent_out) bent_out[oi] = make_float4(0.f, 0.f, 0.f, 0.f);
 			if (DIR && lane == 0)
@@ -746,6 +779,14 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 				V3 dir = add(add(mul(nrm, cosa), mul(tg, sm.fx[k])), mul(bt, sm.fy[k]));
 				if (LEARNED) {
 					recs[oi * Q + k] = first_hit(g, origin, dir, s.tri, overflow);
+				} else if (WF) {
+					const uint32_t pth = (uint32_t)ti * Q + k;
+					wf.eye[pth] = make_float4(origin.x, origin.y, origin.z, __uint_as_float(s.tri));
+					wf.dir[pth] = make_float4(dir.x, dir.y, dir.z, __uint_as_float(0u));
+					wf.T[pth] = make_float4(1.f, 1.f, 1.f, 1e10f);
+					wf.L[pth] = make_float4(0.f, 0.f, 0.f, 0.f);
+					wf.dir0[pth] = make_float4(dir.x, dir.y, dir.z, 0.f);
+					wf.live[atomicAdd(&wf.counts[0], 1u)] = pth;
 				} else {
 					float ft = 1e10f;
 					const V3 Lk = trace_path(g, origin, dir, s.tri, sid, overflow, nullptr, &ft);
@@ -794,14 +835,22 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 		__syncwarp();
 		if (lane == 0) {
 			V3 hemi = mk(0.f, 0.f, 0.f), lights = mk(0.f, 0.f, 0.f);
-			if (!LEARNED)
+			if (!LEARNED && !WF)
 				for (uint32_t k = 0; k < Q; k++) hemi = add(hemi, sm.hemi[k]);
 			uint32_t shot = rounds < (uint32_t)kMaxRounds ? rounds : (uint32_t)kMaxRounds;
 			for (uint32_t r = 0; r < shot; r++)
 				for (int li = 0; li < 2; li++)
 					if (sm.lit[r][li]) lights = add(lights, sm.light[r][li]);
 			lights = divf(lights, (float)shot);
-			if (LEARNED) {
+			if (WF) {
+				V3 bl = mk(0.f, 0.f, 0.f);
+				for (uint32_t r = 0; r < shot; r++)
+					for (int li = 0; li < 2; li++)
+						if (sm.lit[r][li]) bl = add(bl, sm.lbent[r][li]);
+				wf.slot_tid[ti] = tid;
+				wf.slot_lights[ti] = make_float4(lights.x, lights.y, lights.z, 0.f);
+				wf.slot_bl[ti] = make_float4(bl.x, bl.y, bl.z, 0.f);
+			} else if (LEARNED) {
 				out[oi] = make_float4(lights.x, lights.y, lights.z, texel_alpha(g, tid));
 			} else {
 				float f = __fdiv_rn(1.f, (float)Q);
@@ -845,6 +894,142 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 		__syncwarp();
 	}
 	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// Closest hit of every live path (trace_path's traversal and hit fields).
+__global__ void __launch_bounds__(128) k_wf_closest(GatherScene g, WfState w, int cur, uint32_t* status) {
+	const uint32_t n = w.counts[cur];
+	const uint32_t* live = w.live + (size_t)cur * w.cap;
+	bool overflow = false;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const uint32_t p = live[i];
+		const float4 e = w.eye[p], d = w.dir[p];
+		const V3 eye = mk(e.x, e.y, e.z), dir = mk(d.x, d.y, d.z);
+		const uint32_t skip = __float_as_uint(e.w), depth = __float_as_uint(d.w);
+		RayState r;
+		set_ray(r, eye, dir, g.tmin, depth == 0 ? g.locality : 1e10f);
+		GatherFilter f = make_filter(g, skip, true);
+		float tb = r.tmax;
+		uint32_t tri = 0xFFFFFFFFu;
+		const int slot = traverse<false, true>(g.nodes, g.tris, r, g.nnodes, g.ntris, tb, tri, overflow, &f);
+		if (slot < 0) continue;   // the path ends with what it has gathered
+		float4 a, b, c;
+		load_tri(g.tris, slot, a, b, c);
+		const Fastest fs = fastest_fields(r, a, b, c);
+		if (depth == 0) w.T[p].w = fs.dist;   // the first hit's distance, for ambient occlusion
+		const V3 hp = add(eye, mul(dir, fs.dist));
+		w.hitp[p] = make_float4(hp.x, hp.y, hp.z, __uint_as_float(tri));
+		w.hitn[p] = make_float4(fs.n[0], fs.n[1], fs.n[2], 0.f);
+		w.hits[atomicAdd(&w.counts[2], 1u)] = p;
+	}
+	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// The rest of trace_path's loop body for every path that hit: next event
+// estimation toward both lights, Russian roulette, the next direction.
+// Paths that continue go to the other live list.
+__global__ void __launch_bounds__(128) k_wf_shade(GatherScene g, WfState w, int cur, uint32_t* status) {
+	const uint32_t n = w.counts[2];
+	uint32_t* next = w.live + (size_t)(cur ^ 1) * w.cap;
+	bool overflow = false;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const uint32_t p = w.hits[i];
+		const float4 hp4 = w.hitp[p], hn4 = w.hitn[p], T4 = w.T[p], L4 = w.L[p], d4 = w.dir[p];
+		const V3 pnt = mk(hp4.x, hp4.y, hp4.z), nrm = mk(hn4.x, hn4.y, hn4.z);
+		const uint32_t tri = __float_as_uint(hp4.w), depth = __float_as_uint(d4.w);
+		V3 T = mk(T4.x, T4.y, T4.z), L = mk(L4.x, L4.y, L4.z);
+		const uint64_t sid = w.slot_tid[p / w.Q] * w.N + p % w.Q;
+		const V3 alb = ld3(g.albedo + 3 * (size_t)tri);
+		for (int li = 0; li < 2; li++) {
+			V3 sdir;
+			float smax;
+			if (li == 0) {
+				sdir = neg(g.dir_direction);
+				smax = 1e10f;
+			} else {
+				V3 dd = sub(g.point_position, pnt);
+				sdir = normalized(dd);
+				smax = len(dd);
+			}
+			if (!(dot(nrm, sdir) > 0.f)) continue;
+			V3 unob = li == 0 ? g.dir_color : point_irr(g, pnt);
+			float dif = clampf(-dot(neg(sdir), nrm), 0.f, 1.f);
+			V3 contrib = mulv(unob, mul(alb, dif));
+			if (contrib.x == 0.f && contrib.y == 0.f && contrib.z == 0.f) continue;
+			if (occluded(g, pnt, sdir, g.tmin, smax, tri, overflow)) continue;
+			L = add(L, mulv(T, contrib));
+		}
+		w.L[p] = make_float4(L.x, L.y, L.z, 0.f);
+		float pdiff = avg3(alb);
+		if (pdiff < 0.f) pdiff = 0.f;
+		float pstop = __fsub_rn(1.f, pdiff);
+		if (pstop < 0.f) pstop = 0.f;
+		float rr = rng01(g.seed, S_ROULETTE, sid * 16 + depth);
+		if (!(rr < pdiff && depth < g.max_depth)) continue;
+		float intensity = __fdiv_rn(__fadd_rn(pdiff, pstop), pdiff);
+		float x = 0.f, y = 0.f;
+		for (int j = 0; j < kDiskTries; j++) {
+			uint64_t cc = (sid * 16 + depth) * kDiskTries + j;
+			float ax = __fsub_rn(__fmul_rn(rng01(g.seed, S_DISKX, cc), 2.0f), 1.0f);
+			float by = __fsub_rn(__fmul_rn(rng01(g.seed, S_DISKY, cc), 2.0f), 1.0f);
+			if (__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(by, by)) < 1.0f) { x = ax; y = by; break; }
+		}
+		float cosT = __fsqrt_rn(__fsub_rn(1.0f, __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y))));
+		V3 tg, bt;
+		basis_from_normal(nrm, tg, bt);
+		V3 s = add(add(mul(nrm, cosT), mul(tg, x)), mul(bt, y));
+		float pdf = cosT;
+		V3 dirIn = neg(s);
+		float dif = clampf(-dot(dirIn, nrm), 0.f, 1.f);
+		V3 colorOut = mul(alb, dif);
+		if (!(pdf > 0.f && dot(dirIn, nrm) < 0.f)) continue;
+		V3 rs = mul(colorOut, __fdiv_rn(intensity, pdf));
+		if (!(avg3(rs) > kStopAtVisibility)) continue;
+		T = mulv(T, rs);
+		w.T[p] = make_float4(T.x, T.y, T.z, T4.w);
+		w.eye[p] = make_float4(pnt.x, pnt.y, pnt.z, __uint_as_float(tri));
+		w.dir[p] = make_float4(s.x, s.y, s.z, __uint_as_float(depth + 1));
+		next[atomicAdd(&w.counts[cur ^ 1], 1u)] = p;
+	}
+	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// Texel sums (the warp-per-texel kernel's lane-0 tail): the samples' radiance
+// in sample order, the ambient-occlusion factor, the bent normal.
+__global__ void k_wf_reduce(GatherScene g, WfState w, uint32_t nslots, uint64_t out_base, float4* __restrict__ out,
+                            float4* __restrict__ bent_out) {
+	const uint32_t Q = w.Q;
+	for (uint32_t sl = blockIdx.x * blockDim.x + threadIdx.x; sl < nslots; sl += gridDim.x * blockDim.x) {
+		const uint64_t tid = w.slot_tid[sl];
+		if (tid == ~0ull) continue;   // uncovered: written by the set-up
+		const uint64_t oi = tid - out_base;
+		V3 hemi = mk(0.f, 0.f, 0.f);
+		uint32_t nd = 0;
+		for (uint32_t k = 0; k < Q; k++) {
+			const float4 l = w.L[(size_t)sl * Q + k];
+			hemi = add(hemi, mk(l.x, l.y, l.z));
+			nd += w.T[(size_t)sl * Q + k].w > g.ao_size ? 1u : 0u;
+		}
+		const float4 l4 = w.slot_lights[sl];
+		const V3 lights = mk(l4.x, l4.y, l4.z);
+		float f = __fdiv_rn(1.f, (float)Q);
+		if (g.ao_intensity > 0.f && g.ao_size > 0.f) f = __fmul_rn(f, powf(__fdiv_rn((float)nd, (float)Q), g.ao_intensity));
+		hemi = mul(hemi, f);
+		const V3 res = add(lights, hemi);
+		out[oi] = make_float4(res.x, res.y, res.z, texel_alpha(g, tid));
+		if (bent_out) {
+			const float4 b4 = w.slot_bl[sl];
+			V3 bl = mk(b4.x, b4.y, b4.z), bh = mk(0.f, 0.f, 0.f);
+			for (uint32_t k = 0; k < Q; k++) {
+				const float4 l = w.L[(size_t)sl * Q + k], d0 = w.dir0[(size_t)sl * Q + k];
+				bh = add(bh, mul(mk(d0.x, d0.y, d0.z), absavg3(mk(l.x, l.y, l.z))));
+			}
+			V3 b = add(bl, bh);
+			if (b.x != 0.f || b.y != 0.f || b.z != 0.f) b = divf(b, len(b));
+			bent_out[oi] = make_float4(__fmul_rn(__fadd_rn(b.x, 1.f), 0.5f), __fmul_rn(__fadd_rn(b.y, 1.f), 0.5f),
+			                           __fmul_rn(__fadd_rn(b.z, 1.f), 0.5f), texel_alpha(g, tid));
+		}
+	}
 }
 
 // Training paths for the radiance cache: path i starts at covered texel
@@ -953,6 +1138,10 @@ struct Lightmapper {
 	std::vector<float> h_uv;
 	std::vector<int32_t> h_atlas;
 	LightmapFilter* filter = nullptr;   // filter scratch and seams (rrg_filter.cu)
+	// wavefront gather state (grown on demand): 7 float4 per path, 2 float4 +
+	// 1 id per texel of a batch, 3 path lists, 3 counters
+	void* d_wf = nullptr;
+	size_t wf_bytes = 0;
 	uint64_t ncovered = 0;
 	// learned-gather work buffers (grown on demand)
 	CacheRec* d_recs = nullptr;
@@ -966,6 +1155,7 @@ struct Lightmapper {
 static void free_lm(Lightmapper* L) {
 	if (!L) return;
 	filter_free(L->filter);
+	cudaFree(L->d_wf);
 	cudaFree(L->d_albedo);
 	cudaFree(L->d_flags);
 	cudaFree(L->d_off);
@@ -1034,13 +1224,89 @@ static int launch_gather_kernel(Lightmapper* L, const GatherScene& g, uint64_t f
 	return RRG_OK;
 }
 
+// The wavefront gather of texels [first, first + count): batches of texels,
+// each set up by k_gather<0, 0, 1> (first rays and light rounds), advanced
+// bounce by bounce (k_wf_closest, k_wf_shade; the path counts stay on the
+// device) and summed (k_wf_reduce).
+constexpr uint64_t kWfMinTexels = 16384;
+constexpr uint64_t kWfMaxPaths = 1ull << 23;
+
+static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first, uint64_t count, float4* out,
+                            float4* bent, cudaStream_t s) {
+	const uint32_t Q = g.quality;
+	const uint32_t rounds = Q / 10 + 1;
+	const uint32_t N = Q > rounds ? Q : rounds;
+	const uint64_t B = std::min<uint64_t>(count, kWfMaxPaths / Q);   // texels per batch
+	const uint64_t cap = B * Q;                                       // paths per batch
+	const size_t bytes = 7 * 16 * cap + 2 * 16 * B + 8 * B + 3 * 4 * cap + 16;
+	if (bytes > L->wf_bytes) {
+		cudaFree(L->d_wf);
+		L->d_wf = nullptr;
+		L->wf_bytes = 0;
+		RRG_CUDA(cudaMalloc(&L->d_wf, bytes));
+		L->wf_bytes = bytes;
+	}
+	WfState w;
+	float4* f4 = reinterpret_cast<float4*>(L->d_wf);
+	w.eye = f4;
+	w.dir = f4 + cap;
+	w.T = f4 + 2 * cap;
+	w.L = f4 + 3 * cap;
+	w.dir0 = f4 + 4 * cap;
+	w.hitp = f4 + 5 * cap;
+	w.hitn = f4 + 6 * cap;
+	w.slot_lights = f4 + 7 * cap;
+	w.slot_bl = f4 + 7 * cap + B;
+	w.slot_tid = reinterpret_cast<uint64_t*>(f4 + 7 * cap + 2 * B);
+	w.live = reinterpret_cast<uint32_t*>(w.slot_tid + B);
+	w.hits = w.live + 2 * cap;
+	w.counts = w.hits + cap;
+	w.cap = (uint32_t)cap;
+	w.Q = Q;
+	w.N = N;
+	int per_sm = 0;
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather<false, false, true>, kGatherWarps * 32, 0));
+	int per_sm_c = 0;
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c, k_wf_closest, 128, 0));
+	const int grid_c = std::max(1, per_sm_c) * L->c->num_sms;
+	for (uint64_t b0 = 0; b0 < count; b0 += B) {
+		const uint64_t nb = std::min<uint64_t>(B, count - b0);
+		RRG_CUDA(cudaMemsetAsync(L->d_counter, 0, 8, s));
+		RRG_CUDA(cudaMemsetAsync(w.counts, 0, 3 * sizeof(uint32_t), s));
+		const uint64_t want = (nb + kGatherWarps - 1) / kGatherWarps;
+		const uint64_t capb = (uint64_t)(per_sm > 0 ? per_sm : 1) * L->c->num_sms;
+		const int grid = (int)(want < capb ? want : capb);
+		k_gather<false, false, true><<<grid, kGatherWarps * 32, 0, s>>>(
+		    g, L->d_off, L->d_sub, first + b0, nb, nullptr, first, out, nullptr, reinterpret_cast<uint32_t*>(L->d_counter),
+		    L->d_status, nullptr, DirOut{}, w);
+		RRG_CUDA(cudaGetLastError());
+		int cur = 0;
+		for (uint32_t depth = 0; depth <= g.max_depth; depth++) {
+			RRG_CUDA(cudaMemsetAsync(w.counts + 2, 0, sizeof(uint32_t), s));
+			RRG_CUDA(cudaMemsetAsync(w.counts + (cur ^ 1), 0, sizeof(uint32_t), s));
+			k_wf_closest<<<grid_c, 128, 0, s>>>(g, w, cur, L->d_status);
+			k_wf_shade<<<grid_c, 128, 0, s>>>(g, w, cur, L->d_status);
+			cur ^= 1;
+		}
+		k_wf_reduce<<<(int)((nb + 127) / 128), 128, 0, s>>>(g, w, (uint32_t)nb, first, out, bent);
+		RRG_CUDA(cudaGetLastError());
+	}
+	return RRG_OK;
+}
+
 static int gather_launch(Lightmapper* L, const rrg_gather_params* p, uint64_t first, uint64_t count, float* out_dev,
                          cudaStream_t s, float* bent_dev = nullptr, const DirOut* dirs = nullptr) {
 	GatherScene g;
 	int st = make_scene(L, p, g);
 	if (st) return st;
 	if (first + count > L->ntexels) return RRG_ERR_INVALID;
-	if (dirs && (dirs->d[0] || dirs->d[1] || dirs->d[2]))
+	if (p->mode > RRG_GATHER_WAVEFRONT) return RRG_ERR_INVALID;
+	const bool directional = dirs && (dirs->d[0] || dirs->d[1] || dirs->d[2]);
+	if (!directional && count &&
+	    (p->mode == RRG_GATHER_WAVEFRONT || (p->mode == RRG_GATHER_AUTO && count >= kWfMinTexels)))
+		return gather_wavefront(L, g, first, count, reinterpret_cast<float4*>(out_dev),
+		                        reinterpret_cast<float4*>(bent_dev), s);
+	if (directional)
 		return launch_gather_kernel<false, true>(L, g, first, count, nullptr, first, reinterpret_cast<float4*>(out_dev),
 		                                         nullptr, s, reinterpret_cast<float4*>(bent_dev), *dirs);
 	return launch_gather_kernel<false>(L, g, first, count, nullptr, first, reinterpret_cast<float4*>(out_dev), nullptr,

@@ -19,7 +19,7 @@ SUBTEXEL_DTYPE = np.dtype([("tri", "<u4"), ("uv", "<f4", (3, 2)), ("area", "<f4"
 
 class GatherParams(C.Structure):
     _fields_ = [("size", C.c_uint32), ("quality", C.c_uint32), ("max_depth", C.c_uint32),
-                ("reserved0", C.c_uint32), ("seed", C.c_uint64), ("ray_length_min", C.c_float),
+                ("mode", C.c_uint32), ("seed", C.c_uint64), ("ray_length_min", C.c_float),
                 ("locality", C.c_float), ("dir_direction", C.c_float * 3), ("dir_color", C.c_float * 3),
                 ("point_position", C.c_float * 3), ("point_color", C.c_float * 3), ("ao_intensity", C.c_float),
                 ("ao_size", C.c_float)]
@@ -68,9 +68,13 @@ def _lib():
     return L
 
 
+GATHER_AUTO, GATHER_WARP, GATHER_WAVEFRONT = 0, 1, 2
+
+
 def make_params(lights: dict, quality: int = 64, max_depth: int = 8, seed: int = 0xC2, ray_length_min: float = 0.0,
-                locality: float = 100000.0, ao_intensity: float = 0.0, ao_size: float = 0.0) -> GatherParams:
-    return GatherParams(C.sizeof(GatherParams), quality, max_depth, 0, seed, ray_length_min, locality,
+                locality: float = 100000.0, ao_intensity: float = 0.0, ao_size: float = 0.0,
+                mode: int = GATHER_AUTO) -> GatherParams:
+    return GatherParams(C.sizeof(GatherParams), quality, max_depth, mode, seed, ray_length_min, locality,
                         (C.c_float * 3)(*lights["dir_direction"]), (C.c_float * 3)(*lights["dir_color"]),
                         (C.c_float * 3)(*lights["point_position"]), (C.c_float * 3)(*lights["point_color"]),
                         ao_intensity, ao_size)

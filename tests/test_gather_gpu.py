@@ -209,3 +209,41 @@ def test_directional_lightmaps_match_oracle(setup):
     plain = gpu_gather(L, params, tids)
     np.testing.assert_allclose(got[:, :3], plain[:, :3], rtol=1e-5, atol=1e-7)
     assert np.all(gdir[..., :3] >= 0) and gdir[..., :3].sum() > 0
+
+
+@pytest.mark.parametrize("ao", [False, True])
+def test_wavefront_equals_warp_per_texel(setup, ao):
+    """The two schedules of the plain gather (RRG_GATHER_WARP: a warp per
+    texel; RRG_GATHER_WAVEFRONT: the paths of a batch advance bounce by
+    bounce) give every texel bit for bit the same value and bent normal: a
+    range over an atlas boundary, covered and uncovered texels, with and
+    without ambient occlusion."""
+    gs, c, L, G = setup
+    S = gs.size * gs.size
+    first, count = 9 * S - 3000, 9000
+    kw = dict(ao_intensity=1.0, ao_size=0.5) if ao else {}
+    pw = lm.make_params(gs.lights, quality=32, mode=lm.GATHER_WARP, **kw)
+    pf = lm.make_params(gs.lights, quality=32, mode=lm.GATHER_WAVEFRONT, **kw)
+    a, ab = L.gather_bent(pw, first, count)
+    b, bb = L.gather_bent(pf, first, count)
+    assert (a[:, 3] > 0).sum() > 1000 and (a[:, 3] == 0).sum() > 100
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(ab, bb)
+
+
+def test_wavefront_large_call_matches_oracle(setup):
+    """A call large enough for the automatic choice to take the wavefront
+    (>= 16,384 texels), checked against the oracle on sampled texels."""
+    gs, c, L, G = setup
+    S = gs.size * gs.size
+    params = lm.make_params(gs.lights)
+    out = L.gather(params, 75 * S, S)   # one whole atlas
+    off, st = L.subtexels()
+    cov = np.nonzero(np.diff(off[75 * S:76 * S + 1]) > 0)[0]
+    rng = np.random.default_rng(5)
+    sel = np.sort(rng.choice(cov, size=48, replace=False))
+    tids = 75 * S + sel
+    ref = oracle_gather(G, tids, off, st)
+    rel = np.abs(out[sel, :3] - ref[:, :3]) / np.maximum(np.abs(ref[:, :3]), 1e-6)
+    assert rel.max() <= 1e-4, rel.max()
+    np.testing.assert_array_equal(out[sel, 3], ref[:, 3])
