@@ -622,11 +622,13 @@ struct WarpSmem {
 // advance bounce by bounce, one thread per live path, instead of one warp per
 // texel following its lanes' paths to the end (where the warp waits for its
 // longest path: about 5 of 32 lanes busy).  Each bounce is trace_path's loop
-// body split in two: k_wf_closest (the closest hit and its fields) and
-// k_wf_shade (next event estimation, roulette, next direction), with the same
-// arithmetic in the same order, so every path's radiance is bit-identical to
-// trace_path's; k_wf_reduce sums each texel's samples in the order the
-// warp-per-texel kernel does.  Path state is structure-of-arrays in HBM.
+// body split into kernels: k_wf_closest (the closest hit and its fields),
+// k_wf_nee (the contributions toward the lights), k_wf_shadow (one thread per
+// shadow ray), k_wf_shade (the unoccluded contributions added in light order,
+// roulette, next direction), with the same arithmetic in the same order, so
+// every path's radiance is bit-identical to trace_path's; k_wf_reduce sums
+// each texel's samples in the order the warp-per-texel kernel does.  Path
+// state is structure-of-arrays in HBM.
 struct WfState {
 	float4* eye;           // eye.xyz, skip triangle (bits)
 	float4* dir;           // dir.xyz, depth (bits)
@@ -638,9 +640,12 @@ struct WfState {
 	float4* slot_lights;   // per texel of the batch: the light rounds' average (xyz)
 	float4* slot_bl;       // per texel of the batch: the light rounds' bent-normal sum (xyz)
 	uint64_t* slot_tid;    // per texel of the batch: texel id (~0: uncovered)
+	float4* nee;           // 2 x cap: next-event contribution toward light li of path p at [2p + li];
+	                       // w = 1: a shadow ray decides, 2: unoccluded, 0: nothing to add
 	uint32_t* live;        // 2 x cap: live path lists, ping-pong
 	uint32_t* hits;        // cap: paths that hit in this bounce
-	uint32_t* counts;      // [0], [1]: live counts (ping-pong), [2]: hits
+	uint32_t* shadow;      // 2 x cap: shadow rays of this bounce (2p + li)
+	uint32_t* counts;      // [0], [1]: live counts (ping-pong), [2]: hits, [3]: shadow rays
 	uint32_t cap;          // paths
 	uint32_t Q, N;
 };
@@ -925,13 +930,71 @@ __global__ void __launch_bounds__(128) k_wf_closest(GatherScene g, WfState w, in
 	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
 }
 
-// The rest of trace_path's loop body for every path that hit: next event
-// estimation toward both lights, Russian roulette, the next direction.
+// Next event estimation of every path that hit (trace_path's loop body after
+// the closest hit): the contribution toward each light, and a shadow ray
+// where the light is above the surface and the contribution is not zero.
+__global__ void __launch_bounds__(128) k_wf_nee(GatherScene g, WfState w) {
+	const uint32_t n = w.counts[2];
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const uint32_t p = w.hits[i];
+		const float4 hp4 = w.hitp[p], hn4 = w.hitn[p];
+		const V3 pnt = mk(hp4.x, hp4.y, hp4.z), nrm = mk(hn4.x, hn4.y, hn4.z);
+		const uint32_t tri = __float_as_uint(hp4.w);
+		const V3 alb = ld3(g.albedo + 3 * (size_t)tri);
+		for (int li = 0; li < 2; li++) {
+			float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+			V3 sdir;
+			if (li == 0) {
+				sdir = neg(g.dir_direction);
+			} else {
+				V3 dd = sub(g.point_position, pnt);
+				sdir = normalized(dd);
+			}
+			if (dot(nrm, sdir) > 0.f) {
+				V3 unob = li == 0 ? g.dir_color : point_irr(g, pnt);
+				float dif = clampf(-dot(neg(sdir), nrm), 0.f, 1.f);
+				V3 contrib = mulv(unob, mul(alb, dif));
+				if (!(contrib.x == 0.f && contrib.y == 0.f && contrib.z == 0.f)) {
+					e = make_float4(contrib.x, contrib.y, contrib.z, 1.f);
+					w.shadow[atomicAdd(&w.counts[3], 1u)] = 2 * p + (uint32_t)li;
+				}
+			}
+			w.nee[2 * (size_t)p + li] = e;
+		}
+	}
+}
+
+// The shadow rays of this bounce, one thread each (the same ray and test as
+// trace_path's occluded() call).
+__global__ void __launch_bounds__(128) k_wf_shadow(GatherScene g, WfState w, uint32_t* status) {
+	const uint32_t n = w.counts[3];
+	bool overflow = false;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const uint32_t q = w.shadow[i], p = q >> 1, li = q & 1u;
+		const float4 hp4 = w.hitp[p];
+		const V3 pnt = mk(hp4.x, hp4.y, hp4.z);
+		const uint32_t tri = __float_as_uint(hp4.w);
+		V3 sdir;
+		float smax;
+		if (li == 0) {
+			sdir = neg(g.dir_direction);
+			smax = 1e10f;
+		} else {
+			V3 dd = sub(g.point_position, pnt);
+			sdir = normalized(dd);
+			smax = len(dd);
+		}
+		if (!occluded(g, pnt, sdir, g.tmin, smax, tri, overflow)) w.nee[q].w = 2.f;
+	}
+	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// The rest of trace_path's loop body for every path that hit: the unoccluded
+// contributions added in light order, Russian roulette, the next direction.
 // Paths that continue go to the other live list.
-__global__ void __launch_bounds__(128) k_wf_shade(GatherScene g, WfState w, int cur, uint32_t* status) {
+__global__ void __launch_bounds__(128) k_wf_shade(GatherScene g, WfState w, int cur) {
 	const uint32_t n = w.counts[2];
 	uint32_t* next = w.live + (size_t)(cur ^ 1) * w.cap;
-	bool overflow = false;
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		const uint32_t p = w.hits[i];
 		const float4 hp4 = w.hitp[p], hn4 = w.hitn[p], T4 = w.T[p], L4 = w.L[p], d4 = w.dir[p];
@@ -941,23 +1004,8 @@ __global__ void __launch_bounds__(128) k_wf_shade(GatherScene g, WfState w, int 
 		const uint64_t sid = w.slot_tid[p / w.Q] * w.N + p % w.Q;
 		const V3 alb = ld3(g.albedo + 3 * (size_t)tri);
 		for (int li = 0; li < 2; li++) {
-			V3 sdir;
-			float smax;
-			if (li == 0) {
-				sdir = neg(g.dir_direction);
-				smax = 1e10f;
-			} else {
-				V3 dd = sub(g.point_position, pnt);
-				sdir = normalized(dd);
-				smax = len(dd);
-			}
-			if (!(dot(nrm, sdir) > 0.f)) continue;
-			V3 unob = li == 0 ? g.dir_color : point_irr(g, pnt);
-			float dif = clampf(-dot(neg(sdir), nrm), 0.f, 1.f);
-			V3 contrib = mulv(unob, mul(alb, dif));
-			if (contrib.x == 0.f && contrib.y == 0.f && contrib.z == 0.f) continue;
-			if (occluded(g, pnt, sdir, g.tmin, smax, tri, overflow)) continue;
-			L = add(L, mulv(T, contrib));
+			const float4 e = w.nee[2 * (size_t)p + li];
+			if (e.w == 2.f) L = add(L, mulv(T, mk(e.x, e.y, e.z)));
 		}
 		w.L[p] = make_float4(L.x, L.y, L.z, 0.f);
 		float pdiff = avg3(alb);
@@ -991,7 +1039,6 @@ __global__ void __launch_bounds__(128) k_wf_shade(GatherScene g, WfState w, int 
 		w.dir[p] = make_float4(s.x, s.y, s.z, __uint_as_float(depth + 1));
 		next[atomicAdd(&w.counts[cur ^ 1], 1u)] = p;
 	}
-	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
 }
 
 // Texel sums (the warp-per-texel kernel's lane-0 tail): the samples' radiance
@@ -1226,8 +1273,8 @@ static int launch_gather_kernel(Lightmapper* L, const GatherScene& g, uint64_t f
 
 // The wavefront gather of texels [first, first + count): batches of texels,
 // each set up by k_gather<0, 0, 1> (first rays and light rounds), advanced
-// bounce by bounce (k_wf_closest, k_wf_shade; the path counts stay on the
-// device) and summed (k_wf_reduce).
+// bounce by bounce (k_wf_closest, k_wf_nee, k_wf_shadow, k_wf_shade; the
+// path counts stay on the device) and summed (k_wf_reduce).
 constexpr uint64_t kWfMinTexels = 16384;
 constexpr uint64_t kWfMaxPaths = 1ull << 23;
 
@@ -1238,7 +1285,7 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 	const uint32_t N = Q > rounds ? Q : rounds;
 	const uint64_t B = std::min<uint64_t>(count, kWfMaxPaths / Q);   // texels per batch
 	const uint64_t cap = B * Q;                                       // paths per batch
-	const size_t bytes = 7 * 16 * cap + 2 * 16 * B + 8 * B + 3 * 4 * cap + 16;
+	const size_t bytes = 9 * 16 * cap + 2 * 16 * B + 8 * B + 5 * 4 * cap + 16;
 	if (bytes > L->wf_bytes) {
 		cudaFree(L->d_wf);
 		L->d_wf = nullptr;
@@ -1255,12 +1302,14 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 	w.dir0 = f4 + 4 * cap;
 	w.hitp = f4 + 5 * cap;
 	w.hitn = f4 + 6 * cap;
-	w.slot_lights = f4 + 7 * cap;
-	w.slot_bl = f4 + 7 * cap + B;
-	w.slot_tid = reinterpret_cast<uint64_t*>(f4 + 7 * cap + 2 * B);
+	w.nee = f4 + 7 * cap;
+	w.slot_lights = f4 + 9 * cap;
+	w.slot_bl = f4 + 9 * cap + B;
+	w.slot_tid = reinterpret_cast<uint64_t*>(f4 + 9 * cap + 2 * B);
 	w.live = reinterpret_cast<uint32_t*>(w.slot_tid + B);
 	w.hits = w.live + 2 * cap;
-	w.counts = w.hits + cap;
+	w.shadow = w.hits + cap;
+	w.counts = w.shadow + 2 * cap;
 	w.cap = (uint32_t)cap;
 	w.Q = Q;
 	w.N = N;
@@ -1272,7 +1321,7 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 	for (uint64_t b0 = 0; b0 < count; b0 += B) {
 		const uint64_t nb = std::min<uint64_t>(B, count - b0);
 		RRG_CUDA(cudaMemsetAsync(L->d_counter, 0, 8, s));
-		RRG_CUDA(cudaMemsetAsync(w.counts, 0, 3 * sizeof(uint32_t), s));
+		RRG_CUDA(cudaMemsetAsync(w.counts, 0, 4 * sizeof(uint32_t), s));
 		const uint64_t want = (nb + kGatherWarps - 1) / kGatherWarps;
 		const uint64_t capb = (uint64_t)(per_sm > 0 ? per_sm : 1) * L->c->num_sms;
 		const int grid = (int)(want < capb ? want : capb);
@@ -1282,10 +1331,12 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 		RRG_CUDA(cudaGetLastError());
 		int cur = 0;
 		for (uint32_t depth = 0; depth <= g.max_depth; depth++) {
-			RRG_CUDA(cudaMemsetAsync(w.counts + 2, 0, sizeof(uint32_t), s));
+			RRG_CUDA(cudaMemsetAsync(w.counts + 2, 0, 2 * sizeof(uint32_t), s));
 			RRG_CUDA(cudaMemsetAsync(w.counts + (cur ^ 1), 0, sizeof(uint32_t), s));
 			k_wf_closest<<<grid_c, 128, 0, s>>>(g, w, cur, L->d_status);
-			k_wf_shade<<<grid_c, 128, 0, s>>>(g, w, cur, L->d_status);
+			k_wf_nee<<<grid_c, 128, 0, s>>>(g, w);
+			k_wf_shadow<<<grid_c, 128, 0, s>>>(g, w, L->d_status);
+			k_wf_shade<<<grid_c, 128, 0, s>>>(g, w, cur);
 			cur ^= 1;
 		}
 		k_wf_reduce<<<(int)((nb + 127) / 128), 128, 0, s>>>(g, w, (uint32_t)nb, first, out, bent);
