@@ -295,18 +295,47 @@ __global__ void k_table_init(float* __restrict__ t, uint64_t n, uint64_t seed) {
 	}
 }
 
+// One Adam step of a table entry (entries whose gradient is not finite keep
+// their state).
+__device__ __forceinline__ void adam_entry(float gr, float& mi, float& vi, float& wi, float lr, float b1, float b2,
+                                           float eps, float c1, float c2) {
+	if (!isfinite(gr)) return;
+	mi = b1 * mi + (1.f - b1) * gr;
+	vi = b2 * vi + (1.f - b2) * gr * gr;
+	wi -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// Adam over the whole table (every entry's moments decay each step), four
+// entries per thread and iteration with all four arrays read up front: the
+// kernel is a stream over 32 B per entry, bound by HBM.
 __global__ void k_table_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                              float* __restrict__ grad, uint64_t n, float lr, float b1, float b2, float eps, float c1,
                              float c2) {
-	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-		float gr = grad[i];
+	const uint64_t n4 = n / 4, stride = (uint64_t)gridDim.x * blockDim.x;
+	float4* w4 = reinterpret_cast<float4*>(w);
+	float4* m4 = reinterpret_cast<float4*>(m);
+	float4* v4 = reinterpret_cast<float4*>(v);
+	float4* g4 = reinterpret_cast<float4*>(grad);
+	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
+		const float4 gr = g4[i];
+		float4 mm = m4[i], vv = v4[i], ww = w4[i];
+		g4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+		adam_entry(gr.x, mm.x, vv.x, ww.x, lr, b1, b2, eps, c1, c2);
+		adam_entry(gr.y, mm.y, vv.y, ww.y, lr, b1, b2, eps, c1, c2);
+		adam_entry(gr.z, mm.z, vv.z, ww.z, lr, b1, b2, eps, c1, c2);
+		adam_entry(gr.w, mm.w, vv.w, ww.w, lr, b1, b2, eps, c1, c2);
+		m4[i] = mm;
+		v4[i] = vv;
+		w4[i] = ww;
+	}
+	for (uint64_t i = 4 * n4 + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+		const float gr = grad[i];
 		grad[i] = 0.f;
-		if (!isfinite(gr)) continue;
-		float mi = b1 * m[i] + (1.f - b1) * gr;
-		float vi = b2 * v[i] + (1.f - b2) * gr * gr;
+		float mi = m[i], vi = v[i], wi = w[i];
+		adam_entry(gr, mi, vi, wi, lr, b1, b2, eps, c1, c2);
 		m[i] = mi;
 		v[i] = vi;
-		w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+		w[i] = wi;
 	}
 }
 
