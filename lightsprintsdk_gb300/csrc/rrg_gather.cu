@@ -902,7 +902,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 }
 
 // Closest hit of every live path (trace_path's traversal and hit fields).
-__global__ void __launch_bounds__(128) k_wf_closest(GatherScene g, WfState w, int cur, uint32_t* status) {
+__global__ void __launch_bounds__(128, 8) k_wf_closest(GatherScene g, WfState w, int cur, uint32_t* status) {
 	const uint32_t n = w.counts[cur];
 	const uint32_t* live = w.live + (size_t)cur * w.cap;
 	bool overflow = false;
@@ -966,7 +966,7 @@ __global__ void __launch_bounds__(128) k_wf_nee(GatherScene g, WfState w) {
 
 // The shadow rays of this bounce, one thread each (the same ray and test as
 // trace_path's occluded() call).
-__global__ void __launch_bounds__(128) k_wf_shadow(GatherScene g, WfState w, uint32_t* status) {
+__global__ void __launch_bounds__(128, 8) k_wf_shadow(GatherScene g, WfState w, uint32_t* status) {
 	const uint32_t n = w.counts[3];
 	bool overflow = false;
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
