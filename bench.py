@@ -468,10 +468,12 @@ def run_gather(args, world, rank, local):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     clk.mark_start()
+    lc0 = col.launch_count()
     e0.record(stream)
     for _ in range(steps):
         step()
     e1.record(stream)
+    launches = col.launch_count() - lc0
     torch.cuda.synchronize()
     clk.mark_end()
     clk.__exit__()
@@ -506,7 +508,7 @@ def run_gather(args, world, rank, local):
                                        f"quality 64, 8 bounces, {natl} atlases of 256x256 on the "
                                        f"{gs.scene.ntri}-triangle interior", "texels": n, "covered": covered,
                            "subtexels": L.nsubtexels, "enumeration_s": enum_s, **extra},
-                "gpu_launches": steps, "clocks": clk.summary()}
+                "gpu_launches": launches, "clocks": clk.summary()}
         if not args.no_cpu_baseline and not learned:
             line["cpu_baseline"] = gather_cpu_baseline(gs, L)
         print(json.dumps(line), flush=True)
@@ -519,6 +521,7 @@ def run_batch(args, world, rank, local):
     import torch
     from lightsprintsdk_gb300 import autotune
     from lightsprintsdk_gb300 import batch as rb
+    from lightsprintsdk_gb300 import collider as col
     from lightsprintsdk_gb300 import scenes
     mb, counts = c3_workload(args.meshes)
     dev = f"cuda:{local}"
@@ -547,10 +550,12 @@ def run_batch(args, world, rank, local):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     clk.mark_start()
+    lc0 = col.launch_count()
     e0.record(stream)
     for _ in range(args.steps):
         step()
     e1.record(stream)
+    launches = col.launch_count() - lc0
     torch.cuda.synchronize()
     clk.mark_end()
     clk.__exit__()
@@ -577,7 +582,7 @@ def run_batch(args, world, rank, local):
                          "frac": achieved / peak, "traffic": None,
                          "note": f"algorithmic {BYTES_PER_RAY} B/ray; peak {peak_src}"},
             "e2e": None,
-            "gpu_launches": args.steps,
+            "gpu_launches": launches,
             "clocks": clk.summary(),
         }
         if world == 1 and not args.no_cpu_baseline:
@@ -651,10 +656,12 @@ def main():
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     clk.mark_start()
+    lc0 = col.launch_count()
     e0.record(stream)
     for _ in range(args.steps):
         step()
     e1.record(stream)
+    launches = col.launch_count() - lc0
     torch.cuda.synchronize()
     clk.mark_end()
     clk.__exit__()
@@ -706,7 +713,7 @@ def main():
                                  f"is issue-bound, so the HBM fraction is low by design"},
             "e2e": {"value": world * n / e2e_s / 1e9, "unit": "Grays/s", "h2d_bytes_per_step": 32 * n,
                     "d2h_bytes_per_step": 16 * n},
-            "gpu_launches": args.steps,
+            "gpu_launches": launches,
             "clocks": clk.summary(),
         }
         if world == 1 and not args.no_cpu_baseline:

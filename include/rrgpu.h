@@ -216,6 +216,10 @@ RRG_API const char* rrg_status_string(int status);
 RRG_API const char* rrg_last_cuda_error(void);
 /* Library version, (major << 16) | minor. */
 RRG_API uint32_t rrg_version(void);
+/* Kernels this library has launched in this process so far, on every
+ * device and thread (a kernel inside a CUDA graph counts once per graph
+ * launch).  No reference counterpart: a profiling aid. */
+RRG_API uint64_t rrg_launch_count(void);
 
 #ifdef __cplusplus
 }

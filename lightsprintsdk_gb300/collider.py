@@ -94,12 +94,19 @@ def _lib():
         L.rrg_status_string.restype = C.c_char_p
         L.rrg_last_cuda_error.restype = C.c_char_p
         L.rrg_version.restype = U
+        L.rrg_launch_count.restype = C.c_uint64
         _L = L
     return _L
 
 
 def library_path() -> str:
     return _build.LIB
+
+
+def launch_count() -> int:
+    """Kernels the library has launched in this process so far (all threads
+    and devices; a kernel inside a CUDA graph counts once per graph launch)."""
+    return int(_lib().rrg_launch_count())
 
 
 def _check(st: int, what: str):

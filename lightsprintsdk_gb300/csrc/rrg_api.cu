@@ -114,6 +114,9 @@ static int ensure_pipeline(Collider* c) {
 // hits out per chunk).
 constexpr uint32_t kHostChunk = 1u << 22;
 
+std::atomic<uint64_t> g_launches{0};
+thread_local int t_capturing = 0;
+
 }  // namespace rrg
 
 using namespace rrg;
@@ -121,6 +124,8 @@ using namespace rrg;
 extern "C" {
 
 uint32_t rrg_version(void) { return (1u << 16) | 0u; }
+
+uint64_t rrg_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 const char* rrg_last_cuda_error(void) { return g_cuda_err; }
 

@@ -17,6 +17,7 @@ struct Batch {
 	int blocks = 0;                 // persistent grid (occupancy x SMs)
 	cudaStream_t cap = nullptr;     // private stream the graph is captured on
 	cudaGraphExec_t exec = nullptr;
+	uint32_t graph_kernels = 0;   // kernel nodes of exec
 	// arguments the captured graph was made for
 	const void* g_rays = nullptr;
 	const void* g_off = nullptr;
@@ -146,14 +147,27 @@ int rrg_batch_intersect_device(rrg_batch* h, const float* rays_dev, const uint32
 		}
 		cudaGraph_t g = nullptr;
 		RRG_CUDA(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
+		t_capturing = 1;   // recorded, not launched: counted per graph launch below
 		int st = launch_batch_closest(b->c, reinterpret_cast<const float4*>(rays_dev), n, ray_off_dev, b->nmesh,
 		                              b->fetch, b->blocks, reinterpret_cast<float4*>(hits_dev), b->cap);
+		t_capturing = 0;
 		cudaError_t e = cudaStreamEndCapture(b->cap, &g);
 		if (st) {
 			if (g) cudaGraphDestroy(g);
 			return st;
 		}
 		if (e != cudaSuccess) return cuda_fail(e);
+		b->graph_kernels = 0;
+		size_t nn = 0;
+		if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn) {
+			std::vector<cudaGraphNode_t> nodes(nn);
+			if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+				for (size_t i = 0; i < nn; i++) {
+					cudaGraphNodeType t;
+					if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+						b->graph_kernels++;
+				}
+		}
 		e = cudaGraphInstantiate(&b->exec, g, 0);
 		cudaGraphDestroy(g);
 		if (e != cudaSuccess) {
@@ -167,6 +181,7 @@ int rrg_batch_intersect_device(rrg_batch* h, const float* rays_dev, const uint32
 		b->g_fetch = b->fetch;
 	}
 	RRG_CUDA(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+	note_launches(b->graph_kernels);
 	return RRG_OK;
 }
 

@@ -207,12 +207,12 @@ int bin_rays(Collider* c, const float4* rays, uint32_t n, cudaStream_t s, int sl
 		s3[k] = ext > 0.f ? 8.f / ext : 0.f;
 	}
 	const size_t smem = kBins * sizeof(uint32_t);
-	k_bin_hist<<<nblocks, kBinThreads, smem, s>>>(rays, n, chunk, c->aabb_lo[0], c->aabb_lo[1], c->aabb_lo[2], s3[0],
+	rrg::note_launch(), k_bin_hist<<<nblocks, kBinThreads, smem, s>>>(rays, n, chunk, c->aabb_lo[0], c->aabb_lo[1], c->aabb_lo[2], s3[0],
 	                                              s3[1], s3[2], keys, hist, nblocks);
-	k_scan_block_sums<<<(unsigned)nsum, kScanThreads, 0, s>>>(hist, nh, bsum);
-	k_scan_sums_exclusive<<<1, kScanThreads, 0, s>>>(bsum, (uint32_t)nsum);
-	k_scan_apply_exclusive<<<(unsigned)nsum, kScanThreads, 0, s>>>(hist, nh, bsum);
-	k_bin_scatter<<<nblocks, kBinThreads, smem, s>>>(keys, n, chunk, hist, nblocks, perm);
+	rrg::note_launch(), k_scan_block_sums<<<(unsigned)nsum, kScanThreads, 0, s>>>(hist, nh, bsum);
+	rrg::note_launch(), k_scan_sums_exclusive<<<1, kScanThreads, 0, s>>>(bsum, (uint32_t)nsum);
+	rrg::note_launch(), k_scan_apply_exclusive<<<(unsigned)nsum, kScanThreads, 0, s>>>(hist, nh, bsum);
+	rrg::note_launch(), k_bin_scatter<<<nblocks, kBinThreads, smem, s>>>(keys, n, chunk, hist, nblocks, perm);
 	RRG_CUDA(cudaGetLastError());
 	*perm_out = perm;
 	return RRG_OK;

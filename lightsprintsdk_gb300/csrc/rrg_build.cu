@@ -376,7 +376,7 @@ __global__ void k_globalize_indices(uint32_t* __restrict__ idx, uint32_t nt, con
 }
 
 int globalize_batch_indices(Collider* c, const uint32_t* d_vert_off, cudaStream_t s) {
-	k_globalize_indices<<<(c->nt + 255) / 256, 256, 0, s>>>(c->d_idx, c->nt, c->d_tri_off, d_vert_off, c->nroots);
+	rrg::note_launch(), k_globalize_indices<<<(c->nt + 255) / 256, 256, 0, s>>>(c->d_idx, c->nt, c->d_tri_off, d_vert_off, c->nroots);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }
@@ -1047,9 +1047,9 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 	RRG_CUDA(sc.get(&rb, 12));
 	RRG_CUDA(cudaMemsetAsync(st, 0, sizeof(BuildState), s));
 
-	k_prep<<<(nt + 255) / 256, 256, 0, s>>>(c->d_xyz, c->nv, c->d_idx, nt, plo, phi, valid, st);
-	k_block_count<<<nb, kBT, 0, s>>>(valid, nt, bsum);
-	k_scan_blocks<<<1, kBT, 0, s>>>(bsum, nb, total);
+	rrg::note_launch(), k_prep<<<(nt + 255) / 256, 256, 0, s>>>(c->d_xyz, c->nv, c->d_idx, nt, plo, phi, valid, st);
+	rrg::note_launch(), k_block_count<<<nb, kBT, 0, s>>>(valid, nt, bsum);
+	rrg::note_launch(), k_scan_blocks<<<1, kBT, 0, s>>>(bsum, nb, total);
 	RRG_CUDA(cudaGetLastError());
 	uint32_t nvalid = 0;
 	BuildState hst;
@@ -1064,7 +1064,7 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 	RRG_CUDA(sc.get(&idsA, nvalid));
 	RRG_CUDA(sc.get(&idsB, nvalid));
 	RRG_CUDA(sc.get(&final_ids, nvalid));
-	k_compact<<<nb, kBT, 0, s>>>(valid, nt, bsum, idsA);
+	rrg::note_launch(), k_compact<<<nb, kBT, 0, s>>>(valid, nt, bsum, idsA);
 
 	const uint32_t nroots = c->d_tri_off ? c->nroots : 1;
 	const int max_nodes = 2 * (int)nvalid + (int)nroots;
@@ -1104,7 +1104,7 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 	{
 		int vgrid = (int)((c->nv + 255) / 256);
 		if (vgrid > 4 * 152) vgrid = 4 * 152;
-		k_vertex_aabb<<<vgrid, 256, 0, s>>>(c->d_xyz, c->nv, rb);
+		rrg::note_launch(), k_vertex_aabb<<<vgrid, 256, 0, s>>>(c->d_xyz, c->nv, rb);
 		int hb[6];
 		RRG_CUDA(cudaMemcpyAsync(hb, rb, sizeof(hb), cudaMemcpyDeviceToHost, s));
 		RRG_CUDA(cudaStreamSynchronize(s));
@@ -1122,13 +1122,13 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 		int* rbm;
 		RRG_CUDA(sc.get(&pos, nroots + 1));
 		RRG_CUDA(sc.get(&rbm, 12 * (size_t)nroots));
-		k_mesh_ranges<<<(nroots + 1 + 255) / 256, 256, 0, s>>>(idsA, nvalid, c->d_tri_off, nroots, pos);
-		k_fill_root_bounds<<<(12 * nroots + 255) / 256, 256, 0, s>>>(rbm, nroots);
-		k_root_bounds_multi<<<rgrid, 256, 0, s>>>(idsA, nvalid, plo, phi, pos, nroots, rbm);
-		k_root_init_multi<<<(nroots + 255) / 256, 256, 0, s>>>(rbm, pos, nroots, bnodes, largeA, small, st);
+		rrg::note_launch(), k_mesh_ranges<<<(nroots + 1 + 255) / 256, 256, 0, s>>>(idsA, nvalid, c->d_tri_off, nroots, pos);
+		rrg::note_launch(), k_fill_root_bounds<<<(12 * nroots + 255) / 256, 256, 0, s>>>(rbm, nroots);
+		rrg::note_launch(), k_root_bounds_multi<<<rgrid, 256, 0, s>>>(idsA, nvalid, plo, phi, pos, nroots, rbm);
+		rrg::note_launch(), k_root_init_multi<<<(nroots + 255) / 256, 256, 0, s>>>(rbm, pos, nroots, bnodes, largeA, small, st);
 	} else {
-		k_root_bounds<<<rgrid, 256, 0, s>>>(idsA, nvalid, plo, phi, rb);
-		k_root_init<<<1, 1, 0, s>>>(rb, nvalid, bnodes, largeA, small, st);
+		rrg::note_launch(), k_root_bounds<<<rgrid, 256, 0, s>>>(idsA, nvalid, plo, phi, rb);
+		rrg::note_launch(), k_root_init<<<1, 1, 0, s>>>(rb, nvalid, bnodes, largeA, small, st);
 	}
 	RRG_CUDA(cudaGetLastError());
 
@@ -1145,12 +1145,12 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 		// reset per-level counters (keep node_count and nsmall)
 		RRG_CUDA(cudaMemsetAsync(&st->nlarge_next, 0, 4, s));
 		RRG_CUDA(cudaMemsetAsync(&st->nchunks, 0, 4, s));
-		k_level_setup<<<ntasks < grid ? ntasks : grid, kBT, 0, s>>>(cur, ntasks, gbins, chunks, st);
-		k_bin_chunks<<<grid, kBT, 0, s>>>(cur, chunks, st, ids_bufs, plo, phi, gbins);
-		k_decide_large<<<ntasks < grid ? ntasks : grid, 128, 0, s>>>(cur, ntasks, gbins, splits, bnodes, nxt, small, st);
-		k_part_count<<<grid, kBT, 0, s>>>(cur, chunks, st, splits, ids_bufs, plo, phi, chunk_left);
-		k_part_scan<<<(ntasks + 127) / 128, 128, 0, s>>>(cur, ntasks, chunk_left);
-		k_part_scatter<<<grid, kBT, 0, s>>>(cur, chunks, st, splits, ids_bufs, plo, phi, chunk_left, st);
+		rrg::note_launch(), k_level_setup<<<ntasks < grid ? ntasks : grid, kBT, 0, s>>>(cur, ntasks, gbins, chunks, st);
+		rrg::note_launch(), k_bin_chunks<<<grid, kBT, 0, s>>>(cur, chunks, st, ids_bufs, plo, phi, gbins);
+		rrg::note_launch(), k_decide_large<<<ntasks < grid ? ntasks : grid, 128, 0, s>>>(cur, ntasks, gbins, splits, bnodes, nxt, small, st);
+		rrg::note_launch(), k_part_count<<<grid, kBT, 0, s>>>(cur, chunks, st, splits, ids_bufs, plo, phi, chunk_left);
+		rrg::note_launch(), k_part_scan<<<(ntasks + 127) / 128, 128, 0, s>>>(cur, ntasks, chunk_left);
+		rrg::note_launch(), k_part_scatter<<<grid, kBT, 0, s>>>(cur, chunks, st, splits, ids_bufs, plo, phi, chunk_left, st);
 		RRG_CUDA(cudaGetLastError());
 		Task* tmp = cur;
 		cur = nxt;
@@ -1161,7 +1161,7 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 	if (aborting && *aborting) return RRG_ERR_ABORTED;
 	if (hst.nsmall > 0) {
 		int sgrid = hst.nsmall < c->num_sms * 8 ? hst.nsmall : c->num_sms * 8;
-		k_small<<<sgrid, kSmallThreads, 0, s>>>(small, st, ids_bufs, plo, phi, bnodes, final_ids, max_leaf, st);
+		rrg::note_launch(), k_small<<<sgrid, kSmallThreads, 0, s>>>(small, st, ids_bufs, plo, phi, bnodes, final_ids, max_leaf, st);
 		RRG_CUDA(cudaGetLastError());
 	}
 	RRG_CUDA(cudaMemcpyAsync(&hst, st, sizeof(hst), cudaMemcpyDeviceToHost, s));
@@ -1179,9 +1179,9 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 	RRG_CUDA(dalloc(&c->d_tris, 3 * (size_t)nvalid));
 	float* pad;
 	RRG_CUDA(sc.get(&pad, 1));
-	k_root_pad<<<1, 256, 0, s>>>(bnodes, nroots, pad);
-	k_emit_nodes<<<(nnodes + 255) / 256, 256, 0, s>>>(bnodes, nnodes, (int)nroots, pad, c->d_nodes);
-	k_emit_tris<<<(nvalid + 255) / 256, 256, 0, s>>>(final_ids, nvalid, c->d_xyz, c->d_idx, c->d_tris);
+	rrg::note_launch(), k_root_pad<<<1, 256, 0, s>>>(bnodes, nroots, pad);
+	rrg::note_launch(), k_emit_nodes<<<(nnodes + 255) / 256, 256, 0, s>>>(bnodes, nnodes, (int)nroots, pad, c->d_nodes);
+	rrg::note_launch(), k_emit_tris<<<(nvalid + 255) / 256, 256, 0, s>>>(final_ids, nvalid, c->d_xyz, c->d_idx, c->d_tris);
 	RRG_CUDA(cudaGetLastError());
 	if (c->width == 8) {
 		int wst = build_wide(c, bnodes, nnodes, pad, s);

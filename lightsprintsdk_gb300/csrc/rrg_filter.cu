@@ -480,7 +480,7 @@ static int seam_runs(LightmapFilter* F, const std::vector<Seam>& seams, uint32_t
 	RRG_CUDA(cudaMemcpy(dseams.p, seams.data(), sizeof(Seam) * ns, cudaMemcpyHostToDevice));
 	RRG_CUDA(cudaMalloc(&cnt.p, sizeof(uint32_t) * ns));
 	const int grid = (int)std::min<uint64_t>((ns * 32 + 255) / 256, (uint64_t)num_sms * 16);
-	k_seam_runs<true><<<grid, 256>>>((const Seam*)dseams.p, ns, size, (uint32_t*)cnt.p, nullptr, nullptr);
+	rrg::note_launch(), k_seam_runs<true><<<grid, 256>>>((const Seam*)dseams.p, ns, size, (uint32_t*)cnt.p, nullptr, nullptr);
 	RRG_CUDA(cudaGetLastError());
 	std::vector<uint32_t> counts(ns);
 	RRG_CUDA(cudaMemcpy(counts.data(), cnt.p, sizeof(uint32_t) * ns, cudaMemcpyDeviceToHost));
@@ -495,7 +495,7 @@ static int seam_runs(LightmapFilter* F, const std::vector<Seam>& seams, uint32_t
 	RRG_CUDA(cudaMalloc(&F->d_run_off, sizeof(uint32_t) * (ns + 1)));
 	RRG_CUDA(cudaMemcpy(F->d_run_off, off.data(), sizeof(uint32_t) * (ns + 1), cudaMemcpyHostToDevice));
 	RRG_CUDA(cudaMalloc(&F->d_runs, sizeof(uint32_t) * 3 * (off[ns] ? off[ns] : 1)));
-	k_seam_runs<false><<<grid, 256>>>((const Seam*)dseams.p, ns, size, nullptr, F->d_run_off, F->d_runs);
+	rrg::note_launch(), k_seam_runs<false><<<grid, 256>>>((const Seam*)dseams.p, ns, size, nullptr, F->d_run_off, F->d_runs);
 	RRG_CUDA(cudaGetLastError());
 	RRG_CUDA(cudaDeviceSynchronize());
 	return RRG_OK;
@@ -658,7 +658,7 @@ int rrg_lightmap_filter(rrg_lightmapper* h, const rrg_filter_params* p, uint32_t
 		if (seams)
 			RRG_CUDA(cudaFuncSetAttribute(k_smooth_seams, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			                              (int)seam_smem));
-		k_smooth_prep<<<grid, threads, 0, s>>>(lm, F->d_a, F->d_bits, v.size, n, wrap);
+		rrg::note_launch(), k_smooth_prep<<<grid, threads, 0, s>>>(lm, F->d_a, F->d_bits, v.size, n, wrap);
 		if (sigma > 10.f) sigma = 10.f;
 		float sum = sigma * sigma;
 		float4* src = F->d_a;
@@ -668,22 +668,22 @@ int rrg_lightmap_filter(rrg_lightmapper* h, const rrg_filter_params* p, uint32_t
 			// the kernel weights come from the host's expf, as the reference's do
 			const float k1 = expf(-0.5f / s2), k2 = expf(-1.f / s2);
 			sum -= s2;
-			k_smooth_pass<<<grid, threads, 0, s>>>(src, dst, F->d_bits, v.size, n, k1, k2);
+			rrg::note_launch(), k_smooth_pass<<<grid, threads, 0, s>>>(src, dst, F->d_bits, v.size, n, k1, k2);
 			if (seams)
-				k_smooth_seams<<<natlas, 32, seam_smem, s>>>(dst, F->d_runs, F->d_run_off, F->d_seam_off, first_atlas,
+				rrg::note_launch(), k_smooth_seams<<<natlas, 32, seam_smem, s>>>(dst, F->d_runs, F->d_run_off, F->d_seam_off, first_atlas,
 				                                             v.size, used_in_smem);
 			std::swap(src, dst);
 		}
-		k_smooth_store<<<grid, threads, 0, s>>>(lm, src, n);
+		rrg::note_launch(), k_smooth_store<<<grid, threads, 0, s>>>(lm, src, n);
 		RRG_CUDA(cudaGetLastError());
 	}
 	if (p->stages & RRG_FILTER_GROW_BILINEAR) {
 		RRG_CUDA(cudaMemcpyAsync(F->d_a, lm, sizeof(float4) * n, cudaMemcpyDeviceToDevice, s));
-		k_grow_bilinear<<<grid, threads, 0, s>>>(F->d_a, lm, v.size, n, wrap);
+		rrg::note_launch(), k_grow_bilinear<<<grid, threads, 0, s>>>(F->d_a, lm, v.size, n, wrap);
 		RRG_CUDA(cudaGetLastError());
 	}
 	if ((p->stages & RRG_FILTER_GROW) && p->spread_foreground) {
-		k_grow_prep<<<grid, threads, 0, s>>>(lm, F->d_a, n);
+		rrg::note_launch(), k_grow_prep<<<grid, threads, 0, s>>>(lm, F->d_a, n);
 		float4* src = F->d_a;
 		float4* dst = F->d_b;
 		uint32_t* chg[2] = {F->d_chg, F->d_chg + (natlas + 1)};
@@ -691,7 +691,7 @@ int rrg_lightmap_filter(rrg_lightmapper* h, const rrg_filter_params* p, uint32_t
 			uint32_t* cur = chg[step & 1];
 			const uint32_t* prev = chg[(step + 1) & 1];
 			RRG_CUDA(cudaMemsetAsync(cur, 0, sizeof(uint32_t) * (natlas + 1), s));
-			k_grow_step<<<grid, threads, 0, s>>>(src, dst, v.size, n, wrap, prev, cur, step == 0);
+			rrg::note_launch(), k_grow_step<<<grid, threads, 0, s>>>(src, dst, v.size, n, wrap, prev, cur, step == 0);
 			std::swap(src, dst);
 			// stop once a step changed nothing anywhere (checked every 8 steps)
 			if ((step & 7) == 7 || step + 1 == p->spread_foreground) {
@@ -700,11 +700,11 @@ int rrg_lightmap_filter(rrg_lightmapper* h, const rrg_filter_params* p, uint32_t
 				if (!*F->h_any) break;
 			}
 		}
-		k_grow_store<<<grid, threads, 0, s>>>(lm, src, n);
+		rrg::note_launch(), k_grow_store<<<grid, threads, 0, s>>>(lm, src, n);
 		RRG_CUDA(cudaGetLastError());
 	}
 	if (p->stages & RRG_FILTER_FILL_BACKGROUND) {
-		k_fill_background<<<grid, threads, 0, s>>>(lm, n, make_float4(p->background[0], p->background[1],
+		rrg::note_launch(), k_fill_background<<<grid, threads, 0, s>>>(lm, n, make_float4(p->background[0], p->background[1],
 		                                                              p->background[2], p->background[3]));
 		RRG_CUDA(cudaGetLastError());
 	}

@@ -1264,7 +1264,7 @@ static int launch_gather_kernel(Lightmapper* L, const GatherScene& g, uint64_t f
 	uint64_t want = (count + kGatherWarps - 1) / kGatherWarps;
 	uint64_t cap = (uint64_t)(per_sm > 0 ? per_sm : 1) * L->c->num_sms;
 	int grid = (int)(want < cap ? want : cap);
-	k_gather<LEARNED, DIR><<<grid, kGatherWarps * 32, 0, s>>>(g, L->d_off, L->d_sub, first, count, list, out_base, out,
+	rrg::note_launch(), k_gather<LEARNED, DIR><<<grid, kGatherWarps * 32, 0, s>>>(g, L->d_off, L->d_sub, first, count, list, out_base, out,
 	                                                          recs, reinterpret_cast<uint32_t*>(L->d_counter), L->d_status,
 	                                                          LEARNED ? nullptr : bent, dout);
 	RRG_CUDA(cudaGetLastError());
@@ -1325,7 +1325,7 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 		const uint64_t want = (nb + kGatherWarps - 1) / kGatherWarps;
 		const uint64_t capb = (uint64_t)(per_sm > 0 ? per_sm : 1) * L->c->num_sms;
 		const int grid = (int)(want < capb ? want : capb);
-		k_gather<false, false, true><<<grid, kGatherWarps * 32, 0, s>>>(
+		rrg::note_launch(), k_gather<false, false, true><<<grid, kGatherWarps * 32, 0, s>>>(
 		    g, L->d_off, L->d_sub, first + b0, nb, nullptr, first, out, nullptr, reinterpret_cast<uint32_t*>(L->d_counter),
 		    L->d_status, nullptr, DirOut{}, w);
 		RRG_CUDA(cudaGetLastError());
@@ -1333,13 +1333,13 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 		for (uint32_t depth = 0; depth <= g.max_depth; depth++) {
 			RRG_CUDA(cudaMemsetAsync(w.counts + 2, 0, 2 * sizeof(uint32_t), s));
 			RRG_CUDA(cudaMemsetAsync(w.counts + (cur ^ 1), 0, sizeof(uint32_t), s));
-			k_wf_closest<<<grid_c, 128, 0, s>>>(g, w, cur, L->d_status);
-			k_wf_nee<<<grid_c, 128, 0, s>>>(g, w);
-			k_wf_shadow<<<grid_c, 128, 0, s>>>(g, w, L->d_status);
-			k_wf_shade<<<grid_c, 128, 0, s>>>(g, w, cur);
+			rrg::note_launch(), k_wf_closest<<<grid_c, 128, 0, s>>>(g, w, cur, L->d_status);
+			rrg::note_launch(), k_wf_nee<<<grid_c, 128, 0, s>>>(g, w);
+			rrg::note_launch(), k_wf_shadow<<<grid_c, 128, 0, s>>>(g, w, L->d_status);
+			rrg::note_launch(), k_wf_shade<<<grid_c, 128, 0, s>>>(g, w, cur);
 			cur ^= 1;
 		}
-		k_wf_reduce<<<(int)((nb + 127) / 128), 128, 0, s>>>(g, w, (uint32_t)nb, first, out, bent);
+		rrg::note_launch(), k_wf_reduce<<<(int)((nb + 127) / 128), 128, 0, s>>>(g, w, (uint32_t)nb, first, out, bent);
 		RRG_CUDA(cudaGetLastError());
 	}
 	return RRG_OK;
@@ -1424,15 +1424,15 @@ int rrg_lightmapper_create(rrg_collider* ch, const float* albedo, const int32_t*
 	const int grid = c->num_sms * 16;
 	if ((e = cudaMalloc(&L->d_flags, (ntexels + 3) / 4 * 4)) != cudaSuccess) return fail(e);
 	if ((e = cudaMemset(L->d_flags, 0, (ntexels + 3) / 4 * 4)) != cudaSuccess) return fail(e);
-	k_enumerate<true><<<grid, 256>>>(d_uv, d_atlas, nt, size, natlas, d_counts, nullptr, nullptr, nullptr, nullptr, 0, d_err,
+	rrg::note_launch(), k_enumerate<true><<<grid, 256>>>(d_uv, d_atlas, nt, size, natlas, d_counts, nullptr, nullptr, nullptr, nullptr, 0, d_err,
 	                                 reinterpret_cast<uint32_t*>(L->d_flags));
 	if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
 	const uint32_t nb = (uint32_t)((ntexels + kScanPer - 1) / kScanPer);
 	if ((e = cudaMalloc(&d_bsum, sizeof(uint32_t) * (nb + 1))) != cudaSuccess) return fail(e);
 	if ((e = cudaMalloc(&L->d_off, sizeof(uint32_t) * (ntexels + 1))) != cudaSuccess) return fail(e);
-	k_scan_sums<<<nb, kScanBT>>>(d_counts, ntexels, d_bsum);
-	k_scan_top<<<1, 32>>>(d_bsum, nb);
-	k_scan_apply<<<nb, kScanBT>>>(d_counts, ntexels, d_bsum, L->d_off);
+	rrg::note_launch(), k_scan_sums<<<nb, kScanBT>>>(d_counts, ntexels, d_bsum);
+	rrg::note_launch(), k_scan_top<<<1, 32>>>(d_bsum, nb);
+	rrg::note_launch(), k_scan_apply<<<nb, kScanBT>>>(d_counts, ntexels, d_bsum, L->d_off);
 	if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
 	uint32_t total = 0;
 	if ((e = cudaMemcpy(&total, L->d_off + ntexels, 4, cudaMemcpyDeviceToHost)) != cudaSuccess) return fail(e);
@@ -1441,9 +1441,9 @@ int rrg_lightmapper_create(rrg_collider* ch, const float* albedo, const int32_t*
 	if ((e = cudaMalloc(&d_fan, sizeof(uint32_t) * (total ? total : 1))) != cudaSuccess) return fail(e);
 	if ((e = cudaMalloc(&d_cursor, sizeof(uint32_t) * ntexels)) != cudaSuccess) return fail(e);
 	if ((e = cudaMemset(d_cursor, 0, sizeof(uint32_t) * ntexels)) != cudaSuccess) return fail(e);
-	k_enumerate<false><<<grid, 256>>>(d_uv, d_atlas, nt, size, natlas, nullptr, L->d_off, d_cursor, L->d_sub, d_fan, total, d_err,
+	rrg::note_launch(), k_enumerate<false><<<grid, 256>>>(d_uv, d_atlas, nt, size, natlas, nullptr, L->d_off, d_cursor, L->d_sub, d_fan, total, d_err,
 	                                  nullptr);
-	k_sort_texels<<<grid, 256>>>(L->d_off, ntexels, L->d_sub, d_fan);
+	rrg::note_launch(), k_sort_texels<<<grid, 256>>>(L->d_off, ntexels, L->d_sub, d_fan);
 	if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
 	uint32_t herr = 0;
 	if ((e = cudaMemcpy(&herr, d_err, 4, cudaMemcpyDeviceToHost)) != cudaSuccess) return fail(e);
@@ -1459,15 +1459,15 @@ int rrg_lightmapper_create(rrg_collider* ch, const float* albedo, const int32_t*
 		if ((e = cudaMalloc(&flag, sizeof(uint32_t) * ntexels)) != cudaSuccess) return fail(e);
 		if ((e = cudaMalloc(&pos, sizeof(uint32_t) * (ntexels + 1))) != cudaSuccess) { cudaFree(flag); return fail(e); }
 		if ((e = cudaMalloc(&bs, sizeof(uint32_t) * (nb + 1))) != cudaSuccess) { cudaFree(flag); cudaFree(pos); return fail(e); }
-		k_covered_flags<<<grid, 256>>>(L->d_off, ntexels, flag);
-		k_scan_sums<<<nb, kScanBT>>>(flag, ntexels, bs);
-		k_scan_top<<<1, 32>>>(bs, nb);
-		k_scan_apply<<<nb, kScanBT>>>(flag, ntexels, bs, pos);
+		rrg::note_launch(), k_covered_flags<<<grid, 256>>>(L->d_off, ntexels, flag);
+		rrg::note_launch(), k_scan_sums<<<nb, kScanBT>>>(flag, ntexels, bs);
+		rrg::note_launch(), k_scan_top<<<1, 32>>>(bs, nb);
+		rrg::note_launch(), k_scan_apply<<<nb, kScanBT>>>(flag, ntexels, bs, pos);
 		uint32_t ncov = 0;
 		e = cudaMemcpy(&ncov, pos + ntexels, 4, cudaMemcpyDeviceToHost);
 		if (e == cudaSuccess) e = cudaMalloc(&L->d_covered, sizeof(uint32_t) * (ncov ? ncov : 1));
 		if (e == cudaSuccess) {
-			k_covered_scatter<<<grid, 256>>>(flag, pos, ntexels, L->d_covered);
+			rrg::note_launch(), k_covered_scatter<<<grid, 256>>>(flag, pos, ntexels, L->d_covered);
 			e = cudaGetLastError();
 		}
 		cudaFree(flag);
@@ -1581,7 +1581,7 @@ int rrg_lightmap_train_samples(rrg_lightmapper* h, const rrg_gather_params* p, u
 	const uint64_t npaths = (L->ncovered + stride - 1) / stride * paths_per_texel;
 	RRG_CUDA(cudaMemsetAsync(L->d_counter, 0, 8, s));
 	int grid = L->c->num_sms * 8;
-	k_train_paths<<<grid, 128, 0, s>>>(g, L->d_off, L->d_sub, L->d_covered, (uint32_t)L->ncovered, stride,
+	rrg::note_launch(), k_train_paths<<<grid, 128, 0, s>>>(g, L->d_off, L->d_sub, L->d_covered, (uint32_t)L->ncovered, stride,
 	                                   paths_per_texel, npaths, p->seed ^ 0x7A1Dull, reinterpret_cast<CacheRec*>(recs_dev),
 	                                   cap, reinterpret_cast<unsigned long long*>(L->d_counter), L->d_status);
 	RRG_CUDA(cudaGetLastError());
@@ -1633,7 +1633,7 @@ int rrg_lightmap_gather_learned(rrg_lightmapper* h, rrg_cache* cache, const rrg_
 		st = rrg_cache_infer(cache, L->d_recs, n * Q, reinterpret_cast<float*>(L->d_rad), stream);
 		if (st) return st;
 		RRG_CUDA(cudaMemsetAsync(L->d_fbcount, 0, sizeof(unsigned int), s));
-		k_learned_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+		rrg::note_launch(), k_learned_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
 		    L->d_off, c0, n, Q, L->d_recs, L->d_rad, oc, grid, res, lo[0], lo[1], lo[2], ie[0], ie[1], ie[2],
 		    fallback_frac, grid ? L->d_fb : nullptr, L->d_fbcount);
 		RRG_CUDA(cudaGetLastError());

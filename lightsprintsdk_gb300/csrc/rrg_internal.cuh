@@ -4,6 +4,7 @@
 #include <stdint.h>
 #include <stddef.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "../../include/rrgpu.h"
@@ -174,6 +175,15 @@ struct LightmapView {
 LightmapView lightmapper_view(::rrg_lightmapper* lm);
 
 // api (rrg_api.cu)
+// Kernels this library has launched in the process (rrg_launch_count):
+// every launch site bumps it through note_launch(); launches recorded into a
+// CUDA graph are counted when the graph is launched, not while it is captured.
+extern std::atomic<uint64_t> g_launches;
+extern thread_local int t_capturing;
+inline void note_launch() {
+	if (!t_capturing) g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+inline void note_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 int cuda_fail(cudaError_t e);
 int init_collider(Collider* c, const rrg_build_params* params);
 void free_collider(Collider* c);

@@ -454,7 +454,7 @@ static int ensure_batch(RadianceCache* C, uint32_t B) {
 }
 
 static int pack(RadianceCache* C, cudaStream_t s) {
-	k_mlp_pack<<<(kMlpFragWords + 255) / 256, 256, 0, s>>>(C->w, C->fwd, C->bwd);
+	rrg::note_launch(), k_mlp_pack<<<(kMlpFragWords + 255) / 256, 256, 0, s>>>(C->w, C->fwd, C->bwd);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }
@@ -465,10 +465,10 @@ static int fwd_bwd(RadianceCache* C, const CacheRec* recs, uint32_t nrec, uint32
 	int st = ensure_batch(C, B);
 	if (st) return st;
 	const int warps = B / 16;
-	k_mlp_fwd_bwd<<<(warps + 3) / 4, 128, 0, s>>>(recs, nrec, B, seed, C->steps, order, C->fwd, C->bwd, C->buf,
+	rrg::note_launch(), k_mlp_fwd_bwd<<<(warps + 3) / 4, 128, 0, s>>>(recs, nrec, B, seed, C->steps, order, C->fwd, C->bwd, C->buf,
 	                                              C->lo[0], C->lo[1], C->lo[2], C->ie[0], C->ie[1], C->ie[2], pred,
 	                                              C->hg);
-	k_mlp_wgrad<<<5 * (B / kWgRows), 128, 0, s>>>(C->buf, B);
+	rrg::note_launch(), k_mlp_wgrad<<<5 * (B / kWgRows), 128, 0, s>>>(C->buf, B);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }
@@ -544,7 +544,7 @@ static int infer_impl(RadianceCache* C, const void* recs_dev, uint64_t n, float*
 	uint64_t ntiles = (n + 15) / 16;
 	uint64_t blocks = (ntiles + kInferWarps - 1) / kInferWarps;
 	uint64_t cap = (uint64_t)C->num_sms * 4;
-	k_mlp_infer<<<(int)(blocks < cap ? blocks : cap), kInferWarps * 32, smem, (cudaStream_t)stream>>>(
+	rrg::note_launch(), k_mlp_infer<<<(int)(blocks < cap ? blocks : cap), kInferWarps * 32, smem, (cudaStream_t)stream>>>(
 	    reinterpret_cast<const CacheRec*>(recs_dev), n, C->fwd, C->lo[0], C->lo[1], C->lo[2], C->ie[0], C->ie[1],
 	    C->ie[2], reinterpret_cast<float4*>(out_dev), C->hg, all_valid);
 	RRG_CUDA(cudaGetLastError());
@@ -582,10 +582,10 @@ int rrg_cache_build_error_grid_ex(rrg_cache* h, const void* recs_dev, uint64_t n
 	RRG_CUDA(cudaMemsetAsync(nrel, 0, sizeof(unsigned int), s));
 	int st = infer_impl(C, recs_dev, nrec, reinterpret_cast<float*>(pred), 1, s);
 	if (!st) {
-		k_grid_accum<<<C->num_sms * 8, 256, 0, s>>>(reinterpret_cast<const CacheRec*>(recs_dev), pred, nrec, (int)res,
+		rrg::note_launch(), k_grid_accum<<<C->num_sms * 8, 256, 0, s>>>(reinterpret_cast<const CacheRec*>(recs_dev), pred, nrec, (int)res,
 		                                             C->lo[0], C->lo[1], C->lo[2], C->ie[0], C->ie[1], C->ie[2], sums,
 		                                             sums + ncell, sums + 2 * ncell);
-		k_grid_flags<<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(sums, sums + ncell, sums + 2 * ncell,
+		rrg::note_launch(), k_grid_flags<<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(sums, sums + ncell, sums + 2 * ncell,
 		                                                            sums + 3 * ncell, ncell, rel_threshold,
 		                                                            (float)min_count, plain_samples, C->grid, nrel);
 		cudaError_t e = cudaGetLastError();
@@ -649,7 +649,7 @@ int rrg_cache_create_ex(const rrg_cache_params* params, rrg_cache** out) {
 	if (e == cudaSuccess) e = cudaMemset(C->v, 0, sizeof(float) * kMlpParams);
 	if (e == cudaSuccess) e = cudaMemset(C->buf.grad, 0, sizeof(float) * kMlpParams);
 	if (e != cudaSuccess) { free_cache(C); return cuda_fail(e); }
-	k_mlp_init<<<(kMlpParams + 255) / 256, 256>>>(C->w, seed);
+	rrg::note_launch(), k_mlp_init<<<(kMlpParams + 255) / 256, 256>>>(C->w, seed);
 	if (params->encoding == RRG_CACHE_HASHGRID) {
 		const uint32_t T = 1u << log2T;
 		C->table_floats = (uint64_t)kHashLevels * T * 2;
@@ -662,7 +662,7 @@ int rrg_cache_create_ex(const rrg_cache_params* params, rrg_cache** out) {
 		if (e == cudaSuccess) e = cudaMemset(C->tv, 0, bytes);
 		if (e == cudaSuccess) e = cudaMemset(C->tgrad, 0, bytes);
 		if (e != cudaSuccess) { free_cache(C); return cuda_fail(e); }
-		k_table_init<<<C->num_sms * 8, 256>>>(C->table, C->table_floats, seed);
+		rrg::note_launch(), k_table_init<<<C->num_sms * 8, 256>>>(C->table, C->table_floats, seed);
 		C->hg.table = reinterpret_cast<const float2*>(C->table);
 		C->hg.tgrad = C->tgrad;
 		C->hg.T = T;
@@ -789,10 +789,10 @@ int rrg_cache_train(rrg_cache* h, const void* recs_dev, uint32_t nrec, uint32_t 
 		if (st) return st;
 		C->steps++;
 		float c1 = 1.f - powf(C->b1, (float)C->steps), c2 = 1.f - powf(C->b2, (float)C->steps);
-		k_mlp_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(C->w, C->m, C->v, C->buf.grad, C->lr, C->b1, C->b2,
+		rrg::note_launch(), k_mlp_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(C->w, C->m, C->v, C->buf.grad, C->lr, C->b1, C->b2,
 		                                                    C->eps, c1, c2);
 		if (C->table)
-			k_table_adam<<<C->num_sms * 8, 256, 0, s>>>(C->table, C->tm, C->tv, C->tgrad, C->table_floats, C->lr,
+			rrg::note_launch(), k_table_adam<<<C->num_sms * 8, 256, 0, s>>>(C->table, C->tm, C->tv, C->tgrad, C->table_floats, C->lr,
 			                                           C->b1, C->b2, C->eps, c1, c2);
 		st = pack(C, s);
 		if (st) return st;

@@ -485,7 +485,7 @@ int rrg_scene_intersect_device(rrg_scene* h, const float* rays_dev, uint32_t n, 
 	const uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
 	const int grid = (int)(want < (uint32_t)S->blocks ? want : (uint32_t)S->blocks);
 	const Collider* c = S->c;
-	k_scene_closest<<<grid, kTraceThreads, 0, s>>>(S->d_tl, (int)S->ntl, S->d_tl_obj, (int)S->ntl_obj, S->d_obj,
+	rrg::note_launch(), k_scene_closest<<<grid, kTraceThreads, 0, s>>>(S->d_tl, (int)S->ntl, S->d_tl_obj, (int)S->ntl_obj, S->d_obj,
 	                                               (int)S->nobj, c->d_nodes, (int)c->nnodes, c->d_tris,
 	                                               (int)c->nvalid, reinterpret_cast<const float4*>(rays_dev), n,
 	                                               reinterpret_cast<float4*>(hits_dev), objects_dev, S->d_counter);

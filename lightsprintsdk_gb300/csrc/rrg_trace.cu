@@ -444,14 +444,14 @@ int launch_closest_on(Collider* c, const float4* rays, uint32_t n, float4* hits,
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
 	if (c->width == 8 && c->d_wnodes) {
 		int grid = (int)(want < (uint32_t)c->wide_blocks ? want : (uint32_t)c->wide_blocks);
-		k_closest_w<<<grid, kTraceThreads, 0, s>>>(c->d_wnodes, (int)c->nwnodes, c->d_wtris, (int)c->nvalid, rays, n,
+		rrg::note_launch(), k_closest_w<<<grid, kTraceThreads, 0, s>>>(c->d_wnodes, (int)c->nwnodes, c->d_wtris, (int)c->nvalid, rays, n,
 		                                           hits, planes, points, words);
 		RRG_CUDA(cudaGetLastError());
 		return RRG_OK;
 	}
 	if (c->traversal != RRG_TRAVERSAL_IF_IF) {
 		int grid = (int)(want < (uint32_t)c->ww_blocks ? want : (uint32_t)c->ww_blocks);
-		k_trace_ww<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays,
+		rrg::note_launch(), k_trace_ww<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays,
 		                                                  n, hits, planes, points, nullptr, words);
 		RRG_CUDA(cudaGetLastError());
 		return RRG_OK;
@@ -461,10 +461,10 @@ int launch_closest_on(Collider* c, const float4* rays, uint32_t n, float4* hits,
 		const uint32_t* perm = nullptr;
 		int st = bin_rays(c, rays, n, s, bin_slot, &perm);
 		if (st) return st;
-		k_closest<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
+		rrg::note_launch(), k_closest<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
 		                                               hits, planes, points, words, perm);
 	} else {
-		k_closest<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
+		rrg::note_launch(), k_closest<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
 		                                                hits, planes, points, words, nullptr);
 	}
 	RRG_CUDA(cudaGetLastError());
@@ -482,14 +482,14 @@ int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, c
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
 	if (c->width == 8 && c->d_wnodes) {
 		int grid = (int)(want < (uint32_t)c->wide_blocks ? want : (uint32_t)c->wide_blocks);
-		k_occluded_w<<<grid, kTraceThreads, 0, s>>>(c->d_wnodes, (int)c->nwnodes, c->d_wtris, (int)c->nvalid, rays,
+		rrg::note_launch(), k_occluded_w<<<grid, kTraceThreads, 0, s>>>(c->d_wnodes, (int)c->nwnodes, c->d_wtris, (int)c->nvalid, rays,
 		                                            n, occ, c->d_counter);
 		RRG_CUDA(cudaGetLastError());
 		return RRG_OK;
 	}
 	if (c->traversal != RRG_TRAVERSAL_IF_IF) {
 		int grid = (int)(want < (uint32_t)c->ww_blocks ? want : (uint32_t)c->ww_blocks);
-		k_trace_ww<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays,
+		rrg::note_launch(), k_trace_ww<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays,
 		                                                 n, nullptr, nullptr, nullptr, occ, c->d_counter);
 		RRG_CUDA(cudaGetLastError());
 		return RRG_OK;
@@ -499,10 +499,10 @@ int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, c
 		const uint32_t* perm = nullptr;
 		int st = bin_rays(c, rays, n, s, 3, &perm);
 		if (st) return st;
-		k_occluded<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
+		rrg::note_launch(), k_occluded<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
 		                                                occ, c->d_counter, perm);
 	} else {
-		k_occluded<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
+		rrg::note_launch(), k_occluded<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
 		                                                 occ, c->d_counter, nullptr);
 	}
 	RRG_CUDA(cudaGetLastError());
@@ -514,7 +514,7 @@ int launch_rrray(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, cu
 	RRG_CUDA(cudaMemsetAsync(c->d_counter, 0, 4, s));
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
 	int grid = (int)(want < (uint32_t)c->trace_blocks ? want : (uint32_t)c->trace_blocks);
-	k_rrray<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, (uint8_t*)rrrays_dev, n, hit_dev, c->d_counter);
+	rrg::note_launch(), k_rrray<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, (uint8_t*)rrrays_dev, n, hit_dev, c->d_counter);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }
@@ -526,7 +526,7 @@ int launch_rrray_scratch(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit
 	if (!n) return RRG_OK;
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
 	int grid = (int)(want < (uint32_t)c->trace_blocks ? want : (uint32_t)c->trace_blocks);
-	k_rrray<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, (uint8_t*)rrrays_dev, n, hit_dev, words);
+	rrg::note_launch(), k_rrray<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, (uint8_t*)rrrays_dev, n, hit_dev, words);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }
@@ -554,11 +554,11 @@ int launch_batch_closest(Collider* c, const float4* rays, uint32_t n, const uint
 	const int grid = (int)(want < (uint32_t)blocks ? want : (uint32_t)blocks);
 	const size_t smem = sizeof(uint32_t) * (nmesh + 1);
 	if (c->width == 8 && c->d_wnodes)
-		k_batch_closest<true><<<grid, kTraceThreads, smem, s>>>(c->d_nodes, (int)c->nnodes, c->d_wnodes,
+		rrg::note_launch(), k_batch_closest<true><<<grid, kTraceThreads, smem, s>>>(c->d_nodes, (int)c->nnodes, c->d_wnodes,
 		                                                       (int)c->nwnodes, c->d_wtris, (int)c->nvalid, rays, n,
 		                                                       ray_off, c->d_tri_off, nmesh, fetch, hits, c->d_counter);
 	else
-		k_batch_closest<false><<<grid, kTraceThreads, smem, s>>>(c->d_nodes, (int)c->nnodes, c->d_wnodes,
+		rrg::note_launch(), k_batch_closest<false><<<grid, kTraceThreads, smem, s>>>(c->d_nodes, (int)c->nnodes, c->d_wnodes,
 		                                                        (int)c->nwnodes, c->d_tris, (int)c->nvalid, rays, n,
 		                                                        ray_off, c->d_tri_off, nmesh, fetch, hits, c->d_counter);
 	RRG_CUDA(cudaGetLastError());

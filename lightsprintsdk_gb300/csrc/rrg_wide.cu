@@ -217,11 +217,11 @@ int build_wide(Collider* c, const BNode* bnodes, int nnodes, const float* pad, c
 	int ncur = nroots;
 	WideCounters h{};
 	if (!st) {
-		k_wide_roots<<<(nroots + 255) / 256, 256, 0, s>>>(cur, nroots, cnt);
+		rrg::note_launch(), k_wide_roots<<<(nroots + 255) / 256, 256, 0, s>>>(cur, nroots, cnt);
 		for (int level = 0; level < 128 && ncur > 0; level++) {
 			e = cudaMemsetAsync(&cnt->next, 0, sizeof(int), s);
 			if (e != cudaSuccess) { st = cuda_fail(e); break; }
-			k_wide_level<<<(ncur + 127) / 128, 128, 0, s>>>(bnodes, nnodes, cur, ncur, nxt, cnt, pad, c->d_tris,
+			rrg::note_launch(), k_wide_level<<<(ncur + 127) / 128, 128, 0, s>>>(bnodes, nnodes, cur, ncur, nxt, cnt, pad, c->d_tris,
 			                                               (int)c->nvalid, wn, max_wnodes, wt);
 			e = cudaGetLastError();
 			if (e == cudaSuccess) e = cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s);

@@ -126,3 +126,20 @@ def test_index_outside_its_mesh_is_invalid():
     with pytest.raises(col.RRGError) as e:
         rb.RRColliderBatch.create(mb.vertices, bad, mb.vert_off, mb.tri_off)
     assert e.value.status == 1
+
+
+def test_launch_count_counts_graph_replays_not_captures(small_batch):
+    """rrg_launch_count: a replay of the captured batch graph adds its kernel
+    nodes; the capture itself launches nothing."""
+    import torch
+    mb, counts, rays, off, off_d, b = small_batch
+    hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device="cuda")
+    b.set_rays_per_warp(32)
+    deltas = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        n0 = col.launch_count()
+        b.intersect_device(rays.data_ptr(), off_d.data_ptr(), rays.shape[0], hits.data_ptr())
+        deltas.append(col.launch_count() - n0)
+    torch.cuda.synchronize()
+    assert deltas[0] >= 1 and deltas[0] == deltas[1] == deltas[2], deltas

@@ -245,6 +245,22 @@ def test_traversal_variants_agree(c0):
         np.testing.assert_array_equal(a[f], b[f])
 
 
+def test_launch_count_counts_device_calls(c0):
+    """rrg_launch_count grows by the same positive number for each identical
+    device call (the bench reports its growth over the timed region)."""
+    import torch
+    v, t, rays, _, c = c0
+    d_rays = torch.from_numpy(np.ascontiguousarray(rays, dtype=np.float32)).cuda()
+    d_hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device="cuda")
+    deltas = []
+    for _ in range(3):
+        n0 = col.launch_count()
+        c.intersect_device(d_rays.data_ptr(), rays.shape[0], d_hits.data_ptr())
+        deltas.append(col.launch_count() - n0)
+    torch.cuda.synchronize()
+    assert deltas[0] >= 1 and deltas[0] == deltas[1] == deltas[2], deltas
+
+
 def test_ray_orders_agree():
     """Binned and given ray order give bit-identical closest and any hits
     (config-1 sample of camera, surface and shadow rays)."""
