@@ -39,7 +39,7 @@ enum {
 typedef struct rrg_gather_params {
 	uint32_t size;
 	uint32_t quality;          /* hemisphere rays per texel (UpdateParameters::quality), 1..256 */
-	uint32_t max_depth;        /* diffuse bounces (PathTracingParameters::stopAtDepth) */
+	uint32_t max_depth;        /* diffuse bounces (PathTracingParameters::stopAtDepth); above 255 acts as 255 */
 	uint32_t mode;             /* RRG_GATHER_*: how the plain gather is scheduled (results do not depend on it) */
 	uint64_t seed;             /* sample streams */
 	float ray_length_min;      /* 0 = the solver's minimalSafeDistance of the mesh */

@@ -58,6 +58,9 @@ __device__ __forceinline__ float rng01(uint64_t seed, uint64_t stream, uint64_t 
 enum { S_FILLER = 60, S_PU = 61, S_PV = 62, S_ROULETTE = 63, S_DISKX = 64, S_DISKY = 65 };
 constexpr uint32_t kM24 = 16777215u;
 constexpr int kDiskTries = 32;
+// Bounce b of sample sid draws its numbers at counter sid * 256 + b, so a
+// path has 256 bounces of its own; deeper limits act as 255.
+constexpr uint32_t kMaxDepth = 255;
 constexpr float kPreventInf = 0.000000000137289f;   // RRLight.cpp:21
 constexpr float kStopAtVisibility = 0.001f;         // PathTracingParameters default
 
@@ -530,12 +533,12 @@ __device__ V3 trace_path(const GatherScene& g, V3 eye, V3 dir, uint32_t skip, ui
 		if (pdiff < 0.f) pdiff = 0.f;
 		float pstop = __fsub_rn(1.f, pdiff);
 		if (pstop < 0.f) pstop = 0.f;
-		float rr = rng01(g.seed, S_ROULETTE, sid * 16 + depth);
+		float rr = rng01(g.seed, S_ROULETTE, sid * (kMaxDepth + 1) + depth);
 		if (!(rr < pdiff && depth < g.max_depth)) break;
 		float intensity = __fdiv_rn(__fadd_rn(pdiff, pstop), pdiff);
 		float x = 0.f, y = 0.f;
 		for (int j = 0; j < kDiskTries; j++) {
-			uint64_t cc = (sid * 16 + depth) * kDiskTries + j;
+			uint64_t cc = (sid * (kMaxDepth + 1) + depth) * kDiskTries + j;
 			float ax = __fsub_rn(__fmul_rn(rng01(g.seed, S_DISKX, cc), 2.0f), 1.0f);
 			float by = __fsub_rn(__fmul_rn(rng01(g.seed, S_DISKY, cc), 2.0f), 1.0f);
 			if (__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(by, by)) < 1.0f) { x = ax; y = by; break; }
@@ -1012,12 +1015,12 @@ __global__ void __launch_bounds__(128) k_wf_shade(GatherScene g, WfState w, int 
 		if (pdiff < 0.f) pdiff = 0.f;
 		float pstop = __fsub_rn(1.f, pdiff);
 		if (pstop < 0.f) pstop = 0.f;
-		float rr = rng01(g.seed, S_ROULETTE, sid * 16 + depth);
+		float rr = rng01(g.seed, S_ROULETTE, sid * (kMaxDepth + 1) + depth);
 		if (!(rr < pdiff && depth < g.max_depth)) continue;
 		float intensity = __fdiv_rn(__fadd_rn(pdiff, pstop), pdiff);
 		float x = 0.f, y = 0.f;
 		for (int j = 0; j < kDiskTries; j++) {
-			uint64_t cc = (sid * 16 + depth) * kDiskTries + j;
+			uint64_t cc = (sid * (kMaxDepth + 1) + depth) * kDiskTries + j;
 			float ax = __fsub_rn(__fmul_rn(rng01(g.seed, S_DISKX, cc), 2.0f), 1.0f);
 			float by = __fsub_rn(__fmul_rn(rng01(g.seed, S_DISKY, cc), 2.0f), 1.0f);
 			if (__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(by, by)) < 1.0f) { x = ax; y = by; break; }
@@ -1244,7 +1247,7 @@ static int make_scene(Lightmapper* L, const rrg_gather_params* p, GatherScene& g
 	g.tmin = p->ray_length_min > 0.f ? p->ray_length_min : L->tmin_default;
 	g.locality = p->locality > 0.f ? p->locality : 100000.f;
 	g.quality = p->quality;
-	g.max_depth = p->max_depth;
+	g.max_depth = p->max_depth < kMaxDepth ? p->max_depth : kMaxDepth;
 	g.seed = p->seed;
 	const bool has_ao = p->size >= sizeof(rrg_gather_params);
 	g.ao_intensity = has_ao ? p->ao_intensity : 0.f;

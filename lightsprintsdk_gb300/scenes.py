@@ -581,6 +581,16 @@ def gather_c2(sc: Scene | None = None, seed: int = 0xC2, natlas: int = 256, size
     return GatherScene(sc, albedo, tri_atlas, uv, natlas, size, lights)
 
 
+def gather_room(seed: int = 0xC2) -> GatherScene:
+    """A small version of the config-2 scene (9,8xx triangles): the same room
+    of slabs tessellated at 2.0, 10 boxes, 3 displaced icospheres of
+    frequency 4, 16 atlases of 64 x 64 texels, the config-2 lights and
+    albedo generator.  Small enough for the reference's own CPU gather to
+    cover whole atlases at high quality in seconds."""
+    sc = interior_c1(seed=0xC1, cell=2.0, nboxes=10, ninst=3, sphere_freq=4)
+    return gather_c2(sc, seed=seed, natlas=16, size=64)
+
+
 # ------------------------------------------------------- uneven mesh batches
 def geodesic_sphere_grid(freq: int):
     """The class-I geodesic sphere of geodesic_sphere(freq) (same vertex

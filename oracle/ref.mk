@@ -48,7 +48,7 @@ OBJS := $(addprefix $(OUT)/obj/,$(SOURCES:.cpp=.o))
 
 # Drivers (our code) that run the reference collider and gather on the
 # workloads' binary inputs and write binary outputs.
-DRIVERS := $(OUT)/ref_collide $(OUT)/ref_filter $(OUT)/ref_enumerate
+DRIVERS := $(OUT)/ref_collide $(OUT)/ref_filter $(OUT)/ref_enumerate $(OUT)/ref_gather
 
 all: $(OUT)/libLightsprintCore.a $(DRIVERS)
 

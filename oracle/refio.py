@@ -146,3 +146,36 @@ def run_ref_enumerate(v, normals, t, uv, size: int):
     rec = np.dtype([("tri", "<u4"), ("uv", "<f4", (3, 2)), ("area", "<f4")])
     st = np.frombuffer(b, rec, total, 12 + 5 * S).copy()
     return flags, off, st
+
+
+# SCENE  "RGS1": u32 nv, nt, natlas, size, quality, nout, seed; f32 xyz[3nv];
+#                u32 idx[3nt]; f32 uv[6nt]; f32 albedo[3nt]; i32 atlas[nt];
+#                f32 lights[12]; u32 out_atlas[nout]
+# GATHER "RGG1": u32 nout, u32 size, f32 rgba[nout*size*size*4]
+def run_ref_gather(gs, atlases, quality: int, seed: int = 1, threads: int = 0) -> np.ndarray:
+    """The reference's own processTexel over whole atlases of a GatherScene,
+    with no radiosity solver (the plain N-bounce estimator, stopAtDepth 20).
+    Returns (len(atlases), size, size, 4) float32 RGBA, alpha = flags / 255."""
+    exe = os.path.join(REF_DIR, "ref_gather")
+    sc = gs.scene
+    atlases = np.asarray(atlases, np.uint32)
+    L = gs.lights
+    lights = np.concatenate([L["dir_direction"], L["dir_color"], L["point_position"], L["point_color"]]).astype(np.float32)
+    with tempfile.TemporaryDirectory() as d:
+        sp, op = os.path.join(d, "s"), os.path.join(d, "o")
+        with open(sp, "wb") as f:
+            f.write(b"RGS1")
+            f.write(np.array([sc.vertices.shape[0], sc.ntri, gs.natlas, gs.size, quality, atlases.shape[0], seed],
+                             np.uint32).tobytes())
+            f.write(np.ascontiguousarray(sc.vertices, np.float32).tobytes())
+            f.write(np.ascontiguousarray(sc.indices, np.uint32).tobytes())
+            f.write(np.ascontiguousarray(gs.uv, np.float32).tobytes())
+            f.write(np.ascontiguousarray(gs.albedo, np.float32).tobytes())
+            f.write(np.ascontiguousarray(gs.tri_atlas, np.int32).tobytes())
+            f.write(lights.tobytes())
+            f.write(atlases.tobytes())
+        subprocess.run([exe, sp, op, str(threads)], capture_output=True, text=True, check=True)
+        b = open(op, "rb").read()
+    assert b[:4] == b"RGG1"
+    nout, size = (int(x) for x in np.frombuffer(b, np.uint32, 2, 4))
+    return np.frombuffer(b, np.float32, nout * size * size * 4, 12).reshape(nout, size, size, 4).copy()

@@ -33,6 +33,8 @@ static float rng01(uint64_t seed, uint64_t stream, uint64_t index) {
 enum { S_FILLER = 60, S_PU = 61, S_PV = 62, S_ROULETTE = 63, S_DISKX = 64, S_DISKY = 65 };
 #define M24 16777215u
 #define DISK_TRIES 32
+/* bounce b of sample sid draws at counter sid * 256 + b; deeper limits act as 255 */
+#define MAX_DEPTH 255u
 #define PREVENT_INF 0.000000000137289f   /* RRLight.cpp:21 */
 #define STOP_AT_VISIBILITY 0.001f        /* PathTracingParameters default, RRSolver.h:998 */
 
@@ -321,12 +323,12 @@ static void path(const orc_bvh* bvh, const orc_gather_scene* sc, v3 eye, v3 dir,
 		if (pdiff < 0) pdiff = 0;
 		float pstop = 1 - pdiff;
 		if (pstop < 0) pstop = 0;
-		float r = rng01(sc->seed, S_ROULETTE, sid * 16 + depth);
-		if (!(r < pdiff && depth < sc->max_depth)) break;
+		float r = rng01(sc->seed, S_ROULETTE, sid * (MAX_DEPTH + 1) + depth);
+		if (!(r < pdiff && depth < (sc->max_depth < MAX_DEPTH ? sc->max_depth : MAX_DEPTH))) break;
 		float intensity = (pdiff + pstop) / pdiff;
 		float x = 0, y = 0;
 		for (uint32_t j = 0; j < DISK_TRIES; j++) {
-			uint64_t c = (sid * 16 + depth) * DISK_TRIES + j;
+			uint64_t c = (sid * (MAX_DEPTH + 1) + depth) * DISK_TRIES + j;
 			float a = rng01(sc->seed, S_DISKX, c) * 2.0f - 1.0f;
 			float b = rng01(sc->seed, S_DISKY, c) * 2.0f - 1.0f;
 			if (a * a + b * b < 1.0f) { x = a; y = b; break; }

@@ -9,8 +9,9 @@ check that the generators reproduce the same bytes on the machine they run on,
 and the reference outputs of the rays that hit (ray index, hitTriangle,
 hitDistance, hitPoint2d, hitPlane, hitFrontSide).  The lightmap fixture
 holds the reference's texel enumeration (TexelFlags, sub-texel counts and a
-hash of the sub-texels) and hashes of its post-filter outputs.  Test
-infrastructure only.
+hash of the sub-texels) and hashes of its post-filter outputs.  The gather
+fixture holds the reference's own per-texel gather (processTexel, no
+radiosity solver) of four atlases of a small room.  Test infrastructure only.
 """
 from __future__ import annotations
 
@@ -151,6 +152,25 @@ def lightmaps():
     save("lightmap_ref.npz", **kw)
 
 
+# Reference gather: atlases of the small room scene (scenes.gather_room) at a
+# quality high enough that its own noise is small against the tests' runs.
+GATHER_ATLASES = (0, 5, 9, 13)   # floor slab, wall slab, a sphere, boxes
+GATHER_QUALITY = 1024
+GATHER_SEED = 1
+
+
+def gather():
+    """The reference's own processTexel (no radiosity solver: the plain
+    N-bounce estimator, stopAtDepth 20) over whole atlases of the room."""
+    gs = scenes.gather_room()
+    out = refio.run_ref_gather(gs, GATHER_ATLASES, GATHER_QUALITY, GATHER_SEED)
+    flags = np.rint(out[..., 3] * 255).astype(np.uint8)
+    assert np.array_equal(flags.astype(np.float32) / np.float32(255), out[..., 3])
+    save("gather_ref.npz", scene_md5=md5(gs.scene.vertices, gs.scene.indices, gs.albedo, gs.uv, gs.tri_atlas),
+         atlases=np.array(GATHER_ATLASES, np.uint32), quality=np.uint32(GATHER_QUALITY), flags=flags,
+         rgb=np.ascontiguousarray(out[..., :3]))
+
+
 def main():
     assert refio.ref_available(), "build oracle/_ref first: make -f oracle/ref.mk -j8"
     # 1. HelloCollider known answer
@@ -197,9 +217,14 @@ def main():
     # 5. lightmaps: texel enumeration and flags, post-filters
     lightmaps()
 
+    # 6. the reference's plain per-texel gather
+    gather()
+
 
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "lightmaps":
         lightmaps()
+    elif len(sys.argv) > 1 and sys.argv[1] == "gather":
+        gather()
     else:
         main()

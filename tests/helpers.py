@@ -97,3 +97,64 @@ def classify_mismatches(v, t, rays, ref: dict, got: dict, tie_rel: float = 1e-6)
         else:
             res["other"].append(int(i))
     return res
+
+
+# Bounds of the statistical comparison with the reference's own gather
+# (tests/golden/gather_ref.npz).  Under a correct estimator the largest |z|
+# of an atlas-channel mean is about 2, the noise ratio about 1 and the
+# largest 8x8-block |z| about 3.5 (768 blocks); a gather cut at 3 bounces
+# instead of 20 reaches |z| > 11.
+GATHER_Z_MEAN = 4.5
+GATHER_Z_BLOCK = 5.5
+GATHER_NOISE_RATIO = 1.25
+GATHER_REL_MEAN = 0.01
+
+
+def reference_gather_stats(g: dict, o1: np.ndarray, o2: np.ndarray, q_ours: int) -> list[dict]:
+    """Compares two independent runs (o1, o2: (natlas, size, size, 4)) of a
+    gather with the reference's own gather of the same atlases (g: the
+    gather_ref fixture), texel by texel over the covered texels of each atlas:
+      z_mean    largest |mean difference| / its standard error over RGB
+      rel_mean  largest |mean difference| / reference mean over RGB
+      noise     mean squared difference to the reference over what the two
+                runs' own spread predicts for it (reference noise included)
+      z_block   largest |z| of the mean difference over 8x8 texel blocks
+      alpha     the runs' alpha equals the reference's TexelFlags / 255."""
+    ref, flags = g["rgb"].astype(np.float64), g["flags"]
+    q_ref = int(g["quality"])
+    size = flags.shape[1]
+    out = []
+    for k in range(flags.shape[0]):
+        cov = flags[k] > 0
+        r = ref[k][cov]
+        x = o1[k][cov][:, :3].astype(np.float64)
+        y = o2[k][cov][:, :3].astype(np.float64)
+        d = r - x
+        z = d.mean(0) / (d.std(0) / np.sqrt(d.shape[0]))
+        predicted = ((x - y) ** 2).mean() / 2 * (1 + q_ours / q_ref)
+        dd = np.zeros((size, size, 3))
+        dd[cov] = d
+        nb = size // 8
+        cb = cov.reshape(nb, 8, nb, 8).transpose(0, 2, 1, 3).reshape(nb * nb, 64)
+        db = dd.reshape(nb, 8, nb, 8, 3).transpose(0, 2, 1, 3, 4).reshape(nb * nb, 64, 3)
+        zb = 0.0
+        for b in range(nb * nb):
+            m = cb[b]
+            if m.sum() < 16:
+                continue
+            v = db[b][m]
+            sd = v.std(0)
+            for c in range(3):
+                if sd[c] < 1e-6:   # every texel equal (unlit in both): the difference itself must vanish
+                    zb = max(zb, 0.0 if abs(v[:, c].mean()) < 1e-5 else np.inf)
+                else:
+                    zb = max(zb, abs(v[:, c].mean()) / (sd[c] / np.sqrt(m.sum())))
+        alpha = np.array_equal(o1[k][..., 3], flags[k].astype(np.float32) / np.float32(255))
+        out.append({"z_mean": float(np.abs(z).max()), "rel_mean": float(np.abs(d.mean(0) / r.mean(0)).max()),
+                    "noise": float(((r - x) ** 2).mean() / predicted), "z_block": float(zb), "alpha": alpha})
+    return out
+
+
+def reference_gather_ok(s: dict) -> bool:
+    return (s["alpha"] and s["z_mean"] < GATHER_Z_MEAN and s["rel_mean"] < GATHER_REL_MEAN
+            and s["noise"] < GATHER_NOISE_RATIO and s["z_block"] < GATHER_Z_BLOCK)

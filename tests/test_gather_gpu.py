@@ -247,3 +247,36 @@ def test_wavefront_large_call_matches_oracle(setup):
     rel = np.abs(out[sel, :3] - ref[:, :3]) / np.maximum(np.abs(ref[:, :3]), 1e-6)
     assert rel.max() <= 1e-4, rel.max()
     np.testing.assert_array_equal(out[sel, 3], ref[:, 3])
+
+
+@pytest.mark.parametrize("mode", [lm.GATHER_WARP, lm.GATHER_WAVEFRONT])
+def test_gpu_gather_matches_the_reference_gather_statistically(mode):
+    """The GPU gather against the reference's own processTexel (no radiosity
+    solver: the plain N-bounce estimator, stopAtDepth 20; four whole atlases
+    of the small room at quality 1024, tests/golden/gather_ref.npz), by the
+    same statistics as the oracle's test: different random numbers, so per
+    atlas and channel the mean difference within 4.5 standard errors and 1 %,
+    every 8x8 block within 5.5, the spread what the noise predicts, alpha
+    (TexelFlags / 255) bit-exact."""
+    import torch
+    from tests.helpers import load_golden, md5, reference_gather_ok, reference_gather_stats
+    g = load_golden("gather_ref.npz")
+    gs = scenes.gather_room()
+    assert md5(gs.scene.vertices, gs.scene.indices, gs.albedo, gs.uv, gs.tri_atlas) == str(g["scene_md5"])
+    c = col.RRCollider.create(gs.scene.vertices, gs.scene.indices)
+    L = lm.RRLightmapper.from_scene(c, gs)
+    S = gs.size * gs.size
+    q = 1024
+    runs = []
+    for seed in (21, 22):
+        p = lm.make_params(gs.lights, quality=q, max_depth=20, seed=seed, mode=mode)
+        per = []
+        for a in g["atlases"]:
+            out = torch.empty((S, 4), dtype=torch.float32, device="cuda")
+            L.gather_device(p, int(a) * S, S, out.data_ptr())
+            per.append(out)
+        torch.cuda.synchronize()
+        L.check()
+        runs.append(np.stack([o.cpu().numpy().reshape(gs.size, gs.size, 4) for o in per]))
+    for a, s in zip(g["atlases"], reference_gather_stats(g, runs[0], runs[1], q)):
+        assert reference_gather_ok(s), (int(a), s)
