@@ -250,14 +250,14 @@ def test_wavefront_large_call_matches_oracle(setup):
 
 
 @pytest.mark.parametrize("mode", [lm.GATHER_WARP, lm.GATHER_WAVEFRONT])
-def test_gpu_gather_matches_the_reference_gather_statistically(mode):
+def test_gpu_gather_matches_the_reference_gather(mode):
     """The GPU gather against the reference's own processTexel (no radiosity
-    solver: the plain N-bounce estimator, stopAtDepth 20; four whole atlases
-    of the small room at quality 1024, tests/golden/gather_ref.npz), by the
-    same statistics as the oracle's test: different random numbers, so per
-    atlas and channel the mean difference within 4.5 standard errors and 1 %,
-    every 8x8 block within 5.5, the spread what the noise predicts, alpha
-    (TexelFlags / 255) bit-exact."""
+    solver: the plain N-bounce estimator, stopAtDepth 20; two runs over four
+    whole atlases of the small room at quality 256, tests/golden/
+    gather_ref.npz), as the oracle's test does: the texels no random number
+    changes agree with the reference to float rounding (1e-6), the rest
+    statistically (means within 4.5 standard errors and 1 %, 8x8 blocks
+    within 5.5, spread as both sides' noise predicts), alpha bit-exact."""
     import torch
     from tests.helpers import load_golden, md5, reference_gather_ok, reference_gather_stats
     g = load_golden("gather_ref.npz")
@@ -266,17 +266,16 @@ def test_gpu_gather_matches_the_reference_gather_statistically(mode):
     c = col.RRCollider.create(gs.scene.vertices, gs.scene.indices)
     L = lm.RRLightmapper.from_scene(c, gs)
     S = gs.size * gs.size
-    q = 1024
     runs = []
     for seed in (21, 22):
-        p = lm.make_params(gs.lights, quality=q, max_depth=20, seed=seed, mode=mode)
-        per = []
-        for a in g["atlases"]:
-            out = torch.empty((S, 4), dtype=torch.float32, device="cuda")
-            L.gather_device(p, int(a) * S, S, out.data_ptr())
-            per.append(out)
+        p = lm.make_params(gs.lights, quality=int(g["quality"]), max_depth=20, seed=seed, mode=mode)
+        out = torch.empty((len(g["atlases"]), S, 4), dtype=torch.float32, device="cuda")
+        for k, a in enumerate(g["atlases"]):
+            L.gather_device(p, int(a) * S, S, out[k].data_ptr())
         torch.cuda.synchronize()
         L.check()
-        runs.append(np.stack([o.cpu().numpy().reshape(gs.size, gs.size, 4) for o in per]))
-    for a, s in zip(g["atlases"], reference_gather_stats(g, runs[0], runs[1], q)):
-        assert reference_gather_ok(s), (int(a), s)
+        runs.append(out.cpu().numpy().reshape(-1, gs.size, gs.size, 4))
+    stats = reference_gather_stats(g, runs[0], runs[1])
+    for a, s in zip(g["atlases"], stats):
+        assert reference_gather_ok(s, det_rel=1e-6), (int(a), s)
+    assert stats[0]["det_n"] > 1000 and stats[1]["det_n"] > 1000, stats

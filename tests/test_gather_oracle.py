@@ -1,6 +1,8 @@
 """CPU checks of the gather oracle (oracle/rr_gather.c): the sample-stream
-hash matches the Python generators, the enumeration conserves area, and the
-float gather agrees with its FP64-accumulated twin."""
+hash matches the Python generators, the enumeration conserves area, the
+float gather agrees with its FP64-accumulated twin, and the gather matches
+the reference's own per-texel gather (bit-exact where no random number
+matters, statistically elsewhere)."""
 import numpy as np
 
 from lightsprintsdk_gb300 import scenes
@@ -96,29 +98,34 @@ def _room_oracle_runs(g, quality: int, max_depth: int, seeds=(11, 12)):
     return runs
 
 
-def test_oracle_gather_matches_the_reference_gather_statistically():
+def test_oracle_gather_matches_the_reference_gather():
     """The oracle's plain N-bounce gather against the reference's own
     processTexel (gather.cpp:600-836, run with no radiosity solver so that
     its PathtracerWorker shoots shadow rays at every hit and continues by
-    Russian roulette up to stopAtDepth 20; tests/golden/gather_ref.npz, four
-    whole atlases of the small room at quality 1024).  The two use different
-    random numbers, so the comparison is statistical: per atlas and channel
-    the mean difference within 4.5 standard errors and 1 %, every 8x8 block
-    within 5.5, the texel-by-texel spread what the noise predicts, and alpha
+    Russian roulette up to stopAtDepth 20; tests/golden/gather_ref.npz: two
+    runs over four whole atlases of the small room at quality 256, the
+    quality of the runs here, since the sub-texel stepping depends on it).
+    The texels whose value no random number changes (about 2,300 on each
+    slab atlas) are bit-exact; the rest use other random numbers, so they
+    are compared statistically: per atlas and channel the mean difference
+    within 4.5 standard errors and 1 %, every 8x8 block within 5.5, the
+    texel-by-texel spread what both sides' measured noise predicts, alpha
     (TexelFlags / 255) bit-exact."""
     g = load_golden("gather_ref.npz")
     gs = scenes.gather_room()
     assert md5(gs.scene.vertices, gs.scene.indices, gs.albedo, gs.uv, gs.tri_atlas) == str(g["scene_md5"])
-    o1, o2 = _room_oracle_runs(g, 256, 20)
-    for a, s in zip(g["atlases"], reference_gather_stats(g, o1, o2, 256)):
-        assert reference_gather_ok(s), (int(a), s)
+    o1, o2 = _room_oracle_runs(g, int(g["quality"]), 20)
+    stats = reference_gather_stats(g, o1, o2)
+    for a, s in zip(g["atlases"], stats):
+        assert reference_gather_ok(s, det_rel=0.0), (int(a), s)
+    assert stats[0]["det_n"] > 1000 and stats[1]["det_n"] > 1000, stats
 
 
 def test_reference_gather_comparison_detects_missing_bounces():
     """The comparison's power, with a mistake planted in the oracle: paths
     cut at 3 bounces instead of 20 fail it on every atlas."""
     g = load_golden("gather_ref.npz")
-    o1, o2 = _room_oracle_runs(g, 256, 3)
-    for a, s in zip(g["atlases"], reference_gather_stats(g, o1, o2, 256)):
+    o1, o2 = _room_oracle_runs(g, int(g["quality"]), 3)
+    for a, s in zip(g["atlases"], reference_gather_stats(g, o1, o2)):
         assert not reference_gather_ok(s), (int(a), s)
-        assert s["z_mean"] > 2 * GATHER_Z_MEAN, (int(a), s)
+        assert s["z_mean"] > GATHER_Z_MEAN, (int(a), s)
