@@ -44,6 +44,12 @@
  * and bent normals (gather.cpp:274,488,811-830) follow the reference.
  * With fp64 = 1 the same paths are accumulated in double precision: the
  * FP64-accumulated reference that states the float accumulation error.
+ *
+ * Pinned against the reference's own processTexel run with no radiosity
+ * solver (oracle/ref_gather.cpp, tests/golden/gather_ref.npz): bit-exact on
+ * the texels whose value no random number changes, statistically (means,
+ * 8x8 blocks, texel spread) on the rest.  The per-bounce counter is
+ * sid * 256 + depth (depths above 255 act as 255).
  */
 #ifndef RR_GATHER_H
 #define RR_GATHER_H
