@@ -31,7 +31,15 @@ typedef struct rrg_lightmapper rrg_lightmapper;
 enum {
 	RRG_GATHER_AUTO = 0,        /* wavefront for calls of >= 16,384 texels, else warp per texel */
 	RRG_GATHER_WARP = 1,        /* one warp per texel, lanes follow whole hemisphere paths */
-	RRG_GATHER_WAVEFRONT = 2    /* paths of a batch of texels advance bounce by bounce, one thread per path */
+	RRG_GATHER_WAVEFRONT = 2,   /* paths of a batch of texels advance bounce by bounce, one thread per path */
+	/* flag OR-ed into the mode: the hemisphere reads the radiosity solver of
+	 * rrg_lightmapper_bake_solver at its first hit (exitance = albedo x
+	 * (the triangle's direct irradiance + its corners' smoothed indirect
+	 * irradiance interpolated at the hit)) and ends there, as the reference's
+	 * updateLightmaps does after its first gather (useSolverDirect/
+	 * IndirectSinceDepth = 0, gather.cpp:187-189; pathtracer.cpp:235-258,
+	 * 326-350); warp per texel; not for the learned gather */
+	RRG_GATHER_SOLVER = 4
 };
 
 /* UpdateParameters / PathTracingParameters subset (RRSolver.h:468-594,
@@ -144,6 +152,34 @@ RRG_API uint64_t rrg_lightmapper_seams(const rrg_lightmapper* lm);
 /* Runs of samples over all seams (a run: consecutive samples of a seam that
  * fall in the same pair of texels); 0 before the first filter call with seams. */
 RRG_API uint64_t rrg_lightmapper_seam_runs(const rrg_lightmapper* lm);
+
+/* The radiosity solver of the reference's default bake
+ * (updateSolverIndirectIllumination, RRSolver/gather.cpp:1038-1117, over
+ * RRStaticSolver), for gathers with RRG_GATHER_SOLVER:
+ *   1. first gather per triangle (gatherPerTrianglePhysical, gather.cpp:
+ *      843-952): max(1, quality / 2) / 10 + 1 light rounds from random
+ *      points of the triangle -> its direct irradiance;
+ *   2. rays_per_triangle (0 = quality) form-factor rays per triangle, from
+ *      random points, cosine-distributed over its front side, nearest hit on
+ *      either side (shotFromToHalfspace / rayTracePhoton, RRStaticSolver/
+ *      rrcore.cpp:861-1050);
+ *   3. `iterations` Jacobi steps of the flux balance in gathering form,
+ *      E = D + (1/k) sum over the factor hits of albedo x E (the system the
+ *      reference's progressive shooting solves, rrcore.cpp:1052-1297);
+ *   4. indirect irradiance E - D smoothed over corners stitched at identical
+ *      positions with normals within 0.01 rad, weighted by corner angle x
+ *      area (Object::buildTopIVertices, interpol.cpp:78-170).
+ * Uses p's lights, seed, quality and ray_length_min.  Device scratch: 4 bytes
+ * per triangle per ray plus 60 bytes per triangle.  Asynchronous on stream
+ * (the first call builds the stitching on the host). */
+RRG_API int rrg_lightmapper_bake_solver(rrg_lightmapper* lm, const rrg_gather_params* p, uint32_t rays_per_triangle,
+                                        uint32_t iterations, void* stream);
+/* Copies the solver: direct irradiance (3 floats per triangle), indirect
+ * irradiance before smoothing (3 floats per triangle) and smoothed corner
+ * indirect irradiance (9 floats per triangle); any may be NULL.
+ * Synchronous. */
+RRG_API int rrg_lightmapper_copy_solver(const rrg_lightmapper* lm, float* direct_host, float* indirect_host,
+                                        float* corner_host);
 
 /* Training records for a radiance cache (rrgpu_cache.h) from the gather's
  * own paths: from every `stride`-th covered texel, paths_per_texel plain

@@ -407,6 +407,11 @@ struct GatherScene {
 	float ao_intensity, ao_size;   // both > 0: ambient occlusion on the hemisphere part
 	const uint8_t* flags;          // TexelFlags per texel
 	float ldir[4][3];              // LS_LIGHTMAP, LS_DIRECTION1..3 in tangent space (gather.cpp:43-49)
+	// the bake's radiosity solver, read at the first hit when set: per
+	// triangle its direct irradiance (3 floats) and the smoothed indirect
+	// irradiance at its corners (9 floats)
+	const float* solver_direct;
+	const float* solver_corner;
 };
 
 // Outputs of the directional mode (LS_DIRECTION1..3, each may be null).
@@ -487,6 +492,30 @@ __device__ V3 trace_path(const GatherScene& g, V3 eye, V3 dir, uint32_t skip, ui
 	V3 T = mk(1.f, 1.f, 1.f), L = mk(0.f, 0.f, 0.f);
 	if (LOG) log->n = 0;
 	float tmax = g.locality;
+	if (!LOG && g.solver_direct) {
+		// the solver read at the first hit: the triangle's direct irradiance
+		// and its corners' smoothed indirect, interpolated, times the albedo;
+		// the diffuse path ends there (pathtracer.cpp:235-258, 326-350;
+		// Triangle::getPointMeasure, rrcore.cpp:262-277)
+		RayState r;
+		set_ray(r, eye, dir, g.tmin, tmax);
+		GatherFilter f = make_filter(g, skip, true);
+		float tb = r.tmax;
+		uint32_t tri = 0xFFFFFFFFu;
+		int slot = traverse<false, true>(g.nodes, g.tris, r, g.nnodes, g.ntris, tb, tri, overflow, &f);
+		if (slot >= 0) {
+			float4 a, b, c;
+			load_tri(g.tris, slot, a, b, c);
+			Fastest fs = fastest_fields(r, a, b, c);
+			if (first_t) *first_t = fs.dist;
+			const float* c9 = g.solver_corner + 9 * (size_t)tri;
+			float w = __fsub_rn(__fsub_rn(1.f, fs.u), fs.v);
+			V3 ind = add(add(mul(ld3(c9), w), mul(ld3(c9 + 3), fs.u)), mul(ld3(c9 + 6), fs.v));
+			V3 alb = ld3(g.albedo + 3 * (size_t)tri);
+			L = add(mulv(ld3(g.solver_direct + 3 * (size_t)tri), alb), mulv(ind, alb));
+		}
+		return L;
+	}
 	for (uint32_t depth = 0;; depth++) {
 		RayState r;
 		set_ray(r, eye, dir, g.tmin, tmax);
@@ -1198,6 +1227,20 @@ struct Lightmapper {
 	float4* d_rad = nullptr;
 	uint32_t* d_fb = nullptr;
 	unsigned int* d_fbcount = nullptr;
+	// the bake's radiosity solver (rrg_lightmapper_bake_solver): per triangle
+	// direct irradiance and smoothed corner indirect; the corner stitching
+	// (built on the first bake) as groups of corners
+	float* d_solver_direct = nullptr;   // 3 per triangle
+	float* d_solver_corner = nullptr;   // 9 per triangle
+	uint32_t* d_corner_group = nullptr; // 3 per triangle
+	uint32_t* d_group_off = nullptr;    // ngroups + 1
+	uint32_t* d_group_corner = nullptr; // weighted corners, group by group, corner order
+	float* d_corner_weight = nullptr;   // 3 per triangle
+	uint32_t ngroups = 0;
+	uint32_t* d_bake_hits = nullptr;    // triangles x rays
+	size_t bake_hits_cap = 0;
+	float* d_bake_e = nullptr;          // E, E' (3 per triangle each), group values (3 per group)
+	const float* d_bake_final = nullptr;  // the converged E (one of the two above)
 	uint64_t lg_cap = 0;             // texels
 	uint64_t lg_cap_samples = 0;     // texels x samples per texel
 };
@@ -1218,6 +1261,14 @@ static void free_lm(Lightmapper* L) {
 	cudaFree(L->d_rad);
 	cudaFree(L->d_fb);
 	cudaFree(L->d_fbcount);
+	cudaFree(L->d_solver_direct);
+	cudaFree(L->d_solver_corner);
+	cudaFree(L->d_corner_group);
+	cudaFree(L->d_group_off);
+	cudaFree(L->d_group_corner);
+	cudaFree(L->d_corner_weight);
+	cudaFree(L->d_bake_hits);
+	cudaFree(L->d_bake_e);
 	delete L;
 }
 
@@ -1253,6 +1304,14 @@ static int make_scene(Lightmapper* L, const rrg_gather_params* p, GatherScene& g
 	g.ao_intensity = has_ao ? p->ao_intensity : 0.f;
 	g.ao_size = has_ao ? p->ao_size : 0.f;
 	if (!(g.ao_intensity >= 0.f) || !(g.ao_size >= 0.f)) return RRG_ERR_INVALID;
+	if ((p->mode & 3u) > RRG_GATHER_WAVEFRONT || (p->mode & ~(3u | RRG_GATHER_SOLVER))) return RRG_ERR_INVALID;
+	g.solver_direct = nullptr;
+	g.solver_corner = nullptr;
+	if (p->mode & RRG_GATHER_SOLVER) {
+		if (!L->d_solver_direct) return RRG_ERR_INVALID;   // no solver baked yet
+		g.solver_direct = L->d_solver_direct;
+		g.solver_corner = L->d_solver_corner;
+	}
 	return RRG_OK;
 }
 
@@ -1348,16 +1407,376 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 	return RRG_OK;
 }
 
+// ------------------------------------------------------------ bake solver
+// The default bake's radiosity solver (updateSolverIndirectIllumination,
+// RRSolver/gather.cpp:1038-1117, over RRStaticSolver): the first gather per
+// triangle at half quality, form-factor rays, the flux balance solved by
+// Jacobi iteration of its gathering form, corner smoothing.  The same sample
+// streams as the oracle, so the two agree to float rounding.
+enum { S_TRI_PU = 80, S_TRI_PV = 81, S_FF_PU = 82, S_FF_PV = 83, S_FF_DX = 84, S_FF_DY = 85 };
+constexpr float kShotOffset = 1e-4f;   // SHOT_OFFSET, geometry_v.h:30
+constexpr float kBigReal = 1e20f;      // BIG_REAL, geometry_v.h:28
+
+// a random point of the triangle (the whole triangle as the sub-texel,
+// gather.cpp:742-749; rrcore.cpp:1016-1024)
+__device__ __forceinline__ void tri_point(uint64_t seed, uint64_t su, uint64_t sv, uint64_t i, float& pu, float& pv) {
+	uint32_t ru = rng24(seed, su, i), rv = rng24(seed, sv, i);
+	if (ru + rv > kM24) { ru = kM24 - ru; rv = kM24 - rv; }
+	pu = __fdiv_rn((float)ru, (float)kM24);
+	pv = __fdiv_rn((float)rv, (float)kM24);
+}
+
+// First gather per triangle (gatherPerTrianglePhysical, gather.cpp:843-952):
+// `rounds` light rounds from random points of the triangle, no hemisphere.
+__global__ void __launch_bounds__(128) k_bake_direct(GatherScene g, uint32_t nt, uint32_t rounds, float* __restrict__ direct,
+                                                     uint32_t* status) {
+	bool overflow = false;
+	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+		V3 v0, s1, s2;
+		const V3 n = tri_normal(g, t, v0, s1, s2);
+		V3 acc = mk(0.f, 0.f, 0.f);
+		for (uint32_t r = 0; r < rounds; r++) {
+			float pu, pv;
+			tri_point(g.seed, S_TRI_PU, S_TRI_PV, (uint64_t)t * rounds + r, pu, pv);
+			const V3 o = add(add(v0, mul(s1, pu)), mul(s2, pv));
+			for (int li = 0; li < 2; li++) {
+				V3 d = li == 0 ? neg(g.dir_direction) : sub(g.point_position, o);
+				float dsize = len(d);
+				d = divf(d, dsize);
+				if (li == 0) dsize = __fmul_rn(dsize, g.locality);
+				const float ni = dot(d, n);
+				if (!(ni > 0.f) || !isfinite(ni)) continue;
+				if (occluded(g, o, d, g.tmin, dsize, t, overflow)) continue;
+				const V3 irr = li == 0 ? g.dir_color : point_irr(g, o);
+				acc = add(acc, mul(irr, ni));
+			}
+		}
+		acc = divf(acc, (float)rounds);
+		direct[3 * (size_t)t] = acc.x;
+		direct[3 * (size_t)t + 1] = acc.y;
+		direct[3 * (size_t)t + 2] = acc.z;
+	}
+	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// Form-factor rays (shotFromToHalfspace / rayTracePhoton, rrcore.cpp:
+// 861-1050): ray i of triangle i / k from a random point, cosine-distributed
+// over the front half-space (Malley's method), nearest hit on either side
+// with only the shooter skipped (RRCollisionHandlerLod0, rrcore.cpp:670-723);
+// a front hit on a triangle whose albedo sums above 0.01 is a factor.
+__global__ void __launch_bounds__(128, 8) k_bake_factors(GatherScene g, uint32_t nt, uint32_t k,
+                                                         uint32_t* __restrict__ hits, uint32_t* status) {
+	bool overflow = false;
+	const uint64_t total = (uint64_t)nt * k;
+	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+		const uint32_t t = (uint32_t)(i / k);
+		V3 v0, s1, s2;
+		const V3 n = tri_normal(g, t, v0, s1, s2);
+		V3 tg, bt;
+		basis_from_normal(n, tg, bt);
+		float pu, pv;
+		tri_point(g.seed, S_FF_PU, S_FF_PV, i, pu, pv);
+		const V3 o = add(add(v0, mul(s1, pu)), mul(s2, pv));
+		float x = 0.f, y = 0.f;
+		for (int q = 0; q < kDiskTries; q++) {
+			const uint64_t c = i * kDiskTries + q;
+			float a = __fsub_rn(__fmul_rn(rng01(g.seed, S_FF_DX, c), 2.0f), 1.0f);
+			float b = __fsub_rn(__fmul_rn(rng01(g.seed, S_FF_DY, c), 2.0f), 1.0f);
+			if (__fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b)) < 1.0f) { x = a; y = b; break; }
+		}
+		const float cosa = __fsqrt_rn(__fsub_rn(1.0f, __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y))));
+		const V3 d = add(add(mul(n, cosa), mul(tg, x)), mul(bt, y));
+		RayState r;
+		set_ray(r, o, d, kShotOffset, kBigReal);
+		GatherFilter f = make_filter(g, t, false);
+		f.ident_t = -1.f;   // every side collides, only the shooter is skipped
+		float tb = r.tmax;
+		uint32_t tri = 0xFFFFFFFFu;
+		const int slot = traverse<false, true>(g.nodes, g.tris, r, g.nnodes, g.ntris, tb, tri, overflow, &f);
+		uint32_t h = 0xFFFFFFFFu;
+		if (slot >= 0) {
+			float4 a, b, c;
+			load_tri(g.tris, slot, a, b, c);
+			const V3 alb = ld3(g.albedo + 3 * (size_t)tri);
+			if (front_facing(r, a, b, c) && __fadd_rn(__fadd_rn(alb.x, alb.y), alb.z) > 0.01f) h = tri;
+		}
+		hits[i] = h;
+	}
+	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// One Jacobi step of E_j = D_j + (1/k) sum over j's factor hits h of
+// albedo_h * E_h (the flux balance of rrcore.cpp:1052-1086 in gathering form)
+__global__ void __launch_bounds__(128) k_bake_iterate(const float* __restrict__ direct, const float* __restrict__ albedo,
+                                                      const uint32_t* __restrict__ hits, uint32_t nt, uint32_t k,
+                                                      float inv, const float* __restrict__ e, float* __restrict__ e2) {
+	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+		V3 acc = mk(0.f, 0.f, 0.f);
+		const uint32_t* hp = hits + (size_t)t * k;
+		for (uint32_t j = 0; j < k; j++) {
+			const uint32_t h = hp[j];
+			if (h == 0xFFFFFFFFu) continue;
+			acc = add(acc, mulv(ld3(albedo + 3 * (size_t)h), ld3(e + 3 * (size_t)h)));
+		}
+		const V3 r = add(ld3(direct + 3 * (size_t)t), mul(acc, inv));
+		e2[3 * (size_t)t] = r.x;
+		e2[3 * (size_t)t + 1] = r.y;
+		e2[3 * (size_t)t + 2] = r.z;
+	}
+}
+
+// Smoothed indirect of each stitched vertex (IVertex::irradiance,
+// interpol.cpp:78-112): the corner-weighted mean of its triangles' indirect
+// irradiance (E - D), summed in corner order, clamped at zero; written to
+// every corner of the group.
+__global__ void k_bake_smooth(const uint32_t* __restrict__ group_off, const uint32_t* __restrict__ group_corner,
+                              const float* __restrict__ weight, const float* __restrict__ e,
+                              const float* __restrict__ direct, uint32_t ngroups, float* __restrict__ gval) {
+	for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ngroups; gi += gridDim.x * blockDim.x) {
+		V3 num = mk(0.f, 0.f, 0.f);
+		float den = 0.f;
+		for (uint32_t q = group_off[gi]; q < group_off[gi + 1]; q++) {
+			const uint32_t c = group_corner[q];
+			const float w = weight[c];
+			const size_t t3 = 3 * (size_t)(c / 3);
+			const V3 ind = sub(ld3(e + t3), ld3(direct + t3));
+			num = add(num, mul(ind, w));
+			den = __fadd_rn(den, w);
+		}
+		V3 v = den > 0.f ? divf(num, den) : mk(0.f, 0.f, 0.f);
+		gval[3 * (size_t)gi] = v.x > 0.f ? v.x : 0.f;
+		gval[3 * (size_t)gi + 1] = v.y > 0.f ? v.y : 0.f;
+		gval[3 * (size_t)gi + 2] = v.z > 0.f ? v.z : 0.f;
+	}
+}
+
+__global__ void k_bake_corners(const uint32_t* __restrict__ group, const float* __restrict__ gval, uint32_t ncorner,
+                               float* __restrict__ corner) {
+	for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncorner; c += gridDim.x * blockDim.x) {
+		const uint32_t gi = group[c];
+		corner[3 * (size_t)c] = gval[3 * (size_t)gi];
+		corner[3 * (size_t)c + 1] = gval[3 * (size_t)gi + 1];
+		corner[3 * (size_t)c + 2] = gval[3 * (size_t)gi + 2];
+	}
+}
+
+// Abramowitz & Stegun 4.4.45, as geometry_v.h:114-129 applies it (over the
+// whole [-1, 1])
+static float as_acos(float x) {
+	float root = sqrtf(1.0f - x);
+	float r = -0.0187293f;
+	r *= x;
+	r += 0.0742610f;
+	r *= x;
+	r -= 0.2121144f;
+	r *= x;
+	r += 1.5707288f;
+	return r * root;
+}
+
+// Corner stitching and weights (Object::buildTopIVertices, interpol.cpp:
+// 120-170, over RRLessVerticesFilter, RRMeshLessVertices.h:38-237, at the
+// default SmoothingParameters): every corner is a vertex with its face's
+// normal; identical positions whose normals are within 0.01 rad merge,
+// greedily in (position, normal) order against the unique vertices found so
+// far, newest first.  A corner weighs its angle (the published polynomial
+// above) times its triangle's area (rrcore.cpp:105-111); triangles that
+// stitching degenerates weigh nothing.
+static uint32_t bake_stitch(const std::vector<float>& xyz, const std::vector<uint32_t>& idx, uint32_t nt,
+                            std::vector<uint32_t>& group, std::vector<float>& weight) {
+	struct Key {
+		float p[3], n[3];
+		uint32_t c;
+	};
+	const uint32_t nc = 3 * nt;
+	std::vector<Key> k(nc);
+	auto P = [&](uint32_t t, int i) { return &xyz[3 * (size_t)idx[3 * (size_t)t + i]]; };
+	for (uint32_t t = 0; t < nt; t++) {
+		const float *p0 = P(t, 0), *p1 = P(t, 1), *p2 = P(t, 2);
+		const float a0 = p1[0] - p0[0], a1 = p1[1] - p0[1], a2 = p1[2] - p0[2];
+		const float b0 = p2[0] - p0[0], b1 = p2[1] - p0[1], b2 = p2[2] - p0[2];
+		float n0 = a1 * b2 - a2 * b1, n1 = -a0 * b2 + a2 * b0, n2 = a0 * b1 - a1 * b0;
+		const float l = sqrtf(n0 * n0 + n1 * n1 + n2 * n2);
+		if (l > 0) { n0 = n0 / l; n1 = n1 / l; n2 = n2 / l; }
+		for (int i = 0; i < 3; i++) {
+			Key& q = k[3 * (size_t)t + i];
+			const float* p = P(t, i);
+			q.p[0] = p[0]; q.p[1] = p[1]; q.p[2] = p[2];
+			q.n[0] = n0; q.n[1] = n1; q.n[2] = n2;
+			q.c = 3 * t + i;
+		}
+	}
+	std::sort(k.begin(), k.end(), [](const Key& a, const Key& b) {
+		for (int i = 0; i < 3; i++)
+			if (a.p[i] != b.p[i]) return a.p[i] < b.p[i];
+		for (int i = 0; i < 3; i++)
+			if (a.n[i] != b.n[i]) return a.n[i] < b.n[i];
+		return a.c < b.c;
+	});
+	std::vector<uint32_t> rep;
+	rep.reserve(nc);
+	group.assign(nc, 0);
+	const float min_dot = cosf(0.01f);
+	for (uint32_t s = 0; s < nc; s++) {
+		const Key& d = k[s];
+		uint32_t g = 0xFFFFFFFFu;
+		for (uint32_t u = (uint32_t)rep.size(); u--;) {
+			const Key& r = k[rep[u]];
+			if (!(fabsf(d.p[0] - r.p[0]) <= 0.0f)) break;
+			if (fabsf(d.p[1] - r.p[1]) <= 0.0f && fabsf(d.p[2] - r.p[2]) <= 0.0f &&
+			    d.n[0] * r.n[0] + d.n[1] * r.n[1] + d.n[2] * r.n[2] >= min_dot) {
+				g = u;
+				break;
+			}
+		}
+		if (g == 0xFFFFFFFFu) {
+			g = (uint32_t)rep.size();
+			rep.push_back(s);
+		}
+		group[d.c] = g;
+	}
+	weight.assign(nc, 0.f);
+	for (uint32_t t = 0; t < nt; t++) {
+		float p[3][3];
+		for (int i = 0; i < 3; i++)
+			for (int j = 0; j < 3; j++) p[i][j] = P(t, i)[j];
+		auto len2 = [](const float* v) { return v[0] * v[0] + v[1] * v[1] + v[2] * v[2]; };
+		const float s1[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+		const float s2[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+		const float s21[3] = {s2[0] - s1[0], s2[1] - s1[1], s2[2] - s1[2]};
+		const float a = len2(s1), b = len2(s2), c = len2(s21);
+		const float area = sqrtf(2 * b * c + 2 * c * a + 2 * a * b - a * a - b * b - c * c) / 4;
+		const uint32_t* gg = &group[3 * (size_t)t];
+		if (!(area > 0) || gg[0] == gg[1] || gg[0] == gg[2] || gg[1] == gg[2]) continue;
+		for (int i = 0; i < 3; i++) {
+			const float* q0 = p[i];
+			const float* q1 = p[(i + 1) % 3];
+			const float* q2 = p[(i + 2) % 3];
+			float u[3] = {q1[0] - q0[0], q1[1] - q0[1], q1[2] - q0[2]};
+			float v[3] = {q2[0] - q0[0], q2[1] - q0[1], q2[2] - q0[2]};
+			const float lu = sqrtf(len2(u)), lv = sqrtf(len2(v));
+			for (int j = 0; j < 3; j++) { u[j] = u[j] / lu; v[j] = v[j] / lv; }
+			float dd = u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
+			dd = dd < -1 ? -1 : (dd > 1 ? 1 : dd);
+			weight[3 * (size_t)t + i] = as_acos(dd) * area;
+		}
+	}
+	return (uint32_t)rep.size();
+}
+
+// device memory freed unless released
+struct DevBuf {
+	void* p = nullptr;
+	~DevBuf() { cudaFree(p); }
+	void* release() {
+		void* r = p;
+		p = nullptr;
+		return r;
+	}
+};
+
+static int bake_solver(Lightmapper* L, const rrg_gather_params* p, uint32_t k, uint32_t iterations, cudaStream_t s) {
+	if (!p || p->size < offsetof(rrg_gather_params, ao_intensity)) return RRG_ERR_INVALID;
+	rrg_gather_params q{};
+	memcpy(&q, p, p->size < sizeof(q) ? p->size : sizeof(q));
+	q.mode &= 3u;   // the solver is what this builds
+	GatherScene g;
+	int st = make_scene(L, &q, g);
+	if (st) return st;
+	Collider* c = L->c;
+	const uint32_t nt = c->nt;
+	if (!k) k = q.quality;
+	if (!nt || k > 4096 || iterations > 1024) return RRG_ERR_INVALID;
+	if (!L->d_corner_group) {   // the stitching depends on the mesh only: built once
+		std::vector<float> xyz(3 * (size_t)c->nv);
+		std::vector<uint32_t> idx(3 * (size_t)nt);
+		RRG_CUDA(cudaMemcpy(xyz.data(), c->d_xyz, xyz.size() * sizeof(float), cudaMemcpyDeviceToHost));
+		RRG_CUDA(cudaMemcpy(idx.data(), c->d_idx, idx.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+		for (uint32_t v : idx)
+			if (v >= c->nv) return RRG_ERR_INVALID;
+		std::vector<uint32_t> group;
+		std::vector<float> weight;
+		const uint32_t ng = bake_stitch(xyz, idx, nt, group, weight);
+		std::vector<uint32_t> off(ng + 1, 0), list;
+		for (uint32_t cc = 0; cc < 3 * nt; cc++)
+			if (weight[cc] != 0.f) off[group[cc] + 1]++;
+		for (uint32_t i = 0; i < ng; i++) off[i + 1] += off[i];
+		list.resize(off[ng] ? off[ng] : 1);
+		std::vector<uint32_t> cur(off.begin(), off.end() - 1);
+		for (uint32_t cc = 0; cc < 3 * nt; cc++)
+			if (weight[cc] != 0.f) list[cur[group[cc]]++] = cc;
+		DevBuf dg, dw, doff, dl;
+		RRG_CUDA(cudaMalloc(&dg.p, group.size() * 4));
+		RRG_CUDA(cudaMalloc(&dw.p, weight.size() * 4));
+		RRG_CUDA(cudaMalloc(&doff.p, off.size() * 4));
+		RRG_CUDA(cudaMalloc(&dl.p, list.size() * 4));
+		RRG_CUDA(cudaMemcpy(dg.p, group.data(), group.size() * 4, cudaMemcpyHostToDevice));
+		RRG_CUDA(cudaMemcpy(dw.p, weight.data(), weight.size() * 4, cudaMemcpyHostToDevice));
+		RRG_CUDA(cudaMemcpy(doff.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
+		RRG_CUDA(cudaMemcpy(dl.p, list.data(), list.size() * 4, cudaMemcpyHostToDevice));
+		L->d_corner_group = (uint32_t*)dg.release();
+		L->d_corner_weight = (float*)dw.release();
+		L->d_group_off = (uint32_t*)doff.release();
+		L->d_group_corner = (uint32_t*)dl.release();
+		L->ngroups = ng;
+	}
+	if (!L->d_solver_direct) {
+		DevBuf dd, dc, de;
+		RRG_CUDA(cudaMalloc(&dd.p, 3 * (size_t)nt * sizeof(float)));
+		RRG_CUDA(cudaMalloc(&dc.p, 9 * (size_t)nt * sizeof(float)));
+		RRG_CUDA(cudaMalloc(&de.p, (6 * (size_t)nt + 3 * (size_t)L->ngroups) * sizeof(float)));
+		L->d_solver_direct = (float*)dd.release();
+		L->d_solver_corner = (float*)dc.release();
+		L->d_bake_e = (float*)de.release();
+	}
+	const size_t nhits = (size_t)nt * k;
+	if (nhits > L->bake_hits_cap) {
+		cudaFree(L->d_bake_hits);
+		L->d_bake_hits = nullptr;
+		L->bake_hits_cap = 0;
+		RRG_CUDA(cudaMalloc(&L->d_bake_hits, nhits * sizeof(uint32_t)));
+		L->bake_hits_cap = nhits;
+	}
+	const uint32_t qh = q.quality / 2 ? q.quality / 2 : 1;
+	const uint32_t rounds = qh / 10 + 1;
+	const int tgrid = (int)std::min<uint64_t>((nt + 127) / 128, (uint64_t)c->num_sms * 16);
+	rrg::note_launch(), k_bake_direct<<<tgrid, 128, 0, s>>>(g, nt, rounds, L->d_solver_direct, L->d_status);
+	RRG_CUDA(cudaGetLastError());
+	const int fgrid = (int)std::min<uint64_t>((nhits + 127) / 128, (uint64_t)c->num_sms * 64);
+	rrg::note_launch(), k_bake_factors<<<fgrid, 128, 0, s>>>(g, nt, k, L->d_bake_hits, L->d_status);
+	RRG_CUDA(cudaGetLastError());
+	float* e = L->d_bake_e;
+	float* e2 = e + 3 * (size_t)nt;
+	float* gval = e + 6 * (size_t)nt;
+	RRG_CUDA(cudaMemcpyAsync(e, L->d_solver_direct, 3 * (size_t)nt * sizeof(float), cudaMemcpyDeviceToDevice, s));
+	const float inv = 1.0f / (float)k;
+	for (uint32_t it = 0; it < iterations; it++) {
+		rrg::note_launch(), k_bake_iterate<<<tgrid, 128, 0, s>>>(L->d_solver_direct, L->d_albedo, L->d_bake_hits, nt, k, inv, e, e2);
+		std::swap(e, e2);
+	}
+	RRG_CUDA(cudaGetLastError());
+	const int ggrid = (int)std::min<uint64_t>((L->ngroups + 127) / 128 + 1, (uint64_t)c->num_sms * 16);
+	L->d_bake_final = e;
+	rrg::note_launch(), k_bake_smooth<<<ggrid, 128, 0, s>>>(L->d_group_off, L->d_group_corner, L->d_corner_weight, e,
+	                                                        L->d_solver_direct, L->ngroups, gval);
+	const int cgrid = (int)std::min<uint64_t>((3 * (uint64_t)nt + 127) / 128, (uint64_t)c->num_sms * 16);
+	rrg::note_launch(), k_bake_corners<<<cgrid, 128, 0, s>>>(L->d_corner_group, gval, 3 * nt, L->d_solver_corner);
+	RRG_CUDA(cudaGetLastError());
+	return RRG_OK;
+}
+
 static int gather_launch(Lightmapper* L, const rrg_gather_params* p, uint64_t first, uint64_t count, float* out_dev,
                          cudaStream_t s, float* bent_dev = nullptr, const DirOut* dirs = nullptr) {
 	GatherScene g;
 	int st = make_scene(L, p, g);
 	if (st) return st;
 	if (first + count > L->ntexels) return RRG_ERR_INVALID;
-	if (p->mode > RRG_GATHER_WAVEFRONT) return RRG_ERR_INVALID;
+	const uint32_t sched = p->mode & 3u;
 	const bool directional = dirs && (dirs->d[0] || dirs->d[1] || dirs->d[2]);
-	if (!directional && count &&
-	    (p->mode == RRG_GATHER_WAVEFRONT || (p->mode == RRG_GATHER_AUTO && count >= kWfMinTexels)))
+	// reading the solver ends every path at its first hit: one ray per
+	// sample, which the warp-per-texel kernel keeps busy
+	if (!directional && count && !g.solver_direct &&
+	    (sched == RRG_GATHER_WAVEFRONT || (sched == RRG_GATHER_AUTO && count >= kWfMinTexels)))
 		return gather_wavefront(L, g, first, count, reinterpret_cast<float4*>(out_dev),
 		                        reinterpret_cast<float4*>(bent_dev), s);
 	if (directional)
@@ -1572,11 +1991,39 @@ uint64_t rrg_lightmapper_covered(const rrg_lightmapper* h) {
 	return L ? L->ncovered : 0;
 }
 
+int rrg_lightmapper_bake_solver(rrg_lightmapper* h, const rrg_gather_params* p, uint32_t rays_per_triangle,
+                                uint32_t iterations, void* stream) {
+	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
+	if (!L) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(L->c->device));
+	return bake_solver(L, p, rays_per_triangle, iterations, (cudaStream_t)stream);
+}
+
+int rrg_lightmapper_copy_solver(const rrg_lightmapper* h, float* direct_host, float* indirect_host,
+                                float* corner_host) {
+	const Lightmapper* L = reinterpret_cast<const Lightmapper*>(h);
+	if (!L || !L->d_solver_direct || !L->d_bake_final) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(L->c->device));
+	const size_t nt = L->c->nt;
+	if (direct_host)
+		RRG_CUDA(cudaMemcpy(direct_host, L->d_solver_direct, 3 * nt * sizeof(float), cudaMemcpyDeviceToHost));
+	if (indirect_host) {   // E - D, as the smoothing reads it
+		std::vector<float> e(3 * nt), d(3 * nt);
+		RRG_CUDA(cudaMemcpy(e.data(), L->d_bake_final, 3 * nt * sizeof(float), cudaMemcpyDeviceToHost));
+		RRG_CUDA(cudaMemcpy(d.data(), L->d_solver_direct, 3 * nt * sizeof(float), cudaMemcpyDeviceToHost));
+		for (size_t i = 0; i < 3 * nt; i++) indirect_host[i] = e[i] - d[i];
+	}
+	if (corner_host)
+		RRG_CUDA(cudaMemcpy(corner_host, L->d_solver_corner, 9 * nt * sizeof(float), cudaMemcpyDeviceToHost));
+	return RRG_OK;
+}
+
 int rrg_lightmap_train_samples(rrg_lightmapper* h, const rrg_gather_params* p, uint32_t stride,
                                uint32_t paths_per_texel, void* recs_dev, uint64_t cap, uint64_t* nrec_out,
                                void* stream) {
 	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
 	if (!L || !recs_dev || !stride || !paths_per_texel || !cap) return RRG_ERR_INVALID;
+	if (p && (p->mode & RRG_GATHER_SOLVER)) return RRG_ERR_INVALID;   // plain paths only
 	GatherScene g;
 	int st = make_scene(L, p, g);
 	if (st) return st;
@@ -1600,6 +2047,7 @@ int rrg_lightmap_gather_learned(rrg_lightmapper* h, rrg_cache* cache, const rrg_
                                 void* stream) {
 	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
 	if (!L || !cache || !out_dev || ((uintptr_t)out_dev & 15)) return RRG_ERR_INVALID;
+	if (p && (p->mode & RRG_GATHER_SOLVER)) return RRG_ERR_INVALID;   // the cache replaces the plain paths only
 	GatherScene g;
 	int st = make_scene(L, p, g);
 	if (st) return st;

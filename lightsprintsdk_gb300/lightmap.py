@@ -57,6 +57,8 @@ def _lib():
                                                       P, P]
         L.rrg_lightmapper_status.argtypes = [P, P]
         L.rrg_lightmapper_copy_flags.argtypes = [P, P]
+        L.rrg_lightmapper_bake_solver.argtypes = [P, C.POINTER(GatherParams), U, U, P]
+        L.rrg_lightmapper_copy_solver.argtypes = [P, P, P, P]
         L.rrg_lightmap_filter.argtypes = [P, C.POINTER(FilterParams), C.c_uint32, C.c_uint32, P, P]
         L.rrg_lightmapper_seams.argtypes = [P]
         L.rrg_lightmapper_seams.restype = C.c_uint64
@@ -69,6 +71,8 @@ def _lib():
 
 
 GATHER_AUTO, GATHER_WARP, GATHER_WAVEFRONT = 0, 1, 2
+# flag OR-ed into the mode: the hemisphere reads the baked radiosity solver at its first hit
+GATHER_SOLVER = 4
 
 
 def make_params(lights: dict, quality: int = 64, max_depth: int = 8, seed: int = 0xC2, ray_length_min: float = 0.0,
@@ -186,6 +190,28 @@ class RRLightmapper:
                            bent.data_ptr())
         self.check(torch.cuda.current_stream().cuda_stream)
         return out[:count].cpu().numpy(), bent[:count].cpu().numpy()
+
+    def bake_solver(self, params: GatherParams, rays_per_triangle: int = 0, iterations: int = 32,
+                    stream: int = 0) -> None:
+        """The reference's default-bake radiosity solver on the device
+        (rrg_lightmapper_bake_solver): first gather per triangle, form-factor
+        rays, Jacobi propagation, corner smoothing.  Gathers with
+        mode | GATHER_SOLVER then read it at the first hit."""
+        r = _lib().rrg_lightmapper_bake_solver(self._h, C.byref(params), rays_per_triangle, iterations, stream or None)
+        if r:
+            raise col.RRGError(r, "rrg_lightmapper_bake_solver")
+
+    def solver(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(direct irradiance (T,3), indirect irradiance (T,3), smoothed
+        corner indirect irradiance (T,3,3))."""
+        T = int(self.albedo.shape[0])
+        d = np.zeros((T, 3), np.float32)
+        i = np.zeros((T, 3), np.float32)
+        c = np.zeros((T, 3, 3), np.float32)
+        r = _lib().rrg_lightmapper_copy_solver(self._h, d.ctypes.data, i.ctypes.data, c.ctypes.data)
+        if r:
+            raise col.RRGError(r, "rrg_lightmapper_copy_solver")
+        return d, i, c
 
     def flags(self) -> np.ndarray:
         """TexelFlags of every texel (ntexels,) uint8."""

@@ -64,6 +64,12 @@ def lib():
         L.orc_gather_ex.argtypes = [P, C.POINTER(GatherScene), P, U, P, P, C.c_int, C.c_int, P, P]
         L.orc_gather_dir.argtypes = [P, C.POINTER(GatherScene), P, U, P, P, C.c_int, C.c_int, P, P, P]
         L.orc_hash.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
+        L.orc_bake_direct.argtypes = [P, C.POINTER(GatherScene), C.c_int, P]
+        L.orc_bake_factors.argtypes = [P, C.POINTER(GatherScene), U, C.c_int, P]
+        L.orc_bake_propagate.argtypes = [C.POINTER(GatherScene), P, P, U, U, P]
+        L.orc_bake_stitch.argtypes = [P, P, U, P, P]
+        L.orc_bake_stitch.restype = U
+        L.orc_bake_smooth.argtypes = [U, P, P, U, P, P]
         L.orc_hash.restype = C.c_uint64
         L.orc_mlp_encode.argtypes = [P, P, P, P, P, P]
         L.orc_mlp_grad.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P]
@@ -150,7 +156,8 @@ class GatherScene(C.Structure):
                 ("dir_direction", C.c_float * 3), ("dir_color", C.c_float * 3), ("point_position", C.c_float * 3),
                 ("point_color", C.c_float * 3), ("ray_length_min", C.c_float), ("locality", C.c_float),
                 ("quality", C.c_uint32), ("max_depth", C.c_uint32), ("seed", C.c_uint64),
-                ("ao_intensity", C.c_float), ("ao_size", C.c_float), ("flags", C.c_void_p)]
+                ("ao_intensity", C.c_float), ("ao_size", C.c_float), ("flags", C.c_void_p),
+                ("solver_direct", C.c_void_p), ("solver_corner", C.c_void_p)]
 
 
 def hash_u64(seed: int, stream: int, index: int) -> int:
@@ -254,6 +261,33 @@ class GatherOracle:
                              (C.c_float * 3)(*L["point_position"]), (C.c_float * 3)(*L["point_color"]),
                              min_safe_distance(sc.vertices), locality, quality, max_depth, seed, ao_intensity,
                              ao_size, None if self.flags is None else self.flags.ctypes.data)
+
+    def bake_solver(self, rays_per_triangle: int = 0, iterations: int = 32, threads: int = 0):
+        """The default bake's radiosity solver (rr_gather.c, bake section) at
+        this oracle's quality and seed: per-triangle direct irradiance (first
+        gather at half quality), form-factor rays (rays_per_triangle, 0 =
+        the quality), Jacobi propagation, corner smoothing.  Returns
+        (direct (T,3), indirect (T,3), corner (T,3,3)) and makes the later
+        gathers read the solver at the first hit."""
+        sc = self.s
+        T = int(sc.nt)
+        k = int(rays_per_triangle or sc.quality)
+        L = lib()
+        direct = np.zeros((T, 3), np.float32)
+        L.orc_bake_direct(self.fo.h, C.byref(sc), threads, _ptr(direct))
+        hits = np.zeros(T * k, np.uint32)
+        L.orc_bake_factors(self.fo.h, C.byref(sc), k, threads, _ptr(hits))
+        indirect = np.zeros((T, 3), np.float32)
+        L.orc_bake_propagate(C.byref(sc), _ptr(direct), _ptr(hits), k, iterations, _ptr(indirect))
+        group = np.zeros(3 * T, np.uint32)
+        weight = np.zeros(3 * T, np.float32)
+        ng = L.orc_bake_stitch(self.fo.v.ctypes.data, self.fo.t.ctypes.data, T, _ptr(group), _ptr(weight))
+        corner = np.zeros((T, 3, 3), np.float32)
+        L.orc_bake_smooth(T, _ptr(group), _ptr(weight), ng, _ptr(indirect), _ptr(corner))
+        self.solver = (direct, corner)
+        self.s.solver_direct = direct.ctypes.data
+        self.s.solver_corner = corner.ctypes.data
+        return direct, indirect, corner
 
     def gather(self, texel_ids: np.ndarray, off: np.ndarray, st: np.ndarray, threads: int = 0,
                fp64: bool = False, bent: bool = False):

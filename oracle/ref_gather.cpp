@@ -5,7 +5,7 @@
 // only: the golden vectors that pin the plain N-bounce estimator of the
 // oracle (oracle/rr_gather.c) and of the GPU gather statistically.
 //
-//   ref_gather SCENE OUT [THREADS]
+//   ref_gather SCENE OUT [THREADS] [bake]
 //
 // SCENE : "RGS1", u32 nv, u32 nt, u32 natlas, u32 size, u32 quality,
 //         u32 nout, u32 seed, f32 xyz[3nv], u32 idx[3nt], f32 uv[6nt]
@@ -15,6 +15,8 @@
 //         u32 out_atlas[nout]
 // OUT   : "RGG1", u32 nout, u32 size, then per output atlas
 //         f32 rgba[size*size*4] (alpha = TexelFlags / 255 where covered)
+// OUT.solver (bake only): "RGB1", u32 nt, then per triangle (our order)
+//         f32 direct[3], indirect[3] (flat), corner indirect[3][3] (smoothed)
 //
 // Atlas a is object a (its triangles in index order, three vertices of their
 // own each, vertex normal = the face normal (v1-v0)x(v2-v0), one one-sided
@@ -28,6 +30,15 @@
 // the plain N-bounce estimator.  UpdateParameters: quality as given,
 // useCurrentSolution = true (so the hemisphere shoots, gather.cpp:197), the
 // rest default (locality 100000, no AO, multipliers 1).
+//
+// With "bake" the reference's whole default bake runs instead:
+// RRSolver::updateLightmaps(layer 0, -1, -1, UpdateParameters(quality),
+// filtering) (lightmap.cpp:943-1163): the first gather per triangle at half
+// quality and the radiosity propagation (updateSolverIndirectIllumination,
+// gather.cpp:1038-1117), then each requested atlas's final gather reading
+// the solver at the first hit.  Filtering: smoothingAmount 0 and
+// spreadForegroundColor 0, so covered texels keep their gathered values
+// (growForBilinear and the background fill touch only empty texels).
 #include "Lightsprint/RRCollider.h"
 #include "Lightsprint/RRLight.h"
 #include "Lightsprint/RRMesh.h"
@@ -39,6 +50,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 namespace rr {
@@ -102,10 +114,13 @@ int main(int argc, char** argv) {
 	// one object per atlas (triangles in index order), then the triangles of no atlas
 	RRObjects objects;
 	bool aborting = false;
+	std::vector<unsigned> multi_of(nt);   // our triangle -> the multi-object's
+	unsigned nmulti = 0;
 	for (unsigned a = 0; a <= natlas; a++) {
 		std::vector<unsigned> tris;
 		for (unsigned t = 0; t < nt; t++)
 			if (a < natlas ? atlas[t] == (int)a : atlas[t] < 0) tris.push_back(t);
+		for (unsigned t : tris) multi_of[t] = nmulti++;
 		if (a == natlas && tris.empty()) break;
 		const unsigned n = (unsigned)tris.size();
 		RRMeshArrays* mesh = new RRMeshArrays();
@@ -154,6 +169,65 @@ int main(int argc, char** argv) {
 	RRVec3 mini, maxi, center;
 	multi->getCollider()->getMesh()->getAABB(&mini, &maxi, &center);
 	const float msd = (maxi - mini).avg() * 1e-6f;
+
+	const bool bake = argc > 4 && !strcmp(argv[4], "bake");
+	if (bake) {
+		std::vector<RRBuffer*> bufs;
+		for (unsigned o = 0; o < nout; o++) {
+			const unsigned a = out_atlas[o];
+			if (a >= natlas) { fprintf(stderr, "bad atlas\n"); return 6; }
+			RRBuffer* b = RRBuffer::create(BT_2D_TEXTURE, size, size, 1, BF_RGBAF, false, nullptr);
+			objects[a]->illumination.getLayer(0) = b;
+			bufs.push_back(b);
+		}
+		RRSolver::UpdateParameters params(quality);
+		RRSolver::FilteringParameters filtering;
+		filtering.smoothingAmount = 0;
+		filtering.spreadForegroundColor = 0;
+		const unsigned updated = solver->updateLightmaps(0, -1, -1, &params, &filtering);
+		if (updated != nout) { fprintf(stderr, "updated %u of %u\n", updated, nout); return 8; }
+		FILE* f = fopen(argv[2], "wb");
+		if (!f) return 5;
+		fwrite("RGG1", 1, 4, f);
+		fwrite(&nout, 4, 1, f);
+		fwrite(&size, 4, 1, f);
+		for (unsigned o = 0; o < nout; o++) {
+			std::vector<float> px((size_t)size * size * 4);
+			for (unsigned i = 0; i < size * size; i++) {
+				RRVec4 e = bufs[o]->getElement(i, nullptr);
+				for (int c = 0; c < 4; c++) px[4 * (size_t)i + c] = e[c];
+			}
+			fwrite(px.data(), sizeof(float), px.size(), f);
+		}
+		fclose(f);
+		// the solver the final gather read, per triangle of ours: direct and
+		// indirect irradiance (flat) and the smoothed indirect at each corner
+		std::string sp = std::string(argv[2]) + ".solver";
+		f = fopen(sp.c_str(), "wb");
+		if (!f) return 5;
+		fwrite("RGB1", 1, 4, f);
+		fwrite(&nt, 4, 1, f);
+		for (unsigned t = 0; t < nt; t++) {
+			float rec[15];
+			RRVec3 v;
+			RRRadiometricMeasure md(0, 0, 0, 1, 0), mi(0, 0, 0, 0, 1);
+			md.smoothed = 0;
+			RRRadiometricMeasure mif = mi;
+			mif.smoothed = 0;
+			solver->getTriangleMeasure(multi_of[t], 3, md, v);
+			for (int c = 0; c < 3; c++) rec[c] = v[c];
+			solver->getTriangleMeasure(multi_of[t], 3, mif, v);
+			for (int c = 0; c < 3; c++) rec[3 + c] = v[c];
+			for (unsigned k = 0; k < 3; k++) {
+				solver->getTriangleMeasure(multi_of[t], k, mi, v);
+				for (int c = 0; c < 3; c++) rec[6 + 3 * k + c] = v[c];
+			}
+			fwrite(rec, sizeof(float), 15, f);
+		}
+		fclose(f);
+		printf("ok bake\n");
+		return 0;
+	}
 
 	RRSolver::UpdateParameters params(quality);
 	params.useCurrentSolution = true;

@@ -152,10 +152,14 @@ def run_ref_enumerate(v, normals, t, uv, size: int):
 #                u32 idx[3nt]; f32 uv[6nt]; f32 albedo[3nt]; i32 atlas[nt];
 #                f32 lights[12]; u32 out_atlas[nout]
 # GATHER "RGG1": u32 nout, u32 size, f32 rgba[nout*size*size*4]
-def run_ref_gather(gs, atlases, quality: int, seed: int = 1, threads: int = 0) -> np.ndarray:
+def run_ref_gather(gs, atlases, quality: int, seed: int = 1, threads: int = 0, bake: bool = False) -> np.ndarray:
     """The reference's own processTexel over whole atlases of a GatherScene,
-    with no radiosity solver (the plain N-bounce estimator, stopAtDepth 20).
-    Returns (len(atlases), size, size, 4) float32 RGBA, alpha = flags / 255."""
+    with no radiosity solver (the plain N-bounce estimator, stopAtDepth 20),
+    or with bake=True its whole default updateLightmaps (first gather,
+    radiosity, final gather reading the solver; no smoothing or spreading).
+    Returns (len(atlases), size, size, 4) float32 RGBA, alpha = flags / 255;
+    with bake also the solver the final gather read, per triangle: dict of
+    direct (T,3), indirect (T,3) and smoothed corner indirect (T,3,3)."""
     exe = os.path.join(REF_DIR, "ref_gather")
     sc = gs.scene
     atlases = np.asarray(atlases, np.uint32)
@@ -174,8 +178,17 @@ def run_ref_gather(gs, atlases, quality: int, seed: int = 1, threads: int = 0) -
             f.write(np.ascontiguousarray(gs.tri_atlas, np.int32).tobytes())
             f.write(lights.tobytes())
             f.write(atlases.tobytes())
-        subprocess.run([exe, sp, op, str(threads)], capture_output=True, text=True, check=True)
+        subprocess.run([exe, sp, op, str(threads)] + (["bake"] if bake else []), capture_output=True, text=True,
+                       check=True)
         b = open(op, "rb").read()
+        sb = open(op + ".solver", "rb").read() if bake else None
     assert b[:4] == b"RGG1"
     nout, size = (int(x) for x in np.frombuffer(b, np.uint32, 2, 4))
-    return np.frombuffer(b, np.float32, nout * size * size * 4, 12).reshape(nout, size, size, 4).copy()
+    out = np.frombuffer(b, np.float32, nout * size * size * 4, 12).reshape(nout, size, size, 4).copy()
+    if not bake:
+        return out
+    assert sb[:4] == b"RGB1"
+    nt = int(np.frombuffer(sb, np.uint32, 1, 4)[0])
+    rec = np.frombuffer(sb, np.float32, nt * 15, 8).reshape(nt, 15)
+    solver = {"direct": rec[:, 0:3].copy(), "indirect": rec[:, 3:6].copy(), "corner": rec[:, 6:15].reshape(nt, 3, 3).copy()}
+    return out, solver

@@ -284,6 +284,27 @@ static void path(const orc_bvh* bvh, const orc_gather_scene* sc, v3 eye, v3 dir,
 	d3 LD = {0, 0, 0};
 	float tmax = sc->locality;
 	const float tmin = sc->ray_length_min;
+	if (sc->solver_direct) {
+		/* the solver read at the first hit: direct from the triangle, indirect
+		 * interpolated from its corners, times the albedo; the diffuse path
+		 * ends there (pathtracer.cpp:235-258, 326-350; rrcore.cpp:262-277) */
+		float dist, uv[2];
+		uint32_t tri = orc_cast_uv(bvh, &eye.x, &dir.x, tmin, tmax, skip, &dist, uv);
+		if (tri != 0xFFFFFFFFu) {
+			*first_t = dist;
+			const float* c = sc->solver_corner + 9 * (size_t)tri;
+			float w = 1 - uv[0] - uv[1];
+			v3 ind = add(add(mul(ld3(c), w), mul(ld3(c + 3), uv[0])), mul(ld3(c + 6), uv[1]));
+			v3 alb = ld3(sc->albedo + 3 * (size_t)tri);
+			L = add(mulv(ld3(sc->solver_direct + 3 * (size_t)tri), alb), mulv(ind, alb));
+			LD.x = L.x;
+			LD.y = L.y;
+			LD.z = L.z;
+		}
+		*Lf = L;
+		*Ld = LD;
+		return;
+	}
 	for (uint32_t depth = 0;; depth++) {
 		float dist, plane[4];
 		uint32_t tri = orc_cast(bvh, &eye.x, &dir.x, tmin, tmax, 0, skip, &dist, plane);
@@ -555,4 +576,245 @@ void orc_gather_ex(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_
 void orc_gather(const orc_bvh* bvh, const orc_gather_scene* sc, const uint64_t* texel_id, uint32_t ntexels,
                 const uint64_t* off, const orc_subtexel* st, int threads, int fp64, float* out) {
 	orc_gather_ex(bvh, sc, texel_id, ntexels, off, st, threads, fp64, out, NULL);
+}
+
+/* ---------------------------------------------------------------- bake */
+/* The default bake's radiosity solver.  Deliberate differences from the
+ * reference, shared with the GPU: the same hash streams instead of rand()
+ * and boost::rand48; factor-ray directions by Malley's method (the
+ * distribution of rrcore.cpp:1026-1038); the converged solution of the flux
+ * balance by Jacobi iteration of its gathering form (each triangle's own
+ * rays estimate the form factors it receives through; by reciprocity the
+ * same system the reference's progressive shooting solves, rrcore.cpp:
+ * 1052-1297), where the reference stops at its accuracy target. */
+enum { S_TRI_PU = 80, S_TRI_PV = 81, S_FF_PU = 82, S_FF_PV = 83, S_FF_DX = 84, S_FF_DY = 85 };
+#define SHOT_OFFSET 1e-4f   /* geometry_v.h:30 */
+#define BIG_REAL 1e20f      /* geometry_v.h:28 */
+
+/* a random point of the triangle (gather.cpp:742-749 with the whole
+ * triangle as sub-texel; rrcore.cpp:1016-1024) */
+static void tri_point(uint64_t seed, uint64_t su, uint64_t sv, uint64_t i, float* pu, float* pv) {
+	uint32_t ru = rng24(seed, su, i), rv = rng24(seed, sv, i);
+	if (ru + rv > M24) { ru = M24 - ru; rv = M24 - rv; }
+	*pu = (float)ru / (float)M24;
+	*pv = (float)rv / (float)M24;
+}
+
+static float sum3(v3 a) { return a.x + a.y + a.z; }
+
+void orc_bake_direct(const orc_bvh* bvh, const orc_gather_scene* sc, int threads, float* direct) {
+	const uint32_t qh = sc->quality / 2 ? sc->quality / 2 : 1;
+	const uint32_t rounds = qh / 10 + 1;
+	if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 64)
+	for (int64_t ti = 0; ti < (int64_t)sc->nt; ti++) {
+		const uint32_t t = (uint32_t)ti;
+		v3 v0, s1, s2;
+		v3 n = tri_normal(sc, t, &v0, &s1, &s2);
+		v3 acc = mk(0, 0, 0);
+		for (uint32_t r = 0; r < rounds; r++) {
+			float pu, pv;
+			tri_point(sc->seed, S_TRI_PU, S_TRI_PV, (uint64_t)t * rounds + r, &pu, &pv);
+			v3 o = add(add(v0, mul(s1, pu)), mul(s2, pv));
+			for (int li = 0; li < 2; li++) {
+				v3 d = li == 0 ? neg(ld3(sc->dir_direction)) : sub(ld3(sc->point_position), o);
+				float dsize = len(d);
+				d = divf(d, dsize);
+				if (li == 0) dsize *= sc->locality;
+				float ni = dot(d, n);
+				if (ni <= 0 || !isfinite(ni)) continue;
+				if (orc_cast(bvh, &o.x, &d.x, sc->ray_length_min, dsize, 1, t, NULL, NULL) != 0xFFFFFFFFu) continue;
+				v3 irr = li == 0 ? ld3(sc->dir_color) : point_irradiance(sc, o);
+				acc = add(acc, mul(irr, ni));
+			}
+		}
+		acc = divf(acc, (float)rounds);
+		direct[3 * (size_t)t] = acc.x;
+		direct[3 * (size_t)t + 1] = acc.y;
+		direct[3 * (size_t)t + 2] = acc.z;
+	}
+}
+
+void orc_bake_factors(const orc_bvh* bvh, const orc_gather_scene* sc, uint32_t k, int threads, uint32_t* hits) {
+	if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 64)
+	for (int64_t ti = 0; ti < (int64_t)sc->nt; ti++) {
+		const uint32_t t = (uint32_t)ti;
+		v3 v0, s1, s2;
+		v3 n = tri_normal(sc, t, &v0, &s1, &s2);
+		v3 tg, bt;
+		basis_from_normal(n, &tg, &bt);
+		for (uint32_t j = 0; j < k; j++) {
+			const uint64_t i = (uint64_t)t * k + j;
+			float pu, pv;
+			tri_point(sc->seed, S_FF_PU, S_FF_PV, i, &pu, &pv);
+			v3 o = add(add(v0, mul(s1, pu)), mul(s2, pv));
+			float x = 0, y = 0;
+			for (uint32_t q = 0; q < DISK_TRIES; q++) {
+				uint64_t c = i * DISK_TRIES + q;
+				float a = rng01(sc->seed, S_FF_DX, c) * 2.0f - 1.0f;
+				float b = rng01(sc->seed, S_FF_DY, c) * 2.0f - 1.0f;
+				if (a * a + b * b < 1.0f) { x = a; y = b; break; }
+			}
+			float cosa = sqrtf(1.0f - (x * x + y * y));
+			v3 d = add(add(mul(n, cosa), mul(tg, x)), mul(bt, y));
+			int front = 0;
+			uint32_t h = orc_cast_photon(bvh, &o.x, &d.x, SHOT_OFFSET, BIG_REAL, t, &front);
+			hits[i] = (h != 0xFFFFFFFFu && front && sum3(ld3(sc->albedo + 3 * (size_t)h)) > 0.01f) ? h : 0xFFFFFFFFu;
+		}
+	}
+}
+
+void orc_bake_propagate(const orc_gather_scene* sc, const float* direct, const uint32_t* hits, uint32_t k,
+                        uint32_t iterations, float* indirect) {
+	const size_t n3 = 3 * (size_t)sc->nt;
+	float* e = (float*)malloc(n3 * sizeof(float));
+	float* f = (float*)malloc(n3 * sizeof(float));
+	memcpy(e, direct, n3 * sizeof(float));
+	const float inv = 1.0f / (float)(k ? k : 1);
+	for (uint32_t it = 0; it < iterations; it++) {
+#pragma omp parallel for schedule(static)
+		for (int64_t ti = 0; ti < (int64_t)sc->nt; ti++) {
+			v3 acc = mk(0, 0, 0);
+			for (uint32_t j = 0; j < k; j++) {
+				const uint32_t h = hits[(size_t)ti * k + j];
+				if (h == 0xFFFFFFFFu) continue;
+				acc = add(acc, mulv(ld3(sc->albedo + 3 * (size_t)h), ld3(e + 3 * (size_t)h)));
+			}
+			v3 r = add(ld3(direct + 3 * ti), mul(acc, inv));
+			f[3 * ti] = r.x;
+			f[3 * ti + 1] = r.y;
+			f[3 * ti + 2] = r.z;
+		}
+		float* tmp = e;
+		e = f;
+		f = tmp;
+	}
+	for (size_t i = 0; i < n3; i++) indirect[i] = e[i] - direct[i];
+	free(e);
+	free(f);
+}
+
+/* Abramowitz & Stegun 4.4.45, as geometry_v.h:114-129 applies it (over the
+ * whole [-1, 1]) */
+static float as_acos(float x) {
+	float root = sqrtf(1.0f - x);
+	float r = -0.0187293f;
+	r *= x;
+	r += 0.0742610f;
+	r *= x;
+	r -= 0.2121144f;
+	r *= x;
+	r += 1.5707288f;
+	return r * root;
+}
+
+/* rrcore.cpp:105-111 */
+static float tri_area(v3 s1, v3 s2) {
+	float a = len2(s1), b = len2(s2), c = len2(sub(s2, s1));
+	return sqrtf(2 * b * c + 2 * c * a + 2 * a * b - a * a - b * b - c * c) / 4;
+}
+
+typedef struct { float p[3], n[3]; uint32_t c; } corner_key;
+
+static int cmp_corner(const void* x, const void* y) {
+	const corner_key* a = (const corner_key*)x;
+	const corner_key* b = (const corner_key*)y;
+	for (int i = 0; i < 3; i++)
+		if (a->p[i] != b->p[i]) return a->p[i] < b->p[i] ? -1 : 1;
+	for (int i = 0; i < 3; i++)
+		if (a->n[i] != b->n[i]) return a->n[i] < b->n[i] ? -1 : 1;
+	return a->c < b->c ? -1 : (a->c > b->c);
+}
+
+uint32_t orc_bake_stitch(const float* xyz, const uint32_t* idx, uint32_t nt, uint32_t* group, float* weight) {
+	/* every corner is a vertex of its own with its face's normal (the mesh
+	 * has flat normals); RRLessVerticesFilter merges identical positions
+	 * whose normals are within 0.01 rad, greedily in (position, normal) order
+	 * against the unique vertices found so far, newest first */
+	const uint32_t nc = 3 * nt;
+	corner_key* k = (corner_key*)malloc((size_t)(nc ? nc : 1) * sizeof(corner_key));
+	for (uint32_t t = 0; t < nt; t++) {
+		v3 p0 = ld3(xyz + 3 * (size_t)idx[3 * t]);
+		v3 n = cross(sub(ld3(xyz + 3 * (size_t)idx[3 * t + 1]), p0), sub(ld3(xyz + 3 * (size_t)idx[3 * t + 2]), p0));
+		float l = len(n);
+		if (l > 0) n = divf(n, l);
+		for (int i = 0; i < 3; i++) {
+			corner_key* c = &k[3 * t + i];
+			const float* p = xyz + 3 * (size_t)idx[3 * t + i];
+			c->p[0] = p[0]; c->p[1] = p[1]; c->p[2] = p[2];
+			c->n[0] = n.x; c->n[1] = n.y; c->n[2] = n.z;
+			c->c = 3 * t + i;
+		}
+	}
+	qsort(k, nc, sizeof(corner_key), cmp_corner);
+	uint32_t* rep = (uint32_t*)malloc((size_t)(nc ? nc : 1) * sizeof(uint32_t));   /* unique -> sorted slot */
+	uint32_t nu = 0;
+	const float min_dot = cosf(0.01f);
+	for (uint32_t s = 0; s < nc; s++) {
+		const corner_key* d = &k[s];
+		uint32_t g = 0xFFFFFFFFu;
+		for (uint32_t u = nu; u--;) {
+			const corner_key* r = &k[rep[u]];
+			if (!(fabsf(d->p[0] - r->p[0]) <= 0.0f)) break;
+			if (fabsf(d->p[1] - r->p[1]) <= 0.0f && fabsf(d->p[2] - r->p[2]) <= 0.0f &&
+			    d->n[0] * r->n[0] + d->n[1] * r->n[1] + d->n[2] * r->n[2] >= min_dot) {
+				g = u;
+				break;
+			}
+		}
+		if (g == 0xFFFFFFFFu) {
+			rep[nu] = s;
+			g = nu++;
+		}
+		group[d->c] = g;
+	}
+	/* Object::buildTopIVertices (interpol.cpp:120-170): corner weight =
+	 * corner angle x triangle area; triangles that stitching degenerates or
+	 * that have no area get none */
+	for (uint32_t t = 0; t < nt; t++) {
+		v3 p[3];
+		for (int i = 0; i < 3; i++) p[i] = ld3(xyz + 3 * (size_t)idx[3 * t + i]);
+		float area = tri_area(sub(p[1], p[0]), sub(p[2], p[0]));
+		const uint32_t* g = group + 3 * t;
+		int ok = area > 0 && g[0] != g[1] && g[0] != g[2] && g[1] != g[2];
+		for (int i = 0; i < 3; i++) {
+			float w = 0;
+			if (ok) {
+				v3 a = normalized(sub(p[(i + 1) % 3], p[i])), b = normalized(sub(p[(i + 2) % 3], p[i]));
+				float dd = dot(a, b);
+				dd = dd < -1 ? -1 : (dd > 1 ? 1 : dd);
+				w = as_acos(dd) * area;
+			}
+			weight[3 * t + i] = w;
+		}
+	}
+	free(rep);
+	free(k);
+	return nu;
+}
+
+void orc_bake_smooth(uint32_t nt, const uint32_t* group, const float* weight, uint32_t ngroups,
+                     const float* indirect, float* corner) {
+	float* num = (float*)calloc(3 * (size_t)(ngroups ? ngroups : 1), sizeof(float));
+	float* den = (float*)calloc((size_t)(ngroups ? ngroups : 1), sizeof(float));
+	for (uint32_t c = 0; c < 3 * nt; c++) {
+		const uint32_t g = group[c];
+		const float w = weight[c];
+		if (w == 0) continue;
+		const float* I = indirect + 3 * (size_t)(c / 3);
+		num[3 * (size_t)g] += I[0] * w;
+		num[3 * (size_t)g + 1] += I[1] * w;
+		num[3 * (size_t)g + 2] += I[2] * w;
+		den[g] += w;
+	}
+	for (uint32_t c = 0; c < 3 * nt; c++) {
+		const uint32_t g = group[c];
+		for (int i = 0; i < 3; i++) {
+			float v = den[g] > 0 ? num[3 * (size_t)g + i] / den[g] : 0;
+			corner[3 * (size_t)c + i] = v > 0 ? v : 0;   /* clampToZero (interpol.cpp:104) */
+		}
+	}
+	free(num);
+	free(den);
 }

@@ -82,6 +82,11 @@ typedef struct orc_gather_scene {
 	float ao_intensity;     /* UpdateParameters::aoIntensity (used when both are > 0) */
 	float ao_size;          /* UpdateParameters::aoSize */
 	const uint8_t* flags;   /* TexelFlags by texel id (alpha = flags/255, gather.cpp:801); NULL: alpha 1 */
+	/* radiosity solver read at the first hit (NULL: the plain N-bounce
+	 * estimator): per triangle its direct irradiance (3 floats) and the
+	 * smoothed indirect irradiance at its three corners (9 floats) */
+	const float* solver_direct;
+	const float* solver_corner;
 } orc_gather_scene;
 
 /* Sub-texels of one atlas.  uv: n triangles x 3 corners x 2 in map space
@@ -129,6 +134,37 @@ int orc_lightmap_smooth(float* rgba, uint32_t width, uint32_t height, float sigm
 int orc_lightmap_grow_bilinear(float* rgba, uint32_t width, uint32_t height, int wrap);
 int orc_lightmap_grow(float* rgba, uint32_t width, uint32_t height, uint32_t steps, int wrap);
 void orc_lightmap_fill_background(float* rgba, uint32_t width, uint32_t height, const float* background);
+
+/* ---- the default bake's solver (updateSolverIndirectIllumination,
+ * RRSolver/gather.cpp:959-1117, and RRStaticSolver) ---- */
+
+/* First gather per triangle (gatherPerTrianglePhysical, gather.cpp:843-952):
+ * processTexel with the whole triangle as its one sub-texel at quality
+ * max(1, quality / 2): (that / 10 + 1) light rounds from random points of
+ * the triangle, no hemisphere rays.  direct[3 * nt]. */
+void orc_bake_direct(const orc_bvh* bvh, const orc_gather_scene* sc, int threads, float* direct);
+/* Form-factor rays (shotFromToHalfspace / rayTracePhoton, rrcore.cpp:861-1050):
+ * k rays per triangle from random points, cosine-distributed over its front
+ * half-space, nearest hit on either side (shooter skipped, tmin 1e-4);
+ * hits[nt * k] = the triangle whose front side was hit (and whose diffuse
+ * reflectance sums above 0.01), else 0xFFFFFFFF. */
+void orc_bake_factors(const orc_bvh* bvh, const orc_gather_scene* sc, uint32_t k, int threads, uint32_t* hits);
+/* Radiosity by Jacobi iteration of the gathering form of the solver's flux
+ * balance: E_j <- D_j + (1/k) sum over j's hits h of albedo_h * E_h, from
+ * E = D, `iterations` times.  indirect[3 * nt] = E - D. */
+void orc_bake_propagate(const orc_gather_scene* sc, const float* direct, const uint32_t* hits, uint32_t k,
+                        uint32_t iterations, float* indirect);
+/* Corner smoothing (Object::buildTopIVertices, interpol.cpp:120-170, with
+ * the stitching of RRLessVerticesFilter, RRMeshLessVertices.h:38-237, at
+ * the default SmoothingParameters: identical positions, normals within
+ * 0.01 rad): group[3 * nt] = each corner's stitched vertex, weight[3 * nt] =
+ * its corner angle x triangle area (0 for degenerate triangles).  Returns
+ * the number of groups. */
+uint32_t orc_bake_stitch(const float* xyz, const uint32_t* idx, uint32_t nt, uint32_t* group, float* weight);
+/* corner[9 * nt]: each corner's smoothed indirect irradiance (IVertex::
+ * irradiance, interpol.cpp:78-112): the weighted mean over its group. */
+void orc_bake_smooth(uint32_t nt, const uint32_t* group, const float* weight, uint32_t ngroups,
+                     const float* indirect, float* corner);
 
 #ifdef __cplusplus
 }

@@ -575,8 +575,10 @@ static int same_vertices(const orc_bvh* b, uint32_t t, uint32_t s) {
 	return 1;
 }
 
-uint32_t orc_cast(const orc_bvh* b, const float* o, const float* d, float tmin, float tmax, int shadow,
-                  uint32_t skip, float* dist_out, float* plane_out) {
+/* mode 0: hemisphere, 1: shadow, 2: photon (RRCollisionHandlerLod0,
+ * rrcore.cpp:670-723: every side collides, only the shooter is skipped) */
+static uint32_t cast_impl(const orc_bvh* b, const float* o, const float* d, float tmin, float tmax, int shadow,
+                          uint32_t skip, float* dist_out, float* plane_out, int* front_out, float* uv_out) {
 	float hmin, hmax;
 	if (!b->nnodes) return 0xFFFFFFFFu;
 	if (!orc_box_intersect(b->bmin, b->bmax, o, d, tmin, tmax, &hmin, &hmax)) return 0xFFFFFFFFu;
@@ -586,6 +588,8 @@ uint32_t orc_cast(const orc_bvh* b, const float* o, const float* d, float tmin, 
 	stack[sp++] = 0;
 	float best = hmax;
 	uint32_t best_tri = 0xFFFFFFFFu;
+	int best_fr = 0;
+	float best_u = 0, best_v = 0;
 	while (sp) {
 		const onode* nd = &b->nodes[stack[--sp]];
 		float slack = 1e-6f * (fabsf(best) + fabsf(hmin)) + b->pad;
@@ -600,13 +604,16 @@ uint32_t orc_cast(const orc_bvh* b, const float* o, const float* d, float tmin, 
 				int fr;
 				if (!orc_tri_fastest(tr, o, d, dp, &u, &v, &fr)) continue;
 				if (t == skip) continue;
-				if (skip != 0xFFFFFFFFu && dp < 1000 * tmin && same_vertices(b, t, skip)) continue;
+				if (shadow != 2 && skip != 0xFFFFFFFFu && dp < 1000 * tmin && same_vertices(b, t, skip)) continue;
 				if (!shadow && !fr) continue;
 				if (dp < best || t < best_tri) {
 					best = dp;
 					best_tri = t;
+					best_fr = fr;
+					best_u = u;
+					best_v = v;
 				}
-				if (shadow) { sp = 0; break; }
+				if (shadow == 1) { sp = 0; break; }
 			}
 		} else {
 			const onode* l = &b->nodes[nd->left];
@@ -622,6 +629,24 @@ uint32_t orc_cast(const orc_bvh* b, const float* o, const float* d, float tmin, 
 		if (dist_out) *dist_out = best;
 		if (plane_out)
 			for (int k = 0; k < 4; k++) plane_out[k] = b->tris[best_tri].n4[k];
+		if (front_out) *front_out = best_fr;
+		if (uv_out) { uv_out[0] = best_u; uv_out[1] = best_v; }
 	}
 	return best_tri;
+}
+
+uint32_t orc_cast(const orc_bvh* b, const float* o, const float* d, float tmin, float tmax, int shadow,
+                  uint32_t skip, float* dist_out, float* plane_out) {
+	return cast_impl(b, o, d, tmin, tmax, shadow ? 1 : 0, skip, dist_out, plane_out, NULL, NULL);
+}
+
+uint32_t orc_cast_uv(const orc_bvh* b, const float* o, const float* d, float tmin, float tmax, uint32_t skip,
+                     float* dist, float* uv) {
+	return cast_impl(b, o, d, tmin, tmax, 0, skip, dist, NULL, NULL, uv);
+}
+
+uint32_t orc_cast_photon(const orc_bvh* b, const float* o, const float* d, float tmin, float tmax, uint32_t skip,
+                         int* front) {
+	*front = 0;
+	return cast_impl(b, o, d, tmin, tmax, 2, skip, NULL, NULL, front, NULL);
 }

@@ -87,6 +87,14 @@ int orc_max_threads(void);
 /* Ray cast with the final-gathering handler semantics (see rr_oracle.c). */
 uint32_t orc_cast(const orc_bvh* b, const float* o, const float* d, float tmin, float tmax, int shadow,
                   uint32_t skip, float* dist, float* plane);
+/* Photon ray of the radiosity solver (RRCollisionHandlerLod0): the nearest
+ * hit on either side, the shooter skipped; *front = the side hit. */
+uint32_t orc_cast_photon(const orc_bvh* b, const float* o, const float* d, float tmin, float tmax, uint32_t skip,
+                         int* front);
+/* Hemisphere cast (as orc_cast with shadow = 0) that also returns the hit's
+ * barycentric u, v (hitPoint2d). */
+uint32_t orc_cast_uv(const orc_bvh* b, const float* o, const float* d, float tmin, float tmax, uint32_t skip,
+                     float* dist, float* uv);
 
 #ifdef __cplusplus
 }

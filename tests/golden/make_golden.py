@@ -11,7 +11,9 @@ hitDistance, hitPoint2d, hitPlane, hitFrontSide).  The lightmap fixture
 holds the reference's texel enumeration (TexelFlags, sub-texel counts and a
 hash of the sub-texels) and hashes of its post-filter outputs.  The gather
 fixture holds the reference's own per-texel gather (processTexel, no
-radiosity solver) of four atlases of a small room.  Test infrastructure only.
+radiosity solver) of four atlases of a small room, the bake fixture summaries
+of its default bake (updateLightmaps with the radiosity solver) of the same
+atlases.  Test infrastructure only.
 """
 from __future__ import annotations
 
@@ -174,6 +176,54 @@ def gather():
          rgb=np.ascontiguousarray(outs[0][..., :3]), rgb2=np.ascontiguousarray(outs[1][..., :3]))
 
 
+# Reference bake: updateLightmaps with its radiosity solver on the same
+# atlases.  Its photon shooting seeds each thread's generator with the thread
+# number, so runs on different thread counts are its independent realizations.
+BAKE_THREADS = (1, 2, 3, 5)
+
+
+def room_classes(gs):
+    """Triangle masks of the room's object classes: slabs, boxes, spheres."""
+    obj = gs.scene.tri_object
+    return [(obj >= 0) & (obj < 9), (obj >= 9) & (obj < 19), obj >= 19]
+
+
+def triangle_areas(gs):
+    v = gs.scene.vertices.astype(np.float64)
+    t = gs.scene.indices
+    return 0.5 * np.linalg.norm(np.cross(v[t[:, 1]] - v[t[:, 0]], v[t[:, 2]] - v[t[:, 0]]), axis=1)
+
+
+def bake():
+    """The reference's default bake (first gather, radiosity, final gather
+    reading the solver; no smoothing or spreading) of four atlases of the
+    room, one run per thread count: per run the atlas means over covered
+    texels, the area-weighted indirect irradiance of each object class and
+    (first two runs) every triangle's direct irradiance; the texels equal in
+    every run, with their values."""
+    gs = scenes.gather_room()
+    area = triangle_areas(gs)
+    classes = room_classes(gs)
+    outs, solvers = [], []
+    for k, th in enumerate(BAKE_THREADS):
+        out, sol = refio.run_ref_gather(gs, GATHER_ATLASES, GATHER_QUALITY, seed=10 + k, threads=th, bake=True)
+        outs.append(out)
+        solvers.append(sol)
+    flags = np.rint(outs[0][..., 3] * 255).astype(np.uint8)
+    cov = flags > 0
+    atlas_means = np.stack([[o[a][cov[a]][:, :3].mean(0) for a in range(len(GATHER_ATLASES))] for o in outs])
+    class_indirect = np.stack([[(s["indirect"][m] * area[m, None]).sum(0) / area[m].sum() for m in classes]
+                               for s in solvers])
+    same = cov.copy()
+    for o in outs[1:]:
+        same &= np.all(o[..., :3] == outs[0][..., :3], axis=-1)
+    save("bake_ref.npz", scene_md5=md5(gs.scene.vertices, gs.scene.indices, gs.albedo, gs.uv, gs.tri_atlas),
+         atlases=np.array(GATHER_ATLASES, np.uint32), quality=np.uint32(GATHER_QUALITY), flags=flags,
+         atlas_means=atlas_means.astype(np.float32), class_indirect=class_indirect.astype(np.float32),
+         direct=np.stack([solvers[0]["direct"], solvers[1]["direct"]]).astype(np.float32),
+         det_mask=same, det_rgb=outs[0][..., :3][same].astype(np.float32))
+
+
 def main():
     assert refio.ref_available(), "build oracle/_ref first: make -f oracle/ref.mk -j8"
     # 1. HelloCollider known answer
@@ -223,11 +273,16 @@ def main():
     # 6. the reference's plain per-texel gather
     gather()
 
+    # 7. the reference's default bake (radiosity solver read at the first hit)
+    bake()
+
 
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "lightmaps":
         lightmaps()
     elif len(sys.argv) > 1 and sys.argv[1] == "gather":
         gather()
+    elif len(sys.argv) > 1 and sys.argv[1] == "bake":
+        bake()
     else:
         main()

@@ -180,3 +180,87 @@ def reference_gather_stats(g: dict, o1: np.ndarray, o2: np.ndarray) -> list[dict
 def reference_gather_ok(s: dict, det_rel: float = 0.0) -> bool:
     return (s["alpha"] and s["z_mean"] < GATHER_Z_MEAN and s["rel_mean"] < GATHER_REL_MEAN
             and s["spread"] < GATHER_SPREAD and s["z_block"] < GATHER_Z_BLOCK and s["det_rel"] <= det_rel)
+
+
+# The reference's default bake (tests/golden/bake_ref.npz) against ours.
+# Its radiosity solver stops at an accuracy target where ours iterates the
+# same balance to convergence, and its photon shooting spreads the noise
+# differently, so means are compared within both sides' measured scatter
+# plus an allowance: 0.5 % for atlas means, 1 % for class indirect.
+BAKE_Z = 4.0
+BAKE_ATLAS_ALLOW = 0.005
+BAKE_CLASS_ALLOW = 0.01
+
+
+def room_classes(gs):
+    """Triangle masks of the small room's object classes: slabs, boxes, spheres."""
+    obj = gs.scene.tri_object
+    return [(obj >= 0) & (obj < 9), (obj >= 9) & (obj < 19), obj >= 19]
+
+
+def triangle_areas(gs):
+    v = gs.scene.vertices.astype(np.float64)
+    t = gs.scene.indices
+    return 0.5 * np.linalg.norm(np.cross(v[t[:, 1]] - v[t[:, 0]], v[t[:, 2]] - v[t[:, 0]]), axis=1)
+
+
+def _within(ours: np.ndarray, ref: np.ndarray, allow: float) -> np.ndarray:
+    """ours (n, ...) and ref (m, ...) realizations: |mean difference| over
+    BAKE_Z x the combined scatter of the means plus allow x the reference
+    mean; values below 1 pass."""
+    mo, mr = ours.mean(0), ref.mean(0)
+    so = ours.std(0, ddof=1) / np.sqrt(ours.shape[0])
+    sr = ref.std(0, ddof=1) / np.sqrt(ref.shape[0])
+    return np.abs(mo - mr) / (BAKE_Z * np.sqrt(so ** 2 + sr ** 2) + allow * np.abs(mr))
+
+
+def reference_bake_stats(g: dict, gs, runs: list, directs: list, indirects: list) -> dict:
+    """runs: our gathered atlases per run ((natlas, size, size, 4) each),
+    directs / indirects: our solver's per-triangle direct and indirect
+    irradiance per run.  Returns
+      atlas     per atlas and channel, the mean difference over the bound
+                (below 1 passes)
+      cls       the same for the area-weighted indirect of each object class
+      direct_z  largest |z| of the mean per-triangle direct difference per
+                class (the first gather is the same estimator on both sides)
+      det_n, det_rel
+                texels equal in every reference run and in every run of
+                ours, and the largest relative difference of ours there
+      alpha     our alpha equals the reference's TexelFlags / 255."""
+    flags = g["flags"]
+    cov = flags > 0
+    area = triangle_areas(gs)
+    classes = room_classes(gs)
+    ours_means = np.stack([[r[a][cov[a]][:, :3].astype(np.float64).mean(0) for a in range(flags.shape[0])]
+                           for r in runs])
+    ours_cls = np.stack([[(ind[m] * area[m, None]).sum(0) / area[m].sum() for m in classes] for ind in indirects])
+    dz = 0.0
+    for m in classes:
+        for d in directs:
+            for k in range(g["direct"].shape[0]):
+                diff = (g["direct"][k][m] - d[m]).astype(np.float64)
+                sd = diff.std(0)
+                ok = sd > 0
+                if ok.any():
+                    dz = max(dz, float(np.abs(diff.mean(0)[ok] / (sd[ok] / np.sqrt(diff.shape[0]))).max()))
+    # texels equal in every reference run and in every run of ours (as the
+    # plain gather's check: on faces pressed flat against another face a
+    # grazing ray may meet the coplanar face, which varies between runs)
+    det_ref = g["det_mask"]
+    ours_same = np.ones_like(det_ref)
+    for r in runs[1:]:
+        ours_same &= np.all(r[..., :3] == runs[0][..., :3], axis=-1)
+    keep = ours_same[det_ref]
+    det = det_ref & ours_same
+    ours_det = runs[0][..., :3][det].astype(np.float64)
+    ref_det = g["det_rgb"].astype(np.float64)[keep]
+    det_rel = float((np.abs(ours_det - ref_det) / np.maximum(np.abs(ref_det), 1e-30)).max()) if det.any() else 0.0
+    alpha = all(np.array_equal(r[..., 3], flags.astype(np.float32) / np.float32(255)) for r in runs)
+    return {"atlas": _within(ours_means, g["atlas_means"].astype(np.float64), BAKE_ATLAS_ALLOW),
+            "cls": _within(ours_cls, g["class_indirect"].astype(np.float64), BAKE_CLASS_ALLOW),
+            "direct_z": dz, "det_n": int(det.sum()), "det_rel": det_rel, "alpha": alpha}
+
+
+def reference_bake_ok(s: dict, det_rel: float = 0.0) -> bool:
+    return (s["alpha"] and float(s["atlas"].max()) < 1 and float(s["cls"].max()) < 1 and s["direct_z"] < GATHER_Z_MEAN
+            and s["det_rel"] <= det_rel)

@@ -7,7 +7,8 @@ import numpy as np
 
 from lightsprintsdk_gb300 import scenes
 from oracle import orc
-from tests.helpers import GATHER_Z_MEAN, load_golden, md5, reference_gather_ok, reference_gather_stats
+from tests.helpers import (GATHER_Z_MEAN, load_golden, md5, reference_bake_ok, reference_bake_stats,
+                           reference_gather_ok, reference_gather_stats)
 
 
 def test_hash_matches_python_generators():
@@ -129,3 +130,68 @@ def test_reference_gather_comparison_detects_missing_bounces():
     for a, s in zip(g["atlases"], reference_gather_stats(g, o1, o2)):
         assert not reference_gather_ok(s), (int(a), s)
         assert s["z_mean"] > GATHER_Z_MEAN, (int(a), s)
+
+
+def _room_bake_runs(g, seeds=(11, 12, 13), max_depth: int = 20):
+    gs = scenes.gather_room()
+    atl = [int(a) for a in g["atlases"]]
+    S = gs.size * gs.size
+    flags = orc.gather_flags(gs, atl)
+    subs = []
+    for a in atl:
+        ids = np.nonzero(gs.tri_atlas == a)[0]
+        subs.append(orc.enumerate_atlas(gs.uv[ids], ids, gs.size))
+    runs, directs, indirects = [], [], []
+    for seed in seeds:
+        G = orc.GatherOracle(gs, quality=int(g["quality"]), max_depth=max_depth, seed=seed, flags=flags)
+        d, ind, _ = G.bake_solver()
+        runs.append(np.stack([G.gather((a * S + np.arange(S)).astype(np.uint64), off, st, 0)
+                              .reshape(gs.size, gs.size, 4) for a, (off, st) in zip(atl, subs)]))
+        directs.append(d)
+        indirects.append(ind)
+    return gs, runs, directs, indirects
+
+
+def test_oracle_bake_matches_the_reference_bake():
+    """The oracle's restatement of the default bake (first gather per
+    triangle, radiosity, final gather reading the solver at the first hit)
+    against the reference's own updateLightmaps with its radiosity solver
+    (tests/golden/bake_ref.npz: four realizations, quality 256, four atlases
+    of the small room).  The texels no random number changes are bit-exact;
+    the per-triangle first gather agrees statistically; atlas means and the
+    class indirect agree within both sides' scatter plus 0.5 % and 1 % (the
+    reference stops propagating at its accuracy target, ours converges)."""
+    g = load_golden("bake_ref.npz")
+    gs, runs, directs, indirects = _room_bake_runs(g)
+    assert md5(gs.scene.vertices, gs.scene.indices, gs.albedo, gs.uv, gs.tri_atlas) == str(g["scene_md5"])
+    s = reference_bake_stats(g, gs, runs, directs, indirects)
+    assert reference_bake_ok(s, det_rel=0.0), s
+    assert s["det_n"] > 2000, s
+
+
+def test_reference_bake_comparison_detects_a_missing_solver():
+    """The comparison's power: the plain N-bounce gather cut at one bounce
+    (direct light at the first hit, no radiosity) in place of the solver
+    fails it."""
+    g = load_golden("bake_ref.npz")
+    gs = scenes.gather_room()
+    atl = [int(a) for a in g["atlases"]]
+    S = gs.size * gs.size
+    flags = orc.gather_flags(gs, atl)
+    runs, directs, indirects = [], [], []
+    for seed in (11, 12, 13):
+        G = orc.GatherOracle(gs, quality=int(g["quality"]), max_depth=0, seed=seed, flags=flags)
+        d, ind, _ = G.bake_solver()
+        G.s.solver_direct = None
+        G.s.solver_corner = None
+        out = []
+        for a in atl:
+            ids = np.nonzero(gs.tri_atlas == a)[0]
+            off, st = orc.enumerate_atlas(gs.uv[ids], ids, gs.size)
+            out.append(G.gather((a * S + np.arange(S)).astype(np.uint64), off, st, 0).reshape(gs.size, gs.size, 4))
+        runs.append(np.stack(out))
+        directs.append(d)
+        indirects.append(ind)
+    s = reference_bake_stats(g, gs, runs, directs, indirects)
+    assert not reference_bake_ok(s), s
+    assert float(s["atlas"].max()) > 2, s
