@@ -180,6 +180,10 @@ RRG_API int rrg_lightmapper_bake_solver(rrg_lightmapper* lm, const rrg_gather_pa
  * Synchronous. */
 RRG_API int rrg_lightmapper_copy_solver(const rrg_lightmapper* lm, float* direct_host, float* indirect_host,
                                         float* corner_host);
+/* The last bake's form-factor rays: ray j of triangle t at t * rays + j, the
+ * triangle whose front it hit, else 0xFFFFFFFF.  Returns their number (0
+ * before a bake); copies them when cap is large enough.  Synchronous. */
+RRG_API uint64_t rrg_lightmapper_copy_factor_hits(const rrg_lightmapper* lm, uint32_t* hits_host, uint64_t cap);
 
 /* Training records for a radiance cache (rrgpu_cache.h) from the gather's
  * own paths: from every `stride`-th covered texel, paths_per_texel plain

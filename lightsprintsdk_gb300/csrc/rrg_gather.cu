@@ -1239,6 +1239,7 @@ struct Lightmapper {
 	uint32_t ngroups = 0;
 	uint32_t* d_bake_hits = nullptr;    // triangles x rays
 	size_t bake_hits_cap = 0;
+	uint64_t bake_hits_used = 0;
 	float* d_bake_e = nullptr;          // E, E' (3 per triangle each), group values (3 per group)
 	const float* d_bake_final = nullptr;  // the converged E (one of the two above)
 	uint64_t lg_cap = 0;             // texels
@@ -1737,6 +1738,7 @@ static int bake_solver(Lightmapper* L, const rrg_gather_params* p, uint32_t k, u
 		RRG_CUDA(cudaMalloc(&L->d_bake_hits, nhits * sizeof(uint32_t)));
 		L->bake_hits_cap = nhits;
 	}
+	L->bake_hits_used = nhits;
 	const uint32_t qh = q.quality / 2 ? q.quality / 2 : 1;
 	const uint32_t rounds = qh / 10 + 1;
 	const int tgrid = (int)std::min<uint64_t>((nt + 127) / 128, (uint64_t)c->num_sms * 16);
@@ -2016,6 +2018,16 @@ int rrg_lightmapper_copy_solver(const rrg_lightmapper* h, float* direct_host, fl
 	if (corner_host)
 		RRG_CUDA(cudaMemcpy(corner_host, L->d_solver_corner, 9 * nt * sizeof(float), cudaMemcpyDeviceToHost));
 	return RRG_OK;
+}
+
+uint64_t rrg_lightmapper_copy_factor_hits(const rrg_lightmapper* h, uint32_t* hits_host, uint64_t cap) {
+	const Lightmapper* L = reinterpret_cast<const Lightmapper*>(h);
+	if (!L || !L->d_bake_hits || !L->d_bake_final) return 0;
+	if (cudaSetDevice(L->c->device) != cudaSuccess) return 0;
+	const uint64_t n = L->bake_hits_used;
+	if (hits_host && cap >= n && cudaMemcpy(hits_host, L->d_bake_hits, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return 0;
+	return n;
 }
 
 int rrg_lightmap_train_samples(rrg_lightmapper* h, const rrg_gather_params* p, uint32_t stride,

@@ -59,6 +59,8 @@ def _lib():
         L.rrg_lightmapper_copy_flags.argtypes = [P, P]
         L.rrg_lightmapper_bake_solver.argtypes = [P, C.POINTER(GatherParams), U, U, P]
         L.rrg_lightmapper_copy_solver.argtypes = [P, P, P, P]
+        L.rrg_lightmapper_copy_factor_hits.argtypes = [P, P, C.c_uint64]
+        L.rrg_lightmapper_copy_factor_hits.restype = C.c_uint64
         L.rrg_lightmap_filter.argtypes = [P, C.POINTER(FilterParams), C.c_uint32, C.c_uint32, P, P]
         L.rrg_lightmapper_seams.argtypes = [P]
         L.rrg_lightmapper_seams.restype = C.c_uint64
@@ -212,6 +214,14 @@ class RRLightmapper:
         if r:
             raise col.RRGError(r, "rrg_lightmapper_copy_solver")
         return d, i, c
+
+    def factor_hits(self) -> np.ndarray:
+        """The last bake's form-factor ray hits (triangles x rays) uint32."""
+        n = int(_lib().rrg_lightmapper_copy_factor_hits(self._h, None, 0))
+        out = np.zeros(n, np.uint32)
+        if n and int(_lib().rrg_lightmapper_copy_factor_hits(self._h, out.ctypes.data, n)) != n:
+            raise col.RRGError(1, "rrg_lightmapper_copy_factor_hits")
+        return out
 
     def flags(self) -> np.ndarray:
         """TexelFlags of every texel (ntexels,) uint8."""

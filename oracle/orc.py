@@ -277,6 +277,7 @@ class GatherOracle:
         L.orc_bake_direct(self.fo.h, C.byref(sc), threads, _ptr(direct))
         hits = np.zeros(T * k, np.uint32)
         L.orc_bake_factors(self.fo.h, C.byref(sc), k, threads, _ptr(hits))
+        self.factor_hits = hits
         indirect = np.zeros((T, 3), np.float32)
         L.orc_bake_propagate(C.byref(sc), _ptr(direct), _ptr(hits), k, iterations, _ptr(indirect))
         group = np.zeros(3 * T, np.uint32)
