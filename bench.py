@@ -421,6 +421,45 @@ def filter_timing(L, out, natl, stream, sp, gs, cpu: bool) -> dict:
     return res
 
 
+def bake_timing(L, gs, natl, stream, sp, quality: int = 64, iterations: int = 32) -> dict:
+    """The default bake's radiosity solver (rrg_lightmapper_bake_solver: first
+    gather per triangle at half quality, `quality` form-factor rays per
+    triangle, Jacobi propagation, corner smoothing) on the whole scene, then
+    the final gather of every atlas reading it at the first hit.  The first
+    solve also stitches the corners on the host; the second is timed with
+    CUDA events, and so is the gather."""
+    import torch
+    from lightsprintsdk_gb300 import lightmap as lm
+    p = lm.make_params(gs.lights, quality=quality, max_depth=8)
+    t0 = time.perf_counter()
+    L.bake_solver(p, quality, iterations, sp)
+    torch.cuda.synchronize()
+    first_s = time.perf_counter() - t0
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    L.bake_solver(p, quality, iterations, sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    solve_ms = e0.elapsed_time(e1)
+    n = natl * gs.size * gs.size
+    work = torch.empty((n, 4), dtype=torch.float32, device=f"cuda:{torch.cuda.current_device()}")
+    ps = lm.make_params(gs.lights, quality=quality, max_depth=8, mode=lm.GATHER_SOLVER)
+    L.gather_device(ps, 0, min(n, 4 * gs.size * gs.size), work.data_ptr(), sp)
+    e0.record(stream)
+    L.gather_device(ps, 0, n, work.data_ptr(), sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    L.check(sp)
+    gather_ms = e0.elapsed_time(e1)
+    T = int(gs.scene.ntri)
+    del work
+    return {"quality": quality, "rays_per_triangle": quality, "iterations": iterations, "triangles": T,
+            "solver_ms": solve_ms, "first_call_s_with_stitching": first_s,
+            "factor_rays_per_s": T * quality / (solve_ms * 1e-3),
+            "solver_gather_ms": gather_ms, "solver_gather_texels_per_s": n / (gather_ms * 1e-3)}
+
+
 def run_gather(args, world, rank, local):
     """Config 2: plain 8-bounce lightmap gather, 64 rays per texel, 256 atlases
     of 256 x 256 texels on the interior scene."""
@@ -496,6 +535,7 @@ def run_gather(args, world, rank, local):
         extra.update(learned_errors(L, gs, params, out, natl, stream, sp))
     elif rank == 0:
         extra["filters"] = filter_timing(L, out, natl, stream, sp, gs, not args.no_cpu_baseline)
+        extra["bake"] = bake_timing(L, gs, natl, stream, sp)
     if rank == 0:
         metric = "learned lightmap texels/s" if learned else "plain lightmap texels/s"
         line = {"metric": metric, "value": world * n / (ms * 1e-3), "unit": "texels/s",
