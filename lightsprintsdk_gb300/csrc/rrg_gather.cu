@@ -1237,9 +1237,10 @@ struct Lightmapper {
 	uint32_t* d_group_corner = nullptr; // weighted corners, group by group, corner order
 	float* d_corner_weight = nullptr;   // 3 per triangle
 	uint32_t ngroups = 0;
-	uint32_t* d_bake_hits = nullptr;    // triangles x rays
+	uint32_t* d_bake_hits = nullptr;    // rays x triangles (ray j of triangle t at j * triangles + t)
 	size_t bake_hits_cap = 0;
 	uint64_t bake_hits_used = 0;
+	uint32_t bake_k = 0;
 	float* d_bake_e = nullptr;          // E, E' (3 per triangle each), group values (3 per group)
 	const float* d_bake_final = nullptr;  // the converged E (one of the two above)
 	uint64_t lg_cap = 0;             // texels
@@ -1469,8 +1470,13 @@ __global__ void __launch_bounds__(128, 8) k_bake_factors(GatherScene g, uint32_t
                                                          uint32_t* __restrict__ hits, uint32_t* status) {
 	bool overflow = false;
 	const uint64_t total = (uint64_t)nt * k;
-	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-		const uint32_t t = (uint32_t)(i / k);
+	// thread q traces ray j = q / nt of triangle t = q % nt (neighbouring
+	// threads: neighbouring triangles, so the ray-major hit writes coalesce);
+	// the ray's sample streams are indexed by i = t * k + j
+	for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < total; q += (uint64_t)gridDim.x * blockDim.x) {
+		const uint32_t j = (uint32_t)(q / nt);
+		const uint32_t t = (uint32_t)(q - (uint64_t)j * nt);
+		const uint64_t i = (uint64_t)t * k + j;
 		V3 v0, s1, s2;
 		const V3 n = tri_normal(g, t, v0, s1, s2);
 		V3 tg, bt;
@@ -1501,7 +1507,7 @@ __global__ void __launch_bounds__(128, 8) k_bake_factors(GatherScene g, uint32_t
 			const V3 alb = ld3(g.albedo + 3 * (size_t)tri);
 			if (front_facing(r, a, b, c) && __fadd_rn(__fadd_rn(alb.x, alb.y), alb.z) > 0.01f) h = tri;
 		}
-		hits[i] = h;
+		hits[q] = h;   // ray-major (q = j * nt + t): the iteration reads them coalesced
 	}
 	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
 }
@@ -1513,9 +1519,8 @@ __global__ void __launch_bounds__(128) k_bake_iterate(const float* __restrict__ 
                                                       float inv, const float* __restrict__ e, float* __restrict__ e2) {
 	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
 		V3 acc = mk(0.f, 0.f, 0.f);
-		const uint32_t* hp = hits + (size_t)t * k;
 		for (uint32_t j = 0; j < k; j++) {
-			const uint32_t h = hp[j];
+			const uint32_t h = hits[(size_t)j * nt + t];
 			if (h == 0xFFFFFFFFu) continue;
 			acc = add(acc, mulv(ld3(albedo + 3 * (size_t)h), ld3(e + 3 * (size_t)h)));
 		}
@@ -1618,14 +1623,20 @@ static uint32_t bake_stitch(const std::vector<float>& xyz, const std::vector<uin
 	rep.reserve(nc);
 	group.assign(nc, 0);
 	const float min_dot = cosf(0.01f);
+	// The reference scans, newest first, every unique vertex with the same x
+	// (quadratic on axis-aligned planes).  With weld distance 0 only an
+	// identical position can merge, and after the sort identical positions
+	// are contiguous, so the scan over the unique vertices of the current
+	// position finds the same first match.
+	uint32_t block = 0;   // first unique vertex of the current position
 	for (uint32_t s = 0; s < nc; s++) {
 		const Key& d = k[s];
+		if (s == 0 || d.p[0] != k[s - 1].p[0] || d.p[1] != k[s - 1].p[1] || d.p[2] != k[s - 1].p[2])
+			block = (uint32_t)rep.size();
 		uint32_t g = 0xFFFFFFFFu;
-		for (uint32_t u = (uint32_t)rep.size(); u--;) {
+		for (uint32_t u = (uint32_t)rep.size(); u-- > block;) {
 			const Key& r = k[rep[u]];
-			if (!(fabsf(d.p[0] - r.p[0]) <= 0.0f)) break;
-			if (fabsf(d.p[1] - r.p[1]) <= 0.0f && fabsf(d.p[2] - r.p[2]) <= 0.0f &&
-			    d.n[0] * r.n[0] + d.n[1] * r.n[1] + d.n[2] * r.n[2] >= min_dot) {
+			if (d.n[0] * r.n[0] + d.n[1] * r.n[1] + d.n[2] * r.n[2] >= min_dot) {
 				g = u;
 				break;
 			}
@@ -1739,6 +1750,7 @@ static int bake_solver(Lightmapper* L, const rrg_gather_params* p, uint32_t k, u
 		L->bake_hits_cap = nhits;
 	}
 	L->bake_hits_used = nhits;
+	L->bake_k = k;
 	const uint32_t qh = q.quality / 2 ? q.quality / 2 : 1;
 	const uint32_t rounds = qh / 10 + 1;
 	const int tgrid = (int)std::min<uint64_t>((nt + 127) / 128, (uint64_t)c->num_sms * 16);
@@ -2025,8 +2037,13 @@ uint64_t rrg_lightmapper_copy_factor_hits(const rrg_lightmapper* h, uint32_t* hi
 	if (!L || !L->d_bake_hits || !L->d_bake_final) return 0;
 	if (cudaSetDevice(L->c->device) != cudaSuccess) return 0;
 	const uint64_t n = L->bake_hits_used;
-	if (hits_host && cap >= n && cudaMemcpy(hits_host, L->d_bake_hits, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
-		return 0;
+	if (hits_host && cap >= n) {   // to triangle-major order
+		std::vector<uint32_t> h(n);
+		if (cudaMemcpy(h.data(), L->d_bake_hits, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+		const uint64_t k = L->bake_k, nt = k ? n / k : 0;
+		for (uint64_t j = 0; j < k; j++)
+			for (uint64_t t = 0; t < nt; t++) hits_host[t * k + j] = h[j * nt + t];
+	}
 	return n;
 }
 

@@ -364,3 +364,25 @@ def test_gpu_bake_matches_the_reference_bake():
     print(s)
     assert reference_bake_ok(s, det_rel=1e-6), s
     assert s["det_n"] > 2000, s
+
+
+def test_solver_mode_needs_a_bake():
+    """A gather that asks for the solver before any bake is refused, and so
+    is the learned gather with the solver flag."""
+    import torch
+    gs = scenes.gather_room()
+    c = col.RRCollider.create(gs.scene.vertices, gs.scene.indices)
+    L = lm.RRLightmapper.from_scene(c, gs)
+    out = torch.empty((64, 4), dtype=torch.float32, device="cuda")
+    ps = lm.make_params(gs.lights, quality=16, mode=lm.GATHER_SOLVER)
+    with pytest.raises(col.RRGError):
+        L.gather_device(ps, 0, 64, out.data_ptr())
+    with pytest.raises(col.RRGError):
+        L.solver()
+    L.bake_solver(lm.make_params(gs.lights, quality=16), 16, 4)
+    L.gather_device(ps, 0, 64, out.data_ptr())
+    torch.cuda.synchronize()
+    L.check()
+    bad = lm.make_params(gs.lights, quality=16, mode=lm.GATHER_SOLVER | 8)
+    with pytest.raises(col.RRGError):
+        L.gather_device(bad, 0, 64, out.data_ptr())
