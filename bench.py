@@ -55,6 +55,17 @@ WORKLOAD_DESC = {
 }
 
 
+def max_over_ranks(x: float, world: int, device) -> float:
+    """The largest x over the ranks of the job (each rank times the same
+    replica workload; the job ends when the slowest one does)."""
+    if world <= 1:
+        return x
+    import torch
+    tt = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -506,6 +517,9 @@ def run_gather(args, world, rank, local):
     clk.wait_first_sample()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
     clk.mark_start()
     lc0 = col.launch_count()
     e0.record(stream)
@@ -517,7 +531,7 @@ def run_gather(args, world, rank, local):
     clk.mark_end()
     clk.__exit__()
     L.check(sp)
-    ms = e0.elapsed_time(e1) / steps
+    ms = max_over_ranks(e0.elapsed_time(e1) / steps, world, f"cuda:{local}")
     covered = int((out[:, 3] > 0).sum().item())
     if learned and rank == 0:
         # the plain gather of the same texels, timed the same way, for the ratio
@@ -599,11 +613,7 @@ def run_batch(args, world, rank, local):
     torch.cuda.synchronize()
     clk.mark_end()
     clk.__exit__()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        tt = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
     assert b.status(sp) == 0, "traversal reported an error"
     hit_ratio = float((hits[:, 1].view(torch.int32) != -1).float().mean().item())
     if rank == 0:
@@ -705,11 +715,7 @@ def main():
     torch.cuda.synchronize()
     clk.mark_end()
     clk.__exit__()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        tt = torch.tensor([ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, f"cuda:{local}")
     assert c.status(sp) == 0, "traversal reported an error"
     hits_total = int((d_hits[:, 1].view(torch.int32) != -1).sum().item())
 
@@ -725,11 +731,7 @@ def main():
     for _ in range(e2e_steps):
         st = L.rrg_intersect_host(c.handle, h_rays.data_ptr(), n, h_hits.data_ptr(), sp)
         assert st == 0
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    if world > 1:
-        tt = torch.tensor([e2e_s], device=f"cuda:{local}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world, f"cuda:{local}")
 
     if rank == 0:
         peak, peak_src = load_peaks()
