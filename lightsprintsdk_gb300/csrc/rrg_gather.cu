@@ -1242,6 +1242,7 @@ struct Lightmapper {
 	uint64_t bake_hits_used = 0;
 	uint32_t bake_k = 0;
 	float* d_bake_e = nullptr;          // E, E' (3 per triangle each), group values (3 per group)
+	float4* d_bake_re = nullptr;        // albedo * E, two per triangle (ping-pong)
 	const float* d_bake_final = nullptr;  // the converged E (one of the two above)
 	uint64_t lg_cap = 0;             // texels
 	uint64_t lg_cap_samples = 0;     // texels x samples per texel
@@ -1271,6 +1272,7 @@ static void free_lm(Lightmapper* L) {
 	cudaFree(L->d_corner_weight);
 	cudaFree(L->d_bake_hits);
 	cudaFree(L->d_bake_e);
+	cudaFree(L->d_bake_re);
 	delete L;
 }
 
@@ -1513,21 +1515,36 @@ __global__ void __launch_bounds__(128, 8) k_bake_factors(GatherScene g, uint32_t
 }
 
 // One Jacobi step of E_j = D_j + (1/k) sum over j's factor hits h of
-// albedo_h * E_h (the flux balance of rrcore.cpp:1052-1086 in gathering form)
+// albedo_h * E_h (the flux balance of rrcore.cpp:1052-1086 in gathering
+// form).  re holds albedo * E of every triangle (one 16-byte load per hit);
+// the step writes E' and albedo * E' for the next.
 __global__ void __launch_bounds__(128) k_bake_iterate(const float* __restrict__ direct, const float* __restrict__ albedo,
                                                       const uint32_t* __restrict__ hits, uint32_t nt, uint32_t k,
-                                                      float inv, const float* __restrict__ e, float* __restrict__ e2) {
+                                                      float inv, const float4* __restrict__ re,
+                                                      float* __restrict__ e2, float4* __restrict__ re2) {
 	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
 		V3 acc = mk(0.f, 0.f, 0.f);
 		for (uint32_t j = 0; j < k; j++) {
 			const uint32_t h = hits[(size_t)j * nt + t];
 			if (h == 0xFFFFFFFFu) continue;
-			acc = add(acc, mulv(ld3(albedo + 3 * (size_t)h), ld3(e + 3 * (size_t)h)));
+			const float4 r = re[h];
+			acc = add(acc, mk(r.x, r.y, r.z));
 		}
 		const V3 r = add(ld3(direct + 3 * (size_t)t), mul(acc, inv));
 		e2[3 * (size_t)t] = r.x;
 		e2[3 * (size_t)t + 1] = r.y;
 		e2[3 * (size_t)t + 2] = r.z;
+		const V3 q = mulv(ld3(albedo + 3 * (size_t)t), r);
+		re2[t] = make_float4(q.x, q.y, q.z, 0.f);
+	}
+}
+
+// albedo * D: the propagation's first source term
+__global__ void k_bake_re_init(const float* __restrict__ direct, const float* __restrict__ albedo, uint32_t nt,
+                               float4* __restrict__ re) {
+	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+		const V3 q = mulv(ld3(albedo + 3 * (size_t)t), ld3(direct + 3 * (size_t)t));
+		re[t] = make_float4(q.x, q.y, q.z, 0.f);
 	}
 }
 
@@ -1733,13 +1750,15 @@ static int bake_solver(Lightmapper* L, const rrg_gather_params* p, uint32_t k, u
 		L->ngroups = ng;
 	}
 	if (!L->d_solver_direct) {
-		DevBuf dd, dc, de;
+		DevBuf dd, dc, de, dr;
 		RRG_CUDA(cudaMalloc(&dd.p, 3 * (size_t)nt * sizeof(float)));
 		RRG_CUDA(cudaMalloc(&dc.p, 9 * (size_t)nt * sizeof(float)));
 		RRG_CUDA(cudaMalloc(&de.p, (6 * (size_t)nt + 3 * (size_t)L->ngroups) * sizeof(float)));
+		RRG_CUDA(cudaMalloc(&dr.p, 2 * (size_t)nt * sizeof(float4)));
 		L->d_solver_direct = (float*)dd.release();
 		L->d_solver_corner = (float*)dc.release();
 		L->d_bake_e = (float*)de.release();
+		L->d_bake_re = (float4*)dr.release();
 	}
 	const size_t nhits = (size_t)nt * k;
 	if (nhits > L->bake_hits_cap) {
@@ -1762,11 +1781,16 @@ static int bake_solver(Lightmapper* L, const rrg_gather_params* p, uint32_t k, u
 	float* e = L->d_bake_e;
 	float* e2 = e + 3 * (size_t)nt;
 	float* gval = e + 6 * (size_t)nt;
+	float4* re = L->d_bake_re;
+	float4* re2 = re + nt;
 	RRG_CUDA(cudaMemcpyAsync(e, L->d_solver_direct, 3 * (size_t)nt * sizeof(float), cudaMemcpyDeviceToDevice, s));
+	rrg::note_launch(), k_bake_re_init<<<tgrid, 128, 0, s>>>(L->d_solver_direct, L->d_albedo, nt, re);
 	const float inv = 1.0f / (float)k;
 	for (uint32_t it = 0; it < iterations; it++) {
-		rrg::note_launch(), k_bake_iterate<<<tgrid, 128, 0, s>>>(L->d_solver_direct, L->d_albedo, L->d_bake_hits, nt, k, inv, e, e2);
+		rrg::note_launch(), k_bake_iterate<<<tgrid, 128, 0, s>>>(L->d_solver_direct, L->d_albedo, L->d_bake_hits, nt, k,
+		                                                         inv, re, e2, re2);
 		std::swap(e, e2);
+		std::swap(re, re2);
 	}
 	RRG_CUDA(cudaGetLastError());
 	const int ggrid = (int)std::min<uint64_t>((L->ngroups + 127) / 128 + 1, (uint64_t)c->num_sms * 16);
