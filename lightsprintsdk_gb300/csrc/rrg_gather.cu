@@ -1238,6 +1238,7 @@ struct Lightmapper {
 	float* d_corner_weight = nullptr;   // 3 per triangle
 	uint32_t ngroups = 0;
 	uint32_t* d_bake_hits = nullptr;    // rays x triangles (ray j of triangle t at j * triangles + t)
+	uint32_t* d_bake_hits_tm = nullptr; // the same, triangle-major, as the rays write them
 	size_t bake_hits_cap = 0;
 	uint64_t bake_hits_used = 0;
 	uint32_t bake_k = 0;
@@ -1271,6 +1272,7 @@ static void free_lm(Lightmapper* L) {
 	cudaFree(L->d_group_corner);
 	cudaFree(L->d_corner_weight);
 	cudaFree(L->d_bake_hits);
+	cudaFree(L->d_bake_hits_tm);
 	cudaFree(L->d_bake_e);
 	cudaFree(L->d_bake_re);
 	delete L;
@@ -1472,13 +1474,11 @@ __global__ void __launch_bounds__(128, 8) k_bake_factors(GatherScene g, uint32_t
                                                          uint32_t* __restrict__ hits, uint32_t* status) {
 	bool overflow = false;
 	const uint64_t total = (uint64_t)nt * k;
-	// thread q traces ray j = q / nt of triangle t = q % nt (neighbouring
-	// threads: neighbouring triangles, so the ray-major hit writes coalesce);
-	// the ray's sample streams are indexed by i = t * k + j
-	for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < total; q += (uint64_t)gridDim.x * blockDim.x) {
-		const uint32_t j = (uint32_t)(q / nt);
-		const uint32_t t = (uint32_t)(q - (uint64_t)j * nt);
-		const uint64_t i = (uint64_t)t * k + j;
+	// thread i traces ray j = i % k of triangle t = i / k (a warp's rays leave
+	// one triangle: coherent traversal); hits are written triangle-major and
+	// transposed for the iteration by k_bake_transpose
+	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+		const uint32_t t = (uint32_t)(i / k);
 		V3 v0, s1, s2;
 		const V3 n = tri_normal(g, t, v0, s1, s2);
 		V3 tg, bt;
@@ -1509,9 +1509,25 @@ __global__ void __launch_bounds__(128, 8) k_bake_factors(GatherScene g, uint32_t
 			const V3 alb = ld3(g.albedo + 3 * (size_t)tri);
 			if (front_facing(r, a, b, c) && __fadd_rn(__fadd_rn(alb.x, alb.y), alb.z) > 0.01f) h = tri;
 		}
-		hits[q] = h;   // ray-major (q = j * nt + t): the iteration reads them coalesced
+		hits[i] = h;
 	}
 	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// Triangle-major hits (t * k + j) to ray-major (j * nt + t) through a 32 x 32
+// tile in shared memory, both sides coalesced.  Block 32 x 8.
+__global__ void k_bake_transpose(const uint32_t* __restrict__ in, uint32_t nt, uint32_t k, uint32_t* __restrict__ out) {
+	__shared__ uint32_t tile[32][33];
+	const uint32_t t0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+	for (uint32_t y = threadIdx.y; y < 32; y += 8) {
+		const uint32_t t = t0 + y, j = j0 + threadIdx.x;
+		if (t < nt && j < k) tile[y][threadIdx.x] = in[(size_t)t * k + j];
+	}
+	__syncthreads();
+	for (uint32_t y = threadIdx.y; y < 32; y += 8) {
+		const uint32_t j = j0 + y, t = t0 + threadIdx.x;
+		if (t < nt && j < k) out[(size_t)j * nt + t] = tile[threadIdx.x][y];
+	}
 }
 
 // One Jacobi step of E_j = D_j + (1/k) sum over j's factor hits h of
@@ -1763,9 +1779,11 @@ static int bake_solver(Lightmapper* L, const rrg_gather_params* p, uint32_t k, u
 	const size_t nhits = (size_t)nt * k;
 	if (nhits > L->bake_hits_cap) {
 		cudaFree(L->d_bake_hits);
-		L->d_bake_hits = nullptr;
+		cudaFree(L->d_bake_hits_tm);
+		L->d_bake_hits = L->d_bake_hits_tm = nullptr;
 		L->bake_hits_cap = 0;
 		RRG_CUDA(cudaMalloc(&L->d_bake_hits, nhits * sizeof(uint32_t)));
+		RRG_CUDA(cudaMalloc(&L->d_bake_hits_tm, nhits * sizeof(uint32_t)));
 		L->bake_hits_cap = nhits;
 	}
 	L->bake_hits_used = nhits;
@@ -1776,7 +1794,10 @@ static int bake_solver(Lightmapper* L, const rrg_gather_params* p, uint32_t k, u
 	rrg::note_launch(), k_bake_direct<<<tgrid, 128, 0, s>>>(g, nt, rounds, L->d_solver_direct, L->d_status);
 	RRG_CUDA(cudaGetLastError());
 	const int fgrid = (int)std::min<uint64_t>((nhits + 127) / 128, (uint64_t)c->num_sms * 64);
-	rrg::note_launch(), k_bake_factors<<<fgrid, 128, 0, s>>>(g, nt, k, L->d_bake_hits, L->d_status);
+	rrg::note_launch(), k_bake_factors<<<fgrid, 128, 0, s>>>(g, nt, k, L->d_bake_hits_tm, L->d_status);
+	RRG_CUDA(cudaGetLastError());
+	rrg::note_launch(), k_bake_transpose<<<dim3((nt + 31) / 32, (k + 31) / 32), dim3(32, 8), 0, s>>>(L->d_bake_hits_tm, nt, k,
+	                                                                                              L->d_bake_hits);
 	RRG_CUDA(cudaGetLastError());
 	float* e = L->d_bake_e;
 	float* e2 = e + 3 * (size_t)nt;
@@ -2061,13 +2082,8 @@ uint64_t rrg_lightmapper_copy_factor_hits(const rrg_lightmapper* h, uint32_t* hi
 	if (!L || !L->d_bake_hits || !L->d_bake_final) return 0;
 	if (cudaSetDevice(L->c->device) != cudaSuccess) return 0;
 	const uint64_t n = L->bake_hits_used;
-	if (hits_host && cap >= n) {   // to triangle-major order
-		std::vector<uint32_t> h(n);
-		if (cudaMemcpy(h.data(), L->d_bake_hits, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
-		const uint64_t k = L->bake_k, nt = k ? n / k : 0;
-		for (uint64_t j = 0; j < k; j++)
-			for (uint64_t t = 0; t < nt; t++) hits_host[t * k + j] = h[j * nt + t];
-	}
+	if (hits_host && cap >= n && cudaMemcpy(hits_host, L->d_bake_hits_tm, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return 0;
 	return n;
 }
 
