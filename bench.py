@@ -15,10 +15,11 @@ device-resident rays (1 GiB of rays, larger than L2, so no flush is needed);
 `e2e` times the C-ABI host call rrg_intersect_host: pinned host rays in,
 host hit records out, copies inside the timed region.
 
---impl reference times the reference collider's CPU algorithm on this machine's
-host cores: the C oracle (oracle/rr_oracle.c, a restatement of
-IT_BSP_FASTEST's arithmetic over its own BVH; the reference binary itself is
-built for x86-64 only in the container where the reference sources are).
+--impl reference times the reference's own collider on this machine's host
+cores: RRCollider::create(..., IT_BSP_FASTEST) and intersect() from the
+reference library, built from the reference sources on this host into
+oracle/_ref (the tree build is timed apart; the steps cover every ray when
+they fit in about 90 s).  The oracle port's rate is reported beside it.
 Multi-GPU: replicas only (each rank traces its own copy of the workload).
 """
 from __future__ import annotations
@@ -167,9 +168,42 @@ class ClockSampler:
                 "in_timed_region": bool(inside)}
 
 
+def ref_collider_rates(v, t, rays, budget_s: float = 20.0):
+    """The reference's own collider (RRCollider::create(..., IT_BSP_FASTEST),
+    built from its sources into oracle/_ref) timed in-process on this host:
+    its build, then intersect() over a sample of the rays in an OpenMP loop on
+    every core and on one core.  The sample on all cores is every k-th ray,
+    sized to about budget_s / 2 of work; one core gets a tenth of it."""
+    from oracle import refio
+    threads = os.cpu_count() or 1
+    R = refio.RefCollider(v, t, refio.IT_BSP_FASTEST)
+    probe = np.ascontiguousarray(rays[:: max(1, len(rays) // 262144)][:262144])
+    s, _ = R.trace(probe, 0, outputs=False)
+    rate = len(probe) / s
+    n_all = int(min(len(rays), max(262144, rate * budget_s / 2)))
+    sub = np.ascontiguousarray(rays[:: max(1, len(rays) // n_all)][:n_all])
+    s_all, _ = R.trace(sub, 0, outputs=False)
+    sub1 = np.ascontiguousarray(sub[:: 10])
+    s_one, _ = R.trace(sub1, 1, outputs=False)
+    out = {"all": len(sub) / s_all, "one": len(sub1) / s_one, "cores": threads, "build_s": R.build_s,
+           "memory": R.memory, "technique": R.technique, "n_all": len(sub), "n_one": len(sub1)}
+    R.close()
+    return out
+
+
 def cpu_baseline(v, t, rays, sample: int):
-    """The oracle port on all host cores over a bounded sample of the rays
-    (every (n/sample)-th ray, so both ray families are represented)."""
+    """The reference's own collider on this host's cores (oracle/_ref), on a
+    bounded sample; the oracle port (oracle/rr_oracle.c over its own BVH)
+    where the reference library was not built."""
+    from oracle import refio
+    if refio.ref_bench_available():
+        r = ref_collider_rates(v, t, rays)
+        return {"value": r["all"] / 1e9, "unit": "Grays/s", "cores": r["cores"], "kind": "reference",
+                "library": "LightsprintCore RRCollider IT_BSP_FASTEST (oracle/_ref, built from the reference "
+                           "sources on this host)",
+                "sample": f"{r['n_all']} of {len(rays)} rays (evenly spaced) on {r['cores']} threads; "
+                          f"{r['n_one']} on 1 thread; tree build {r['build_s']:.2f} s timed apart",
+                "one_core_value": r["one"] / 1e9, "build_s": r["build_s"], "memory_bytes": r["memory"]}
     from oracle import orc
     step = max(1, len(rays) // sample)
     sub = np.ascontiguousarray(rays[::step][:sample])
@@ -304,29 +338,53 @@ def run_reference(args, rank: int):
         print(json.dumps(line), flush=True)
         return
     v, t, rays = make_workload(args.workload)
-    sample = 2_000_000 if args.workload == "c1" else len(rays)
-    from oracle import orc
+    from oracle import refio
     threads = os.cpu_count() or 1
-    step = max(1, len(rays) // sample)
-    sub = np.ascontiguousarray(rays[::step][:sample])
-    O = orc.FastestOracle(v, t)
+    cfg = {"workload": WORKLOAD_DESC[args.workload], "parallelism": "cpu threads",
+           "rays_per_step": len(rays)}
+    if not refio.ref_bench_available():
+        print(json.dumps({"impl": "reference", "unavailable": "the reference library (oracle/_ref) was not built "
+                                                              "on this host"}), flush=True)
+        return
+    # RRCollider::create(..., IT_BSP_FASTEST) once (timed apart), then each
+    # step is intersect() over the step's rays in an OpenMP loop on every
+    # core (samples/BunnyBenchmark/BunnyBenchmark.cpp:66-106).  A step covers
+    # every ray of the workload when (steps + warmup) such steps fit in about
+    # 90 s at the rate a probe measures; otherwise it is an evenly spaced
+    # sample of that size, and the line reports the sample's own time.
+    R = refio.RefCollider(v, t, refio.IT_BSP_FASTEST)
+    probe = np.ascontiguousarray(rays[:: max(1, len(rays) // 262144)][:262144])
+    ps, _ = R.trace(probe, 0, outputs=False)
+    per_step = int(min(len(rays), max(262144, len(probe) / ps * 90.0 / max(1, args.steps + args.warmup))))
+    sub = rays if per_step >= len(rays) else np.ascontiguousarray(rays[:: max(1, len(rays) // per_step)][:per_step])
     for _ in range(args.warmup):
-        O.collide(sub[:65536], threads)
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        O.collide(sub, threads)
-        times.append(time.perf_counter() - t0)
+        R.trace(sub, 0, outputs=False)
+    times = [R.trace(sub, 0, outputs=False)[0] for _ in range(args.steps)]
     sec = sum(times) / len(times)
     val = len(sub) / sec / 1e9
+    # the oracle port (oracle/rr_oracle.c over its own BVH), for comparison
+    from oracle import orc
+    psub = np.ascontiguousarray(rays[:: max(1, len(rays) // 1_000_000)][:1_000_000])
+    O = orc.FastestOracle(v, t)
+    t0 = time.perf_counter()
+    O.collide(psub, threads)
+    port = len(psub) / (time.perf_counter() - t0) / 1e9
+    whole = len(sub) == len(rays)
     line = {"impl": "reference", "metric": "closest-hit Grays/s", "value": val, "unit": "Grays/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": sec * 1e3 * (len(rays) / len(sub)), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD_DESC[args.workload], "parallelism": "cpu threads"},
-            "cpu_baseline": {"value": val, "unit": "Grays/s", "cores": threads, "kind": "port",
-                             "sample": f"{len(sub)} of {len(rays)} rays per step (every {step}th)"},
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "config": cfg,
+            "cpu_baseline": {"value": val, "unit": "Grays/s", "cores": threads, "kind": "reference",
+                             "library": "LightsprintCore RRCollider IT_BSP_FASTEST (oracle/_ref, built from the "
+                                        "reference sources on this host)",
+                             "sample": ("every ray of the step" if whole else
+                                        f"{len(sub)} of {len(rays)} rays per step (evenly spaced); ms_per_step is "
+                                        f"the sample's own time"),
+                             "build_s": R.build_s, "memory_bytes": R.memory},
+            "port": {"value": port, "unit": "Grays/s", "cores": threads,
+                     "sample": f"oracle/rr_oracle.c over its own BVH, {len(psub)} rays"},
             "e2e": {"value": val, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    R.close()
     print(json.dumps(line), flush=True)
 
 
@@ -531,7 +589,8 @@ def run_gather(args, world, rank, local):
     clk.mark_end()
     clk.__exit__()
     L.check(sp)
-    ms = max_over_ranks(e0.elapsed_time(e1) / steps, world, f"cuda:{local}")
+    local_ms = e0.elapsed_time(e1) / steps
+    ms = max_over_ranks(local_ms, world, f"cuda:{local}")
     covered = int((out[:, 3] > 0).sum().item())
     if learned and rank == 0:
         # the plain gather of the same texels, timed the same way, for the ratio
@@ -543,7 +602,8 @@ def run_gather(args, world, rank, local):
         p1.record(stream)
         torch.cuda.synchronize()
         extra["plain_texels_per_s"] = n / (p0.elapsed_time(p1) * 1e-3)
-        extra["speedup_vs_plain"] = (n / (ms * 1e-3)) / extra["plain_texels_per_s"]
+        # both times from this rank: its own learned step and its own plain gather
+        extra["speedup_vs_plain"] = (n / (local_ms * 1e-3)) / extra["plain_texels_per_s"]
         del plain_out
     if learned:
         extra.update(learned_errors(L, gs, params, out, natl, stream, sp))

@@ -176,6 +176,22 @@ RRG_API int rrg_intersect_rrray(rrg_collider* c, void* rrrays_host, uint32_t n, 
  * went with (that ray may then be left unhit). */
 RRG_API int rrg_intersect_rrray_one(rrg_collider* c, void* rrray_host, uint8_t* hit_host);
 
+/* The next hit of one rr::RRRay after a hit that a collision handler
+ * rejected: the nearest hit (t, triangle) in [rayLengthMin, rayLengthMax]
+ * that comes strictly after (after_t, after_tri) in the order "t, then
+ * triangle index", where t is the distance of the watertight test (the
+ * order the closest hit uses; hitDistance itself is the reference's plane
+ * distance, which can differ from t in the last bits).  *t_out (may be NULL)
+ * receives that t, the key of the following call.  after_t = -INFINITY gives
+ * the closest hit.  Replaying a handler this way offers every hit of the ray
+ * once, nearest first, as IT_BSP colliders do (RRCollider.h:52-55; the
+ * handler loop of RRCollider/IntersectBspFast.cpp:513 and the sorted replay
+ * of RayHits::getHitOrdered, RRCollider/IntersectLinear.cpp:396-437).  Same
+ * threading, fields and status as rrg_intersect_rrray_one; after_t NaN is
+ * RRG_ERR_INVALID. */
+RRG_API int rrg_intersect_rrray_one_after(rrg_collider* c, void* rrray_host, float after_t, uint32_t after_tri,
+                                          float* t_out, uint8_t* hit_host);
+
 /* Batches traced by rrg_intersect_rrray_one so far and the rays in them. */
 RRG_API int rrg_collider_combined(const rrg_collider* c, uint64_t* batches, uint64_t* rays);
 
@@ -196,9 +212,10 @@ RRG_API int rrg_intersect_rrray_device(rrg_collider* c, void* rrrays_dev, uint32
  * is already held (by a caching allocator such as PyTorch's, or by a bake
  * that sized its buffers to fill the GPU), where cudaMalloc would fail.
  *   - n > RRG_NOALLOC_MAX_RAYS returns RRG_ERR_TOO_LARGE and does nothing;
- *   - the first call on a device sets the scratch up (looks up the array's
- *     device address with that device current); make that first call before
- *     any stream capture begins;
+ *   - every call looks up the array's device address with the collider's
+ *     device current (so the call keeps working after cudaDeviceReset); the
+ *     first call on a device also loads the array's module there: make that
+ *     first call before any stream capture begins;
  *   - the status of the trace is returned directly (RRG_ERR_STACK on a
  *     traversal overflow); rrg_collider_status() does not see it;
  *   - every call on a device shares the one array, whichever collider or

@@ -20,8 +20,14 @@
 //     host threads at once are combined into one batch
 //     (rrg_intersect_rrray_one);
 //   * with a collision handler, hits are offered to collides() nearest first
-//     (the IT_BSP contract, RRCollider.h:52-55): after a rejection the query
-//     repeats beyond the rejected distance, up to kMaxHandlerRounds times;
+//     (the IT_BSP contract, RRCollider.h:52-55), each hit once: after a
+//     rejection the next query asks for the nearest hit after the rejected
+//     one in the order (watertight t, triangle index)
+//     (rrg_intersect_rrray_one_after), so hits at equal distances are all
+//     offered and none twice.  As in the reference's handler path
+//     (IntersectBspFast.cpp:500-515 with intersect_triangleSRLNP :189-252),
+//     hitDistance, hitTriangle, hitPoint2d, hitPlane and hitPoint3d are
+//     filled for every offered hit, hitFrontSide when FILL_SIDE asks;
 //   * RRObjects input (multi-object colliders) is not handled here: the
 //     builder returns nullptr and the reference falls back as it does for
 //     any failed builder (RRCollider.cpp:236-239).
@@ -38,7 +44,6 @@
 namespace rrgpu_plugin {
 
 enum { IT_GPU = 100 };
-constexpr unsigned kMaxHandlerRounds = 64;
 
 class GpuCollider : public rr::RRCollider {
 public:
@@ -53,7 +58,7 @@ public:
 		if (rrg_collider_create(xyz.data(), mesh->getNumVertices(), idx.data(), mesh->getNumTriangles(), nullptr,
 		                        &ab, 0, &h) != RRG_OK)
 			return nullptr;
-		return new GpuCollider(mesh, h);
+		return new GpuCollider(mesh, h, mesh->getNumTriangles());
 	}
 
 	virtual void update() override {
@@ -70,19 +75,24 @@ public:
 			return rrg_intersect_rrray_one(h_, &ray, &hit) == RRG_OK && hit;
 		}
 		handler->init(ray);
-		const float lenMin = ray.rayLengthMin;
-		const unsigned flags = ray.rayFlags;
-		ray.rayFlags = flags | rr::RRRay::FILL_DISTANCE | rr::RRRay::FILL_TRIANGLE;
-		for (unsigned round = 0; round < kMaxHandlerRounds; round++) {
+		const unsigned flags = ray.rayFlags;   // after init, which may add flags (RRCollider.h:45-47)
+		ray.rayFlags = flags | rr::RRRay::FILL_DISTANCE | rr::RRRay::FILL_TRIANGLE | rr::RRRay::FILL_POINT2D |
+		               rr::RRRay::FILL_PLANE | rr::RRRay::FILL_POINT3D;
+		float key_t = -INFINITY;
+		unsigned key_tri = 0;
+		// every round moves strictly forward in a finite order, so this ends
+		// after at most one round per triangle
+		for (unsigned round = 0; round <= nt_; round++) {
 			uint8_t hit = 0;
+			float t = 0;
 			ray.collisionHandler = nullptr;
-			int st = rrg_intersect_rrray_one(h_, &ray, &hit);
+			const int st = rrg_intersect_rrray_one_after(h_, &ray, key_t, key_tri, &t, &hit);
 			ray.collisionHandler = handler;
 			if (st != RRG_OK || !hit) break;
 			if (handler->collides(ray)) break;
-			ray.rayLengthMin = std::nextafter(ray.hitDistance, INFINITY);
+			key_t = t;
+			key_tri = ray.hitTriangle;
 		}
-		ray.rayLengthMin = lenMin;
 		ray.rayFlags = flags;
 		return handler->done();
 	}
@@ -98,7 +108,7 @@ public:
 	}
 
 private:
-	GpuCollider(const rr::RRMesh* m, rrg_collider* h) : mesh_(m), h_(h) {}
+	GpuCollider(const rr::RRMesh* m, rrg_collider* h, unsigned nt) : mesh_(m), h_(h), nt_(nt) {}
 	static void flatten(const rr::RRMesh* mesh, std::vector<float>& xyz, std::vector<unsigned>& idx) {
 		unsigned nv = mesh->getNumVertices(), nt = mesh->getNumTriangles();
 		xyz.resize(3 * (size_t)nv);
@@ -120,6 +130,7 @@ private:
 	}
 	const rr::RRMesh* mesh_;
 	rrg_collider* h_;
+	unsigned nt_;
 };
 
 // RRCollider::create registers the built-in builders only while its registry

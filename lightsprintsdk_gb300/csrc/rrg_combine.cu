@@ -18,6 +18,7 @@
 // at most kSlots small batches of one collider are on the GPU together.
 #include "rrg_internal.cuh"
 
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <mutex>
@@ -33,12 +34,16 @@ struct Request {
 	uint8_t* hit;     // optional
 	int status;
 	bool done;
+	float key_t;      // only hits after (key_t, key_tri) in (t, triangle) order;
+	uint32_t key_tri; // key_t = -inf: every hit
+	float* t_out;     // optional: the hit's watertight t
 };
 
 constexpr size_t kRecBytes = 128;   // sizeof(rr::RRRay)
 constexpr size_t kInBytes = 92;     // bytes 0..91: inputs and the output fields
 constexpr size_t kOutOffset = 44;   // hitDistance .. hitFrontSide
 constexpr size_t kOutBytes = 48;
+constexpr size_t kKeyOffset = 92;   // staged copy only: key_t, key_tri, then the hit's t (k_rrray, keyed)
 
 }  // namespace
 
@@ -106,10 +111,15 @@ static int run_batch(Collider* c, Slot* k) {
 	const size_t bytes = kHead + (kRecBytes + 1) * (size_t)n;
 	// the words go up cleared with the records
 	memset(k->h_buf, 0, kHead);
-	for (uint32_t i = 0; i < n; i++) memcpy(h_recs + kRecBytes * i, k->batch[i]->ray, kInBytes);
+	for (uint32_t i = 0; i < n; i++) {
+		uint8_t* rec = h_recs + kRecBytes * i;
+		memcpy(rec, k->batch[i]->ray, kInBytes);
+		memcpy(rec + kKeyOffset, &k->batch[i]->key_t, 4);
+		memcpy(rec + kKeyOffset + 4, &k->batch[i]->key_tri, 4);
+	}
 	RRG_CUDA(cudaMemcpyAsync(k->d_buf, k->h_buf, kHead + kRecBytes * (size_t)n, cudaMemcpyHostToDevice, k->s));
 	st = launch_rrray_scratch(c, d_recs, n, d_recs + kRecBytes * (size_t)n, reinterpret_cast<uint32_t*>(k->d_buf),
-	                          k->s);
+	                          k->s, 1);
 	if (st) return st;
 	RRG_CUDA(cudaMemcpyAsync(k->h_buf, k->d_buf, bytes, cudaMemcpyDeviceToHost, k->s));
 	RRG_CUDA(cudaStreamSynchronize(k->s));
@@ -118,6 +128,7 @@ static int run_batch(Collider* c, Slot* k) {
 		Request* r = k->batch[i];
 		memcpy(static_cast<uint8_t*>(r->ray) + kOutOffset, h_recs + kRecBytes * i + kOutOffset, kOutBytes);
 		if (r->hit) *r->hit = h_hit[i];
+		if (r->t_out) memcpy(r->t_out, h_recs + kRecBytes * i + kKeyOffset + 8, 4);
 	}
 	return h_words[1] ? RRG_ERR_STACK : RRG_OK;
 }
@@ -128,12 +139,9 @@ using namespace rrg;
 
 extern "C" {
 
-int rrg_intersect_rrray_one(rrg_collider* h, void* rrray_host, uint8_t* hit_host) {
-	Collider* c = reinterpret_cast<Collider*>(h);
-	if (!c || !rrray_host) return RRG_ERR_INVALID;
+static int submit(Collider* c, Request& me) {
 	Combiner* k = c->comb;
 	if (!k) return RRG_ERR_OOM;
-	Request me{rrray_host, hit_host, RRG_OK, false};
 	std::unique_lock<std::mutex> lk(k->m);
 	k->queue.push_back(&me);
 	while (!me.done) {
@@ -164,6 +172,21 @@ int rrg_intersect_rrray_one(rrg_collider* h, void* rrray_host, uint8_t* hit_host
 		k->cv.notify_all();
 	}
 	return me.status;
+}
+
+int rrg_intersect_rrray_one(rrg_collider* h, void* rrray_host, uint8_t* hit_host) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c || !rrray_host) return RRG_ERR_INVALID;
+	Request me{rrray_host, hit_host, RRG_OK, false, -INFINITY, 0u, nullptr};
+	return submit(c, me);
+}
+
+int rrg_intersect_rrray_one_after(rrg_collider* h, void* rrray_host, float after_t, uint32_t after_tri,
+                                  float* t_out, uint8_t* hit_host) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c || !rrray_host || after_t != after_t) return RRG_ERR_INVALID;
+	Request me{rrray_host, hit_host, RRG_OK, false, after_t, after_tri, t_out};
+	return submit(c, me);
 }
 
 int rrg_collider_combined(const rrg_collider* h, uint64_t* batches, uint64_t* rays) {

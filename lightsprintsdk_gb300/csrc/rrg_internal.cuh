@@ -148,7 +148,7 @@ int bin_rays(Collider* c, const float4* rays, uint32_t n, cudaStream_t s, int bi
 int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, cudaStream_t s);
 int launch_rrray(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, cudaStream_t s);
 int launch_rrray_scratch(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, uint32_t* words,
-                         cudaStream_t s);
+                         cudaStream_t s, int keyed = 0);
 int trace_occupancy(Collider* c);
 // batches (nmesh roots): ray i belongs to mesh segment_of(ray_off, nmesh, i)
 constexpr uint32_t kBatchMaxMeshes = 8192;

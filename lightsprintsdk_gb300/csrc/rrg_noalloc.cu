@@ -26,9 +26,6 @@
 // and are never read.
 #include "rrg_internal.cuh"
 
-#include <atomic>
-#include <mutex>
-
 namespace rrg {
 namespace {
 
@@ -40,26 +37,16 @@ static_assert(kHitsOffset % 16 == 0, "hit bytes follow whole records");
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-std::atomic<unsigned char*> g_scratch_dev[kMaxDevices];   // address of g_scratch on each device
-
-// Set-up, once per device, with that device current: the device address of
-// g_scratch.  Runs on the first call on each device.
-int scratch_on(int device, unsigned char** out) {
-	if (device < 0 || device >= kMaxDevices) return RRG_ERR_INVALID;
-	unsigned char* p = g_scratch_dev[device].load(std::memory_order_acquire);
-	if (!p) {
-		std::lock_guard<std::mutex> lock(g_setup_mutex);
-		p = g_scratch_dev[device].load(std::memory_order_relaxed);
-		if (!p) {
-			void* sym = nullptr;
-			RRG_CUDA(cudaGetSymbolAddress(&sym, g_scratch));
-			p = static_cast<unsigned char*>(sym);
-			g_scratch_dev[device].store(p, std::memory_order_release);
-		}
-	}
-	*out = p;
+// The device address of g_scratch on the current device.  Looked up on every
+// call rather than cached: a context made after cudaDeviceReset may place the
+// array elsewhere, and a cached address would then point at freed memory.
+// The lookup allocates nothing; the first one on a device loads this file's
+// module there (the set-up), which is why the first call should come before
+// any stream capture.
+int scratch_on(unsigned char** out) {
+	void* sym = nullptr;
+	RRG_CUDA(cudaGetSymbolAddress(&sym, g_scratch));
+	*out = static_cast<unsigned char*>(sym);
 	return RRG_OK;
 }
 
@@ -78,7 +65,7 @@ int rrg_intersect_rrray_noalloc(rrg_collider* h, void* rrrays_host, uint32_t n, 
 	if (n > RRG_NOALLOC_MAX_RAYS) return RRG_ERR_TOO_LARGE;
 	RRG_CUDA(cudaSetDevice(c->device));
 	unsigned char* base = nullptr;
-	int st = scratch_on(c->device, &base);
+	int st = scratch_on(&base);
 	if (st) return st;
 	uint32_t* words = reinterpret_cast<uint32_t*>(base);
 	uint8_t* recs = base + kRecordsOffset;

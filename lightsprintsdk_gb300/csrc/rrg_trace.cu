@@ -221,10 +221,16 @@ __global__ void __launch_bounds__(kTraceThreads) k_batch_closest(const TNode* __
 // include/Lightsprint/RRCollider.h:85-137 on LP64.
 constexpr int kRRRayStride = 128;
 
+// keyed: each record carries a replay key in its hitPadding1 bytes (the
+// reference also keeps collider scratch there, RRCollider/config.h:55):
+// float key_t at byte 92, uint32 key_tri at 96; only hits after
+// (key_t, key_tri) in the order (t, triangle) count, and the hit's own
+// watertight t is written at byte 100.  Records of non-keyed launches are
+// read and written at bytes 0..91 only.
 __global__ void __launch_bounds__(kTraceThreads) k_rrray(const TNode* __restrict__ nodes, int nnodes,
                                                          const float4* __restrict__ tris, int ntris, uint8_t* rrrays,
                                                          uint32_t n, uint8_t* __restrict__ hit_out,
-                                                         uint32_t* counter) {
+                                                         uint32_t* counter, int keyed) {
 	const int lane = threadIdx.x & 31;
 	while (true) {
 		uint32_t base = warp_fetch(counter);
@@ -244,7 +250,17 @@ __global__ void __launch_bounds__(kTraceThreads) k_rrray(const TNode* __restrict
 		uint32_t best_tri = 0xFFFFFFFFu;
 		bool overflow = false;
 		int slot = -1;
-		if (r.tmin <= r.tmax) slot = traverse<false>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow);
+		if (keyed) {
+			const float key_t = *reinterpret_cast<const float*>(rec + 92);
+			const uint32_t key_tri = *reinterpret_cast<const uint32_t*>(rec + 96);
+			if (key_t > r.tmin) r.tmin = key_t;
+			if (r.tmin <= r.tmax)
+				slot = traverse<false, false, true>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow, nullptr,
+				                                    0, key_t, key_tri);
+			*reinterpret_cast<float*>(rec + 100) = tbest;
+		} else if (r.tmin <= r.tmax) {
+			slot = traverse<false>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow);
+		}
 		if (overflow) atomicOr(counter + 1, (uint32_t)RRG_ERR_STACK);
 		if (hit_out) hit_out[i] = slot >= 0 ? 1 : 0;
 		if (slot < 0) continue;   // outputs undefined after a negative test (RRCollider.h:123)
@@ -514,19 +530,19 @@ int launch_rrray(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, cu
 	RRG_CUDA(cudaMemsetAsync(c->d_counter, 0, 4, s));
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
 	int grid = (int)(want < (uint32_t)c->trace_blocks ? want : (uint32_t)c->trace_blocks);
-	rrg::note_launch(), k_rrray<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, (uint8_t*)rrrays_dev, n, hit_dev, c->d_counter);
+	rrg::note_launch(), k_rrray<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, (uint8_t*)rrrays_dev, n, hit_dev, c->d_counter, 0);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }
 
 // k_rrray on caller-owned scratch words ([0] work counter, [1] status), which
-// the caller has cleared on stream s.
+// the caller has cleared on stream s; keyed as k_rrray's argument.
 int launch_rrray_scratch(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, uint32_t* words,
-                         cudaStream_t s) {
+                         cudaStream_t s, int keyed) {
 	if (!n) return RRG_OK;
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
 	int grid = (int)(want < (uint32_t)c->trace_blocks ? want : (uint32_t)c->trace_blocks);
-	rrg::note_launch(), k_rrray<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, (uint8_t*)rrrays_dev, n, hit_dev, words);
+	rrg::note_launch(), k_rrray<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, (uint8_t*)rrrays_dev, n, hit_dev, words, keyed);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }

@@ -199,10 +199,15 @@ __device__ __forceinline__ bool front_facing(const RayState& r, float4 a, float4
 	return __fadd_rn(__fadd_rn(__fmul_rn(r.dx, nx), __fmul_rn(r.dy, ny)), __fmul_rn(r.dz, nz)) < 0.f;
 }
 
-template <bool ANY, bool FILTER = false>
+// KEYED: only hits after (key_t, key_tri) in the order (t, triangle index)
+// count, for replaying a collision handler hit by hit.  The caller raises
+// r.tmin to key_t, so boxes and triangles nearer than key_t are culled as
+// usual; a triangle at exactly key_t is taken only above key_tri.
+template <bool ANY, bool FILTER = false, bool KEYED = false>
 __device__ int traverse(const TNode* __restrict__ nodes, const float4* __restrict__ tris, const RayState& r,
                         int nnodes, int ntris, float& tbest, uint32_t& best_tri, bool& overflow,
-                        const GatherFilter* flt = nullptr, int root = 0) {
+                        const GatherFilter* flt = nullptr, int root = 0, float key_t = 0.f,
+                        uint32_t key_tri = 0) {
 	int stack[kStackSize];
 	int sp = 0;
 	int ref = root;
@@ -237,6 +242,7 @@ __device__ int traverse(const TNode* __restrict__ nodes, const float4* __restric
 				uint32_t tri = (uint32_t)__float_as_int(a.w);
 				float t;
 				if (tri_test(r, a, b, c, tbest, tri, best_tri, t)) {
+					if (KEYED && t == key_t && tri <= key_tri) continue;
 					if (FILTER) {
 						if (tri == flt->skip) continue;
 						if (t < flt->ident_t && in_set(a, *flt) && in_set(b, *flt) && in_set(c, *flt)) continue;

@@ -1,19 +1,31 @@
-# Builds the reference LightsprintCore library from its own sources, where
-# they lie, into oracle/_ref/ (git-ignored).  Test infrastructure only: the
-# result is the parity oracle and the CPU baseline measured in this container;
+# Builds the reference LightsprintCore library from its own sources into
+# oracle/_ref/ (git-ignored).  Test infrastructure only: the result is the
+# parity oracle, the reference side of the plugin tests and the CPU baseline;
 # nothing in the product links it.
 #
-#   make -f oracle/ref.mk -j8 REF=/root/reference
+#   make -f oracle/ref.mk stage REF_SRC=/root/reference   # where the reference lies
+#   make -f oracle/ref.mk -j8                             # build from the staged copy
+#
+# `stage` copies the sources this build reads (src/LightsprintCore and the
+# Lightsprint and embree3 headers) unchanged into oracle/_ref/src, which is
+# git-ignored but travels with the working tree to machines that have no
+# reference checkout (the GPU host), so that the same recipe builds the
+# library there.  cp -p keeps the files' times, so restaging leaves make's
+# view of what is up to date unchanged.
 #
 # Flags follow the reference's own linux configuration (src/configs/
-# linux.common, linux.release: -std=c++17 -O2 -fopenmp, RR_BUILD) with three
-# additions that let it build without Boost: our compat headers under
-# oracle/compat, -D_strdup=strdup and two forced includes.
-REF      ?= /root/reference
+# linux.common, linux.release: -std=c++17 -O2 -fopenmp, RR_BUILD) with these
+# additions: our compat headers under oracle/compat (no Boost),
+# -D_strdup=strdup, two forced includes, and -fsigned-char -ffp-contract=off
+# so that an aarch64 build computes what the x86-64 build does (GCC contracts
+# a*b+c into fused multiply-adds by default for C++ where the target has
+# them, as aarch64 does; x86-64 without -mfma has none).
+REF_SRC  ?= /root/reference
+REF      := oracle/_ref/src
 CORE     := $(REF)/src/LightsprintCore
 OUT      := oracle/_ref
 CXX      ?= g++
-CXXFLAGS := -std=c++17 -O2 -fopenmp -DNDEBUG -DRR_BUILD -D_strdup=strdup \
+CXXFLAGS := -std=c++17 -O2 -fopenmp -DNDEBUG -DRR_BUILD -D_strdup=strdup -fsigned-char -ffp-contract=off \
             -include string -include climits -fPIC -w \
             -I$(REF)/include -I$(CORE) -Ioracle/compat
 
@@ -47,10 +59,17 @@ SOURCES := \
 OBJS := $(addprefix $(OUT)/obj/,$(SOURCES:.cpp=.o))
 
 # Drivers (our code) that run the reference collider and gather on the
-# workloads' binary inputs and write binary outputs.
+# workloads' binary inputs and write binary outputs, and the shared library
+# through which the benchmark times the reference collider in-process.
 DRIVERS := $(OUT)/ref_collide $(OUT)/ref_filter $(OUT)/ref_enumerate $(OUT)/ref_gather
 
-all: $(OUT)/libLightsprintCore.a $(DRIVERS)
+all: $(OUT)/libLightsprintCore.a $(DRIVERS) $(OUT)/libref_bench.so
+
+stage:
+	@test -d $(REF_SRC)/src/LightsprintCore || { echo "no reference sources under $(REF_SRC)"; exit 1; }
+	@mkdir -p $(REF)/src $(REF)/include
+	@cp -rp $(REF_SRC)/src/LightsprintCore $(REF)/src/
+	@cp -rp $(REF_SRC)/include/Lightsprint $(REF_SRC)/include/embree3 $(REF)/include/
 
 $(OUT)/obj/%.o: $(CORE)/%.cpp
 	@mkdir -p $(dir $@)
@@ -60,7 +79,10 @@ $(OUT)/libLightsprintCore.a: $(OBJS)
 	rm -f $@
 	ar rcs $@ $(OBJS)
 
+$(OUT)/libref_bench.so: oracle/ref_bench.cpp $(OUT)/libLightsprintCore.a
+	$(CXX) $(CXXFLAGS) -shared $< -o $@ $(OUT)/libLightsprintCore.a -lgomp -lpthread
+
 $(OUT)/%: oracle/%.cpp $(OUT)/libLightsprintCore.a
 	$(CXX) $(CXXFLAGS) $< -o $@ $(OUT)/libLightsprintCore.a -lgomp -lpthread
 
-.PHONY: all
+.PHONY: all stage

@@ -192,3 +192,79 @@ def run_ref_gather(gs, atlases, quality: int, seed: int = 1, threads: int = 0, b
     rec = np.frombuffer(sb, np.float32, nt * 15, 8).reshape(nt, 15)
     solver = {"direct": rec[:, 0:3].copy(), "indirect": rec[:, 3:6].copy(), "corner": rec[:, 6:15].reshape(nt, 3, 3).copy()}
     return out, solver
+
+
+# ---------------------------------------------------------------------------
+# The reference collider in-process (oracle/_ref/libref_bench.so, built from
+# oracle/ref_bench.cpp): the benchmark's reference arm and CPU baseline.
+IT_LINEAR, IT_BSP_COMPACT, IT_BSP_FAST, IT_BSP_FASTER, IT_BSP_FASTEST = 0, 1, 2, 3, 4
+_bench_lib = None
+
+
+def ref_bench_available() -> bool:
+    return os.path.exists(os.path.join(REF_DIR, "libref_bench.so"))
+
+
+def _ref_bench():
+    global _bench_lib
+    if _bench_lib is None:
+        import ctypes as C
+        L = C.CDLL(os.path.join(REF_DIR, "libref_bench.so"))
+        P = C.c_void_p
+        L.refb_create.argtypes = [P, C.c_uint, P, C.c_uint, C.c_int, C.POINTER(C.c_double)]
+        L.refb_create.restype = P
+        L.refb_technique.argtypes = [P]
+        L.refb_technique.restype = C.c_int
+        L.refb_memory.argtypes = [P]
+        L.refb_memory.restype = C.c_size_t
+        L.refb_trace.argtypes = [P, P, C.c_size_t, C.c_uint, C.c_int, P, P, P, P]
+        L.refb_trace.restype = C.c_double
+        L.refb_destroy.argtypes = [P]
+        _bench_lib = L
+    return _bench_lib
+
+
+class RefCollider:
+    """RRCollider::create(mesh, nullptr, technique) of the reference library,
+    and its intersect() over ray arrays on OpenMP threads."""
+
+    def __init__(self, v, t, technique: int = IT_BSP_FASTEST):
+        import ctypes as C
+        L = _ref_bench()
+        self._v = np.ascontiguousarray(v, np.float32)
+        self._t = np.ascontiguousarray(t, np.uint32)
+        bs = C.c_double(0)
+        self._h = L.refb_create(self._v.ctypes.data, self._v.shape[0], self._t.ctypes.data, self._t.shape[0],
+                                technique, C.byref(bs))
+        if not self._h:
+            raise RuntimeError("RRCollider::create failed")
+        self.build_s = bs.value
+        self.technique = L.refb_technique(self._h)
+        self.memory = L.refb_memory(self._h)
+
+    def trace(self, rays, threads: int = 0, flags: int = FILL_DISTANCE | FILL_TRIANGLE | FILL_POINT2D | FILL_SIDE,
+              outputs: bool = True):
+        """Returns (seconds of the parallel loop, dict hit/tri/dist/uv or None)."""
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        L = _ref_bench()
+        if outputs:
+            out = {"hit": np.zeros(n, np.uint8), "tri": np.zeros(n, np.uint32), "dist": np.zeros(n, np.float32),
+                   "uv": np.zeros((n, 2), np.float32)}
+            s = L.refb_trace(self._h, rays.ctypes.data, n, flags, threads, out["hit"].ctypes.data,
+                             out["tri"].ctypes.data, out["dist"].ctypes.data, out["uv"].ctypes.data)
+            out["hit"] = out["hit"].astype(bool)
+            return s, out
+        s = L.refb_trace(self._h, rays.ctypes.data, n, flags, threads, None, None, None, None)
+        return s, None
+
+    def close(self):
+        if self._h:
+            _ref_bench().refb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

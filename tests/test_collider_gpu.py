@@ -84,11 +84,23 @@ def test_c0_against_reference(c0):
     n_tri_diff = len(cls["tie"]) + len(cls["ref_off"])
     assert n_tri_diff <= 1e-5 * n, cls
     same = ref["hit"] & h["hit"] & (ref["tri"] == h["tri"])
-    d_ok, uv_ok = assert_fields_close(ref, h, same)
-    # the reference's near-coplanar BSP-node plane reuse puts ~1.3 % of its
-    # distances up to 5e-4 away from the exact value; everything else agrees
-    assert d_ok.mean() >= 0.98 and uv_ok.mean() >= 0.98
     np.testing.assert_array_equal(h["side"][same], ref["side"][same])
+    # hitDistance: bit-identical except where the reference took the plane of
+    # another triangle of a near-coplanar BSP node (the rule of the oracle's
+    # own test): wherever the reference is off the exact FP64 distance by
+    # more than 1e-5 relative we are closer to it, and ours stays within
+    # 2e-5 everywhere
+    diff = same & (h["dist"] != ref["dist"])
+    assert diff.sum() <= 0.02 * same.sum()
+    tri64, d64 = orc.FastestOracle(v, t).exact64(rays, 0)
+    err_ours = np.abs(h["dist"][diff] - d64[diff]) / d64[diff]
+    err_ref = np.abs(ref["dist"][diff] - d64[diff]) / d64[diff]
+    assert err_ours.max() <= err_ref.max()
+    big = err_ref > 1e-5
+    assert np.all(err_ours[big] < err_ref[big])
+    assert np.max(np.abs(h["dist"][same] - d64[same]) / d64[same]) < 2e-5
+    # hitPoint2d follows the distance: identical wherever the distance is
+    np.testing.assert_array_equal(h["uv"][same & ~diff], ref["uv"][same & ~diff])
 
 
 def test_c0_against_oracle_bit_exact(c0):
@@ -121,6 +133,12 @@ def test_c0_full_size_vs_oracle():
     assert err.max() < 2e-5
 
 
+# config-1 fixture (49,152 rays): differences from IT_BSP_FASTEST observed
+# for the oracle (84 ties) and on GB300 (88 ties), classified by
+# tests/helpers.py::classify_mismatches
+C1_TIES, C1_TIES_GPU, C1_REF_OFF, C1_HIT_SET = 84, 88, 6, 1
+
+
 def test_c1_sample_against_reference():
     sc = scenes.interior_c1()
     g = load_golden("c1_fastest.npz")
@@ -133,9 +151,22 @@ def test_c1_sample_against_reference():
     c, h = gpu_collide(sc.vertices, sc.indices, rays)
     cls = classify_mismatches(sc.vertices, sc.indices, rays, ref, h)
     assert not cls["other"], cls
-    assert len(cls["tie"]) + len(cls["ref_off"]) <= 0.005 * ref["hit"].sum()
+    # pinned to the differences observed on GB300 (88 ties on coincident
+    # faces, 6 reference non-intersections, 1 of them in the hit set): any
+    # new one fails
+    assert len(cls["tie"]) <= C1_TIES_GPU, cls["tie"]
+    assert len(cls["ref_off"]) <= C1_REF_OFF, cls["ref_off"]
+    assert len(cls["hit_mismatch"]) <= C1_HIT_SET, cls["hit_mismatch"]
+    assert set(cls["hit_mismatch"]) <= set(cls["ref_off"]) | set(cls["tie"])
     ncam = int(g["n_cam"])
     assert np.array_equal(h["tri"][:ncam], ref["tri"][:ncam])
+    # against the oracle (the same exact-nearest rule, evaluated with the
+    # GPU's fused multiply-adds in the shear, which the C oracle does
+    # without) the only differences are ties between coincident faces
+    o = orc.FastestOracle(sc.vertices, sc.indices).collide(rays, 0)
+    co = classify_mismatches(sc.vertices, sc.indices, rays, o, h)
+    assert not co["other"] and not co["ref_off"] and not co["hit_mismatch"], co
+    assert len(co["tie"]) <= C1_TIES_GPU - C1_TIES + 4, co["tie"]
 
 
 def test_any_hit_matches_closest_hit_flag():

@@ -99,6 +99,12 @@ def test_c0_linear_matches_reference():
         np.testing.assert_array_equal(got[f][m], ref[f][m], err_msg=f)
 
 
+# Config-1 fixture (49,152 rays): differences from IT_BSP_FASTEST observed,
+# classified by tests/helpers.py::classify_mismatches.  Any new or other
+# difference fails.
+C1_TIES, C1_REF_OFF, C1_HIT_SET = 84, 6, 1
+
+
 def test_c1_oracle_matches_reference():
     """Config 1 (1.24 M triangles) sample of 16,384 camera, 16,384 surface and
     16,384 shadow rays.  Every difference is a distance tie (coincident faces
@@ -116,10 +122,18 @@ def test_c1_oracle_matches_reference():
     got = orc.FastestOracle(sc.vertices, sc.indices).collide(rays, 0)
     cls = classify_mismatches(sc.vertices, sc.indices, rays, ref, got)
     assert not cls["other"], cls
-    assert len(cls["hit_mismatch"]) <= 2
     ncam = int(g["n_cam"])
     assert np.array_equal(got["tri"][:ncam], ref["tri"][:ncam])
-    n_diff = len(cls["tie"]) + len(cls["ref_off"])
     # differences are confined to rays that start on hidden coincident faces
-    # of abutting slabs (ties) and the reference's plane-reuse artifacts
-    assert n_diff <= 0.005 * ref["hit"].sum()
+    # of abutting slabs (ties) and the reference's plane-reuse artifacts, and
+    # are pinned to the counts observed: 84 ties, 6 reference hits that are
+    # not exact intersections (one of them a hit where the exact test
+    # finds none), of 49,152 rays (99.817 % identical)
+    assert len(cls["tie"]) <= C1_TIES, cls["tie"]
+    assert len(cls["ref_off"]) <= C1_REF_OFF, cls["ref_off"]
+    assert len(cls["hit_mismatch"]) <= C1_HIT_SET, cls["hit_mismatch"]
+    assert set(cls["hit_mismatch"]) <= set(cls["ref_off"]) | set(cls["tie"])
+    # against the exact nearest hit in double precision the oracle is
+    # identical on every ray
+    tri64, _ = orc.FastestOracle(sc.vertices, sc.indices).exact64(rays, 0)
+    assert np.array_equal(np.where(got["hit"], got["tri"], 0xFFFFFFFF), tri64)

@@ -39,6 +39,34 @@ def both(c, rays, flags):
     return a, ha, b, hb
 
 
+def test_noalloc_allocates_no_device_memory():
+    """A fresh collider's first query is a no-alloc call of the largest
+    batch: the device's free memory is the same before and after (measured
+    by cudaMemGetInfo).  A call of the largest batch on another collider
+    comes first, so that the set-up it does on the device (loading the
+    modules that hold the array and the kernel) is not counted; then the
+    result comparison runs on the fresh collider as on any other."""
+    import torch
+    v0, t0 = scenes.icosphere_c0()
+    warm = col.RRCollider.create(v0, t0)
+    w = col.make_rrrays(scenes.shell_rays(MAX_RAYS))
+    assert noalloc()(warm.handle, w.ctypes.data, len(w), None, None) == RRG_OK
+    fresh = col.RRCollider.create(v0, t0)
+    b = col.make_rrrays(scenes.shell_rays(MAX_RAYS))
+    hb = np.zeros(len(b), np.uint8)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    assert noalloc()(fresh.handle, b.ctypes.data, len(b), hb.ctypes.data, None) == RRG_OK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    a, ha, b2, hb2 = both(fresh, scenes.shell_rays(MAX_RAYS), col.FILL_ALL)
+    np.testing.assert_array_equal(hb2, ha)
+    assert a.tobytes() == b2.tobytes()
+    warm.close()
+    fresh.close()
+
+
 def test_noalloc_matches_rrg_intersect_rrray_on_calls_in_a_row():
     v0, t0 = scenes.icosphere_c0()
     sphere = col.RRCollider.create(v0, t0)
