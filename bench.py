@@ -20,7 +20,10 @@ cores: RRCollider::create(..., IT_BSP_FASTEST) and intersect() from the
 reference library, built from the reference sources on this host into
 oracle/_ref (the tree build is timed apart; the steps cover every ray when
 they fit in about 90 s).  The oracle port's rate is reported beside it.
-Multi-GPU: replicas only (each rank traces its own copy of the workload).
+Multi-GPU: `--gpus N` launches N ranks (torch.distributed.run) unless it is
+already one of them; rank r traces its own shard of the job (make_workload's
+shard r, a full single-GPU workload each: weak scaling); the only collective
+is the max of the ranks' times.
 """
 from __future__ import annotations
 
@@ -75,20 +78,46 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def make_workload(name: str, nrays: int = 0):
+CAMERA_EYE = (-8.5, 4.0, -8.5)
+
+
+def make_workload(name: str, nrays: int = 0, shard: int = 0):
     """Scene and rays of a workload.  nrays > 0 takes a smaller case of the
     same workload (the first nrays/2 camera rows' rays and nrays/2 surface
-    rays) for profiling."""
+    rays) for profiling.  shard r is rank r's own part of a multi-GPU job
+    (weak scaling: every rank gets a full workload of its own): config 0's
+    rays r*n .. (r+1)*n-1 of the seeded shell-ray stream; config 1's camera
+    image from an eye moved by r * (0.25, 0, 0.25) and surface rays
+    r*n .. (r+1)*n-1 of the seeded stream.  Shard 0 is the single-GPU
+    workload."""
     from lightsprintsdk_gb300 import scenes
     if name == "c0":
         v, t = scenes.icosphere_c0()
-        rays = scenes.shell_rays(nrays or (1 << 20))
+        n = nrays or (1 << 20)
+        rays = scenes.shell_rays(n, start=shard * n)
         return v, t, rays
     sc = scenes.interior_c1()
     half = (nrays // 2) if nrays else 4096 * 4096
-    cam = scenes.camera_rays(rows=max(1, half // 4096))
-    sur = scenes.surface_rays(sc.vertices, sc.indices, half)
+    eye = (CAMERA_EYE[0] + 0.25 * shard, CAMERA_EYE[1], CAMERA_EYE[2] + 0.25 * shard)
+    cam = scenes.camera_rays(rows=max(1, half // 4096), eye=eye)
+    sur = scenes.surface_rays(sc.vertices, sc.indices, half, start=shard * half)
     return sc.vertices, sc.indices, np.concatenate([cam, sur])
+
+
+def free_port() -> int:
+    import socket
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def spawn_command(gpus: int, argv: list, port: int) -> list:
+    """The launch of `gpus` ranks of this script on one node, one per GPU
+    (torch.distributed.run), with the same arguments."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={gpus}",
+            "--master-addr=127.0.0.1", f"--master-port={port}", os.path.abspath(__file__)] + list(argv)
 
 
 class ClockSampler:
@@ -647,6 +676,7 @@ def run_batch(args, world, rank, local):
     b = rb.RRColliderBatch.from_meshes(mb, build_params={"max_leaf_size": tuned["max_leaf_size"],
                                                          "bvh_width": tuned["bvh_width"]})
     b.set_rays_per_warp(tuned["rays_per_warp"])
+    b.set_stack_smem(tuned.get("stack_smem", 0))
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
 
@@ -720,6 +750,9 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # started as a single process: launch one rank per GPU and pass their output through
+        sys.exit(subprocess.run(spawn_command(args.gpus, sys.argv[1:], free_port())).returncode)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -743,7 +776,7 @@ def main():
             torch.distributed.destroy_process_group()
         return
 
-    v, t, rays = make_workload(args.workload, args.rays)
+    v, t, rays = make_workload(args.workload, args.rays, shard=rank)
     n = rays.shape[0]
     c = col.RRCollider.create(v, t, device=local, build_params={"bvh_width": args.bvh_width})
     build_ms = c.build_ms
@@ -802,7 +835,8 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
             "config": {"workload": WORKLOAD_DESC[args.workload], "rays_per_step": n, "triangles": int(t.shape[0]),
-                       "parallelism": f"replicas x{world}", "l2": "inputs (32 B/ray) larger than L2, no flush",
+                       "parallelism": f"ray shards x{world} (rank r: shard r of the job, a full workload each)",
+                       "l2": "inputs (32 B/ray) larger than L2, no flush",
                        "hit_ratio": hits_total / n, "bvh_build_ms": build_ms, "bvh_nodes": c.nodes,
                        "bvh_width": args.bvh_width or 2},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

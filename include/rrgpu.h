@@ -84,7 +84,10 @@ typedef struct rrg_build_params {
 enum {
 	RRG_TRAVERSAL_DEFAULT = 0,     /* if-if (measured faster on GB300 for both workloads) */
 	RRG_TRAVERSAL_IF_IF = 1,       /* warp takes 32 rays, per-thread if-if walk */
-	RRG_TRAVERSAL_WHILE_WHILE = 2  /* persistent while-while, postponed leaves, per-lane refill */
+	RRG_TRAVERSAL_WHILE_WHILE = 2, /* persistent while-while, postponed leaves, per-lane refill */
+	RRG_TRAVERSAL_COMPACT = 3      /* persistent: a warp claims a block of consecutive rays and each
+	                                  lane walks its share of them one after the other, with no
+	                                  warp-wide step between rays; stack top in shared memory */
 };
 
 typedef struct rrg_collider rrg_collider;
@@ -122,6 +125,20 @@ RRG_API int rrg_collider_set_ray_order(rrg_collider* c, uint32_t order);
 
 /* Selects the traversal kernel of later queries (RRG_TRAVERSAL_*). */
 RRG_API int rrg_collider_set_traversal(rrg_collider* c, uint32_t traversal);
+
+/* Tuning of RRG_TRAVERSAL_COMPACT (the autotuner's knobs; results do not
+ * depend on them):
+ *   stack_smem    traversal-stack entries per thread kept in shared memory:
+ *                 0, 8, 16 or 32 (deeper entries go to local memory);
+ *                 RRG_COMPACT_DEFAULT = 8;
+ *   rays_per_warp rays a warp claims at a time: a multiple of 32 in
+ *                 32..1024; 0 = 32;
+ *   blocks_per_sm 9 caps the kernel's registers (56) so that 9 blocks of
+ *                 128 threads fit on an SM; 0 leaves them uncapped (62,
+ *                 8 blocks); RRG_COMPACT_DEFAULT = 9. */
+#define RRG_COMPACT_DEFAULT 0xFFFFFFFFu
+RRG_API int rrg_collider_set_compact_tuning(rrg_collider* c, uint32_t stack_smem, uint32_t rays_per_warp,
+                                            uint32_t blocks_per_sm);
 
 /* RRCollider::getMemoryOccupied (RRCollider.h:259): device bytes held. */
 RRG_API size_t rrg_collider_memory(const rrg_collider* c);

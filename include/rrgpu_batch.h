@@ -42,6 +42,13 @@ RRG_API void rrg_batch_destroy(rrg_batch* b);
  * (default 32).  The autotuner's rays-per-warp knob. */
 RRG_API int rrg_batch_set_rays_per_warp(rrg_batch* b, uint32_t rays_per_warp);
 
+/* Traversal-stack entries per thread kept in shared memory by the batch's
+ * closest-hit kernel: 0 (the whole stack in local memory, default), 8, 16
+ * or 32 (deeper entries in local memory); binary trees only (the 8-wide
+ * walk keeps its own stack).  The autotuner's stack-depth knob; results do
+ * not depend on it. */
+RRG_API int rrg_batch_set_stack_smem(rrg_batch* b, uint32_t entries);
+
 /* Closest hit for n device rays (float[8] each, as rrg_intersect_device);
  * ray_off_dev = nmesh+1 ascending device offsets, ray_off[nmesh] = n: ray i
  * belongs to the mesh m with ray_off[m] <= i < ray_off[m+1].  Writes one hit
@@ -49,7 +56,7 @@ RRG_API int rrg_batch_set_rays_per_warp(rrg_batch* b, uint32_t rays_per_warp);
  * hitFrontSide << 31, u, v), 0xFFFFFFFF = no hit.  Asynchronous on `stream`:
  * the counter reset and the persistent kernel are replayed from a CUDA graph,
  * captured on the first call and again whenever rays, offsets, n, hits or
- * the rays-per-warp setting change.  Calls on the same batch must not
+ * the rays-per-warp or stack setting change.  Calls on the same batch must not
  * overlap on the GPU (they share its work counter).  n < 2^31. */
 RRG_API int rrg_batch_intersect_device(rrg_batch* b, const float* rays_dev, const uint32_t* ray_off_dev, uint32_t n,
                                        float* hits_dev, void* stream);

@@ -147,6 +147,17 @@ RRG_API void rrg_filter_defaults(rrg_filter_params* p);
  * RRBuffer.cpp:534-628). */
 RRG_API int rrg_lightmap_filter(rrg_lightmapper* lm, const rrg_filter_params* p, uint32_t first_atlas,
                                 uint32_t natlas, float* lightmaps_dev, void* stream);
+/* The whole update of the lightmapper's atlases, host buffer out: every
+ * texel of every atlas gathered with p (the solver-reading gather when
+ * p->mode has RRG_GATHER_SOLVER, after rrg_lightmapper_bake_solver), then
+ * the post-filters of f (NULL or stages 0 = none), then copied to out_host
+ * (float RGBA, natlas x size x size texels, the lightmapper's layout).
+ * Synchronous; the device buffer is the lightmapper's staging buffer.  What
+ * RRSolver::updateLightmap does per lightmap (RRSolver/lightmap.cpp:
+ * 648-930), for all atlases at once. */
+RRG_API int rrg_lightmap_bake_host(rrg_lightmapper* lm, const rrg_gather_params* p, const rrg_filter_params* f,
+                                   float* out_host);
+
 /* Number of unwrap seams found (0 before the first filter call with seams). */
 RRG_API uint64_t rrg_lightmapper_seams(const rrg_lightmapper* lm);
 /* Runs of samples over all seams (a run: consecutive samples of a seam that
@@ -187,9 +198,13 @@ RRG_API uint64_t rrg_lightmapper_copy_factor_hits(const rrg_lightmapper* lm, uin
 
 /* Training records for a radiance cache (rrgpu_cache.h) from the gather's
  * own paths: from every `stride`-th covered texel, paths_per_texel plain
- * N-bounce paths; each path vertex gives one record (position, plane
- * normal, albedo, outgoing radiance toward the previous vertex).  Writes at
- * most cap records to recs_dev (48 bytes each); *nrec_out = records written. */
+ * paths; each of a path's first four vertices gives one record (position,
+ * plane normal, albedo, outgoing radiance toward the previous vertex).  A
+ * record's radiance covers the same bounces the gather traces after a
+ * first hit (that vertex and max_depth more): paths are traced three
+ * bounces deeper than the gather so that every record's window is whole.
+ * Writes at most cap records to recs_dev (48 bytes each); *nrec_out =
+ * records written. */
 RRG_API int rrg_lightmap_train_samples(rrg_lightmapper* lm, const rrg_gather_params* p, uint32_t stride,
                                        uint32_t paths_per_texel, void* recs_dev, uint64_t cap, uint64_t* nrec_out,
                                        void* stream);

@@ -60,6 +60,16 @@ RRG_API int rrg_scene_set_enabled(rrg_scene* s, const uint8_t* enabled);
 RRG_API int rrg_scene_intersect_device(rrg_scene* s, const float* rays_dev, uint32_t n, float* hits_dev,
                                        uint32_t* objects_dev, void* stream);
 
+/* Host buffers in, host buffers out (synchronous): n rays (float[8] each)
+ * -> n hit records and, when objects_host is not NULL, n hit objects, as
+ * rrg_scene_intersect_device.  Staging buffers belong to the scene and grow
+ * on demand; host threads that call it on one scene take turns.  Returns the
+ * traces' status (RRG_ERR_STACK on a traversal overflow).  The query of
+ * RRColliderMulti::intersect for callers holding rays on the host
+ * (RRColliderMulti.cpp:103-147). */
+RRG_API int rrg_scene_intersect_host(rrg_scene* s, const float* rays_host, uint32_t n, float* hits_host,
+                                     uint32_t* objects_host);
+
 /* Status word of the scene's traces (RRG_OK or RRG_ERR_STACK); synchronises
  * the stream and resets the word. */
 RRG_API int rrg_scene_status(rrg_scene* s, void* stream);

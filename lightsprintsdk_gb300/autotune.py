@@ -3,9 +3,11 @@ kernel per GPU and mesh-size bucket by timing candidates on a sample of the
 caller's own rays.  Results persist in a JSON file (the package's _lib
 directory, or $RRG_AUTOTUNE_CACHE) keyed by "<gpu name>|<log2 triangles>|<tag>".
 
-Candidates: max_leaf_size in {2, 4, 8} x traversal in {if-if, while-while}
-for single colliders; max_leaf_size in {2, 4, 8} x rays per warp in
-{32, 64, 128} for mesh batches (tune_batch).
+Candidates: max_leaf_size in {2, 4, 8} x traversal in {if-if, while-while,
+compact} for single colliders; for mesh batches (tune_batch) the BVH width
+and leaf size x rays per warp in {32, 128} x shared-memory stack entries
+per thread in {0, 8, 16} (binary trees; the 8-wide walk has its own
+stack).
 """
 from __future__ import annotations
 
@@ -19,7 +21,7 @@ from . import build as _build
 from . import collider as col
 
 LEAF_SIZES = (2, 4, 8)
-TRAVERSALS = (1, 2)   # RRG_TRAVERSAL_IF_IF, RRG_TRAVERSAL_WHILE_WHILE
+TRAVERSALS = (1, 2, 3)   # RRG_TRAVERSAL_IF_IF, RRG_TRAVERSAL_WHILE_WHILE, RRG_TRAVERSAL_COMPACT
 
 
 def cache_path() -> str:
@@ -96,16 +98,18 @@ def create_tuned(vertices, indices, sample_rays: np.ndarray, tag: str = "closest
 
 
 BATCH_RAYS_PER_WARP = (32, 128)
+BATCH_STACK_SMEM = (0, 8, 16)
 # (bvh width, leaf size): the 8-wide tree takes leaves of at most 4
 BATCH_TREES = ((2, 2), (2, 4), (2, 8), (8, 2), (8, 4))
 
 
 def tune_batch(mb, rays_dev, ray_off_dev, repeats: int = 3, force: bool = False) -> dict:
-    """BVH width and leaf size x rays per warp for a mesh batch (scenes.MeshBatch), timed
-    with CUDA events on the caller's device rays (all of them: the tuner
-    sees the real mix of meshes and ray sets).  Remembered per GPU and
-    log2(total triangles) bucket; returns {"bvh_width", "max_leaf_size",
-    "rays_per_warp", "grays": {...}}."""
+    """BVH width and leaf size x rays per warp x shared-memory stack depth
+    for a mesh batch (scenes.MeshBatch), timed with CUDA events on the
+    caller's device rays (all of them: the tuner sees the real mix of meshes
+    and ray sets).  Remembered per GPU and log2(total triangles) bucket;
+    returns {"bvh_width", "max_leaf_size", "rays_per_warp", "stack_smem",
+    "grays": {...}}."""
     import torch
     from . import batch as rb
     k = key(int(mb.tri_off[-1]), "batch")
@@ -118,21 +122,23 @@ def tune_batch(mb, rays_dev, ray_off_dev, repeats: int = 3, force: bool = False)
     for width, leaf in BATCH_TREES:
         b = rb.RRColliderBatch.from_meshes(mb, build_params={"max_leaf_size": leaf, "bvh_width": width})
         for rpw in BATCH_RAYS_PER_WARP:
-            b.set_rays_per_warp(rpw)
-            b.intersect_device(rays_dev.data_ptr(), ray_off_dev.data_ptr(), n, hits.data_ptr())
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for _ in range(repeats):
+            for sd in (BATCH_STACK_SMEM if width == 2 else (0,)):
+                b.set_rays_per_warp(rpw)
+                b.set_stack_smem(sd)
                 b.intersect_device(rays_dev.data_ptr(), ray_off_dev.data_ptr(), n, hits.data_ptr())
-            e1.record()
-            torch.cuda.synchronize()
-            results[f"w{width}_leaf{leaf}_rpw{rpw}"] = n / (e0.elapsed_time(e1) / repeats * 1e-3) / 1e9
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(repeats):
+                    b.intersect_device(rays_dev.data_ptr(), ray_off_dev.data_ptr(), n, hits.data_ptr())
+                e1.record()
+                torch.cuda.synchronize()
+                results[f"w{width}_leaf{leaf}_rpw{rpw}_sd{sd}"] = n / (e0.elapsed_time(e1) / repeats * 1e-3) / 1e9
         b.close()
     best = max(results, key=results.get)
-    w, leaf, rpw = best.split("_")
+    w, leaf, rpw, sd = best.split("_")
     entry = {"bvh_width": int(w[1:]), "max_leaf_size": int(leaf[4:]), "rays_per_warp": int(rpw[3:]),
-             "grays": results, "rays": int(n)}
+             "stack_smem": int(sd[2:]), "grays": results, "rays": int(n)}
     db[k] = entry
     _save(db)
     return entry

@@ -29,6 +29,7 @@ def _lib():
         L.rrg_batch_destroy.argtypes = [P]
         L.rrg_batch_destroy.restype = None
         L.rrg_batch_set_rays_per_warp.argtypes = [P, U]
+        L.rrg_batch_set_stack_smem.argtypes = [P, U]
         L.rrg_batch_intersect_device.argtypes = [P, P, P, U, P, P]
         L.rrg_batch_status.argtypes = [P, P]
         for f in ("rrg_batch_meshes", "rrg_batch_nodes"):
@@ -89,6 +90,10 @@ class RRColliderBatch:
 
     def set_rays_per_warp(self, k: int) -> None:
         col._check(_lib().rrg_batch_set_rays_per_warp(self._h, int(k)), "rrg_batch_set_rays_per_warp")
+
+    def set_stack_smem(self, entries: int) -> None:
+        """Traversal-stack entries per thread in shared memory (0, 8, 16, 32)."""
+        col._check(_lib().rrg_batch_set_stack_smem(self._h, int(entries)), "rrg_batch_set_stack_smem")
 
     def intersect_device(self, rays_ptr: int, ray_off_ptr: int, n: int, hits_ptr: int, stream: int = 0) -> None:
         """Closest hit for n device rays; ray_off_ptr = (M+1,) uint32 device

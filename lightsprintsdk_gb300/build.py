@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "librrgpu.so")
 SOURCES = ["rrg_api.cu", "rrg_build.cu", "rrg_wide.cu", "rrg_trace.cu", "rrg_gather.cu", "rrg_mlp.cu", "rrg_batch.cu",
-           "rrg_scene.cu", "rrg_binning.cu", "rrg_noalloc.cu", "rrg_combine.cu", "rrg_filter.cu"]
+           "rrg_scene.cu", "rrg_binning.cu", "rrg_noalloc.cu", "rrg_combine.cu", "rrg_filter.cu", "rrg_compact.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "-Xcompiler", "-ffp-contract=off",

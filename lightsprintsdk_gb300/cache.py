@@ -18,6 +18,7 @@ REC_DTYPE = np.dtype([("p", "<f4", 3), ("n", "<f4", 3), ("alb", "<f4", 3), ("t",
 NPARAMS = 4 * 64 * 64 + 64 * 16
 
 FREQUENCY, HASHGRID = 0, 1      # RRG_CACHE_*
+TRAIN_RECORDS_PER_PATH = 4      # records of a training path (rrg_lightmap_train_samples)
 
 
 class CacheParams(C.Structure):
@@ -222,11 +223,21 @@ def bake_learned(L: lm.RRLightmapper, cache: RadianceCache, params, first: int, 
     import torch
     ncov = covered(L)
     npaths = (ncov + stride - 1) // stride * paths_per_texel
-    cap = max(1, int(npaths * (params.max_depth + 1)))
+    cap = max(1, int(npaths * TRAIN_RECORDS_PER_PATH))
+    st = torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    ev[0].record(st)
     recs = torch.empty(cap * REC_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
     nrec = train_samples(L, params, stride, paths_per_texel, recs.data_ptr(), cap, stream)
+    ev[1].record(st)
     loss = cache.train(recs.data_ptr(), nrec, batch, steps, stream)
+    ev[2].record(st)
     nrel = cache.build_error_grid(recs.data_ptr(), nrec, grid_res, rel_threshold, min_count, stream,
                                   float(params.quality) if noise_aware else 0.0) if use_fallback else 0
+    ev[3].record(st)
     nfb = gather_learned(L, cache, params, first, count, out_ptr, fallback_frac if use_fallback else 2.0, stream)
-    return {"train_records": nrec, "loss": loss, "reliable_cells": nrel, "fallback_texels": nfb}
+    ev[4].record(st)
+    ev[4].synchronize()
+    ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(4)]
+    return {"train_records": nrec, "loss": loss, "reliable_cells": nrel, "fallback_texels": nfb,
+            "ms": {"train_paths": ms[0], "train_steps": ms[1], "error_grid": ms[2], "learned_gather": ms[3]}}

@@ -89,6 +89,8 @@ def _lib():
         L.rrg_collider_combined.argtypes = [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.rrg_collider_status.argtypes = [P, P]
         L.rrg_collider_set_traversal.argtypes = [P, U]
+        L.rrg_collider_set_compact_tuning.argtypes = [P, U, U, U]
+        L.rrg_intersect_rrray_one_after.argtypes = [P, P, C.c_float, U, P, P]
         L.rrg_collider_set_ray_order.argtypes = [P, U]
         L.rrg_status_string.argtypes = [I]
         L.rrg_status_string.restype = C.c_char_p
@@ -187,8 +189,17 @@ class RRCollider:
 
     # ------------------------------------------------------------ queries
     def set_traversal(self, traversal: int) -> None:
-        """RRG_TRAVERSAL_IF_IF (1, default) or RRG_TRAVERSAL_WHILE_WHILE (2)."""
+        """RRG_TRAVERSAL_IF_IF (1, default), RRG_TRAVERSAL_WHILE_WHILE (2) or
+        RRG_TRAVERSAL_COMPACT (3)."""
         _check(_lib().rrg_collider_set_traversal(self._h, traversal), "rrg_collider_set_traversal")
+
+    def set_compact_tuning(self, stack_smem: int = 8, rays_per_warp: int = 0, blocks_per_sm: int = 9) -> None:
+        """Knobs of RRG_TRAVERSAL_COMPACT: shared-memory stack entries per
+        thread (0, 8, 16, 32), rays a warp claims at a time (multiple of 32
+        up to 1024; 0 = 32) and the register cap (9 blocks per SM, or 0 =
+        none)."""
+        _check(_lib().rrg_collider_set_compact_tuning(self._h, stack_smem, rays_per_warp, blocks_per_sm),
+               "rrg_collider_set_compact_tuning")
 
     def set_ray_order(self, order: int) -> None:
         """RAY_ORDER_DEFAULT (0: binned from 2^22 rays), RAY_ORDER_AS_GIVEN (1)

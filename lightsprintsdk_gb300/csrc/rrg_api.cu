@@ -54,7 +54,7 @@ int init_collider(Collider* c, const rrg_build_params* params) {
 	}
 	c->params.size = sizeof(rrg_build_params);
 	if (c->params.max_leaf_size > (uint32_t)kMaxLeaf) return RRG_ERR_INVALID;
-	if (c->params.traversal > RRG_TRAVERSAL_WHILE_WHILE) return RRG_ERR_INVALID;
+	if (c->params.traversal > RRG_TRAVERSAL_COMPACT) return RRG_ERR_INVALID;
 	if (c->params.bvh_width != 0 && c->params.bvh_width != 2 && c->params.bvh_width != 8) return RRG_ERR_INVALID;
 	c->width = c->params.bvh_width ? c->params.bvh_width : 2;
 	if (c->width == 8 && c->params.max_leaf_size > (uint32_t)kWideLeafMax) return RRG_ERR_INVALID;
@@ -228,8 +228,23 @@ int rrg_collider_set_ray_order(rrg_collider* h, uint32_t order) {
 
 int rrg_collider_set_traversal(rrg_collider* h, uint32_t traversal) {
 	Collider* c = reinterpret_cast<Collider*>(h);
-	if (!c || traversal > RRG_TRAVERSAL_WHILE_WHILE) return RRG_ERR_INVALID;
+	if (!c || traversal > RRG_TRAVERSAL_COMPACT) return RRG_ERR_INVALID;
 	c->traversal = traversal ? traversal : RRG_TRAVERSAL_IF_IF;
+	return RRG_OK;
+}
+
+int rrg_collider_set_compact_tuning(rrg_collider* h, uint32_t stack_smem, uint32_t rays_per_warp,
+                                    uint32_t blocks_per_sm) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c) return RRG_ERR_INVALID;
+	const uint32_t depth = stack_smem == RRG_COMPACT_DEFAULT ? 8u : stack_smem;
+	const uint32_t rays = rays_per_warp ? rays_per_warp : 32u;
+	const uint32_t minb = blocks_per_sm == RRG_COMPACT_DEFAULT ? 9u : blocks_per_sm;
+	if (!compact_depth_ok(depth) || rays % 32 || rays < 32 || rays > 1024 || (minb && minb != 9))
+		return RRG_ERR_INVALID;
+	c->compact_sdepth = depth;
+	c->compact_fetch = rays / 32;
+	c->compact_minb = minb;
 	return RRG_OK;
 }
 

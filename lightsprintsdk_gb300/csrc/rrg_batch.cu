@@ -14,7 +14,8 @@ struct Batch {
 	Collider* c = nullptr;          // all meshes' geometry; c->nroots = meshes
 	uint32_t nmesh = 0;
 	int fetch = 1;                  // rays per warp / 32
-	int blocks = 0;                 // persistent grid (occupancy x SMs)
+	uint32_t sdepth = 0;            // traversal-stack entries per thread in shared memory (binary tree)
+	int blocks = 0;                 // persistent grid (occupancy x SMs) of the current kernel variant
 	cudaStream_t cap = nullptr;     // private stream the graph is captured on
 	cudaGraphExec_t exec = nullptr;
 	uint32_t graph_kernels = 0;   // kernel nodes of exec
@@ -24,6 +25,7 @@ struct Batch {
 	void* g_hits = nullptr;
 	uint32_t g_n = 0;
 	int g_fetch = 0;
+	uint32_t g_sdepth = 0;
 };
 
 static void free_batch(Batch* b) {
@@ -96,7 +98,7 @@ int rrg_batch_create(const float* xyz, const uint32_t* vert_off, const uint32_t*
 	if (!st) st = globalize_batch_indices(c, d_vert_off, nullptr);
 	if (!st) st = build_bvh(c, nullptr, nullptr);
 	cudaFree(d_vert_off);
-	if (!st) st = batch_trace_blocks(c, nmesh, &b->blocks);
+	if (!st) st = batch_trace_blocks(c, nmesh, 0, &b->blocks);
 	if (!st) {
 		e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
 		if (e != cudaSuccess) st = cuda_fail(e);
@@ -128,6 +130,19 @@ int rrg_batch_set_rays_per_warp(rrg_batch* h, uint32_t rays_per_warp) {
 	return RRG_OK;
 }
 
+int rrg_batch_set_stack_smem(rrg_batch* h, uint32_t entries) {
+	Batch* b = reinterpret_cast<Batch*>(h);
+	if (!b) return RRG_ERR_INVALID;
+	if (entries != 0 && entries != 8 && entries != 16 && entries != 32) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(b->c->device));
+	int blocks = 0;
+	int st = batch_trace_blocks(b->c, b->nmesh, entries, &blocks);
+	if (st) return st;
+	b->sdepth = entries;
+	b->blocks = blocks;
+	return RRG_OK;
+}
+
 int rrg_batch_intersect_device(rrg_batch* h, const float* rays_dev, const uint32_t* ray_off_dev, uint32_t n,
                                float* hits_dev, void* stream) {
 	Batch* b = reinterpret_cast<Batch*>(h);
@@ -138,7 +153,7 @@ int rrg_batch_intersect_device(rrg_batch* h, const float* rays_dev, const uint32
 		return RRG_ERR_INVALID;
 	RRG_CUDA(cudaSetDevice(b->c->device));
 	if (!b->exec || b->g_rays != rays_dev || b->g_off != ray_off_dev || b->g_hits != hits_dev || b->g_n != n ||
-	    b->g_fetch != b->fetch) {
+	    b->g_fetch != b->fetch || b->g_sdepth != b->sdepth) {
 		if (b->exec) {
 			// the previous graph may still be running on the caller's stream
 			RRG_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
@@ -149,7 +164,7 @@ int rrg_batch_intersect_device(rrg_batch* h, const float* rays_dev, const uint32
 		RRG_CUDA(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
 		t_capturing = 1;   // recorded, not launched: counted per graph launch below
 		int st = launch_batch_closest(b->c, reinterpret_cast<const float4*>(rays_dev), n, ray_off_dev, b->nmesh,
-		                              b->fetch, b->blocks, reinterpret_cast<float4*>(hits_dev), b->cap);
+		                              b->fetch, b->blocks, b->sdepth, reinterpret_cast<float4*>(hits_dev), b->cap);
 		t_capturing = 0;
 		cudaError_t e = cudaStreamEndCapture(b->cap, &g);
 		if (st) {
@@ -179,6 +194,7 @@ int rrg_batch_intersect_device(rrg_batch* h, const float* rays_dev, const uint32
 		b->g_hits = hits_dev;
 		b->g_n = n;
 		b->g_fetch = b->fetch;
+		b->g_sdepth = b->sdepth;
 	}
 	RRG_CUDA(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
 	note_launches(b->graph_kernels);

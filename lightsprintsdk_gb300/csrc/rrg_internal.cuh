@@ -101,6 +101,10 @@ struct Collider {
 	int ww_blocks = 0;
 	int wide_blocks = 0;
 	uint32_t traversal = RRG_TRAVERSAL_IF_IF;
+	// RRG_TRAVERSAL_COMPACT tuning (rrg_collider_set_compact_tuning) and its
+	// persistent grid per kernel variant (filled on first use)
+	uint32_t compact_sdepth = 8, compact_fetch = 1, compact_minb = 9;
+	int compact_blocks[32] = {};
 	// batches of meshes (rrg_batch): one BVH root per mesh, nodes 0..nroots-1;
 	// d_tri_off = nroots+1 offsets of each mesh's triangles in d_idx
 	uint32_t nroots = 1;
@@ -150,13 +154,18 @@ int launch_rrray(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, cu
 int launch_rrray_scratch(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, uint32_t* words,
                          cudaStream_t s, int keyed = 0);
 int trace_occupancy(Collider* c);
+// compacting traversal (rrg_compact.cu): closest hit (occ null) or any hit;
+// perm = binned order or null; words[0] work counter (cleared here), [1] status
+int launch_compact(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
+                   uint8_t* occ, uint32_t* words, const uint32_t* perm, cudaStream_t s);
+bool compact_depth_ok(uint32_t sdepth);
 // batches (nmesh roots): ray i belongs to mesh segment_of(ray_off, nmesh, i)
 constexpr uint32_t kBatchMaxMeshes = 8192;
 // the collider holding a batch's meshes (rrg_batch.cu)
 Collider* batch_collider(::rrg_batch* b);
-int batch_trace_blocks(Collider* c, uint32_t nmesh, int* blocks);
+int batch_trace_blocks(Collider* c, uint32_t nmesh, uint32_t sdepth, int* blocks);
 int launch_batch_closest(Collider* c, const float4* rays, uint32_t n, const uint32_t* ray_off, uint32_t nmesh,
-                         int fetch, int blocks, float4* hits, cudaStream_t s);
+                         int fetch, int blocks, uint32_t sdepth, float4* hits, cudaStream_t s);
 
 // combined single-ray queries (rrg_combine.cu)
 Combiner* combiner_new();

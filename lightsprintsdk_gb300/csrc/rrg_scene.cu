@@ -12,6 +12,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -43,6 +44,12 @@ struct Scene {
 	size_t cap_tl = 0, cap_tl_obj = 0;
 	uint32_t* d_counter = nullptr;    // [0] work counter, [1] status
 	int blocks = 0;
+	// host-buffer queries (rrg_scene_intersect_host): one staging buffer
+	// (rays, then hits, then objects), grown on demand; callers take turns
+	std::mutex host_mu;
+	void* d_stage = nullptr;
+	uint32_t stage_cap = 0;
+	cudaStream_t s_host = nullptr;
 };
 
 // RRMatrix3x4::determinant3x3 and invertedTo (RRMath.cpp:605-628) in float,
@@ -373,6 +380,8 @@ static void free_scene(Scene* S) {
 	cudaFree(S->d_tl);
 	cudaFree(S->d_tl_obj);
 	cudaFree(S->d_counter);
+	cudaFree(S->d_stage);
+	if (S->s_host) cudaStreamDestroy(S->s_host);
 	delete S;
 }
 
@@ -491,6 +500,37 @@ int rrg_scene_intersect_device(rrg_scene* h, const float* rays_dev, uint32_t n, 
 	                                               reinterpret_cast<float4*>(hits_dev), objects_dev, S->d_counter);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
+}
+
+int rrg_scene_intersect_host(rrg_scene* h, const float* rays_host, uint32_t n, float* hits_host,
+                             uint32_t* objects_host) {
+	Scene* S = reinterpret_cast<Scene*>(h);
+	if (!S || (n && (!rays_host || !hits_host)) || n >= 0x80000000u) return RRG_ERR_INVALID;
+	if (!n) return RRG_OK;
+	std::lock_guard<std::mutex> lk(S->host_mu);
+	RRG_CUDA(cudaSetDevice(S->c->device));
+	if (!S->s_host) RRG_CUDA(cudaStreamCreateWithFlags(&S->s_host, cudaStreamNonBlocking));
+	const size_t per = 32 + 16 + 4;   // ray, hit record, object
+	if (n > S->stage_cap) {
+		uint32_t cap = S->stage_cap ? S->stage_cap : 256;
+		while (cap < n) cap = cap > 0x40000000u ? n : cap * 2;
+		cudaFree(S->d_stage);
+		S->d_stage = nullptr;
+		S->stage_cap = 0;
+		RRG_CUDA(cudaMalloc(&S->d_stage, per * (size_t)cap));
+		S->stage_cap = cap;
+	}
+	uint8_t* base = static_cast<uint8_t*>(S->d_stage);
+	float* d_rays = reinterpret_cast<float*>(base);
+	float* d_hits = reinterpret_cast<float*>(base + 32 * (size_t)S->stage_cap);
+	uint32_t* d_obj = reinterpret_cast<uint32_t*>(base + 48 * (size_t)S->stage_cap);
+	cudaStream_t s = S->s_host;
+	RRG_CUDA(cudaMemcpyAsync(d_rays, rays_host, 32 * (size_t)n, cudaMemcpyHostToDevice, s));
+	int st = rrg_scene_intersect_device(h, d_rays, n, d_hits, objects_host ? d_obj : nullptr, s);
+	if (st) return st;
+	RRG_CUDA(cudaMemcpyAsync(hits_host, d_hits, 16 * (size_t)n, cudaMemcpyDeviceToHost, s));
+	if (objects_host) RRG_CUDA(cudaMemcpyAsync(objects_host, d_obj, 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
+	return rrg_scene_status(h, s);
 }
 
 int rrg_scene_status(rrg_scene* h, void* stream) {

@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_occluded_w(const uint4* __
 // shared memory) and is traced from that mesh's root, node m; its hit
 // triangle is reported as an index local to mesh m.  A warp takes
 // 32 * fetch consecutive rays per atomic (the rays-per-warp knob).
-template <bool WIDE>
+template <bool WIDE, int SDEPTH>
 __global__ void __launch_bounds__(kTraceThreads) k_batch_closest(const TNode* __restrict__ nodes, int nnodes,
                                                                  const uint4* __restrict__ wn, int nwnodes,
                                                                  const float4* __restrict__ tris, int ntris,
@@ -180,6 +180,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_batch_closest(const TNode* __
                                                                  uint32_t nmesh, int fetch,
                                                                  float4* __restrict__ hits, uint32_t* counter) {
 	extern __shared__ uint32_t s_off[];
+	__shared__ int s_stack[(SDEPTH > 0 ? SDEPTH : 1) * kTraceThreads];
+	int* const sst = s_stack + threadIdx.x;
 	for (uint32_t k = threadIdx.x; k <= nmesh; k += blockDim.x) s_off[k] = ray_off[k];
 	__syncthreads();
 	const int lane = threadIdx.x & 31;
@@ -201,6 +203,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_batch_closest(const TNode* __
 			int slot = -1;
 			if (r.tmin <= r.tmax) {
 				if (WIDE) slot = traverse_wide<false>(wn, tris, r, nwnodes, ntris, tbest, best_tri, overflow, (int)m);
+				else if (SDEPTH > 0)
+					slot = traverse_split<false, SDEPTH>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow, sst,
+					                                     (int)m);
 				else slot = traverse<false>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow, nullptr, (int)m);
 			}
 			if (overflow) atomicOr(counter + 1, (uint32_t)RRG_ERR_STACK);
@@ -465,6 +470,14 @@ int launch_closest_on(Collider* c, const float4* rays, uint32_t n, float4* hits,
 		RRG_CUDA(cudaGetLastError());
 		return RRG_OK;
 	}
+	if (c->traversal == RRG_TRAVERSAL_COMPACT) {
+		const uint32_t* perm = nullptr;
+		if (use_binning(c, n)) {
+			int st = bin_rays(c, rays, n, s, bin_slot, &perm);
+			if (st) return st;
+		}
+		return launch_compact(c, rays, n, hits, planes, points, nullptr, words, perm, s);
+	}
 	if (c->traversal != RRG_TRAVERSAL_IF_IF) {
 		int grid = (int)(want < (uint32_t)c->ww_blocks ? want : (uint32_t)c->ww_blocks);
 		rrg::note_launch(), k_trace_ww<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays,
@@ -494,6 +507,14 @@ int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, fl
 
 int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, cudaStream_t s) {
 	if (!n) return RRG_OK;
+	if (c->traversal == RRG_TRAVERSAL_COMPACT && !(c->width == 8 && c->d_wnodes)) {
+		const uint32_t* perm = nullptr;
+		if (use_binning(c, n)) {
+			int st = bin_rays(c, rays, n, s, 3, &perm);
+			if (st) return st;
+		}
+		return launch_compact(c, rays, n, nullptr, nullptr, nullptr, occ, c->d_counter, perm, s);
+	}
 	RRG_CUDA(cudaMemsetAsync(c->d_counter, 0, 4, s));
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
 	if (c->width == 8 && c->d_wnodes) {
@@ -547,14 +568,25 @@ int launch_rrray_scratch(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit
 	return RRG_OK;
 }
 
-int batch_trace_blocks(Collider* c, uint32_t nmesh, int* blocks) {
+using BatchKernel = void (*)(const TNode*, int, const uint4*, int, const float4*, int, const float4*, uint32_t,
+                             const uint32_t*, const uint32_t*, uint32_t, int, float4*, uint32_t*);
+
+// k_batch_closest for the tree width and the shared-memory stack depth
+// (0, 8, 16 or 32 entries; the wide walk keeps its own local stack)
+static BatchKernel batch_kernel(const Collider* c, uint32_t sdepth) {
+	if (c->width == 8 && c->d_wnodes) return k_batch_closest<true, 0>;
+	switch (sdepth) {
+		case 8: return k_batch_closest<false, 8>;
+		case 16: return k_batch_closest<false, 16>;
+		case 32: return k_batch_closest<false, 32>;
+		default: return k_batch_closest<false, 0>;
+	}
+}
+
+int batch_trace_blocks(Collider* c, uint32_t nmesh, uint32_t sdepth, int* blocks) {
 	int per_sm = 0;
-	if (c->width == 8)
-		RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_closest<true>, kTraceThreads,
-		                                                       sizeof(uint32_t) * (nmesh + 1)));
-	else
-		RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_closest<false>, kTraceThreads,
-		                                                       sizeof(uint32_t) * (nmesh + 1)));
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(c, sdepth), kTraceThreads,
+	                                                       sizeof(uint32_t) * (nmesh + 1)));
 	*blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
 	return RRG_OK;
 }
@@ -562,21 +594,17 @@ int batch_trace_blocks(Collider* c, uint32_t nmesh, int* blocks) {
 // Clears the work counter and launches k_batch_closest on stream s (both
 // stream-ordered, so the pair can be captured in a CUDA graph).
 int launch_batch_closest(Collider* c, const float4* rays, uint32_t n, const uint32_t* ray_off, uint32_t nmesh,
-                         int fetch, int blocks, float4* hits, cudaStream_t s) {
+                         int fetch, int blocks, uint32_t sdepth, float4* hits, cudaStream_t s) {
 	if (!n) return RRG_OK;
 	RRG_CUDA(cudaMemsetAsync(c->d_counter, 0, 4, s));
 	const uint32_t per_fetch = 32u * (uint32_t)fetch;
 	const uint32_t want = (uint32_t)(((uint64_t)n + per_fetch - 1) / per_fetch * 32 / kTraceThreads + 1);
 	const int grid = (int)(want < (uint32_t)blocks ? want : (uint32_t)blocks);
 	const size_t smem = sizeof(uint32_t) * (nmesh + 1);
-	if (c->width == 8 && c->d_wnodes)
-		rrg::note_launch(), k_batch_closest<true><<<grid, kTraceThreads, smem, s>>>(c->d_nodes, (int)c->nnodes, c->d_wnodes,
-		                                                       (int)c->nwnodes, c->d_wtris, (int)c->nvalid, rays, n,
-		                                                       ray_off, c->d_tri_off, nmesh, fetch, hits, c->d_counter);
-	else
-		rrg::note_launch(), k_batch_closest<false><<<grid, kTraceThreads, smem, s>>>(c->d_nodes, (int)c->nnodes, c->d_wnodes,
-		                                                        (int)c->nwnodes, c->d_tris, (int)c->nvalid, rays, n,
-		                                                        ray_off, c->d_tri_off, nmesh, fetch, hits, c->d_counter);
+	const bool wide = c->width == 8 && c->d_wnodes;
+	rrg::note_launch(), batch_kernel(c, sdepth)<<<grid, kTraceThreads, smem, s>>>(
+	    c->d_nodes, (int)c->nnodes, c->d_wnodes, (int)c->nwnodes, wide ? c->d_wtris : c->d_tris, (int)c->nvalid, rays,
+	    n, ray_off, c->d_tri_off, nmesh, fetch, hits, c->d_counter);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }

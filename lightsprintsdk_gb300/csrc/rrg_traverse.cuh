@@ -262,6 +262,62 @@ __device__ int traverse(const TNode* __restrict__ nodes, const float4* __restric
 }
 
 
+// traverse() with a split stack: the top SDEPTH entries of the thread's
+// stack in shared memory at sst[d * kTraceThreads] (sst = the block's stack
+// array + threadIdx.x, so a warp's lanes touch 32 consecutive words), the
+// deeper ones in a local array.  Same visits and results as traverse().
+template <bool ANY, int SDEPTH>
+__device__ __forceinline__ int traverse_split(const TNode* __restrict__ nodes, const float4* __restrict__ tris,
+                                              const RayState& r, int nnodes, int ntris, float& tbest,
+                                              uint32_t& best_tri, bool& overflow, int* sst, int root = 0) {
+	int spill[kStackSize - SDEPTH];
+	int sp = 0;
+	int ref = root;
+	int best_slot = -1;
+	for (uint32_t steps = 0;; steps++) {
+		if (steps >= kMaxSteps) { overflow = true; break; }
+		if (ref >= 0) {
+			if (ref >= nnodes) { overflow = true; break; }
+			const float4* np = reinterpret_cast<const float4*>(nodes + ref);
+			const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
+			const int4 nd = __ldg(reinterpret_cast<const int4*>(np + 3));
+			const float t0 = nd.x != kEmptyRef ? box_enter(r, na.x, na.y, na.z, na.w, nc.x, nc.y, tbest) : INFINITY;
+			const float t1 = nd.y != kEmptyRef ? box_enter(r, nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, tbest) : INFINITY;
+			const bool h0 = t0 != INFINITY, h1 = t1 != INFINITY;
+			if (h0 && h1) {
+				const int nearr = t0 <= t1 ? nd.x : nd.y;
+				const int farr = t0 <= t1 ? nd.y : nd.x;
+				if (sp < SDEPTH) sst[sp++ * kTraceThreads] = farr;
+				else if (sp < kStackSize) { spill[sp - SDEPTH] = farr; sp++; }
+				else overflow = true;
+				ref = nearr;
+				continue;
+			}
+			if (h0) { ref = nd.x; continue; }
+			if (h1) { ref = nd.y; continue; }
+		} else {
+			const int first = ref & 0x07FFFFFF;
+			const int count = ((ref >> 27) & 15) + 1;
+			if (first + count > ntris) { overflow = true; break; }
+			for (int k = 0; k < count; k++) {
+				float4 a, b, c;
+				load_tri(tris, first + k, a, b, c);
+				const uint32_t tri = (uint32_t)__float_as_int(a.w);
+				float t;
+				if (tri_test(r, a, b, c, tbest, tri, best_tri, t)) {
+					tbest = t;
+					best_tri = tri;
+					best_slot = first + k;
+					if (ANY) return best_slot;
+				}
+			}
+		}
+		if (sp == 0) break;
+		--sp;
+		ref = sp < SDEPTH ? sst[sp * kTraceThreads] : spill[sp - SDEPTH];
+	}
+	return best_slot;
+}
 
 // ------------------------------------------------------------ 8-wide BVH
 // Header of the node being walked: child/triangle bases and the slot codes.

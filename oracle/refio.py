@@ -152,6 +152,25 @@ def run_ref_enumerate(v, normals, t, uv, size: int):
 #                u32 idx[3nt]; f32 uv[6nt]; f32 albedo[3nt]; i32 atlas[nt];
 #                f32 lights[12]; u32 out_atlas[nout]
 # GATHER "RGG1": u32 nout, u32 size, f32 rgba[nout*size*size*4]
+def write_gather_scene(path: str, gs, atlases, quality: int, seed: int) -> None:
+    """The "RGS1" scene file of a GatherScene (format above)."""
+    sc = gs.scene
+    atlases = np.asarray(atlases, np.uint32)
+    L = gs.lights
+    lights = np.concatenate([L["dir_direction"], L["dir_color"], L["point_position"], L["point_color"]]).astype(np.float32)
+    with open(path, "wb") as f:
+        f.write(b"RGS1")
+        f.write(np.array([sc.vertices.shape[0], sc.ntri, gs.natlas, gs.size, quality, atlases.shape[0], seed],
+                         np.uint32).tobytes())
+        f.write(np.ascontiguousarray(sc.vertices, np.float32).tobytes())
+        f.write(np.ascontiguousarray(sc.indices, np.uint32).tobytes())
+        f.write(np.ascontiguousarray(gs.uv, np.float32).tobytes())
+        f.write(np.ascontiguousarray(gs.albedo, np.float32).tobytes())
+        f.write(np.ascontiguousarray(gs.tri_atlas, np.int32).tobytes())
+        f.write(lights.tobytes())
+        f.write(atlases.tobytes())
+
+
 def run_ref_gather(gs, atlases, quality: int, seed: int = 1, threads: int = 0, bake: bool = False) -> np.ndarray:
     """The reference's own processTexel over whole atlases of a GatherScene,
     with no radiosity solver (the plain N-bounce estimator, stopAtDepth 20),
@@ -161,23 +180,10 @@ def run_ref_gather(gs, atlases, quality: int, seed: int = 1, threads: int = 0, b
     with bake also the solver the final gather read, per triangle: dict of
     direct (T,3), indirect (T,3) and smoothed corner indirect (T,3,3)."""
     exe = os.path.join(REF_DIR, "ref_gather")
-    sc = gs.scene
     atlases = np.asarray(atlases, np.uint32)
-    L = gs.lights
-    lights = np.concatenate([L["dir_direction"], L["dir_color"], L["point_position"], L["point_color"]]).astype(np.float32)
     with tempfile.TemporaryDirectory() as d:
         sp, op = os.path.join(d, "s"), os.path.join(d, "o")
-        with open(sp, "wb") as f:
-            f.write(b"RGS1")
-            f.write(np.array([sc.vertices.shape[0], sc.ntri, gs.natlas, gs.size, quality, atlases.shape[0], seed],
-                             np.uint32).tobytes())
-            f.write(np.ascontiguousarray(sc.vertices, np.float32).tobytes())
-            f.write(np.ascontiguousarray(sc.indices, np.uint32).tobytes())
-            f.write(np.ascontiguousarray(gs.uv, np.float32).tobytes())
-            f.write(np.ascontiguousarray(gs.albedo, np.float32).tobytes())
-            f.write(np.ascontiguousarray(gs.tri_atlas, np.int32).tobytes())
-            f.write(lights.tobytes())
-            f.write(atlases.tobytes())
+        write_gather_scene(sp, gs, atlases, quality, seed)
         subprocess.run([exe, sp, op, str(threads)] + (["bake"] if bake else []), capture_output=True, text=True,
                        check=True)
         b = open(op, "rb").read()

@@ -102,3 +102,58 @@ def compare_sequences(gpu_seqs, ref_seqs, tie_rel: float = 1e-6):
         counts["differ"] += 1
         bad.append(i)
     return counts, bad
+
+
+MULTI = np.dtype([("hit", "u1"), ("obj", "<i4"), ("tri", "<u4"), ("dist", "<f4"), ("u", "<f4"), ("v", "<f4"),
+                  ("side", "u1")])
+MULTI_HANDLER = np.dtype([("result", "u1"), ("obj", "<i4"), ("tri", "<u4"), ("offers", "<u4")])
+
+
+def run_multi(exe: str, tmp_path, meshes, objects, rays):
+    """meshes: list of (v, t); objects: list of (mesh index, enabled,
+    3x4 world matrix).  Runs plugin_check's multi mode; returns (info,
+    (gpu records, gpu handler records), (ref records, ref handler records))."""
+    d = str(tmp_path)
+    sp, rp, op = os.path.join(d, "scene"), os.path.join(d, "rays"), os.path.join(d, "mlog")
+    with open(sp, "wb") as f:
+        f.write(b"RGO1")
+        f.write(np.array([len(meshes)], np.uint32).tobytes())
+        for v, t in meshes:
+            v = np.ascontiguousarray(v, np.float32)
+            t = np.ascontiguousarray(t, np.uint32)
+            f.write(np.array([v.shape[0], t.shape[0]], np.uint32).tobytes())
+            f.write(v.tobytes())
+            f.write(t.tobytes())
+        f.write(np.array([len(objects)], np.uint32).tobytes())
+        for m, en, w in objects:
+            f.write(np.array([m, 1 if en else 0], np.uint32).tobytes())
+            f.write(np.ascontiguousarray(w, np.float32).reshape(12).tobytes())
+    from oracle import refio
+    refio.write_rays(rp, rays)
+    out = subprocess.run([exe, "multi", sp, rp, op], capture_output=True, text=True, timeout=900,
+                         check=True).stdout
+    info = json.loads(out.strip().splitlines()[-1])
+    n = len(rays)
+    res = []
+    for side in ("gpu", "ref"):
+        b = open(op + "." + side, "rb").read()
+        a = np.frombuffer(b, MULTI, n, 0).copy()
+        h = np.frombuffer(b, MULTI_HANDLER, n, MULTI.itemsize * n).copy()
+        res.append((a, h))
+    return info, res[0], res[1]
+
+
+def run_lightmaps(exe: str, tmp_path, gs, atlases, quality: int, mode: str, seed: int):
+    """plugin_check's lightmaps mode (rrgpu_plugin::updateLightmaps on a
+    reference RRSolver): returns (info, (len(atlases), size, size, 4) RGBA)."""
+    from oracle import refio
+    d = str(tmp_path)
+    sp, op = os.path.join(d, "lscene"), os.path.join(d, "lout")
+    refio.write_gather_scene(sp, gs, atlases, quality, seed)
+    out = subprocess.run([exe, "lightmaps", sp, op, mode, str(seed)], capture_output=True, text=True, timeout=900,
+                         check=True).stdout
+    info = json.loads(out.strip().splitlines()[-1])
+    b = open(op, "rb").read()
+    assert b[:4] == b"RGG1"
+    nout, size = (int(x) for x in np.frombuffer(b, np.uint32, 2, 4))
+    return info, np.frombuffer(b, np.float32, nout * size * size * 4, 12).reshape(nout, size, size, 4).copy()

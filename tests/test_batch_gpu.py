@@ -143,3 +143,19 @@ def test_launch_count_counts_graph_replays_not_captures(small_batch):
         deltas.append(col.launch_count() - n0)
     torch.cuda.synchronize()
     assert deltas[0] >= 1 and deltas[0] == deltas[1] == deltas[2], deltas
+
+
+def test_stack_depths_agree(small_batch):
+    """The autotuner's stack-depth knob (shared-memory entries per thread)
+    changes where the traversal stack lives, never a result."""
+    mb, counts, rays, off, off_d, b = small_batch
+    b.set_stack_smem(0)
+    base = run(b, rays, off_d, 32)
+    for sd in (8, 16, 32):
+        b.set_stack_smem(sd)
+        for k in (32, 128):
+            np.testing.assert_array_equal(run(b, rays, off_d, k).view(np.uint32), base.view(np.uint32),
+                                          err_msg=f"stack {sd} rays per warp {k}")
+    with pytest.raises(col.RRGError):
+        b.set_stack_smem(12)
+    b.set_stack_smem(0)

@@ -140,9 +140,13 @@ def test_handler_replay_config0(exe, tmp_path):
     # (the first 69,451 faces of the subdivided sphere leave a small hole,
     # so a few rays leave it without a second hit)
     assert sum(len(s[0]) >= 2 for s in gpu[0]) >= 0.99 * len(rays)
-    assert counts["differ"] <= 2, (counts, bad[:8])
+    # observed on GB300: 2,038 identical sequences; on 10 rays the reference
+    # offers one triangle twice (a triangle in two kd leaves whose ranges
+    # overlap by DELTA_BSP), ours once
+    assert counts["differ"] == 0 and counts["tie_order"] <= 2, (counts, bad[:8])
+    assert counts["ref_repeat"] <= 12, counts
     same = np.asarray([i for i in range(len(rays)) if np.array_equal(gpu[0][i][0], ref[0][i][0])])
-    assert len(same) >= len(rays) - 4
+    assert len(same) >= len(rays) - 14
     check_accepted(gpu, ref, same, 1, v, t, rays)
 
 
@@ -158,6 +162,116 @@ def test_handler_replay_config1(exe, tmp_path):
     info, gpu, ref = H.run_handler(exe, tmp_path, sc.vertices, sc.indices, rays, accept_at=2)
     counts, bad = H.compare_sequences(gpu[0], ref[0])
     record("handler_config1", {"counts": counts, "bad": bad[:64]})
-    assert counts["differ"] <= 8, (counts, bad[:8])
+    # observed on GB300: 2,018 identical, 9 tie orders (coincident faces),
+    # 17 reference repeats, 4 other (rays grazing abutting slabs, where the
+    # reference's plane-distance test and the watertight test disagree)
+    assert counts["differ"] <= 4, (counts, bad[:8])
+    assert counts["same"] >= 2010, counts
     same = np.asarray([i for i in range(len(rays)) if np.array_equal(gpu[0][i][0], ref[0][i][0])])
     check_accepted(gpu, ref, same, 2, sc.vertices, sc.indices, rays)
+
+
+def test_multi_object_collider_against_rrcollidermulti(exe, tmp_path):
+    """RRCollider::create(nullptr, &objects, GPU technique) against the
+    reference's RRColliderMulti on the same RRObjects (each object's collider
+    IT_BSP_FASTEST): the config-1 interior as a static object and 64 sphere
+    instances, one of them mirrored (negative determinant) and one disabled.
+    Without a handler: the same hit, hitObject and hitTriangle on all but
+    near-tie rays, and where those agree the same hitFrontSide and
+    hitDistance within 1e-5 relative.  With a handler (accept the second
+    hit) the ray goes to the reference's own RRColliderMulti, so the results
+    are identical."""
+    from lightsprintsdk_gb300 import scenes
+    from tests.test_scene_gpu import split_interior
+    sc = scenes.interior_c1()
+    static, sphere, obj_mesh, world, _ = split_interior(sc)
+    world = world.copy()
+    world[5, :, 0] *= -1.0            # a mirrored instance
+    objects = [(int(obj_mesh[i]), i != 9, world[i]) for i in range(len(obj_mesh))]
+    rays = np.concatenate([scenes.camera_rays(rows=8, cols=list(range(0, 4096, 16))),
+                           scenes.surface_rays(sc.vertices, sc.indices, 8192)])
+    info, (g, gh), (r, rh) = H.run_multi(exe, tmp_path, [static, sphere], objects, rays)
+    assert info["gpu_technique"] == 100, info
+    same = (g["hit"] == r["hit"]) & (g["obj"] == r["obj"]) & (g["tri"] == r["tri"])
+    record("multi_object", {"rays": len(rays), "differ": int((~same).sum()), "hits": int(r["hit"].sum()),
+                            "mirrored_hits": int(((r["obj"] == 5) & (r["hit"] == 1)).sum()),
+                            "disabled_hits_gpu": int(((g["obj"] == 9) & (g["hit"] == 1)).sum())})
+    assert (~same).sum() <= max(4, 2e-4 * len(rays)), np.nonzero(~same)[0][:16]
+    assert not np.any((g["obj"] == 9) & (g["hit"] == 1))
+    assert np.any((r["obj"] == 5) & (r["hit"] == 1))
+    m = same & (r["hit"] == 1)
+    np.testing.assert_array_equal(g["side"][m], r["side"][m])
+    np.testing.assert_allclose(g["dist"][m], r["dist"][m], rtol=1e-5)
+    for f in ("result", "obj", "tri", "offers"):
+        np.testing.assert_array_equal(gh[f], rh[f], err_msg=f)
+
+
+def _covered_only(runs, flags):
+    """The fixture is processTexel's output, unfiltered; updateLightmaps
+    then runs updateLightmap's filters, which with smoothing and spreading
+    off change only texels the gather did not cover.  Those are set back to
+    what the unfiltered gather leaves there (zero) before comparing."""
+    out = []
+    for r in runs:
+        r = r.copy()
+        r[flags == 0] = 0.0
+        out.append(r)
+    return out
+
+
+def test_update_lightmaps_adapter_plain_gather(exe, tmp_path):
+    """rrgpu_plugin::updateLightmaps (include/rrgpu_update_lightmaps.hpp) on
+    a reference RRSolver holding the small room (its static objects' collider
+    the GPU technique), with useCurrentSolution (the plain 20-bounce gather),
+    against the reference's own processTexel runs of the same atlases
+    (tests/golden/gather_ref.npz), by the criteria of the GPU gather's own
+    reference test: texels no random number changes to 1e-6, the rest
+    statistically, alpha bit-exact."""
+    from lightsprintsdk_gb300 import scenes
+    from tests.helpers import load_golden, reference_gather_ok, reference_gather_stats
+    g = load_golden("gather_ref.npz")
+    gs = scenes.gather_room()
+    runs = []
+    for seed in (21, 22):
+        info, px = H.run_lightmaps(exe, tmp_path, gs, g["atlases"], int(g["quality"]), "plain", seed)
+        assert info["updated"] == len(g["atlases"]) and info["multi_technique"] == 100, info
+        runs.append(px)
+    runs = _covered_only(runs, g["flags"])
+    stats = reference_gather_stats(g, runs[0], runs[1])
+    record("update_lightmaps_plain", {"stats": [{k: (float(v) if not isinstance(v, (bool, int)) else v)
+                                                 for k, v in s.items()} for s in stats]})
+    for a, s in zip(g["atlases"], stats):
+        assert reference_gather_ok(s, det_rel=1e-6), (int(a), s)
+
+
+def test_update_lightmaps_adapter_default_bake(exe, tmp_path):
+    """The same adapter with UpdateParameters' defaults (useCurrentSolution
+    false: first gather, radiosity, final gather reading the solver) against
+    the reference's own updateLightmaps with its solver (tests/golden/
+    bake_ref.npz, filtering with smoothing and spreading off, as here):
+    each atlas's mean over its covered texels within the bound the GPU
+    bake's own reference test uses, and the texels no random number changes
+    to 1e-6."""
+    from lightsprintsdk_gb300 import scenes
+    from tests.helpers import BAKE_ATLAS_ALLOW, _within, load_golden
+    g = load_golden("bake_ref.npz")
+    gs = scenes.gather_room()
+    runs = []
+    for seed in (11, 12, 13):
+        info, px = H.run_lightmaps(exe, tmp_path, gs, g["atlases"], int(g["quality"]), "bake", seed)
+        assert info["updated"] == len(g["atlases"]), info
+        runs.append(px)
+    cov = g["flags"] > 0
+    ours = np.stack([[r[a][cov[a]][:, :3].astype(np.float64).mean(0) for a in range(cov.shape[0])] for r in runs])
+    within = _within(ours, g["atlas_means"].astype(np.float64), BAKE_ATLAS_ALLOW)
+    det = g["det_mask"]
+    same = np.all(runs[0][..., :3] == runs[1][..., :3], axis=-1) & np.all(runs[0][..., :3] == runs[2][..., :3],
+                                                                       axis=-1)
+    keep = same[det]
+    d = det & same
+    rel = np.abs(runs[0][..., :3][d].astype(np.float64) - g["det_rgb"].astype(np.float64)[keep])
+    rel /= np.maximum(np.abs(g["det_rgb"].astype(np.float64)[keep]), 1e-30)
+    record("update_lightmaps_bake", {"atlas_within": within.tolist(), "det_n": int(d.sum()),
+                                     "det_rel": float(rel.max()) if d.any() else 0.0})
+    assert float(within.max()) < 1, within
+    assert d.sum() > 2000 and float(rel.max()) <= 1e-6
