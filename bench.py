@@ -636,7 +636,7 @@ def run_gather(args, world, rank, local):
         del plain_out
     if learned:
         extra.update(learned_errors(L, gs, params, out, natl, stream, sp))
-    elif rank == 0:
+    elif rank == 0 and not args.gather_only:
         extra["filters"] = filter_timing(L, out, natl, stream, sp, gs, not args.no_cpu_baseline)
         extra["bake"] = bake_timing(L, gs, natl, stream, sp)
     if rank == 0:
@@ -747,6 +747,8 @@ def main():
     ap.add_argument("--rays", type=int, default=0, help="smaller case of the workload (profiling)")
     ap.add_argument("--meshes", type=int, default=512, help="c3: first N meshes only (profiling)")
     ap.add_argument("--bvh-width", type=int, default=0, choices=[0, 2, 8], help="c0/c1: BVH width (0 = default)")
+    ap.add_argument("--gather-only", action="store_true",
+                    help="c2: time the gather alone (no filter or bake timings; small profiling cases)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

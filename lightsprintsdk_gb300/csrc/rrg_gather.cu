@@ -962,6 +962,34 @@ __global__ void __launch_bounds__(128, 8) k_wf_closest(GatherScene g, WfState w,
 	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
 }
 
+// The learned gather's first segments on the wavefront: one thread per path
+// the set-up (k_gather<0, 0, 1>) started, each path's first hit as a cache
+// query record (first_hit, as the warp-per-texel learned kernel writes it),
+// record of path p = ti * Q + k at recs[p] (recs = the batch's first texel's
+// records).
+__global__ void __launch_bounds__(128, 8) k_wf_first_hit(GatherScene g, WfState w, CacheRec* __restrict__ recs,
+                                                       uint32_t* status) {
+	const uint32_t n = w.counts[0];
+	bool overflow = false;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const uint32_t p = w.live[i];
+		const float4 e = w.eye[p], d = w.dir[p];
+		recs[p] = first_hit(g, mk(e.x, e.y, e.z), mk(d.x, d.y, d.z), __float_as_uint(e.w), overflow);
+	}
+	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// The learned texel's first term, the light rounds' average, as the
+// warp-per-texel learned kernel writes it (uncovered texels: the set-up wrote 0).
+__global__ void k_wf_learned_out(GatherScene g, WfState w, uint32_t nb, uint64_t out_base, float4* __restrict__ out) {
+	const uint32_t ti = blockIdx.x * blockDim.x + threadIdx.x;
+	if (ti >= nb) return;
+	const uint64_t tid = w.slot_tid[ti];
+	if (tid == ~0ull) return;
+	const float4 l = w.slot_lights[ti];
+	out[tid - out_base] = make_float4(l.x, l.y, l.z, texel_alpha(g, tid));
+}
+
 // Next event estimation of every path that hit (trace_path's loop body after
 // the closest hit): the contribution toward each light, and a shadow ray
 // where the light is above the surface and the contribution is not zero.
@@ -1362,8 +1390,10 @@ static int launch_gather_kernel(Lightmapper* L, const GatherScene& g, uint64_t f
 constexpr uint64_t kWfMinTexels = 16384;
 constexpr uint64_t kWfMaxPaths = 1ull << 23;
 
+// recs: the learned gather's first segments instead (the records of texel
+// first + i at recs + i * Q, out = the light rounds' average).
 static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first, uint64_t count, float4* out,
-                            float4* bent, cudaStream_t s) {
+                            float4* bent, cudaStream_t s, CacheRec* recs = nullptr) {
 	const uint32_t Q = g.quality;
 	const uint32_t rounds = Q / 10 + 1;
 	const uint32_t N = Q > rounds ? Q : rounds;
@@ -1413,6 +1443,12 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 		    g, L->d_off, L->d_sub, first + b0, nb, nullptr, first, out, nullptr, reinterpret_cast<uint32_t*>(L->d_counter),
 		    L->d_status, nullptr, DirOut{}, w);
 		RRG_CUDA(cudaGetLastError());
+		if (recs) {
+			rrg::note_launch(), k_wf_first_hit<<<grid_c, 128, 0, s>>>(g, w, recs + b0 * Q, L->d_status);
+			rrg::note_launch(), k_wf_learned_out<<<(int)((nb + 127) / 128), 128, 0, s>>>(g, w, (uint32_t)nb, first, out);
+			RRG_CUDA(cudaGetLastError());
+			continue;
+		}
 		int cur = 0;
 		for (uint32_t depth = 0; depth <= g.max_depth; depth++) {
 			RRG_CUDA(cudaMemsetAsync(w.counts + 2, 0, 2 * sizeof(uint32_t), s));
@@ -2195,7 +2231,11 @@ int rrg_lightmap_gather_learned(rrg_lightmapper* h, rrg_cache* cache, const rrg_
 	for (uint64_t c0 = first; c0 < first + count; c0 += chunk) {
 		const uint64_t n = (first + count - c0) < chunk ? (first + count - c0) : chunk;
 		float4* oc = out + (c0 - first);
-		st = launch_gather_kernel<true>(L, g, c0, n, nullptr, c0, oc, L->d_recs, s);
+		const uint32_t sched = p->mode & 3u;
+		if (sched == RRG_GATHER_WAVEFRONT || (sched == RRG_GATHER_AUTO && n >= kWfMinTexels))
+			st = gather_wavefront(L, g, c0, n, oc, nullptr, s, L->d_recs);
+		else
+			st = launch_gather_kernel<true>(L, g, c0, n, nullptr, c0, oc, L->d_recs, s);
 		if (st) return st;
 		st = rrg_cache_infer(cache, L->d_recs, n * Q, reinterpret_cast<float*>(L->d_rad), stream);
 		if (st) return st;

@@ -198,3 +198,30 @@ def test_learned_gather_error_and_gain(gather_setup):
     # the network must gain a lot over the method without it
     assert summary["learned_no_fallback"] < 0.5 * summary["without_cache"], summary
     assert summary["learned"] <= summary["plain64"] * 1.05, summary
+
+
+def test_learned_gather_schedules_agree(gather_setup):
+    """The learned gather's first segments on the wavefront (one thread per
+    path after the wavefront set-up) and on the warp-per-texel kernel: the
+    same cache records and the same texels, bit for bit, with and without
+    the fallback."""
+    import torch
+    gs, c, L = gather_setup
+    S = gs.size * gs.size
+    cache = rc.RadianceCache.for_scene(gs.scene.vertices, seed=7, encoding=rc.HASHGRID, log2_table=15)
+    p = lm.make_params(gs.lights, quality=64, max_depth=8, seed=0xC2)
+    tmp = torch.empty((2 * S, 4), dtype=torch.float32, device="cuda")
+    rc.bake_learned(L, cache, p, 0, 2 * S, tmp.data_ptr(), steps=50, batch=16384)
+    outs = {}
+    for mode in (lm.GATHER_WARP, lm.GATHER_WAVEFRONT):
+        pm = lm.make_params(gs.lights, quality=64, max_depth=8, seed=0xC2, mode=mode)
+        for frac in (2.0, 0.25):
+            out = torch.full((2 * S, 4), 7.0, dtype=torch.float32, device="cuda")
+            nf = rc.gather_learned(L, cache, pm, 9 * S, 2 * S, out.data_ptr(), fallback_frac=frac)
+            torch.cuda.synchronize()
+            outs[(mode, frac)] = (out.cpu().numpy(), nf)
+    for frac in (2.0, 0.25):
+        a, na = outs[(lm.GATHER_WARP, frac)]
+        b, nb = outs[(lm.GATHER_WAVEFRONT, frac)]
+        assert na == nb
+        np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
