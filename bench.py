@@ -479,6 +479,45 @@ def learned_errors(L, gs, params, out, natl, stream, sp, atlases=(0, 9, 100), se
     return {"errors_vs_converged": res}
 
 
+def gather_rays(L, c, gs, params, n, out, ms, stream, sp) -> dict:
+    """The gather as a ray workload: the closest-hit and shadow rays one
+    gather of the timed texels traces (counted on the device in an untimed
+    repeat), their rate at the timed step's duration, and that rate as a
+    fraction of the collider's own on the same scene (closest hit on 4 Mi
+    surface rays and any hit on 4 Mi shadow rays, mixed in the gather's
+    proportion)."""
+    import torch
+    from lightsprintsdk_gb300 import scenes
+    L.count_rays(True)
+    L.gather_device(params, 0, n, out.data_ptr(), sp)
+    closest, shadow = L.count_rays(False)
+    sc = gs.scene
+    k = 1 << 22
+    rs = torch.from_numpy(scenes.surface_rays(sc.vertices, sc.indices, k, seed=0x6A7)).cuda()
+    rsh = torch.from_numpy(scenes.shadow_rays(sc.vertices, sc.indices, k, seed=0x6A7)).cuda()
+    hits = torch.empty((k, 4), dtype=torch.float32, device="cuda")
+    occ = torch.empty(k, dtype=torch.uint8, device="cuda")
+
+    def rate(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return 3 * k / (e0.elapsed_time(e1) * 1e-3)
+    r_closest = rate(lambda: c.intersect_device(rs.data_ptr(), k, hits.data_ptr(), stream=sp))
+    r_any = rate(lambda: c.occluded_device(rsh.data_ptr(), k, occ.data_ptr(), stream=sp))
+    total = closest + shadow
+    per_s = total / (ms * 1e-3)
+    collider_mix = total / (closest / r_closest + shadow / r_any) if total else 0.0
+    return {"closest_rays": closest, "shadow_rays": shadow, "rays_per_s": per_s,
+            "collider_closest_rays_per_s": r_closest, "collider_any_rays_per_s": r_any,
+            "collider_mix_rays_per_s": collider_mix, "fraction_of_collider": per_s / collider_mix if total else None}
+
+
 def filter_timing(L, out, natl, stream, sp, gs, cpu: bool) -> dict:
     """The post-filters of updateLightmap with the reference's default
     FilteringParameters (smoothing 1 with unwrap seams, spread 1000, background
@@ -636,7 +675,9 @@ def run_gather(args, world, rank, local):
         del plain_out
     if learned:
         extra.update(learned_errors(L, gs, params, out, natl, stream, sp))
-    elif rank == 0 and not args.gather_only:
+    if not learned and rank == 0:
+        extra["rays"] = gather_rays(L, c, gs, params, n, out, ms, stream, sp)
+    if not learned and rank == 0 and not args.gather_only:
         extra["filters"] = filter_timing(L, out, natl, stream, sp, gs, not args.no_cpu_baseline)
         extra["bake"] = bake_timing(L, gs, natl, stream, sp)
     if rank == 0:
@@ -706,6 +747,21 @@ def run_batch(args, world, rank, local):
     ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
     assert b.status(sp) == 0, "traversal reported an error"
     hit_ratio = float((hits[:, 1].view(torch.int32) != -1).float().mean().item())
+    # every mesh's tree rebuilt and all rays traced in one graph replay
+    rb_ms = None
+    if tuned["bvh_width"] == 2:
+        for _ in range(2):
+            b.rebuild_intersect_device(rays.data_ptr(), off_d.data_ptr(), n, hits.data_ptr(), stream=sp)
+        torch.cuda.synchronize()
+        r0 = torch.cuda.Event(enable_timing=True)
+        r1 = torch.cuda.Event(enable_timing=True)
+        r0.record(stream)
+        for _ in range(3):
+            b.rebuild_intersect_device(rays.data_ptr(), off_d.data_ptr(), n, hits.data_ptr(), stream=sp)
+        r1.record(stream)
+        torch.cuda.synchronize()
+        assert b.status(sp) == 0, "graph rebuild reported an error"
+        rb_ms = max_over_ranks(r0.elapsed_time(r1) / 3, world, dev)
     if rank == 0:
         peak, peak_src = load_peaks()
         achieved = BYTES_PER_RAY * n / (ms * 1e-3) / 1e9
@@ -717,7 +773,11 @@ def run_batch(args, world, rank, local):
             "config": {"workload": WORKLOAD_DESC["c3"], "meshes": mb.nmesh, "triangles": int(mb.tri_off[-1]),
                        "rays_per_step": n, "parallelism": f"replicas x{world}",
                        "l2": "inputs (32 B/ray, 9.2 GB) larger than L2, no flush", "hit_ratio": hit_ratio,
-                       "bvh_build_ms": b.build_ms, "bvh_nodes": b.nodes, "autotuned": tuned},
+                       "bvh_build_ms": b.build_ms, "bvh_nodes": b.nodes, "autotuned": tuned,
+                       "rebuild_and_trace": ({"ms_per_step": rb_ms, "grays": world * n / (rb_ms * 1e-3) / 1e9,
+                                              "what": "every mesh's tree rebuilt from its vertices and all rays "
+                                                      "traced, one CUDA graph replay per step"}
+                                             if rb_ms else None)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None,
                          "note": f"algorithmic {BYTES_PER_RAY} B/ray; peak {peak_src}"},

@@ -61,6 +61,31 @@ RRG_API int rrg_batch_set_stack_smem(rrg_batch* b, uint32_t entries);
 RRG_API int rrg_batch_intersect_device(rrg_batch* b, const float* rays_dev, const uint32_t* ray_off_dev, uint32_t n,
                                        float* hits_dev, void* stream);
 
+/* New vertex positions for every mesh (same topology): xyz_dev in the
+ * layout of rrg_batch_create's xyz (3 floats per vertex, all meshes in
+ * order), copied on `stream`.  Queries of rrg_batch_intersect_device keep
+ * the trees built at create; rrg_batch_rebuild_intersect_device rebuilds
+ * from these positions. */
+RRG_API int rrg_batch_set_vertices_device(rrg_batch* b, const float* xyz_dev, void* stream);
+
+/* Rebuilds every mesh's tree from the batch's current vertex positions and
+ * traces the rays against the new trees, both in one CUDA graph replay:
+ * the build runs as a fixed sequence of launches whose counts (valid
+ * triangles, tasks per tree level, nodes) stay on the device, with its
+ * scratch allocated on the first call (about 350 bytes per triangle) and
+ * at most 40 levels of large build tasks; then the persistent closest-hit
+ * launch of rrg_batch_intersect_device on those trees.  The graph is
+ * captured on the first call and again whenever rays, offsets, n, hits or
+ * the rays-per-warp or stack setting change.  Binary trees only
+ * (bvh_width 2): RRG_ERR_INVALID for 8-wide batches.  Results are
+ * rrg_batch_intersect_device's on trees built from the same positions;
+ * rrg_batch_status also reports a failed rebuild (RRG_ERR_INVALID).  The
+ * reference builds each mesh's collider once on the host
+ * (RRCollider::create per mesh, RRCollider.cpp:186-241; RRCollider::update
+ * rebuilds one, RRCollider.h:187-190). */
+RRG_API int rrg_batch_rebuild_intersect_device(rrg_batch* b, const float* rays_dev, const uint32_t* ray_off_dev,
+                                               uint32_t n, float* hits_dev, void* stream);
+
 /* Status word of the batch's traces (RRG_OK or RRG_ERR_STACK); synchronises
  * the stream and resets the word. */
 RRG_API int rrg_batch_status(rrg_batch* b, void* stream);

@@ -158,6 +158,13 @@ RRG_API int rrg_lightmap_filter(rrg_lightmapper* lm, const rrg_filter_params* p,
 RRG_API int rrg_lightmap_bake_host(rrg_lightmapper* lm, const rrg_gather_params* p, const rrg_filter_params* f,
                                    float* out_host);
 
+/* Counting of the rays the wavefront gather traces (a measurement aid, no
+ * reference counterpart): returns in *closest and *shadow (may be NULL) the
+ * closest-hit and shadow rays traced since the previous call (light rounds'
+ * shadow rays included), resets them, and counts from now on when enable is
+ * nonzero.  Synchronises the device. */
+RRG_API int rrg_lightmapper_count_rays(rrg_lightmapper* lm, int enable, uint64_t* closest, uint64_t* shadow);
+
 /* Number of unwrap seams found (0 before the first filter call with seams). */
 RRG_API uint64_t rrg_lightmapper_seams(const rrg_lightmapper* lm);
 /* Runs of samples over all seams (a run: consecutive samples of a seam that

@@ -30,6 +30,8 @@ def _lib():
         L.rrg_batch_destroy.restype = None
         L.rrg_batch_set_rays_per_warp.argtypes = [P, U]
         L.rrg_batch_set_stack_smem.argtypes = [P, U]
+        L.rrg_batch_set_vertices_device.argtypes = [P, P, P]
+        L.rrg_batch_rebuild_intersect_device.argtypes = [P, P, P, U, P, P]
         L.rrg_batch_intersect_device.argtypes = [P, P, P, U, P, P]
         L.rrg_batch_status.argtypes = [P, P]
         for f in ("rrg_batch_meshes", "rrg_batch_nodes"):
@@ -94,6 +96,18 @@ class RRColliderBatch:
     def set_stack_smem(self, entries: int) -> None:
         """Traversal-stack entries per thread in shared memory (0, 8, 16, 32)."""
         col._check(_lib().rrg_batch_set_stack_smem(self._h, int(entries)), "rrg_batch_set_stack_smem")
+
+    def set_vertices_device(self, xyz_ptr: int, stream: int = 0) -> None:
+        """New positions for all vertices (device float[3 * nv], create's layout)."""
+        col._check(_lib().rrg_batch_set_vertices_device(self._h, xyz_ptr, stream or None),
+                   "rrg_batch_set_vertices_device")
+
+    def rebuild_intersect_device(self, rays_ptr: int, ray_off_ptr: int, n: int, hits_ptr: int,
+                                 stream: int = 0) -> None:
+        """Every mesh's tree rebuilt from the current positions, then the
+        closest hits, in one CUDA graph replay."""
+        col._check(_lib().rrg_batch_rebuild_intersect_device(self._h, rays_ptr, ray_off_ptr, n, hits_ptr,
+                                                              stream or None), "rrg_batch_rebuild_intersect_device")
 
     def intersect_device(self, rays_ptr: int, ray_off_ptr: int, n: int, hits_ptr: int, stream: int = 0) -> None:
         """Closest hit for n device rays; ray_off_ptr = (M+1,) uint32 device

@@ -26,11 +26,23 @@ struct Batch {
 	uint32_t g_n = 0;
 	int g_fetch = 0;
 	uint32_t g_sdepth = 0;
+	// rebuild + trace in one graph (rrg_batch_rebuild_intersect_device)
+	GraphBuild* gb = nullptr;
+	cudaGraphExec_t exec_rb = nullptr;
+	uint32_t rb_kernels = 0;
+	const void* r_rays = nullptr;
+	const void* r_off = nullptr;
+	void* r_hits = nullptr;
+	uint32_t r_n = 0;
+	int r_fetch = 0;
+	uint32_t r_sdepth = 0;
 };
 
 static void free_batch(Batch* b) {
 	if (!b) return;
 	if (b->exec) cudaGraphExecDestroy(b->exec);
+	if (b->exec_rb) cudaGraphExecDestroy(b->exec_rb);
+	graph_build_free(b->gb);
 	if (b->cap) cudaStreamDestroy(b->cap);
 	free_collider(b->c);
 	delete b;
@@ -46,6 +58,52 @@ static bool ascending(const uint32_t* off, uint32_t n) {
 	for (uint32_t m = 0; m < n; m++)
 		if (off[m + 1] < off[m]) return false;
 	return true;
+}
+
+// Captures on the batch's private stream either the trace alone or the
+// rebuild of every mesh's tree followed by the trace (rebuild), and
+// instantiates it; *kernels = the kernel nodes of the graph.
+static int capture(Batch* b, bool rebuild, const float* rays_dev, const uint32_t* ray_off_dev, uint32_t n,
+                   float* hits_dev, cudaGraphExec_t* exec, uint32_t* kernels) {
+	cudaGraph_t g = nullptr;
+	RRG_CUDA(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
+	t_capturing = 1;   // recorded, not launched: counted per graph launch
+	int st = RRG_OK;
+	if (rebuild) {
+		st = graph_build_enqueue(b->c, b->gb, b->cap);
+		if (!st)
+			st = launch_batch_closest_on(b->c, graph_build_nodes(b->gb), (int)graph_build_max_nodes(b->gb),
+			                             graph_build_tris(b->gb), (int)b->c->nt,
+			                             reinterpret_cast<const float4*>(rays_dev), n, ray_off_dev, b->nmesh, b->fetch,
+			                             b->blocks, b->sdepth, reinterpret_cast<float4*>(hits_dev), b->cap);
+	} else {
+		st = launch_batch_closest(b->c, reinterpret_cast<const float4*>(rays_dev), n, ray_off_dev, b->nmesh, b->fetch,
+		                          b->blocks, b->sdepth, reinterpret_cast<float4*>(hits_dev), b->cap);
+	}
+	t_capturing = 0;
+	cudaError_t e = cudaStreamEndCapture(b->cap, &g);
+	if (st) {
+		if (g) cudaGraphDestroy(g);
+		return st;
+	}
+	if (e != cudaSuccess) return cuda_fail(e);
+	*kernels = 0;
+	size_t nn = 0;
+	if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn) {
+		std::vector<cudaGraphNode_t> nodes(nn);
+		if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+			for (size_t i = 0; i < nn; i++) {
+				cudaGraphNodeType t;
+				if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) (*kernels)++;
+			}
+	}
+	e = cudaGraphInstantiate(exec, g, 0);
+	cudaGraphDestroy(g);
+	if (e != cudaSuccess) {
+		*exec = nullptr;
+		return cuda_fail(e);
+	}
+	return RRG_OK;
 }
 
 }  // namespace rrg
@@ -160,35 +218,8 @@ int rrg_batch_intersect_device(rrg_batch* h, const float* rays_dev, const uint32
 			cudaGraphExecDestroy(b->exec);
 			b->exec = nullptr;
 		}
-		cudaGraph_t g = nullptr;
-		RRG_CUDA(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
-		t_capturing = 1;   // recorded, not launched: counted per graph launch below
-		int st = launch_batch_closest(b->c, reinterpret_cast<const float4*>(rays_dev), n, ray_off_dev, b->nmesh,
-		                              b->fetch, b->blocks, b->sdepth, reinterpret_cast<float4*>(hits_dev), b->cap);
-		t_capturing = 0;
-		cudaError_t e = cudaStreamEndCapture(b->cap, &g);
-		if (st) {
-			if (g) cudaGraphDestroy(g);
-			return st;
-		}
-		if (e != cudaSuccess) return cuda_fail(e);
-		b->graph_kernels = 0;
-		size_t nn = 0;
-		if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn) {
-			std::vector<cudaGraphNode_t> nodes(nn);
-			if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
-				for (size_t i = 0; i < nn; i++) {
-					cudaGraphNodeType t;
-					if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
-						b->graph_kernels++;
-				}
-		}
-		e = cudaGraphInstantiate(&b->exec, g, 0);
-		cudaGraphDestroy(g);
-		if (e != cudaSuccess) {
-			b->exec = nullptr;
-			return cuda_fail(e);
-		}
+		int st = capture(b, false, rays_dev, ray_off_dev, n, hits_dev, &b->exec, &b->graph_kernels);
+		if (st) return st;
 		b->g_rays = rays_dev;
 		b->g_off = ray_off_dev;
 		b->g_hits = hits_dev;
@@ -201,6 +232,49 @@ int rrg_batch_intersect_device(rrg_batch* h, const float* rays_dev, const uint32
 	return RRG_OK;
 }
 
+int rrg_batch_set_vertices_device(rrg_batch* h, const float* xyz_dev, void* stream) {
+	Batch* b = reinterpret_cast<Batch*>(h);
+	if (!b || !xyz_dev) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(b->c->device));
+	RRG_CUDA(cudaMemcpyAsync(b->c->d_xyz, xyz_dev, sizeof(float) * 3 * (size_t)b->c->nv, cudaMemcpyDeviceToDevice,
+	                         (cudaStream_t)stream));
+	return RRG_OK;
+}
+
+int rrg_batch_rebuild_intersect_device(rrg_batch* h, const float* rays_dev, const uint32_t* ray_off_dev, uint32_t n,
+                                       float* hits_dev, void* stream) {
+	Batch* b = reinterpret_cast<Batch*>(h);
+	if (!b) return RRG_ERR_INVALID;
+	if (!rays_dev || !ray_off_dev || !hits_dev || ((uintptr_t)rays_dev & 15) || ((uintptr_t)hits_dev & 15) ||
+	    ((uintptr_t)ray_off_dev & 3) || n == 0 || n >= 0x80000000u)
+		return RRG_ERR_INVALID;
+	if (b->c->width == 8) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(b->c->device));
+	if (!b->gb) {
+		int st = graph_build_new(b->c, &b->gb);
+		if (st) return st;
+	}
+	if (!b->exec_rb || b->r_rays != rays_dev || b->r_off != ray_off_dev || b->r_hits != hits_dev || b->r_n != n ||
+	    b->r_fetch != b->fetch || b->r_sdepth != b->sdepth) {
+		if (b->exec_rb) {
+			RRG_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+			cudaGraphExecDestroy(b->exec_rb);
+			b->exec_rb = nullptr;
+		}
+		int st = capture(b, true, rays_dev, ray_off_dev, n, hits_dev, &b->exec_rb, &b->rb_kernels);
+		if (st) return st;
+		b->r_rays = rays_dev;
+		b->r_off = ray_off_dev;
+		b->r_hits = hits_dev;
+		b->r_n = n;
+		b->r_fetch = b->fetch;
+		b->r_sdepth = b->sdepth;
+	}
+	RRG_CUDA(cudaGraphLaunch(b->exec_rb, (cudaStream_t)stream));
+	note_launches(b->rb_kernels);
+	return RRG_OK;
+}
+
 int rrg_batch_status(rrg_batch* h, void* stream) {
 	Batch* b = reinterpret_cast<Batch*>(h);
 	if (!b) return RRG_ERR_INVALID;
@@ -209,6 +283,10 @@ int rrg_batch_status(rrg_batch* h, void* stream) {
 	RRG_CUDA(cudaMemcpyAsync(&w, b->c->d_counter + 1, 4, cudaMemcpyDeviceToHost, s));
 	RRG_CUDA(cudaStreamSynchronize(s));
 	RRG_CUDA(cudaMemsetAsync(b->c->d_counter + 1, 0, 4, s));
+	if (b->gb && b->exec_rb) {
+		const int gs = graph_build_status(b->gb, s);
+		if (gs) return gs;
+	}
 	return w ? RRG_ERR_STACK : RRG_OK;
 }
 

@@ -21,6 +21,8 @@
 // cannot overflow on valid input.
 #include "rrg_internal.cuh"
 
+#include <new>
+
 #include <vector>
 
 namespace rrg {
@@ -65,7 +67,8 @@ struct BuildState {
 	int nsmall;
 	int nchunks;
 	int error;
-	int pad[3];
+	int ntasks;     // large tasks of the current level (the graph-replayed build)
+	int pad[2];
 };
 
 // ------------------------------------------------------------------ prep
@@ -267,10 +270,14 @@ __global__ void k_root_init(const int* __restrict__ rb, uint32_t n, BNode* nodes
 
 // pos[m] = first position in the ascending id list holding a triangle id
 // >= tri_off[m] (m = 0..nroots).
+// n_dev (may be null): read n there instead (the graph-replayed build, where
+// the count of valid triangles stays on the device).  The same holds for the
+// n_dev / ntasks_dev / nnodes_dev arguments of the kernels below.
 __global__ void k_mesh_ranges(const int* __restrict__ ids, uint32_t n, const uint32_t* __restrict__ tri_off,
-                              uint32_t nroots, uint32_t* __restrict__ pos) {
+                              uint32_t nroots, uint32_t* __restrict__ pos, const uint32_t* n_dev = nullptr) {
 	uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
 	if (m > nroots) return;
+	if (n_dev) n = *n_dev;
 	const int key = (int)tri_off[m];
 	uint32_t lo = 0, hi = n;
 	while (lo < hi) {
@@ -295,8 +302,9 @@ __global__ void k_fill_root_bounds(int* __restrict__ rb, uint32_t nroots) {
 // in registers and issues one atomic per field.
 __global__ void k_root_bounds_multi(const int* __restrict__ ids, uint32_t n, const float4* __restrict__ plo,
                                     const float4* __restrict__ phi, const uint32_t* __restrict__ pos,
-                                    uint32_t nroots, int* __restrict__ rb) {
+                                    uint32_t nroots, int* __restrict__ rb, const uint32_t* n_dev = nullptr) {
 	const int lane = threadIdx.x & 31;
+	if (n_dev) n = *n_dev;
 	const uint32_t stride = gridDim.x * blockDim.x;
 	for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
 		const uint32_t i = base + lane;
@@ -530,8 +538,10 @@ __device__ __forceinline__ void axis_scales(const Task& t, float* scale) {
 }
 
 // ------------------------------------------------------------ large path
-__global__ void k_level_setup(Task* tasks, int ntasks, int* __restrict__ gbins, Chunk* chunks, BuildState* st) {
+__global__ void k_level_setup(Task* tasks, int ntasks, int* __restrict__ gbins, Chunk* chunks, BuildState* st,
+                              const int* ntasks_dev = nullptr) {
 	__shared__ int base;
+	if (ntasks_dev) ntasks = *ntasks_dev;
 	for (int ti = blockIdx.x; ti < ntasks; ti += gridDim.x) {
 		bins_clear(gbins + (size_t)ti * kTaskBinInts, kTaskBinInts);
 		Task t = tasks[ti];
@@ -605,9 +615,10 @@ __device__ void emit_child(int node, int begin, int count, int depth, int buf, c
 // One CTA (>= 96 threads) per large task: SAH decision, children.
 __global__ void k_decide_large(const Task* __restrict__ tasks, int ntasks, const int* __restrict__ gbins,
                                Split* __restrict__ splits, BNode* nodes, Task* next_large, Task* small,
-                               BuildState* st) {
+                               BuildState* st, const int* ntasks_dev = nullptr) {
 	__shared__ int sb[kTaskBinInts];
 	__shared__ Decision dec[3];
+	if (ntasks_dev) ntasks = *ntasks_dev;
 	for (int ti = blockIdx.x; ti < ntasks; ti += gridDim.x) {
 		Task t = tasks[ti];
 		const int* gb = gbins + (size_t)ti * kTaskBinInts;
@@ -694,8 +705,10 @@ __global__ void k_part_count(const Task* __restrict__ tasks, const Chunk* __rest
 
 // per task: exclusive scan of its chunks' left counts (chunks of a task are
 // contiguous and in range order)
-__global__ void k_part_scan(const Task* __restrict__ tasks, int ntasks, int* __restrict__ chunk_left) {
+__global__ void k_part_scan(const Task* __restrict__ tasks, int ntasks, int* __restrict__ chunk_left,
+                            const int* ntasks_dev = nullptr) {
 	int ti = blockIdx.x * blockDim.x + threadIdx.x;
+	if (ntasks_dev) ntasks = *ntasks_dev;
 	if (ti >= ntasks) return;
 	Task t = tasks[ti];
 	int s = 0;
@@ -953,8 +966,9 @@ __device__ __forceinline__ void widen(BNode& n, float pad) {
 }
 
 __global__ void k_emit_nodes(const BNode* __restrict__ bn, int nnodes, int nroots, const float* __restrict__ pad_ptr,
-                             TNode* __restrict__ tn) {
+                             TNode* __restrict__ tn, const int* nnodes_dev = nullptr) {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (nnodes_dev) nnodes = *nnodes_dev;
 	if (i >= nnodes) return;
 	BNode n = bn[i];
 	const float pad = *pad_ptr;
@@ -993,8 +1007,9 @@ __global__ void k_emit_nodes(const BNode* __restrict__ bn, int nnodes, int nroot
 }
 
 __global__ void k_emit_tris(const int* __restrict__ final_ids, uint32_t n, const float* __restrict__ xyz,
-                            const uint32_t* __restrict__ idx, float4* __restrict__ tris) {
+                            const uint32_t* __restrict__ idx, float4* __restrict__ tris, const uint32_t* n_dev = nullptr) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (n_dev) n = *n_dev;
 	if (i >= n) return;
 	int t = final_ids[i];
 	uint32_t i0 = idx[3 * t], i1 = idx[3 * t + 1], i2 = idx[3 * t + 2];
@@ -1196,6 +1211,167 @@ int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting) {
 	c->build_ms = ms;
 	c->nnodes = (uint32_t)nnodes;
 	return RRG_OK;
+}
+
+// ------------------------------------------------------- graph rebuild
+// The build of a batch (binary tree, one root per mesh) as a fixed sequence
+// of launches that a CUDA graph can hold: every count the host build reads
+// back (valid triangles, large tasks per level, small tasks, nodes) stays on
+// the device and the kernels read it there; the scratch is allocated once at
+// its largest (every triangle valid: 2 nt + roots nodes); the level loop runs
+// kGraphLevels times, a level with no large task costing seven empty
+// launches; the error word collects what the host build returns as errors
+// (bit 1 invalid vertex index, 8 bad small task, 16 levels exhausted, 32 too
+// many large tasks).  The result is a tree of the same algorithm over the
+// same input; it may number its nodes differently (the build's task lists
+// fill by atomics), which no query result depends on.
+constexpr int kGraphLevels = 40;
+
+struct GraphBuild {
+	uint32_t nt = 0, nroots = 0, max_nodes = 0;
+	int max_large = 0, max_chunks = 0, max_leaf = 4, grid = 0, rgrid = 0, nb = 0;
+	Scratch sc;
+	float4 *plo = nullptr, *phi = nullptr;
+	uint32_t *valid = nullptr, *bsum = nullptr, *total = nullptr, *pos = nullptr;
+	int *idsA = nullptr, *idsB = nullptr, *final_ids = nullptr, *gbins = nullptr, *chunk_left = nullptr, *rbm = nullptr;
+	int** ids_bufs = nullptr;
+	BuildState* st = nullptr;
+	BNode* bnodes = nullptr;
+	Task *largeA = nullptr, *largeB = nullptr, *small = nullptr;
+	Split* splits = nullptr;
+	Chunk* chunks = nullptr;
+	float* pad = nullptr;
+	TNode* nodes = nullptr;
+	float4* tris = nullptr;
+};
+
+__global__ void k_level_begin(BuildState* st, int max_large) {
+	int n = st->nlarge_next;
+	if (n > max_large) {
+		st->error |= 32;
+		n = 0;
+	}
+	st->ntasks = n;
+	st->nlarge_next = 0;
+	st->nchunks = 0;
+}
+
+__global__ void k_level_end(BuildState* st) {
+	if (st->nlarge_next > 0) st->error |= 16;
+}
+
+int graph_build_new(Collider* c, GraphBuild** out) {
+	*out = nullptr;
+	if (!c->d_tri_off || c->width == 8) return RRG_ERR_INVALID;
+	GraphBuild* g = new (std::nothrow) GraphBuild();
+	if (!g) return RRG_ERR_OOM;
+	const uint32_t nt = c->nt, nroots = c->nroots;
+	g->nt = nt;
+	g->nroots = nroots;
+	g->max_leaf = c->params.max_leaf_size ? (int)c->params.max_leaf_size : 4;
+	if (g->max_leaf > kMaxLeaf) g->max_leaf = kMaxLeaf;
+	g->max_nodes = 2 * nt + nroots;
+	g->max_large = 2 * ((int)nt / kSmall + 2);
+	g->max_chunks = (int)nt / kChunk + g->max_large + 2;
+	g->nb = (int)((nt + kScanItems - 1) / kScanItems);
+	g->grid = c->num_sms * 8;
+	g->rgrid = (int)((nt + 255) / 256) < 4 * c->num_sms ? (int)((nt + 255) / 256) : 4 * c->num_sms;
+	cudaError_t e = cudaSuccess;
+	Scratch& sc = g->sc;
+	if (e == cudaSuccess) e = sc.get(&g->plo, nt);
+	if (e == cudaSuccess) e = sc.get(&g->phi, nt);
+	if (e == cudaSuccess) e = sc.get(&g->valid, nt);
+	if (e == cudaSuccess) e = sc.get(&g->bsum, (size_t)g->nb);
+	if (e == cudaSuccess) e = sc.get(&g->total, 1);
+	if (e == cudaSuccess) e = sc.get(&g->st, 1);
+	if (e == cudaSuccess) e = sc.get(&g->idsA, nt);
+	if (e == cudaSuccess) e = sc.get(&g->idsB, nt);
+	if (e == cudaSuccess) e = sc.get(&g->final_ids, nt);
+	if (e == cudaSuccess) e = sc.get(&g->bnodes, g->max_nodes);
+	if (e == cudaSuccess) e = sc.get(&g->largeA, (size_t)g->max_large);
+	if (e == cudaSuccess) e = sc.get(&g->largeB, (size_t)g->max_large);
+	if (e == cudaSuccess) e = sc.get(&g->small, (size_t)nt + 2);
+	if (e == cudaSuccess) e = sc.get(&g->splits, (size_t)g->max_large);
+	if (e == cudaSuccess) e = sc.get(&g->chunks, (size_t)g->max_chunks);
+	if (e == cudaSuccess) e = sc.get(&g->chunk_left, (size_t)g->max_chunks);
+	if (e == cudaSuccess) e = sc.get(&g->gbins, (size_t)g->max_large * kTaskBinInts);
+	if (e == cudaSuccess) e = sc.get(&g->ids_bufs, 2);
+	if (e == cudaSuccess) e = sc.get(&g->pos, (size_t)nroots + 1);
+	if (e == cudaSuccess) e = sc.get(&g->rbm, 12 * (size_t)nroots);
+	if (e == cudaSuccess) e = sc.get(&g->pad, 1);
+	if (e == cudaSuccess) e = sc.get(&g->nodes, g->max_nodes);
+	if (e == cudaSuccess) e = sc.get(&g->tris, 3 * (size_t)nt);
+	if (e == cudaSuccess) {
+		int* hbufs[2] = {g->idsA, g->idsB};
+		e = cudaMemcpy(g->ids_bufs, hbufs, sizeof(hbufs), cudaMemcpyHostToDevice);
+	}
+	if (e != cudaSuccess) {
+		delete g;
+		return cuda_fail(e);
+	}
+	*out = g;
+	return RRG_OK;
+}
+
+void graph_build_free(GraphBuild* g) { delete g; }
+const TNode* graph_build_nodes(const GraphBuild* g) { return g->nodes; }
+const float4* graph_build_tris(const GraphBuild* g) { return g->tris; }
+uint32_t graph_build_max_nodes(const GraphBuild* g) { return g->max_nodes; }
+
+// Enqueues the whole build of c's current vertex positions (c->d_xyz,
+// c->d_idx) on stream s, reading nothing back.
+int graph_build_enqueue(Collider* c, GraphBuild* g, cudaStream_t s) {
+	const uint32_t nt = g->nt, nroots = g->nroots;
+	BuildState* st = g->st;
+	RRG_CUDA(cudaMemsetAsync(st, 0, sizeof(BuildState), s));
+	rrg::note_launch(), k_prep<<<(nt + 255) / 256, 256, 0, s>>>(c->d_xyz, c->nv, c->d_idx, nt, g->plo, g->phi, g->valid, st);
+	rrg::note_launch(), k_block_count<<<g->nb, kBT, 0, s>>>(g->valid, nt, g->bsum);
+	rrg::note_launch(), k_scan_blocks<<<1, kBT, 0, s>>>(g->bsum, (uint32_t)g->nb, g->total);
+	rrg::note_launch(), k_compact<<<g->nb, kBT, 0, s>>>(g->valid, nt, g->bsum, g->idsA);
+	rrg::note_launch(), k_mesh_ranges<<<(nroots + 1 + 255) / 256, 256, 0, s>>>(g->idsA, 0, c->d_tri_off, nroots, g->pos,
+	                                                                           g->total);
+	rrg::note_launch(), k_fill_root_bounds<<<(12 * nroots + 255) / 256, 256, 0, s>>>(g->rbm, nroots);
+	rrg::note_launch(), k_root_bounds_multi<<<g->rgrid, 256, 0, s>>>(g->idsA, 0, g->plo, g->phi, g->pos, nroots, g->rbm,
+	                                                                g->total);
+	rrg::note_launch(), k_root_init_multi<<<(nroots + 255) / 256, 256, 0, s>>>(g->rbm, g->pos, nroots, g->bnodes, g->largeA,
+	                                                                          g->small, st);
+	RRG_CUDA(cudaGetLastError());
+	Task* cur = g->largeA;
+	Task* nxt = g->largeB;
+	const int grid = g->grid;
+	for (int level = 0; level < kGraphLevels; level++) {
+		rrg::note_launch(), k_level_begin<<<1, 1, 0, s>>>(st, g->max_large);
+		rrg::note_launch(), k_level_setup<<<grid, kBT, 0, s>>>(cur, 0, g->gbins, g->chunks, st, &st->ntasks);
+		rrg::note_launch(), k_bin_chunks<<<grid, kBT, 0, s>>>(cur, g->chunks, st, g->ids_bufs, g->plo, g->phi, g->gbins);
+		rrg::note_launch(), k_decide_large<<<grid, 128, 0, s>>>(cur, 0, g->gbins, g->splits, g->bnodes, nxt, g->small, st,
+		                                                       &st->ntasks);
+		rrg::note_launch(), k_part_count<<<grid, kBT, 0, s>>>(cur, g->chunks, st, g->splits, g->ids_bufs, g->plo, g->phi,
+		                                                     g->chunk_left);
+		rrg::note_launch(), k_part_scan<<<(g->max_large + 127) / 128, 128, 0, s>>>(cur, 0, g->chunk_left, &st->ntasks);
+		rrg::note_launch(), k_part_scatter<<<grid, kBT, 0, s>>>(cur, g->chunks, st, g->splits, g->ids_bufs, g->plo, g->phi,
+		                                                       g->chunk_left, st);
+		Task* tmp = cur;
+		cur = nxt;
+		nxt = tmp;
+	}
+	rrg::note_launch(), k_level_end<<<1, 1, 0, s>>>(st);
+	rrg::note_launch(), k_small<<<grid, kSmallThreads, 0, s>>>(g->small, st, g->ids_bufs, g->plo, g->phi, g->bnodes,
+	                                                          g->final_ids, g->max_leaf, st);
+	rrg::note_launch(), k_root_pad<<<1, 256, 0, s>>>(g->bnodes, nroots, g->pad);
+	rrg::note_launch(), k_emit_nodes<<<(g->max_nodes + 255) / 256, 256, 0, s>>>(g->bnodes, 0, (int)nroots, g->pad, g->nodes,
+	                                                                           &st->node_count);
+	rrg::note_launch(), k_emit_tris<<<(nt + 255) / 256, 256, 0, s>>>(g->final_ids, 0, c->d_xyz, c->d_idx, g->tris, g->total);
+	RRG_CUDA(cudaGetLastError());
+	return RRG_OK;
+}
+
+// The error word of the last enqueued build (synchronises s): RRG_OK, or
+// RRG_ERR_INVALID when the build reported an error.
+int graph_build_status(GraphBuild* g, cudaStream_t s) {
+	BuildState h;
+	RRG_CUDA(cudaMemcpyAsync(&h, g->st, sizeof(h), cudaMemcpyDeviceToHost, s));
+	RRG_CUDA(cudaStreamSynchronize(s));
+	return h.error ? RRG_ERR_INVALID : RRG_OK;
 }
 
 }  // namespace rrg

@@ -680,7 +680,15 @@ struct WfState {
 	uint32_t* counts;      // [0], [1]: live counts (ping-pong), [2]: hits, [3]: shadow rays
 	uint32_t cap;          // paths
 	uint32_t Q, N;
+	unsigned long long* rays = nullptr;   // optional counts of traced rays: [0] closest, [1] shadow
 };
+
+// Adds the rays traced by the calling lanes to a counter (one atomic per
+// converged group of lanes).
+__device__ __forceinline__ void count_ray(unsigned long long* c) {
+	const unsigned m = __activemask();
+	if ((threadIdx.x & 31) == (unsigned)(__ffs(m) - 1)) atomicAdd(c, (unsigned long long)__popc(m));
+}
 
 // Directional mode (gatherAllDirections, lightmap.cpp:820): each hemisphere
 // sample's weights for the four lightmap directions (its cosine to the
@@ -854,6 +862,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 					if (li == 0) dsize = __fmul_rn(dsize, g.locality);
 					float ni = dot(d, nrm);
 					if (ni <= 0.f || !isfinite(ni)) continue;
+					if (WF && wf.rays) count_ray(wf.rays + 1);
 					if (occluded(g, origin, d, g.tmin, dsize, s.tri, overflow)) continue;
 					V3 irr = li == 0 ? g.dir_color : point_irr(g, origin);
 					sm.light[round][li] = mul(irr, ni);
@@ -1054,6 +1063,10 @@ __global__ void __launch_bounds__(128, 8) k_wf_shadow(GatherScene g, WfState w, 
 // Paths that continue go to the other live list.
 __global__ void __launch_bounds__(128) k_wf_shade(GatherScene g, WfState w, int cur) {
 	const uint32_t n = w.counts[2];
+	if (w.rays && blockIdx.x == 0 && threadIdx.x == 0) {
+		atomicAdd(w.rays, (unsigned long long)w.counts[cur]);       // this bounce's closest-hit rays
+		atomicAdd(w.rays + 1, (unsigned long long)w.counts[3]);     // and its shadow rays
+	}
 	uint32_t* next = w.live + (size_t)(cur ^ 1) * w.cap;
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		const uint32_t p = w.hits[i];
@@ -1252,6 +1265,8 @@ struct Lightmapper {
 	Sub* d_sub = nullptr;
 	uint64_t* d_counter = nullptr;
 	uint32_t* d_status = nullptr;
+	unsigned long long* d_rays = nullptr;   // traced-ray counters of the wavefront gather (when counting)
+	bool count_rays = false;
 	float* d_stage = nullptr;
 	size_t stage_bytes = 0;
 	float tmin_default = 0.f;
@@ -1303,6 +1318,7 @@ static void free_lm(Lightmapper* L) {
 	cudaFree(L->d_sub);
 	cudaFree(L->d_counter);
 	cudaFree(L->d_status);
+	cudaFree(L->d_rays);
 	cudaFree(L->d_stage);
 	cudaFree(L->d_covered);
 	cudaFree(L->d_recs);
@@ -1427,6 +1443,7 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 	w.cap = (uint32_t)cap;
 	w.Q = Q;
 	w.N = N;
+	w.rays = L->count_rays ? L->d_rays : nullptr;
 	int per_sm = 0;
 	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather<false, false, true>, kGatherWarps * 32, 0));
 	int per_sm_c = 0;
@@ -2122,6 +2139,24 @@ int rrg_lightmap_bake_host(rrg_lightmapper* h, const rrg_gather_params* p, const
 	RRG_CUDA(cudaMemcpyAsync(out_host, L->d_stage, bytes, cudaMemcpyDeviceToHost, s));
 	RRG_CUDA(cudaStreamSynchronize(s));
 	return rrg_lightmapper_status(h, s);
+}
+
+int rrg_lightmapper_count_rays(rrg_lightmapper* h, int enable, uint64_t* closest, uint64_t* shadow) {
+	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
+	if (!L) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(L->c->device));
+	if (!L->d_rays) {
+		RRG_CUDA(cudaMalloc(&L->d_rays, 2 * sizeof(unsigned long long)));
+		RRG_CUDA(cudaMemset(L->d_rays, 0, 2 * sizeof(unsigned long long)));
+	}
+	unsigned long long h2[2] = {0, 0};
+	RRG_CUDA(cudaDeviceSynchronize());
+	RRG_CUDA(cudaMemcpy(h2, L->d_rays, sizeof(h2), cudaMemcpyDeviceToHost));
+	RRG_CUDA(cudaMemset(L->d_rays, 0, sizeof(h2)));
+	if (closest) *closest = h2[0];
+	if (shadow) *shadow = h2[1];
+	L->count_rays = enable != 0;
+	return RRG_OK;
 }
 
 uint64_t rrg_lightmapper_covered(const rrg_lightmapper* h) {

@@ -163,7 +163,20 @@ bool compact_depth_ok(uint32_t sdepth);
 constexpr uint32_t kBatchMaxMeshes = 8192;
 // the collider holding a batch's meshes (rrg_batch.cu)
 Collider* batch_collider(::rrg_batch* b);
+// the batch build as a graph-capturable launch sequence (rrg_build.cu)
+struct GraphBuild;
+int graph_build_new(Collider* c, GraphBuild** out);
+void graph_build_free(GraphBuild* g);
+int graph_build_enqueue(Collider* c, GraphBuild* g, cudaStream_t s);
+int graph_build_status(GraphBuild* g, cudaStream_t s);
+const TNode* graph_build_nodes(const GraphBuild* g);
+const float4* graph_build_tris(const GraphBuild* g);
+uint32_t graph_build_max_nodes(const GraphBuild* g);
 int batch_trace_blocks(Collider* c, uint32_t nmesh, uint32_t sdepth, int* blocks);
+// launch_batch_closest on explicit binary-tree buffers (a graph build's)
+int launch_batch_closest_on(Collider* c, const TNode* nodes, int nnodes, const float4* tris, int ntris,
+                            const float4* rays, uint32_t n, const uint32_t* ray_off, uint32_t nmesh, int fetch,
+                            int blocks, uint32_t sdepth, float4* hits, cudaStream_t s);
 int launch_batch_closest(Collider* c, const float4* rays, uint32_t n, const uint32_t* ray_off, uint32_t nmesh,
                          int fetch, int blocks, uint32_t sdepth, float4* hits, cudaStream_t s);
 

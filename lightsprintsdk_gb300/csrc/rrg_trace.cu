@@ -593,6 +593,25 @@ int batch_trace_blocks(Collider* c, uint32_t nmesh, uint32_t sdepth, int* blocks
 
 // Clears the work counter and launches k_batch_closest on stream s (both
 // stream-ordered, so the pair can be captured in a CUDA graph).
+int launch_batch_closest_on(Collider* c, const TNode* nodes, int nnodes, const float4* tris, int ntris,
+                            const float4* rays, uint32_t n, const uint32_t* ray_off, uint32_t nmesh, int fetch,
+                            int blocks, uint32_t sdepth, float4* hits, cudaStream_t s) {
+	if (!n) return RRG_OK;
+	RRG_CUDA(cudaMemsetAsync(c->d_counter, 0, 4, s));
+	const uint32_t per_fetch = 32u * (uint32_t)fetch;
+	const uint32_t want = (uint32_t)(((uint64_t)n + per_fetch - 1) / per_fetch * 32 / kTraceThreads + 1);
+	const int grid = (int)(want < (uint32_t)blocks ? want : (uint32_t)blocks);
+	const size_t smem = sizeof(uint32_t) * (nmesh + 1);
+	BatchKernel k = k_batch_closest<false, 0>;
+	if (sdepth == 8) k = k_batch_closest<false, 8>;
+	else if (sdepth == 16) k = k_batch_closest<false, 16>;
+	else if (sdepth == 32) k = k_batch_closest<false, 32>;
+	rrg::note_launch(), k<<<grid, kTraceThreads, smem, s>>>(nodes, nnodes, nullptr, 0, tris, ntris, rays, n, ray_off,
+	                                                      c->d_tri_off, nmesh, fetch, hits, c->d_counter);
+	RRG_CUDA(cudaGetLastError());
+	return RRG_OK;
+}
+
 int launch_batch_closest(Collider* c, const float4* rays, uint32_t n, const uint32_t* ray_off, uint32_t nmesh,
                          int fetch, int blocks, uint32_t sdepth, float4* hits, cudaStream_t s) {
 	if (!n) return RRG_OK;

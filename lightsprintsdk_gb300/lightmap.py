@@ -247,6 +247,16 @@ class RRLightmapper:
     def seam_runs(self) -> int:
         return int(_lib().rrg_lightmapper_seam_runs(self._h))
 
+    def count_rays(self, enable: bool = True) -> tuple[int, int]:
+        """(closest-hit rays, shadow rays) the wavefront gather traced since
+        the previous call; counting continues while enable."""
+        L = _lib()
+        L.rrg_lightmapper_count_rays.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        a = np.zeros(2, np.uint64)
+        col._check(L.rrg_lightmapper_count_rays(self._h, 1 if enable else 0, a[0:].ctypes.data,
+                                                a[1:].ctypes.data), "rrg_lightmapper_count_rays")
+        return int(a[0]), int(a[1])
+
     def check(self, stream: int = 0) -> None:
         r = _lib().rrg_lightmapper_status(self._h, stream or None)
         if r:

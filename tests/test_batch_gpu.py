@@ -159,3 +159,52 @@ def test_stack_depths_agree(small_batch):
     with pytest.raises(col.RRGError):
         b.set_stack_smem(12)
     b.set_stack_smem(0)
+
+
+def test_rebuild_in_graph_equals_per_mesh_colliders(small_batch):
+    """One graph replay rebuilds every mesh's tree from the batch's vertex
+    positions and traces all the rays (rrg_batch_rebuild_intersect_device):
+    the same hit records, bit for bit, as the batch built at create (the
+    same build on the same positions), on two replays; then, with every
+    vertex moved (rrg_batch_set_vertices_device), the same records as
+    colliders built on the moved meshes one by one."""
+    import torch
+    mb, counts, rays, off, off_d, b = small_batch
+    n = rays.shape[0]
+    base = run(b, rays, off_d, 32)
+    hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    lc0 = col.launch_count()
+    for _ in range(2):
+        hits.fill_(7.0)
+        b.rebuild_intersect_device(rays.data_ptr(), off_d.data_ptr(), n, hits.data_ptr())
+        torch.cuda.synchronize()
+        assert b.status() == 0
+        np.testing.assert_array_equal(hits.cpu().numpy().view(np.uint32), base.view(np.uint32))
+    assert col.launch_count() - lc0 > 2 * 40   # the replayed graphs hold the build's launches
+    moved = np.ascontiguousarray(mb.vertices * np.float32(1.25) + np.float32([0.5, -0.25, 0.125]), np.float32)
+    xyz = torch.from_numpy(moved).cuda()
+    b.set_vertices_device(xyz.data_ptr())
+    hits.fill_(7.0)
+    b.rebuild_intersect_device(rays.data_ptr(), off_d.data_ptr(), n, hits.data_ptr())
+    torch.cuda.synchronize()
+    assert b.status() == 0
+    h = hits.cpu().numpy()
+    r = rays.cpu().numpy()
+    checked = 0
+    for m in range(mb.nmesh):
+        a, e = int(off[m]), int(off[m + 1])
+        if a == e or m == 5:
+            continue
+        v, t = mb.mesh(m)
+        vm = moved[int(mb.vert_off[m]):int(mb.vert_off[m + 1])]
+        c = col.RRCollider.create(vm, t)
+        got = col.decode_hits(h[a:e])
+        one = c.intersect_batch(r[a:e])
+        for f in ("hit", "tri", "dist", "uv", "side"):
+            np.testing.assert_array_equal(got[f], one[f], err_msg=f"mesh {m} field {f}")
+        checked += e - a
+        c.close()
+    assert checked > 10000
+    orig = torch.from_numpy(np.ascontiguousarray(mb.vertices, np.float32)).cuda()
+    b.set_vertices_device(orig.data_ptr())
+    torch.cuda.synchronize()
