@@ -46,6 +46,9 @@ BYTES_PER_RAY = 48          # 32 B ray in (two float4) + 16 B hit record out
 # capture of 2 Mi rays, config 0 from a capture of the full 1 Mi-ray launch;
 # the bench scales them to its launch
 MEASURED_DRAM_BYTES_PER_RAY = {"c1": 113.5, "c0": 41.2}
+# L2 -> L1 read bytes per ray of k_closest (ncu l1tex__m_xbar2l1tex_read_bytes.sum / rays, config-1 capture
+# of 2 Mi rays)
+L2_READ_BYTES_PER_RAY = {"c1": 445.0}
 C3_SAMPLE_MESHES = (0, 65, 130, 195, 260, 325, 390, 455)   # CPU-baseline sample (both mesh kinds)
 C3_SAMPLE_RAYS = 25_000                                     # rays per sampled mesh
 WORKLOAD_DESC = {
@@ -862,6 +865,7 @@ def main():
     e1 = torch.cuda.Event(enable_timing=True)
     clk.mark_start()
     lc0 = col.launch_count()
+    c.trace_timing(True)
     e0.record(stream)
     for _ in range(args.steps):
         step()
@@ -870,6 +874,8 @@ def main():
     torch.cuda.synchronize()
     clk.mark_end()
     clk.__exit__()
+    kernel_ms_total, kernel_launches = c.trace_timing(False)
+    kernel_ms = kernel_ms_total / max(1, kernel_launches)
     ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, f"cuda:{local}")
     assert c.status(sp) == 0, "traversal reported an error"
     hits_total = int((d_hits[:, 1].view(torch.int32) != -1).sum().item())
@@ -891,7 +897,8 @@ def main():
     if rank == 0:
         peak, peak_src = load_peaks()
         value = world * n / (ms * 1e-3) / 1e9
-        achieved = BYTES_PER_RAY * n / (ms * 1e-3) / 1e9
+        # the dominant kernel's own launches (CUDA events on its stream)
+        achieved = BYTES_PER_RAY * n / (kernel_ms * 1e-3) / 1e9
         line = {
             "metric": "closest-hit Grays/s", "value": value, "unit": "Grays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -906,9 +913,15 @@ def main():
                          "traffic": (MEASURED_DRAM_BYTES_PER_RAY[args.workload] * n
                                      if args.workload in MEASURED_DRAM_BYTES_PER_RAY and args.bvh_width != 8
                                      else None),
-                         "note": f"algorithmic {BYTES_PER_RAY} B/ray; peak {peak_src}; traffic per launch = ncu "
-                                 f"DRAM bytes per ray of the workload's ncu capture x rays; the kernel "
-                                 f"is issue-bound, so the HBM fraction is low by design"},
+                         "kernel": "k_closest", "kernel_ms": kernel_ms, "kernel_launches_timed": kernel_launches,
+                         "l2": ({"read_bytes_per_ray": L2_READ_BYTES_PER_RAY[args.workload],
+                                 "achieved_gbs": L2_READ_BYTES_PER_RAY[args.workload] * n / (kernel_ms * 1e-3) / 1e9,
+                                 "source": "ncu l1tex__m_xbar2l1tex_read_bytes.sum per ray of the workload's capture"}
+                                if args.workload in L2_READ_BYTES_PER_RAY else None),
+                         "note": f"algorithmic {BYTES_PER_RAY} B/ray over the traversal kernel's own launches; "
+                                 f"peak {peak_src}; traffic per launch = ncu DRAM bytes per ray of the workload's "
+                                 f"ncu capture x rays; the kernel is issue-bound (69 % issue-active, 13.4 of 32 lanes), "
+                                 f"so the HBM fraction is low by design"},
             "e2e": {"value": world * n / e2e_s / 1e9, "unit": "Grays/s", "h2d_bytes_per_step": 32 * n,
                     "d2h_bytes_per_step": 16 * n},
             "gpu_launches": launches,

@@ -140,6 +140,14 @@ RRG_API int rrg_collider_set_traversal(rrg_collider* c, uint32_t traversal);
 RRG_API int rrg_collider_set_compact_tuning(rrg_collider* c, uint32_t stack_smem, uint32_t rays_per_warp,
                                             uint32_t blocks_per_sm);
 
+/* Timing of the closest-hit traversal kernel alone (a measurement aid, no
+ * reference counterpart): while enabled, each binary-tree closest-hit
+ * launch of rrg_intersect_device is bracketed by CUDA events on its stream
+ * (up to 256 launches).  A call returns the summed milliseconds and the
+ * number of timed launches since the previous call (synchronising on their
+ * events), resets them, and enables or disables the timing. */
+RRG_API int rrg_collider_trace_timing(rrg_collider* c, int enable, float* total_ms, uint32_t* launches);
+
 /* RRCollider::getMemoryOccupied (RRCollider.h:259): device bytes held. */
 RRG_API size_t rrg_collider_memory(const rrg_collider* c);
 RRG_API uint32_t rrg_collider_triangles(const rrg_collider* c);

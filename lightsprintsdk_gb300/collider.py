@@ -90,6 +90,7 @@ def _lib():
         L.rrg_collider_status.argtypes = [P, P]
         L.rrg_collider_set_traversal.argtypes = [P, U]
         L.rrg_collider_set_compact_tuning.argtypes = [P, U, U, U]
+        L.rrg_collider_trace_timing.argtypes = [P, C.c_int, P, P]
         L.rrg_intersect_rrray_one_after.argtypes = [P, P, C.c_float, U, P, P]
         L.rrg_collider_set_ray_order.argtypes = [P, U]
         L.rrg_status_string.argtypes = [I]
@@ -200,6 +201,15 @@ class RRCollider:
         none)."""
         _check(_lib().rrg_collider_set_compact_tuning(self._h, stack_smem, rays_per_warp, blocks_per_sm),
                "rrg_collider_set_compact_tuning")
+
+    def trace_timing(self, enable: bool = True) -> tuple[float, int]:
+        """(milliseconds, launches) of the closest-hit traversal kernel timed
+        since the previous call; timing continues while enable."""
+        ms = np.zeros(1, np.float32)
+        k = np.zeros(1, np.uint32)
+        _check(_lib().rrg_collider_trace_timing(self._h, 1 if enable else 0, ms.ctypes.data, k.ctypes.data),
+               "rrg_collider_trace_timing")
+        return float(ms[0]), int(k[0])
 
     def set_ray_order(self, order: int) -> None:
         """RAY_ORDER_DEFAULT (0: binned from 2^22 rays), RAY_ORDER_AS_GIVEN (1)

@@ -31,6 +31,8 @@ void free_collider(Collider* c) {
 		if (c->ev_out[k]) cudaEventDestroy(c->ev_out[k]);
 	}
 	if (c->ev_start) cudaEventDestroy(c->ev_start);
+	for (cudaEvent_t e : c->tev)
+		if (e) cudaEventDestroy(e);
 	if (c->s_in) cudaStreamDestroy(c->s_in);
 	if (c->s_out) cudaStreamDestroy(c->s_out);
 	if (c->s_comp) cudaStreamDestroy(c->s_comp);
@@ -245,6 +247,23 @@ int rrg_collider_set_compact_tuning(rrg_collider* h, uint32_t stack_smem, uint32
 	c->compact_sdepth = depth;
 	c->compact_fetch = rays / 32;
 	c->compact_minb = minb;
+	return RRG_OK;
+}
+
+int rrg_collider_trace_timing(rrg_collider* h, int enable, float* total_ms, uint32_t* launches) {
+	Collider* c = reinterpret_cast<Collider*>(h);
+	if (!c) return RRG_ERR_INVALID;
+	float sum = 0.f;
+	for (uint32_t i = 0; i < c->tev_n; i++) {
+		RRG_CUDA(cudaEventSynchronize(c->tev[2 * i + 1]));
+		float ms = 0.f;
+		RRG_CUDA(cudaEventElapsedTime(&ms, c->tev[2 * i], c->tev[2 * i + 1]));
+		sum += ms;
+	}
+	if (total_ms) *total_ms = sum;
+	if (launches) *launches = c->tev_n;
+	c->tev_n = 0;
+	c->timing = enable != 0;
 	return RRG_OK;
 }
 

@@ -133,7 +133,14 @@ struct Collider {
 	std::mutex host_mu;
 	// single-ray queries combined across host threads (rrg_combine.cu)
 	Combiner* comb = nullptr;
+	// optional CUDA-event pairs around each closest-hit traversal launch
+	// (rrg_collider_trace_timing); tev_n pairs recorded since the reset
+	bool timing = false;
+	cudaEvent_t tev[2 * 256] = {};
+	uint32_t tev_n = 0;
 };
+// records the start (end = false) or end of a timed traversal launch
+int trace_event(Collider* c, cudaStream_t s, bool end);
 
 // build (rrg_build.cu)
 int build_bvh(Collider* c, cudaStream_t s, const volatile int* aborting);

@@ -490,13 +490,27 @@ int launch_closest_on(Collider* c, const float4* rays, uint32_t n, float4* hits,
 		const uint32_t* perm = nullptr;
 		int st = bin_rays(c, rays, n, s, bin_slot, &perm);
 		if (st) return st;
+		if ((st = trace_event(c, s, false))) return st;
 		rrg::note_launch(), k_closest<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
 		                                               hits, planes, points, words, perm);
+		if ((st = trace_event(c, s, true))) return st;
 	} else {
+		int st = trace_event(c, s, false);
+		if (st) return st;
 		rrg::note_launch(), k_closest<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
 		                                                hits, planes, points, words, nullptr);
+		if ((st = trace_event(c, s, true))) return st;
 	}
 	RRG_CUDA(cudaGetLastError());
+	return RRG_OK;
+}
+
+int trace_event(Collider* c, cudaStream_t s, bool end) {
+	if (!c->timing || c->tev_n >= 256) return RRG_OK;
+	cudaEvent_t& e = c->tev[2 * c->tev_n + (end ? 1 : 0)];
+	if (!e) RRG_CUDA(cudaEventCreate(&e));
+	RRG_CUDA(cudaEventRecord(e, s));
+	if (end) c->tev_n++;
 	return RRG_OK;
 }
 
