@@ -536,14 +536,15 @@ static int infer_impl(RadianceCache* C, const void* recs_dev, uint64_t n, float*
 	if (!C || !recs_dev || !out_dev || ((uintptr_t)out_dev & 15)) return RRG_ERR_INVALID;
 	if (!n) return RRG_OK;
 	const size_t smem = sizeof(uint32_t) * (kMlpFragWords + kInferWarps * 16 * 32);
-	static bool attr = false;
-	if (!attr) {
+	static int per_sm = 0;
+	if (!per_sm) {
 		RRG_CUDA(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-		attr = true;
+		RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_infer, kInferWarps * 32, smem));
+		if (per_sm < 1) per_sm = 1;
 	}
 	uint64_t ntiles = (n + 15) / 16;
 	uint64_t blocks = (ntiles + kInferWarps - 1) / kInferWarps;
-	uint64_t cap = (uint64_t)C->num_sms * 4;
+	uint64_t cap = (uint64_t)C->num_sms * per_sm;   // one wave of resident blocks, grid-stride over the tiles
 	rrg::note_launch(), k_mlp_infer<<<(int)(blocks < cap ? blocks : cap), kInferWarps * 32, smem, (cudaStream_t)stream>>>(
 	    reinterpret_cast<const CacheRec*>(recs_dev), n, C->fwd, C->lo[0], C->lo[1], C->lo[2], C->ie[0], C->ie[1],
 	    C->ie[2], reinterpret_cast<float4*>(out_dev), C->hg, all_valid);

@@ -157,14 +157,17 @@ struct HashCorners {
 	float w[3];
 };
 
-__device__ __forceinline__ HashCorners hash_cell(const float* p, const float* lo, const float* ie, float res) {
+// the position scaled to the cache box and clamped to [0, 1]
+__device__ __forceinline__ float hash_unit(float p, float lo, float ie) {
+	return fminf(fmaxf(__fmul_rn(__fsub_rn(p, lo), ie), 0.f), 1.f);
+}
+
+__device__ __forceinline__ HashCorners hash_cell_u(const float* u, float res) {
 	HashCorners h;
 	const int n = (int)res;
 #pragma unroll
 	for (int j = 0; j < 3; j++) {
-		float v = __fmul_rn(__fsub_rn(p[j], lo[j]), ie[j]);
-		float u = fminf(fmaxf(v, 0.f), 1.f);
-		float x = __fmul_rn(u, res);
+		float x = __fmul_rn(u[j], res);
 		int f = (int)floorf(x);
 		f = f < 0 ? 0 : (f > n - 1 ? n - 1 : f);
 		h.x0[j] = (uint32_t)f;
@@ -173,12 +176,24 @@ __device__ __forceinline__ HashCorners hash_cell(const float* p, const float* lo
 	return h;
 }
 
-__device__ __forceinline__ uint32_t hash_index(const HashGrid& g, int l, uint32_t ix, uint32_t iy, uint32_t iz) {
-	if ((g.dense >> l) & 1u) {
-		const uint32_t n1 = (uint32_t)g.res[l] + 1u;
+__device__ __forceinline__ HashCorners hash_cell(const float* p, const float* lo, const float* ie, float res) {
+	const float u[3] = {hash_unit(p[0], lo[0], ie[0]), hash_unit(p[1], lo[1], ie[1]), hash_unit(p[2], lo[2], ie[2])};
+	return hash_cell_u(u, res);
+}
+
+// index within a level: dense levels ((res+1)^3 <= T) by position, the
+// others by the spatial hash
+__device__ __forceinline__ uint32_t hash_index_r(bool dense, float res, uint32_t T, uint32_t ix, uint32_t iy,
+                                                 uint32_t iz) {
+	if (dense) {
+		const uint32_t n1 = (uint32_t)res + 1u;
 		return ix + iy * n1 + iz * n1 * n1;
 	}
-	return (ix ^ (iy * 2654435761u) ^ (iz * 805459861u)) & (g.T - 1u);
+	return (ix ^ (iy * 2654435761u) ^ (iz * 805459861u)) & (T - 1u);
+}
+
+__device__ __forceinline__ uint32_t hash_index(const HashGrid& g, int l, uint32_t ix, uint32_t iy, uint32_t iz) {
+	return hash_index_r((g.dense >> l) & 1u, g.res[l], g.T, ix, iy, iz);
 }
 
 __device__ __forceinline__ float hash_weight(const HashCorners& h, int c) {
@@ -188,38 +203,46 @@ __device__ __forceinline__ float hash_weight(const HashCorners& h, int c) {
 	return __fmul_rn(__fmul_rn(wx, wy), wz);
 }
 
-// Encoding with the hash grid; `half` 0 writes words 0..15 (the 16 levels'
-// feature pairs), 1 words 16..31 (frequencies, normal, albedo, bias).
+// Encoding with the hash grid, split evenly between the two lanes of a
+// sample: `half` 0 writes the even levels' feature pairs (words 0, 2, .., 14)
+// and the x and y octaves (words 16..23), `half` 1 the odd levels' (words 1,
+// 3, .., 15), the z octaves (24..27), normal, albedo and bias (28..31).  Each
+// lane's eight levels are unrolled so their 64 table reads are in flight
+// together; the level's resolution is picked from two kernel-parameter
+// constants (no indexed parameter array, which would live in local memory).
 __device__ __forceinline__ void mlp_encode_half_hash(const float* p, const float* n, const float* alb,
                                                      const float* lo, const float* ie, const HashGrid& g, int half,
                                                      uint32_t* row_words) {
-	if (half == 0) {
-		for (int l = 0; l < kHashLevels; l++) {
-			const HashCorners h = hash_cell(p, lo, ie, g.res[l]);
-			const float2* tl = g.table + (size_t)l * g.T;
-			float f0 = 0.f, f1 = 0.f;
+	const float u[3] = {hash_unit(p[0], lo[0], ie[0]), hash_unit(p[1], lo[1], ie[1]), hash_unit(p[2], lo[2], ie[2])};
 #pragma unroll
-			for (int c = 0; c < 8; c++) {
-				const uint32_t idx = hash_index(g, l, h.x0[0] + (c & 1), h.x0[1] + ((c >> 1) & 1),
-				                                h.x0[2] + ((c >> 2) & 1));
-				const float wc = hash_weight(h, c);
-				const float2 e = __ldg(tl + idx);
-				f0 = fmaf(wc, e.x, f0);
-				f1 = fmaf(wc, e.y, f1);
-			}
-			row_words[l] = pack_bf16(f0, f1);
+	for (int i = 0; i < kHashLevels / 2; i++) {
+		const int l = 2 * i + half;
+		const float res = half ? g.res[2 * i + 1] : g.res[2 * i];
+		const HashCorners h = hash_cell_u(u, res);
+		const float2* tl = g.table + (size_t)l * g.T;
+		const bool dense = (g.dense >> l) & 1u;
+		float f0 = 0.f, f1 = 0.f;
+#pragma unroll
+		for (int c = 0; c < 8; c++) {
+			const uint32_t idx = hash_index_r(dense, res, g.T, h.x0[0] + (c & 1), h.x0[1] + ((c >> 1) & 1),
+			                                  h.x0[2] + ((c >> 2) & 1));
+			const float wc = hash_weight(h, c);
+			const float2 e = __ldg(tl + idx);
+			f0 = fmaf(wc, e.x, f0);
+			f1 = fmaf(wc, e.y, f1);
 		}
-	} else {
+		row_words[l] = pack_bf16(f0, f1);
+	}
+	const int j0 = half ? 2 : 0, j1 = half ? 3 : 2;
+	for (int j = j0; j < j1; j++) {
 #pragma unroll
-		for (int j = 0; j < 3; j++) {
-			float u = fminf(fmaxf(__fmul_rn(__fsub_rn(p[j], lo[j]), ie[j]), 0.f), 1.f);
-#pragma unroll
-			for (int k = 0; k < 4; k++) {
-				float s, c;
-				sincospif((float)(1 << k) * u, &s, &c);
-				row_words[16 + 4 * j + k] = pack_bf16(s, c);
-			}
+		for (int k = 0; k < 4; k++) {
+			float s, c;
+			sincospif((float)(1 << k) * u[j], &s, &c);
+			row_words[16 + 4 * j + k] = pack_bf16(s, c);
 		}
+	}
+	if (half) {
 		row_words[28] = pack_bf16(n[0], n[1]);
 		row_words[29] = pack_bf16(n[2], alb[0]);
 		row_words[30] = pack_bf16(alb[1], alb[2]);
