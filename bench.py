@@ -84,6 +84,10 @@ def load_peaks():
 CAMERA_EYE = (-8.5, 4.0, -8.5)
 
 
+TRAVERSAL_NAMES = {0: "default", 1: "if-if", 2: "while-while", 3: "compact", 4: "root-box queue"}
+TRAVERSAL_KERNELS = {0: "k_closest", 1: "k_closest", 2: "k_trace_ww", 3: "k_trace_compact", 4: "k_closest"}
+
+
 def make_workload(name: str, nrays: int = 0, shard: int = 0):
     """Scene and rays of a workload.  nrays > 0 takes a smaller case of the
     same workload (the first nrays/2 camera rows' rays and nrays/2 surface
@@ -810,6 +814,9 @@ def main():
     ap.add_argument("--rays", type=int, default=0, help="smaller case of the workload (profiling)")
     ap.add_argument("--meshes", type=int, default=512, help="c3: first N meshes only (profiling)")
     ap.add_argument("--bvh-width", type=int, default=0, choices=[0, 2, 8], help="c0/c1: BVH width (0 = default)")
+    ap.add_argument("--traversal", type=int, default=0, choices=[0, 1, 2, 3, 4],
+                    help="c0/c1: RRG_TRAVERSAL_* kernel (0 = default, 1 if-if, 2 while-while, 3 compact, "
+                         "4 root-box queue)")
     ap.add_argument("--gather-only", action="store_true",
                     help="c2: time the gather alone (no filter or bake timings; small profiling cases)")
     args = ap.parse_args()
@@ -844,6 +851,8 @@ def main():
     v, t, rays = make_workload(args.workload, args.rays, shard=rank)
     n = rays.shape[0]
     c = col.RRCollider.create(v, t, device=local, build_params={"bvh_width": args.bvh_width})
+    if args.traversal:
+        c.set_traversal(args.traversal)
     build_ms = c.build_ms
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
@@ -907,13 +916,13 @@ def main():
                        "parallelism": f"ray shards x{world} (rank r: shard r of the job, a full workload each)",
                        "l2": "inputs (32 B/ray) larger than L2, no flush",
                        "hit_ratio": hits_total / n, "bvh_build_ms": build_ms, "bvh_nodes": c.nodes,
-                       "bvh_width": args.bvh_width or 2},
+                       "bvh_width": args.bvh_width or 2, "traversal": TRAVERSAL_NAMES[args.traversal]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
                          "traffic": (MEASURED_DRAM_BYTES_PER_RAY[args.workload] * n
                                      if args.workload in MEASURED_DRAM_BYTES_PER_RAY and args.bvh_width != 8
                                      else None),
-                         "kernel": "k_closest", "kernel_ms": kernel_ms, "kernel_launches_timed": kernel_launches,
+                         "kernel": "k_closest_w" if args.bvh_width == 8 else TRAVERSAL_KERNELS[args.traversal], "kernel_ms": kernel_ms, "kernel_launches_timed": kernel_launches,
                          "l2": ({"read_bytes_per_ray": L2_READ_BYTES_PER_RAY[args.workload],
                                  "achieved_gbs": L2_READ_BYTES_PER_RAY[args.workload] * n / (kernel_ms * 1e-3) / 1e9,
                                  "source": "ncu l1tex__m_xbar2l1tex_read_bytes.sum per ray of the workload's capture"}

@@ -85,9 +85,12 @@ enum {
 	RRG_TRAVERSAL_DEFAULT = 0,     /* if-if (measured faster on GB300 for both workloads) */
 	RRG_TRAVERSAL_IF_IF = 1,       /* warp takes 32 rays, per-thread if-if walk */
 	RRG_TRAVERSAL_WHILE_WHILE = 2, /* persistent while-while, postponed leaves, per-lane refill */
-	RRG_TRAVERSAL_COMPACT = 3      /* persistent: a warp claims a block of consecutive rays and each
+	RRG_TRAVERSAL_COMPACT = 3,     /* persistent: a warp claims a block of consecutive rays and each
 	                                  lane walks its share of them one after the other, with no
 	                                  warp-wide step between rays; stack top in shared memory */
+	RRG_TRAVERSAL_ROOT_QUEUE = 4   /* if-if, rays entering neither child box of the root answered
+	                                  at once and the others queued per warp until 32 fill it
+	                                  (rays around an object, most of which pass it by) */
 };
 
 typedef struct rrg_collider rrg_collider;

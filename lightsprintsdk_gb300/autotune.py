@@ -21,7 +21,7 @@ from . import build as _build
 from . import collider as col
 
 LEAF_SIZES = (2, 4, 8)
-TRAVERSALS = (1, 2, 3)   # RRG_TRAVERSAL_IF_IF, RRG_TRAVERSAL_WHILE_WHILE, RRG_TRAVERSAL_COMPACT
+TRAVERSALS = (1, 2, 3, 4)   # RRG_TRAVERSAL_IF_IF, _WHILE_WHILE, _COMPACT, _ROOT_QUEUE
 
 
 def cache_path() -> str:

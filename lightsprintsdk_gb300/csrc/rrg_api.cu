@@ -56,7 +56,7 @@ int init_collider(Collider* c, const rrg_build_params* params) {
 	}
 	c->params.size = sizeof(rrg_build_params);
 	if (c->params.max_leaf_size > (uint32_t)kMaxLeaf) return RRG_ERR_INVALID;
-	if (c->params.traversal > RRG_TRAVERSAL_COMPACT) return RRG_ERR_INVALID;
+	if (c->params.traversal > RRG_TRAVERSAL_ROOT_QUEUE) return RRG_ERR_INVALID;
 	if (c->params.bvh_width != 0 && c->params.bvh_width != 2 && c->params.bvh_width != 8) return RRG_ERR_INVALID;
 	c->width = c->params.bvh_width ? c->params.bvh_width : 2;
 	if (c->width == 8 && c->params.max_leaf_size > (uint32_t)kWideLeafMax) return RRG_ERR_INVALID;
@@ -113,8 +113,12 @@ static int ensure_pipeline(Collider* c) {
 }
 
 // Rays per chunk of a pipelined host call (128 MiB of rays in, 64 MiB of
-// hits out per chunk).
+// hits out per chunk; the size from which a chunk's rays are binned).
+// Calls of up to kHostSingle rays go up, through and back in one piece;
+// larger calls of up to kHostChunk rays are cut into four chunks so that
+// their copies overlap the tracing too.
 constexpr uint32_t kHostChunk = 1u << 22;
+constexpr uint32_t kHostSingle = 1u << 18;
 
 std::atomic<uint64_t> g_launches{0};
 thread_local int t_capturing = 0;
@@ -230,7 +234,7 @@ int rrg_collider_set_ray_order(rrg_collider* h, uint32_t order) {
 
 int rrg_collider_set_traversal(rrg_collider* h, uint32_t traversal) {
 	Collider* c = reinterpret_cast<Collider*>(h);
-	if (!c || traversal > RRG_TRAVERSAL_COMPACT) return RRG_ERR_INVALID;
+	if (!c || traversal > RRG_TRAVERSAL_ROOT_QUEUE) return RRG_ERR_INVALID;
 	c->traversal = traversal ? traversal : RRG_TRAVERSAL_IF_IF;
 	return RRG_OK;
 }
@@ -317,7 +321,7 @@ int rrg_intersect_host(rrg_collider* h, const float* rays_host, uint32_t n, floa
 	std::lock_guard<std::mutex> lk(c->host_mu);
 	RRG_CUDA(cudaSetDevice(c->device));
 	cudaStream_t s = (cudaStream_t)stream;
-	if (n <= kHostChunk) {
+	if (n <= kHostSingle) {
 		int st = ensure_stage(c, 32 * (size_t)n, 16 * (size_t)n);
 		if (st) return st;
 		RRG_CUDA(cudaMemcpyAsync(c->d_stage_in, rays_host, 32 * (size_t)n, cudaMemcpyHostToDevice, s));
@@ -333,19 +337,20 @@ int rrg_intersect_host(rrg_collider* h, const float* rays_host, uint32_t n, floa
 	// (each slot with its own work counter, so a chunk's kernel can start in
 	// the previous one's tail), hits copied out on s_out: the copies of one
 	// chunk overlap the tracing of its neighbours.
-	int st = ensure_stage(c, 3 * 32 * (size_t)kHostChunk, 3 * 16 * (size_t)kHostChunk);
+	const uint32_t chunk = n > kHostChunk ? kHostChunk : ((n + 3) / 4 + 255) / 256 * 256;
+	int st = ensure_stage(c, 3 * 32 * (size_t)chunk, 3 * 16 * (size_t)chunk);
 	if (!st) st = ensure_pipeline(c);
 	if (st) return st;
 	RRG_CUDA(cudaEventRecord(c->ev_start, s));   // after the caller's earlier work on s
 	RRG_CUDA(cudaStreamWaitEvent(c->s_in, c->ev_start, 0));
 	RRG_CUDA(cudaStreamWaitEvent(c->s_comp, c->ev_start, 0));
-	const uint32_t nchunks = (n + kHostChunk - 1) / kHostChunk;
+	const uint32_t nchunks = (n + chunk - 1) / chunk;
 	for (uint32_t k = 0; k < nchunks; k++) {
 		const int slot = (int)(k % 3);
-		const size_t base = (size_t)k * kHostChunk;
-		const uint32_t m = (uint32_t)((n - base) < kHostChunk ? (n - base) : kHostChunk);
-		float4* in = reinterpret_cast<float4*>(c->d_stage_in) + 2 * (size_t)kHostChunk * slot;
-		float4* out = reinterpret_cast<float4*>(c->d_stage_out) + (size_t)kHostChunk * slot;
+		const size_t base = (size_t)k * chunk;
+		const uint32_t m = (uint32_t)((n - base) < chunk ? (n - base) : chunk);
+		float4* in = reinterpret_cast<float4*>(c->d_stage_in) + 2 * (size_t)chunk * slot;
+		float4* out = reinterpret_cast<float4*>(c->d_stage_out) + (size_t)chunk * slot;
 		if (k >= 3) RRG_CUDA(cudaStreamWaitEvent(c->s_in, c->ev_out[slot], 0));   // slot free again
 		RRG_CUDA(cudaMemcpyAsync(in, rays_host + 8 * base, 32 * (size_t)m, cudaMemcpyHostToDevice, c->s_in));
 		RRG_CUDA(cudaEventRecord(c->ev_in[slot], c->s_in));

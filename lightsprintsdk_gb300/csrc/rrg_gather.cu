@@ -1297,7 +1297,6 @@ struct Lightmapper {
 	float* d_corner_weight = nullptr;   // 3 per triangle
 	uint32_t ngroups = 0;
 	uint32_t* d_bake_hits = nullptr;    // rays x triangles (ray j of triangle t at j * triangles + t)
-	uint32_t* d_bake_hits_tm = nullptr; // the same, triangle-major, as the rays write them
 	size_t bake_hits_cap = 0;
 	uint64_t bake_hits_used = 0;
 	uint32_t bake_k = 0;
@@ -1332,7 +1331,6 @@ static void free_lm(Lightmapper* L) {
 	cudaFree(L->d_group_corner);
 	cudaFree(L->d_corner_weight);
 	cudaFree(L->d_bake_hits);
-	cudaFree(L->d_bake_hits_tm);
 	cudaFree(L->d_bake_e);
 	cudaFree(L->d_bake_re);
 	delete L;
@@ -1403,6 +1401,19 @@ static int launch_gather_kernel(Lightmapper* L, const GatherScene& g, uint64_t f
 // each set up by k_gather<0, 0, 1> (first rays and light rounds), advanced
 // bounce by bounce (k_wf_closest, k_wf_nee, k_wf_shadow, k_wf_shade; the
 // path counts stay on the device) and summed (k_wf_reduce).
+// The lightmapper's device scratch (the wavefront's path state; the bake's
+// triangle-major form-factor hits between k_bake_factors and the transpose),
+// grown on demand.
+static int grow_scratch(Lightmapper* L, size_t bytes) {
+	if (bytes <= L->wf_bytes) return RRG_OK;
+	cudaFree(L->d_wf);
+	L->d_wf = nullptr;
+	L->wf_bytes = 0;
+	RRG_CUDA(cudaMalloc(&L->d_wf, bytes));
+	L->wf_bytes = bytes;
+	return RRG_OK;
+}
+
 constexpr uint64_t kWfMinTexels = 16384;
 constexpr uint64_t kWfMaxPaths = 1ull << 23;
 
@@ -1416,13 +1427,7 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 	const uint64_t B = std::min<uint64_t>(count, kWfMaxPaths / Q);   // texels per batch
 	const uint64_t cap = B * Q;                                       // paths per batch
 	const size_t bytes = 9 * 16 * cap + 2 * 16 * B + 8 * B + 5 * 4 * cap + 16;
-	if (bytes > L->wf_bytes) {
-		cudaFree(L->d_wf);
-		L->d_wf = nullptr;
-		L->wf_bytes = 0;
-		RRG_CUDA(cudaMalloc(&L->d_wf, bytes));
-		L->wf_bytes = bytes;
-	}
+	if (int st = grow_scratch(L, bytes)) return st;
 	WfState w;
 	float4* f4 = reinterpret_cast<float4*>(L->d_wf);
 	w.eye = f4;
@@ -1848,13 +1853,16 @@ static int bake_solver(Lightmapper* L, const rrg_gather_params* p, uint32_t k, u
 	const size_t nhits = (size_t)nt * k;
 	if (nhits > L->bake_hits_cap) {
 		cudaFree(L->d_bake_hits);
-		cudaFree(L->d_bake_hits_tm);
-		L->d_bake_hits = L->d_bake_hits_tm = nullptr;
+		L->d_bake_hits = nullptr;
 		L->bake_hits_cap = 0;
 		RRG_CUDA(cudaMalloc(&L->d_bake_hits, nhits * sizeof(uint32_t)));
-		RRG_CUDA(cudaMalloc(&L->d_bake_hits_tm, nhits * sizeof(uint32_t)));
 		L->bake_hits_cap = nhits;
 	}
+	// the rays write their hits triangle-major into the lightmapper's
+	// scratch (which the final gather reuses for its path state); the
+	// transpose leaves the ray-major copy the Jacobi steps read
+	if (int st = grow_scratch(L, nhits * sizeof(uint32_t))) return st;
+	uint32_t* hits_tm = reinterpret_cast<uint32_t*>(L->d_wf);
 	L->bake_hits_used = nhits;
 	L->bake_k = k;
 	const uint32_t qh = q.quality / 2 ? q.quality / 2 : 1;
@@ -1863,10 +1871,9 @@ static int bake_solver(Lightmapper* L, const rrg_gather_params* p, uint32_t k, u
 	rrg::note_launch(), k_bake_direct<<<tgrid, 128, 0, s>>>(g, nt, rounds, L->d_solver_direct, L->d_status);
 	RRG_CUDA(cudaGetLastError());
 	const int fgrid = (int)std::min<uint64_t>((nhits + 127) / 128, (uint64_t)c->num_sms * 64);
-	rrg::note_launch(), k_bake_factors<<<fgrid, 128, 0, s>>>(g, nt, k, L->d_bake_hits_tm, L->d_status);
+	rrg::note_launch(), k_bake_factors<<<fgrid, 128, 0, s>>>(g, nt, k, hits_tm, L->d_status);
 	RRG_CUDA(cudaGetLastError());
-	rrg::note_launch(), k_bake_transpose<<<dim3((nt + 31) / 32, (k + 31) / 32), dim3(32, 8), 0, s>>>(L->d_bake_hits_tm, nt, k,
-	                                                                                              L->d_bake_hits);
+	rrg::note_launch(), k_bake_transpose<<<dim3((nt + 31) / 32, (k + 31) / 32), dim3(32, 8), 0, s>>>(hits_tm, nt, k, L->d_bake_hits);
 	RRG_CUDA(cudaGetLastError());
 	float* e = L->d_bake_e;
 	float* e2 = e + 3 * (size_t)nt;
@@ -2196,8 +2203,14 @@ uint64_t rrg_lightmapper_copy_factor_hits(const rrg_lightmapper* h, uint32_t* hi
 	if (!L || !L->d_bake_hits || !L->d_bake_final) return 0;
 	if (cudaSetDevice(L->c->device) != cudaSuccess) return 0;
 	const uint64_t n = L->bake_hits_used;
-	if (hits_host && cap >= n && cudaMemcpy(hits_host, L->d_bake_hits_tm, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
-		return 0;
+	if (hits_host && cap >= n) {
+		// ray-major on the device (ray j of triangle t at j * nt + t), triangle-major here
+		std::vector<uint32_t> rm(n);
+		if (cudaMemcpy(rm.data(), L->d_bake_hits, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+		const uint64_t k = L->bake_k, nt = k ? n / k : 0;
+		for (uint64_t j = 0; j < k; j++)
+			for (uint64_t t = 0; t < nt; t++) hits_host[t * k + j] = rm[j * nt + t];
+	}
 	return n;
 }
 

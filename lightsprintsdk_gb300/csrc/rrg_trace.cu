@@ -34,22 +34,107 @@ __device__ __forceinline__ uint32_t warp_fetch(uint32_t* counter) {
 	return __shfl_sync(0xFFFFFFFFu, base, 0);
 }
 
-// PERM: ray j of the launch is ray perm[j] of the batch (binned order, see
-// rrg_binning.cu); hits are written at the ray's own index.
+// Whether the first step of traverse() from node 0 enters either child box
+// (a ray that enters neither ends there as a miss).
+__device__ __forceinline__ bool root_enter(const TNode* __restrict__ nodes, int nnodes, const RayState& r) {
+	if (nnodes <= 0) return true;   // traverse() reports the malformed tree
+	const float4* np = reinterpret_cast<const float4*>(nodes);
+	const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
+	const int4 nd = __ldg(reinterpret_cast<const int4*>(np + 3));
+	const float t0 = nd.x != kEmptyRef ? box_enter(r, na.x, na.y, na.z, na.w, nc.x, nc.y, r.tmax) : INFINITY;
+	const float t1 = nd.y != kEmptyRef ? box_enter(r, nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, r.tmax) : INFINITY;
+	return t0 != INFINITY || t1 != INFINITY;
+}
+
+__device__ __forceinline__ void write_miss(uint32_t i, float4* __restrict__ hits, float4* __restrict__ planes,
+                                           float* __restrict__ points) {
+	hits[i] = make_float4(0.f, __int_as_float((int)0xFFFFFFFFu), 0.f, 0.f);
+	if (planes) planes[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+	if (points) { points[3 * (size_t)i] = 0.f; points[3 * (size_t)i + 1] = 0.f; points[3 * (size_t)i + 2] = 0.f; }
+}
+
+// Root-box queue (RRG_TRAVERSAL_ROOT_QUEUE): a warp takes batches of 32
+// rays, answers at once the rays that enter neither child box of the root
+// (or have tmin > tmax), and queues the others in shared memory until 32
+// of them fill the warp; a batch whose 32 rays all enter is traced at once.
+// Where most rays pass the mesh by (rays around an object), a warp then
+// traces 32 rays that enter the tree instead of a few among 32.  Returns
+// the ray index this lane traces next (0xFFFFFFFF: none), or sets done when
+// the launch's rays and the queue are exhausted.  The same rays get the
+// same answers as without the queue; only the order they are walked in
+// changes.
 template <bool PERM>
-__global__ void __launch_bounds__(kTraceThreads) k_closest(const TNode* __restrict__ nodes, int nnodes,
+__device__ __forceinline__ uint32_t next_queued(const TNode* __restrict__ nodes, int nnodes,
+                                                const float4* __restrict__ rays, uint32_t n,
+                                                const uint32_t* __restrict__ perm, uint32_t* counter,
+                                                uint32_t* q, int& qn, bool& exhausted, bool& done,
+                                                float4* __restrict__ hits, float4* __restrict__ planes,
+                                                float* __restrict__ points, uint8_t* __restrict__ occ) {
+	const int lane = threadIdx.x & 31;
+	while (!exhausted) {
+		const uint32_t base = warp_fetch(counter);
+		if (base >= n) { exhausted = true; break; }
+		const uint32_t j = base + lane;
+		const bool valid = j < n;
+		uint32_t i = 0;
+		bool enter = false;
+		if (valid) {
+			i = PERM ? __ldg(perm + j) : j;
+			RayState r;
+			load_ray(rays, i, r);
+			enter = r.tmin <= r.tmax && root_enter(nodes, nnodes, r);
+			if (!enter) {
+				if (occ) occ[i] = 0;
+				else write_miss(i, hits, planes, points);
+			}
+		}
+		const uint32_t mask = __ballot_sync(0xFFFFFFFFu, enter);
+		if (mask == 0xFFFFFFFFu && qn == 0) return i;   // a full batch: trace it as it is
+		if (enter) q[qn + __popc(mask & ((1u << lane) - 1u))] = i;
+		qn += __popc(mask);
+		__syncwarp();
+		if (qn >= 32) break;
+	}
+	if (qn == 0) {
+		done = true;
+		return 0xFFFFFFFFu;
+	}
+	const int take = qn < 32 ? qn : 32;
+	const uint32_t i = lane < take ? q[qn - take + lane] : 0xFFFFFFFFu;
+	__syncwarp();
+	qn -= take;
+	return i;
+}
+
+// PERM: ray j of the launch is ray perm[j] of the batch (binned order, see
+// rrg_binning.cu); hits are written at the ray's own index.  QUEUE: rays
+// come through the root-box queue (next_queued).
+template <bool PERM, bool QUEUE>
+__global__ void __launch_bounds__(kTraceThreads, QUEUE ? 9 : 0) k_closest(const TNode* __restrict__ nodes, int nnodes,
                                                            const float4* __restrict__ tris, int ntris,
                                                            const float4* __restrict__ rays, uint32_t n,
                                                            float4* __restrict__ hits, float4* __restrict__ planes,
                                                            float* __restrict__ points, uint32_t* counter,
                                                            const uint32_t* __restrict__ perm) {
+	__shared__ uint32_t s_q[QUEUE ? kTraceThreads / 32 : 1][64];
+	uint32_t* q = s_q[QUEUE ? threadIdx.x >> 5 : 0];
+	int qn = 0;
+	bool exhausted = false, done = false;
 	const int lane = threadIdx.x & 31;
 	while (true) {
-		uint32_t base = warp_fetch(counter);
-		if (base >= n) break;
-		const uint32_t j = base + lane;
-		if (j >= n) continue;
-		const uint32_t i = PERM ? __ldg(perm + j) : j;
+		uint32_t i;
+		if (QUEUE) {
+			i = next_queued<PERM>(nodes, nnodes, rays, n, perm, counter, q, qn, exhausted, done, hits, planes, points,
+			                      nullptr);
+			if (done) break;
+			if (i == 0xFFFFFFFFu) continue;
+		} else {
+			uint32_t base = warp_fetch(counter);
+			if (base >= n) break;
+			const uint32_t j = base + lane;
+			if (j >= n) continue;
+			i = PERM ? __ldg(perm + j) : j;
+		}
 		RayState r;
 		load_ray(rays, i, r);
 		float tbest = r.tmax;
@@ -59,9 +144,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_closest(const TNode* __restri
 		if (r.tmin <= r.tmax) slot = traverse<false>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow);
 		if (overflow) atomicOr(counter + 1, (uint32_t)RRG_ERR_STACK);
 		if (slot < 0) {
-			hits[i] = make_float4(0.f, __int_as_float((int)0xFFFFFFFFu), 0.f, 0.f);
-			if (planes) planes[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-			if (points) { points[3 * (size_t)i] = 0.f; points[3 * (size_t)i + 1] = 0.f; points[3 * (size_t)i + 2] = 0.f; }
+			write_miss(i, hits, planes, points);
 			continue;
 		}
 		float4 a, b, c;
@@ -78,19 +161,31 @@ __global__ void __launch_bounds__(kTraceThreads) k_closest(const TNode* __restri
 	}
 }
 
-template <bool PERM>
+template <bool PERM, bool QUEUE>
 __global__ void __launch_bounds__(kTraceThreads) k_occluded(const TNode* __restrict__ nodes, int nnodes,
                                                             const float4* __restrict__ tris, int ntris,
                                                             const float4* __restrict__ rays, uint32_t n,
                                                             uint8_t* __restrict__ occ, uint32_t* counter,
                                                             const uint32_t* __restrict__ perm) {
+	__shared__ uint32_t s_q[QUEUE ? kTraceThreads / 32 : 1][64];
+	uint32_t* q = s_q[QUEUE ? threadIdx.x >> 5 : 0];
+	int qn = 0;
+	bool exhausted = false, done = false;
 	const int lane = threadIdx.x & 31;
 	while (true) {
-		uint32_t base = warp_fetch(counter);
-		if (base >= n) break;
-		const uint32_t j = base + lane;
-		if (j >= n) continue;
-		const uint32_t i = PERM ? __ldg(perm + j) : j;
+		uint32_t i;
+		if (QUEUE) {
+			i = next_queued<PERM>(nodes, nnodes, rays, n, perm, counter, q, qn, exhausted, done, nullptr, nullptr,
+			                      nullptr, occ);
+			if (done) break;
+			if (i == 0xFFFFFFFFu) continue;
+		} else {
+			uint32_t base = warp_fetch(counter);
+			if (base >= n) break;
+			const uint32_t j = base + lane;
+			if (j >= n) continue;
+			i = PERM ? __ldg(perm + j) : j;
+		}
 		RayState r;
 		load_ray(rays, i, r);
 		float tbest = r.tmax;
@@ -435,9 +530,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_ww(const TNode* __restr
 
 int trace_occupancy(Collider* c) {
 	int per_sm = 0;
-	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_closest<false>, kTraceThreads, 0));
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_closest<false, false>, kTraceThreads, 0));
 	c->trace_blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
-	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_occluded<false>, kTraceThreads, 0));
+	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_occluded<false, false>, kTraceThreads, 0));
 	c->occl_blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
 	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_ww<false>, kTraceThreads, 0));
 	c->ww_blocks = (per_sm > 0 ? per_sm : 1) * c->num_sms;
@@ -465,10 +560,12 @@ int launch_closest_on(Collider* c, const float4* rays, uint32_t n, float4* hits,
 	uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
 	if (c->width == 8 && c->d_wnodes) {
 		int grid = (int)(want < (uint32_t)c->wide_blocks ? want : (uint32_t)c->wide_blocks);
+		int st = trace_event(c, s, false);
+		if (st) return st;
 		rrg::note_launch(), k_closest_w<<<grid, kTraceThreads, 0, s>>>(c->d_wnodes, (int)c->nwnodes, c->d_wtris, (int)c->nvalid, rays, n,
 		                                           hits, planes, points, words);
 		RRG_CUDA(cudaGetLastError());
-		return RRG_OK;
+		return trace_event(c, s, true);
 	}
 	if (c->traversal == RRG_TRAVERSAL_COMPACT) {
 		const uint32_t* perm = nullptr;
@@ -476,33 +573,34 @@ int launch_closest_on(Collider* c, const float4* rays, uint32_t n, float4* hits,
 			int st = bin_rays(c, rays, n, s, bin_slot, &perm);
 			if (st) return st;
 		}
-		return launch_compact(c, rays, n, hits, planes, points, nullptr, words, perm, s);
+		int st = trace_event(c, s, false);
+		if (!st) st = launch_compact(c, rays, n, hits, planes, points, nullptr, words, perm, s);
+		return st ? st : trace_event(c, s, true);
 	}
-	if (c->traversal != RRG_TRAVERSAL_IF_IF) {
+	if (c->traversal == RRG_TRAVERSAL_WHILE_WHILE) {
 		int grid = (int)(want < (uint32_t)c->ww_blocks ? want : (uint32_t)c->ww_blocks);
+		int st = trace_event(c, s, false);
+		if (st) return st;
 		rrg::note_launch(), k_trace_ww<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays,
 		                                                  n, hits, planes, points, nullptr, words);
 		RRG_CUDA(cudaGetLastError());
-		return RRG_OK;
+		return trace_event(c, s, true);
 	}
 	int grid = (int)(want < (uint32_t)c->trace_blocks ? want : (uint32_t)c->trace_blocks);
+	const bool queue = c->traversal == RRG_TRAVERSAL_ROOT_QUEUE;
+	const uint32_t* perm = nullptr;
 	if (use_binning(c, n)) {
-		const uint32_t* perm = nullptr;
 		int st = bin_rays(c, rays, n, s, bin_slot, &perm);
 		if (st) return st;
-		if ((st = trace_event(c, s, false))) return st;
-		rrg::note_launch(), k_closest<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
-		                                               hits, planes, points, words, perm);
-		if ((st = trace_event(c, s, true))) return st;
-	} else {
-		int st = trace_event(c, s, false);
-		if (st) return st;
-		rrg::note_launch(), k_closest<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
-		                                                hits, planes, points, words, nullptr);
-		if ((st = trace_event(c, s, true))) return st;
 	}
+	auto kernel = perm ? (queue ? k_closest<true, true> : k_closest<true, false>)
+	                   : (queue ? k_closest<false, true> : k_closest<false, false>);
+	int st = trace_event(c, s, false);
+	if (st) return st;
+	rrg::note_launch(), kernel<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
+	                                                          hits, planes, points, words, perm);
 	RRG_CUDA(cudaGetLastError());
-	return RRG_OK;
+	return trace_event(c, s, true);
 }
 
 int trace_event(Collider* c, cudaStream_t s, bool end) {
@@ -538,7 +636,7 @@ int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, c
 		RRG_CUDA(cudaGetLastError());
 		return RRG_OK;
 	}
-	if (c->traversal != RRG_TRAVERSAL_IF_IF) {
+	if (c->traversal == RRG_TRAVERSAL_WHILE_WHILE) {
 		int grid = (int)(want < (uint32_t)c->ww_blocks ? want : (uint32_t)c->ww_blocks);
 		rrg::note_launch(), k_trace_ww<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays,
 		                                                 n, nullptr, nullptr, nullptr, occ, c->d_counter);
@@ -546,16 +644,16 @@ int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, c
 		return RRG_OK;
 	}
 	int grid = (int)(want < (uint32_t)c->occl_blocks ? want : (uint32_t)c->occl_blocks);
+	const bool queue = c->traversal == RRG_TRAVERSAL_ROOT_QUEUE;
+	const uint32_t* perm = nullptr;
 	if (use_binning(c, n)) {
-		const uint32_t* perm = nullptr;
 		int st = bin_rays(c, rays, n, s, 3, &perm);
 		if (st) return st;
-		rrg::note_launch(), k_occluded<true><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
-		                                                occ, c->d_counter, perm);
-	} else {
-		rrg::note_launch(), k_occluded<false><<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
-		                                                 occ, c->d_counter, nullptr);
 	}
+	auto kernel = perm ? (queue ? k_occluded<true, true> : k_occluded<true, false>)
+	                   : (queue ? k_occluded<false, true> : k_occluded<false, false>);
+	rrg::note_launch(), kernel<<<grid, kTraceThreads, 0, s>>>(c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n,
+	                                                          occ, c->d_counter, perm);
 	RRG_CUDA(cudaGetLastError());
 	return RRG_OK;
 }

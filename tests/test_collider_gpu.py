@@ -318,14 +318,16 @@ def test_ray_orders_agree():
     np.testing.assert_array_equal(out[1][1], out[2][1])
 
 
-def test_host_pipeline_matches_device():
-    """rrg_intersect_host above one 4 Mi-ray chunk (pipelined copies, three
-    staging slots reused) returns what rrg_intersect_device returns."""
+@pytest.mark.parametrize("n", [3 * (1 << 22) + 12345, 1000003, 70001])
+def test_host_pipeline_matches_device(n):
+    """rrg_intersect_host returns what rrg_intersect_device returns: above
+    one 4 Mi-ray chunk (pipelined, binned chunks, three staging slots
+    reused), between 256 Ki and 4 Mi rays (four pipelined chunks) and in one
+    piece."""
     import torch
     v, t = scenes.icosphere_c0()
     c = col.RRCollider.create(v, t)
     rng = np.random.default_rng(5)
-    n = 3 * (1 << 22) + 12345
     rays = np.empty((n, 8), np.float32)
     rays[:, 0:3] = rng.uniform(-2.5, 2.5, (n, 3))
     d = rng.normal(size=(n, 3))
@@ -526,6 +528,49 @@ def test_compact_traversal_is_bit_identical(tuning):
         # bit patterns (a miss record holds 0xFFFFFFFF, a NaN as a float)
         assert torch.equal(got.view(torch.int32), ref.view(torch.int32)), (tuning, order)
         assert torch.equal(occ, occ_ref), (tuning, order)
+    c.close()
+
+
+@pytest.mark.parametrize("scene", ["c0", "c1"])
+def test_root_queue_traversal_is_bit_identical(scene):
+    """RRG_TRAVERSAL_ROOT_QUEUE (rays that enter neither root child box
+    answered at once, the others queued per warp) against the if-if kernel:
+    closest-hit records with planes and points, and any-hit flags, bit for
+    bit, in the given and the binned order; on config 0's shell rays (88 %
+    pass the sphere's box by) with rays of tmin > tmax and a ragged count,
+    and on the config-1 interior (every ray inside the tree's box)."""
+    import torch
+    if scene == "c0":
+        v, t = scenes.icosphere_c0()
+        rays = scenes.shell_rays((1 << 18) + 77)
+        rays[::101, 3] = rays[::101, 7] + 1.0   # empty interval
+    else:
+        sc = scenes.interior_c1()
+        v, t = sc.vertices, sc.indices
+        rays = np.concatenate([scenes.camera_rays(rows=64), scenes.surface_rays(v, t, 1 << 18),
+                               scenes.shadow_rays(v, t, (1 << 16) + 13)])
+    n = len(rays)
+    c = col.RRCollider.create(v, t)
+    dr = torch.from_numpy(rays).cuda()
+    out = {}
+    for trav in (1, 4):
+        c.set_traversal(trav)
+        for order in (col.RAY_ORDER_AS_GIVEN, col.RAY_ORDER_BINNED):
+            c.set_ray_order(order)
+            h = torch.full((n, 4), 7.0, dtype=torch.float32, device="cuda")
+            pl = torch.full((n, 4), 7.0, dtype=torch.float32, device="cuda")
+            pt = torch.full((n, 3), 7.0, dtype=torch.float32, device="cuda")
+            occ = torch.full((n,), 7, dtype=torch.uint8, device="cuda")
+            c.intersect_device(dr.data_ptr(), n, h.data_ptr(), pl.data_ptr(), pt.data_ptr())
+            c.occluded_device(dr.data_ptr(), n, occ.data_ptr())
+            assert c.status() == 0
+            out[trav, order] = (h.view(torch.int32), pl.view(torch.int32), pt.view(torch.int32), occ)
+    for order in (col.RAY_ORDER_AS_GIVEN, col.RAY_ORDER_BINNED):
+        for a, b in zip(out[1, order], out[4, order]):
+            assert torch.equal(a, b), order
+    if scene == "c0":
+        missed = (out[1, col.RAY_ORDER_AS_GIVEN][0][:, 1] == -1).float().mean().item()
+        assert missed > 0.9
     c.close()
 
 
