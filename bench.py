@@ -84,7 +84,7 @@ def load_peaks():
 CAMERA_EYE = (-8.5, 4.0, -8.5)
 
 
-TRAVERSAL_NAMES = {0: "default", 1: "if-if", 2: "while-while", 3: "compact", 4: "root-box queue"}
+TRAVERSAL_NAMES = {0: "root-box queue (default)", 1: "if-if", 2: "while-while", 3: "compact", 4: "root-box queue"}
 TRAVERSAL_KERNELS = {0: "k_closest", 1: "k_closest", 2: "k_trace_ww", 3: "k_trace_compact", 4: "k_closest"}
 
 
@@ -725,6 +725,8 @@ def run_batch(args, world, rank, local):
                                                          "bvh_width": tuned["bvh_width"]})
     b.set_rays_per_warp(tuned["rays_per_warp"])
     b.set_stack_smem(tuned.get("stack_smem", 0))
+    if tuned["bvh_width"] == 2:
+        b.set_root_queue(bool(tuned.get("root_queue", 0)))
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
 

@@ -82,7 +82,7 @@ typedef struct rrg_build_params {
 
 /* Traversal kernels (chosen per collider; rrg_collider_set_traversal). */
 enum {
-	RRG_TRAVERSAL_DEFAULT = 0,     /* if-if (measured faster on GB300 for both workloads) */
+	RRG_TRAVERSAL_DEFAULT = 0,     /* RRG_TRAVERSAL_ROOT_QUEUE (on GB300: config 0 +21 %, config 1 even) */
 	RRG_TRAVERSAL_IF_IF = 1,       /* warp takes 32 rays, per-thread if-if walk */
 	RRG_TRAVERSAL_WHILE_WHILE = 2, /* persistent while-while, postponed leaves, per-lane refill */
 	RRG_TRAVERSAL_COMPACT = 3,     /* persistent: a warp claims a block of consecutive rays and each

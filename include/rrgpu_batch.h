@@ -49,6 +49,12 @@ RRG_API int rrg_batch_set_rays_per_warp(rrg_batch* b, uint32_t rays_per_warp);
  * not depend on it. */
 RRG_API int rrg_batch_set_stack_smem(rrg_batch* b, uint32_t entries);
 
+/* Root-box queue of the batch's closest-hit kernel (binary trees; on = 1):
+ * rays that enter neither child box of their mesh's root are answered at
+ * once and the others traced 32 to a warp, for rays around meshes most of
+ * which pass them by.  A tuning knob; results do not depend on it. */
+RRG_API int rrg_batch_set_root_queue(rrg_batch* b, int on);
+
 /* Closest hit for n device rays (float[8] each, as rrg_intersect_device);
  * ray_off_dev = nmesh+1 ascending device offsets, ray_off[nmesh] = n: ray i
  * belongs to the mesh m with ray_off[m] <= i < ray_off[m+1].  Writes one hit

@@ -4,7 +4,7 @@ caller's own rays.  Results persist in a JSON file (the package's _lib
 directory, or $RRG_AUTOTUNE_CACHE) keyed by "<gpu name>|<log2 triangles>|<tag>".
 
 Candidates: max_leaf_size in {2, 4, 8} x traversal in {if-if, while-while,
-compact} for single colliders; for mesh batches (tune_batch) the BVH width
+compact, root-box queue} for single colliders; for mesh batches (tune_batch) the BVH width
 and leaf size x rays per warp in {32, 128} x shared-memory stack entries
 per thread in {0, 8, 16} (binary trees; the 8-wide walk has its own
 stack).
@@ -104,12 +104,12 @@ BATCH_TREES = ((2, 2), (2, 4), (2, 8), (8, 2), (8, 4))
 
 
 def tune_batch(mb, rays_dev, ray_off_dev, repeats: int = 3, force: bool = False) -> dict:
-    """BVH width and leaf size x rays per warp x shared-memory stack depth
-    for a mesh batch (scenes.MeshBatch), timed with CUDA events on the
-    caller's device rays (all of them: the tuner sees the real mix of meshes
-    and ray sets).  Remembered per GPU and log2(total triangles) bucket;
-    returns {"bvh_width", "max_leaf_size", "rays_per_warp", "stack_smem",
-    "grays": {...}}."""
+    """BVH width and leaf size x rays per warp x shared-memory stack depth x
+    root-box queue (binary trees) for a mesh batch (scenes.MeshBatch), timed
+    with CUDA events on the caller's device rays (all of them: the tuner
+    sees the real mix of meshes and ray sets).  Remembered per GPU and
+    log2(total triangles) bucket; returns {"bvh_width", "max_leaf_size",
+    "rays_per_warp", "stack_smem", "root_queue", "grays": {...}}."""
     import torch
     from . import batch as rb
     k = key(int(mb.tri_off[-1]), "batch")
@@ -123,22 +123,26 @@ def tune_batch(mb, rays_dev, ray_off_dev, repeats: int = 3, force: bool = False)
         b = rb.RRColliderBatch.from_meshes(mb, build_params={"max_leaf_size": leaf, "bvh_width": width})
         for rpw in BATCH_RAYS_PER_WARP:
             for sd in (BATCH_STACK_SMEM if width == 2 else (0,)):
-                b.set_rays_per_warp(rpw)
-                b.set_stack_smem(sd)
-                b.intersect_device(rays_dev.data_ptr(), ray_off_dev.data_ptr(), n, hits.data_ptr())
-                torch.cuda.synchronize()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record()
-                for _ in range(repeats):
+                for q in ((0, 1) if width == 2 else (0,)):
+                    b.set_rays_per_warp(rpw)
+                    b.set_stack_smem(sd)
+                    if width == 2:
+                        b.set_root_queue(bool(q))
                     b.intersect_device(rays_dev.data_ptr(), ray_off_dev.data_ptr(), n, hits.data_ptr())
-                e1.record()
-                torch.cuda.synchronize()
-                results[f"w{width}_leaf{leaf}_rpw{rpw}_sd{sd}"] = n / (e0.elapsed_time(e1) / repeats * 1e-3) / 1e9
+                    torch.cuda.synchronize()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    for _ in range(repeats):
+                        b.intersect_device(rays_dev.data_ptr(), ray_off_dev.data_ptr(), n, hits.data_ptr())
+                    e1.record()
+                    torch.cuda.synchronize()
+                    results[f"w{width}_leaf{leaf}_rpw{rpw}_sd{sd}_q{q}"] = (
+                        n / (e0.elapsed_time(e1) / repeats * 1e-3) / 1e9)
         b.close()
     best = max(results, key=results.get)
-    w, leaf, rpw, sd = best.split("_")
+    w, leaf, rpw, sd, q = best.split("_")
     entry = {"bvh_width": int(w[1:]), "max_leaf_size": int(leaf[4:]), "rays_per_warp": int(rpw[3:]),
-             "stack_smem": int(sd[2:]), "grays": results, "rays": int(n)}
+             "stack_smem": int(sd[2:]), "root_queue": int(q[1:]), "grays": results, "rays": int(n)}
     db[k] = entry
     _save(db)
     return entry

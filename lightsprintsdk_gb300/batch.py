@@ -30,6 +30,7 @@ def _lib():
         L.rrg_batch_destroy.restype = None
         L.rrg_batch_set_rays_per_warp.argtypes = [P, U]
         L.rrg_batch_set_stack_smem.argtypes = [P, U]
+        L.rrg_batch_set_root_queue.argtypes = [P, C.c_int]
         L.rrg_batch_set_vertices_device.argtypes = [P, P, P]
         L.rrg_batch_rebuild_intersect_device.argtypes = [P, P, P, U, P, P]
         L.rrg_batch_intersect_device.argtypes = [P, P, P, U, P, P]
@@ -96,6 +97,10 @@ class RRColliderBatch:
     def set_stack_smem(self, entries: int) -> None:
         """Traversal-stack entries per thread in shared memory (0, 8, 16, 32)."""
         col._check(_lib().rrg_batch_set_stack_smem(self._h, int(entries)), "rrg_batch_set_stack_smem")
+
+    def set_root_queue(self, on: bool) -> None:
+        """Root-box queue in the closest-hit kernel (binary trees)."""
+        col._check(_lib().rrg_batch_set_root_queue(self._h, 1 if on else 0), "rrg_batch_set_root_queue")
 
     def set_vertices_device(self, xyz_ptr: int, stream: int = 0) -> None:
         """New positions for all vertices (device float[3 * nv], create's layout)."""

@@ -190,8 +190,9 @@ class RRCollider:
 
     # ------------------------------------------------------------ queries
     def set_traversal(self, traversal: int) -> None:
-        """RRG_TRAVERSAL_IF_IF (1, default), RRG_TRAVERSAL_WHILE_WHILE (2),
-        RRG_TRAVERSAL_COMPACT (3) or RRG_TRAVERSAL_ROOT_QUEUE (4)."""
+        """RRG_TRAVERSAL_IF_IF (1), RRG_TRAVERSAL_WHILE_WHILE (2),
+        RRG_TRAVERSAL_COMPACT (3) or RRG_TRAVERSAL_ROOT_QUEUE (4, the default;
+        0 selects it too)."""
         _check(_lib().rrg_collider_set_traversal(self._h, traversal), "rrg_collider_set_traversal")
 
     def set_compact_tuning(self, stack_smem: int = 8, rays_per_warp: int = 0, blocks_per_sm: int = 9) -> None:

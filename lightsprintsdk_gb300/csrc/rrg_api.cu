@@ -60,7 +60,7 @@ int init_collider(Collider* c, const rrg_build_params* params) {
 	if (c->params.bvh_width != 0 && c->params.bvh_width != 2 && c->params.bvh_width != 8) return RRG_ERR_INVALID;
 	c->width = c->params.bvh_width ? c->params.bvh_width : 2;
 	if (c->width == 8 && c->params.max_leaf_size > (uint32_t)kWideLeafMax) return RRG_ERR_INVALID;
-	c->traversal = c->params.traversal ? c->params.traversal : RRG_TRAVERSAL_IF_IF;
+	c->traversal = c->params.traversal ? c->params.traversal : RRG_TRAVERSAL_ROOT_QUEUE;
 	RRG_CUDA(cudaGetDevice(&c->device));
 	cudaDeviceProp prop;
 	RRG_CUDA(cudaGetDeviceProperties(&prop, c->device));
@@ -235,7 +235,7 @@ int rrg_collider_set_ray_order(rrg_collider* h, uint32_t order) {
 int rrg_collider_set_traversal(rrg_collider* h, uint32_t traversal) {
 	Collider* c = reinterpret_cast<Collider*>(h);
 	if (!c || traversal > RRG_TRAVERSAL_ROOT_QUEUE) return RRG_ERR_INVALID;
-	c->traversal = traversal ? traversal : RRG_TRAVERSAL_IF_IF;
+	c->traversal = traversal ? traversal : RRG_TRAVERSAL_ROOT_QUEUE;
 	return RRG_OK;
 }
 

@@ -14,7 +14,7 @@ struct Batch {
 	Collider* c = nullptr;          // all meshes' geometry; c->nroots = meshes
 	uint32_t nmesh = 0;
 	int fetch = 1;                  // rays per warp / 32
-	uint32_t sdepth = 0;            // traversal-stack entries per thread in shared memory (binary tree)
+	uint32_t sdepth = 0;            // mode word: stack entries in shared memory | kBatchRootQueue
 	int blocks = 0;                 // persistent grid (occupancy x SMs) of the current kernel variant
 	cudaStream_t cap = nullptr;     // private stream the graph is captured on
 	cudaGraphExec_t exec = nullptr;
@@ -194,9 +194,23 @@ int rrg_batch_set_stack_smem(rrg_batch* h, uint32_t entries) {
 	if (entries != 0 && entries != 8 && entries != 16 && entries != 32) return RRG_ERR_INVALID;
 	RRG_CUDA(cudaSetDevice(b->c->device));
 	int blocks = 0;
-	int st = batch_trace_blocks(b->c, b->nmesh, entries, &blocks);
+	const uint32_t mode = entries | (b->sdepth & kBatchRootQueue);
+	int st = batch_trace_blocks(b->c, b->nmesh, mode, &blocks);
 	if (st) return st;
-	b->sdepth = entries;
+	b->sdepth = mode;
+	b->blocks = blocks;
+	return RRG_OK;
+}
+
+int rrg_batch_set_root_queue(rrg_batch* h, int on) {
+	Batch* b = reinterpret_cast<Batch*>(h);
+	if (!b) return RRG_ERR_INVALID;
+	RRG_CUDA(cudaSetDevice(b->c->device));
+	int blocks = 0;
+	const uint32_t mode = (b->sdepth & ~kBatchRootQueue) | (on ? kBatchRootQueue : 0u);
+	int st = batch_trace_blocks(b->c, b->nmesh, mode, &blocks);
+	if (st) return st;
+	b->sdepth = mode;
 	b->blocks = blocks;
 	return RRG_OK;
 }

@@ -100,7 +100,7 @@ struct Collider {
 	int occl_blocks = 0;
 	int ww_blocks = 0;
 	int wide_blocks = 0;
-	uint32_t traversal = RRG_TRAVERSAL_IF_IF;
+	uint32_t traversal = RRG_TRAVERSAL_ROOT_QUEUE;
 	// RRG_TRAVERSAL_COMPACT tuning (rrg_collider_set_compact_tuning) and its
 	// persistent grid per kernel variant (filled on first use)
 	uint32_t compact_sdepth = 8, compact_fetch = 1, compact_minb = 9;
@@ -179,6 +179,9 @@ int graph_build_status(GraphBuild* g, cudaStream_t s);
 const TNode* graph_build_nodes(const GraphBuild* g);
 const float4* graph_build_tris(const GraphBuild* g);
 uint32_t graph_build_max_nodes(const GraphBuild* g);
+// a batch trace's mode word: shared-memory stack entries (0, 8, 16, 32),
+// or-ed with kBatchRootQueue for the root-box queue
+constexpr uint32_t kBatchRootQueue = 0x10000u;
 int batch_trace_blocks(Collider* c, uint32_t nmesh, uint32_t sdepth, int* blocks);
 // launch_batch_closest on explicit binary-tree buffers (a graph build's)
 int launch_batch_closest_on(Collider* c, const TNode* nodes, int nnodes, const float4* tris, int ntris,

@@ -265,7 +265,42 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_occluded_w(const uint4* __
 // shared memory) and is traced from that mesh's root, node m; its hit
 // triangle is reported as an index local to mesh m.  A warp takes
 // 32 * fetch consecutive rays per atomic (the rays-per-warp knob).
+// QUEUE: the rays of a claimed block pass through the root-box queue
+// (next_queued's scheme, with each ray's own mesh root): rays entering
+// neither child box of their mesh's root are answered at once, the others
+// traced 32 at a time.
 template <bool WIDE, int SDEPTH>
+__device__ __forceinline__ void batch_trace_ray(const TNode* __restrict__ nodes, int nnodes,
+                                                const uint4* __restrict__ wn, int nwnodes,
+                                                const float4* __restrict__ tris, int ntris,
+                                                const float4* __restrict__ rays, uint32_t i, uint32_t m,
+                                                const uint32_t* __restrict__ tri_off, float4* __restrict__ hits,
+                                                uint32_t* counter, int* sst) {
+	RayState r;
+	load_ray(rays, i, r);
+	float tbest = r.tmax;
+	uint32_t best_tri = 0xFFFFFFFFu;
+	bool overflow = false;
+	int slot = -1;
+	if (r.tmin <= r.tmax) {
+		if (WIDE) slot = traverse_wide<false>(wn, tris, r, nwnodes, ntris, tbest, best_tri, overflow, (int)m);
+		else if (SDEPTH > 0)
+			slot = traverse_split<false, SDEPTH>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow, sst, (int)m);
+		else slot = traverse<false>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow, nullptr, (int)m);
+	}
+	if (overflow) atomicOr(counter + 1, (uint32_t)RRG_ERR_STACK);
+	if (slot < 0) {
+		hits[i] = make_float4(0.f, __int_as_float((int)0xFFFFFFFFu), 0.f, 0.f);
+		return;
+	}
+	float4 a, b, c;
+	load_tri(tris, slot, a, b, c);
+	Fastest f = fastest_fields(r, a, b, c);
+	const uint32_t bits = (best_tri - __ldg(tri_off + m)) | (f.front ? 0x80000000u : 0u);
+	hits[i] = make_float4(f.dist, __int_as_float((int)bits), f.u, f.v);
+}
+
+template <bool WIDE, int SDEPTH, bool QUEUE>
 __global__ void __launch_bounds__(kTraceThreads) k_batch_closest(const TNode* __restrict__ nodes, int nnodes,
                                                                  const uint4* __restrict__ wn, int nwnodes,
                                                                  const float4* __restrict__ tris, int ntris,
@@ -276,44 +311,77 @@ __global__ void __launch_bounds__(kTraceThreads) k_batch_closest(const TNode* __
                                                                  float4* __restrict__ hits, uint32_t* counter) {
 	extern __shared__ uint32_t s_off[];
 	__shared__ int s_stack[(SDEPTH > 0 ? SDEPTH : 1) * kTraceThreads];
+	__shared__ uint32_t s_q[QUEUE ? kTraceThreads / 32 : 1][64];
 	int* const sst = s_stack + threadIdx.x;
 	for (uint32_t k = threadIdx.x; k <= nmesh; k += blockDim.x) s_off[k] = ray_off[k];
 	__syncthreads();
 	const int lane = threadIdx.x & 31;
 	const uint32_t per_fetch = 32u * (uint32_t)fetch;
-	while (true) {
-		uint32_t base = 0;
-		if (lane == 0) base = atomicAdd(counter, per_fetch);
-		base = __shfl_sync(0xFFFFFFFFu, base, 0);
-		if (base >= n) break;
-		for (int j = 0; j < fetch; j++) {
-			const uint32_t i = base + 32u * (uint32_t)j + (uint32_t)lane;
-			if (i >= n) break;
-			const uint32_t m = segment_of(s_off, nmesh, i);
-			RayState r;
-			load_ray(rays, i, r);
-			float tbest = r.tmax;
-			uint32_t best_tri = 0xFFFFFFFFu;
-			bool overflow = false;
-			int slot = -1;
-			if (r.tmin <= r.tmax) {
-				if (WIDE) slot = traverse_wide<false>(wn, tris, r, nwnodes, ntris, tbest, best_tri, overflow, (int)m);
-				else if (SDEPTH > 0)
-					slot = traverse_split<false, SDEPTH>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow, sst,
-					                                     (int)m);
-				else slot = traverse<false>(nodes, tris, r, nnodes, ntris, tbest, best_tri, overflow, nullptr, (int)m);
+	if (!QUEUE) {
+		while (true) {
+			uint32_t base = 0;
+			if (lane == 0) base = atomicAdd(counter, per_fetch);
+			base = __shfl_sync(0xFFFFFFFFu, base, 0);
+			if (base >= n) break;
+			for (int j = 0; j < fetch; j++) {
+				const uint32_t i = base + 32u * (uint32_t)j + (uint32_t)lane;
+				if (i >= n) break;
+				batch_trace_ray<WIDE, SDEPTH>(nodes, nnodes, wn, nwnodes, tris, ntris, rays, i,
+				                              segment_of(s_off, nmesh, i), tri_off, hits, counter, sst);
 			}
-			if (overflow) atomicOr(counter + 1, (uint32_t)RRG_ERR_STACK);
-			if (slot < 0) {
-				hits[i] = make_float4(0.f, __int_as_float((int)0xFFFFFFFFu), 0.f, 0.f);
-				continue;
-			}
-			float4 a, b, c;
-			load_tri(tris, slot, a, b, c);
-			Fastest f = fastest_fields(r, a, b, c);
-			const uint32_t bits = (best_tri - __ldg(tri_off + m)) | (f.front ? 0x80000000u : 0u);
-			hits[i] = make_float4(f.dist, __int_as_float((int)bits), f.u, f.v);
 		}
+		return;
+	}
+	uint32_t* q = s_q[QUEUE ? threadIdx.x >> 5 : 0];
+	int qn = 0;
+	bool exhausted = false;
+	uint32_t blk = 0, blk_end = 0;   // the warp's claimed block of rays (warp-uniform)
+	while (true) {
+		uint32_t i = 0xFFFFFFFFu;
+		bool direct = false;
+		while (!exhausted) {
+			if (blk >= blk_end) {
+				uint32_t base = 0;
+				if (lane == 0) base = atomicAdd(counter, per_fetch);
+				base = __shfl_sync(0xFFFFFFFFu, base, 0);
+				if (base >= n) {
+					exhausted = true;
+					break;
+				}
+				blk = base;
+				blk_end = n - base < per_fetch ? n : base + per_fetch;
+			}
+			const uint32_t ri = blk + (uint32_t)lane;
+			blk += 32;
+			bool enter = false;
+			if (ri < blk_end) {
+				const uint32_t m = segment_of(s_off, nmesh, ri);
+				RayState r;
+				load_ray(rays, ri, r);
+				enter = r.tmin <= r.tmax && root_enter(nodes + m, nnodes - (int)m, r);
+				if (!enter) hits[ri] = make_float4(0.f, __int_as_float((int)0xFFFFFFFFu), 0.f, 0.f);
+			}
+			const uint32_t mask = __ballot_sync(0xFFFFFFFFu, enter);
+			if (mask == 0xFFFFFFFFu && qn == 0) {   // a full batch: trace it as it is
+				i = ri;
+				direct = true;
+				break;
+			}
+			if (enter) q[qn + __popc(mask & ((1u << lane) - 1u))] = ri;
+			qn += __popc(mask);
+			__syncwarp();
+			if (qn >= 32) break;
+		}
+		if (!direct) {
+			if (qn == 0) break;   // rays and queue exhausted
+			const int take = qn < 32 ? qn : 32;
+			if (lane < take) i = q[qn - take + lane];
+			__syncwarp();
+			qn -= take;
+		}
+		if (i != 0xFFFFFFFFu)
+			batch_trace_ray<WIDE, SDEPTH>(nodes, nnodes, wn, nwnodes, tris, ntris, rays, i, segment_of(s_off, nmesh, i),
+			                              tri_off, hits, counter, sst);
 	}
 }
 
@@ -684,15 +752,21 @@ using BatchKernel = void (*)(const TNode*, int, const uint4*, int, const float4*
                              const uint32_t*, const uint32_t*, uint32_t, int, float4*, uint32_t*);
 
 // k_batch_closest for the tree width and the shared-memory stack depth
-// (0, 8, 16 or 32 entries; the wide walk keeps its own local stack)
-static BatchKernel batch_kernel(const Collider* c, uint32_t sdepth) {
-	if (c->width == 8 && c->d_wnodes) return k_batch_closest<true, 0>;
-	switch (sdepth) {
-		case 8: return k_batch_closest<false, 8>;
-		case 16: return k_batch_closest<false, 16>;
-		case 32: return k_batch_closest<false, 32>;
-		default: return k_batch_closest<false, 0>;
+// (0, 8, 16 or 32 entries; the wide walk keeps its own local stack);
+// mode = entries | kBatchRootQueue for the root-box queue (binary tree)
+static BatchKernel binary_batch_kernel(uint32_t mode) {
+	const bool q = (mode & kBatchRootQueue) != 0;
+	switch (mode & ~kBatchRootQueue) {
+		case 8: return q ? k_batch_closest<false, 8, true> : k_batch_closest<false, 8, false>;
+		case 16: return q ? k_batch_closest<false, 16, true> : k_batch_closest<false, 16, false>;
+		case 32: return q ? k_batch_closest<false, 32, true> : k_batch_closest<false, 32, false>;
+		default: return q ? k_batch_closest<false, 0, true> : k_batch_closest<false, 0, false>;
 	}
+}
+
+static BatchKernel batch_kernel(const Collider* c, uint32_t mode) {
+	if (c->width == 8 && c->d_wnodes) return k_batch_closest<true, 0, false>;
+	return binary_batch_kernel(mode);
 }
 
 int batch_trace_blocks(Collider* c, uint32_t nmesh, uint32_t sdepth, int* blocks) {
@@ -714,10 +788,7 @@ int launch_batch_closest_on(Collider* c, const TNode* nodes, int nnodes, const f
 	const uint32_t want = (uint32_t)(((uint64_t)n + per_fetch - 1) / per_fetch * 32 / kTraceThreads + 1);
 	const int grid = (int)(want < (uint32_t)blocks ? want : (uint32_t)blocks);
 	const size_t smem = sizeof(uint32_t) * (nmesh + 1);
-	BatchKernel k = k_batch_closest<false, 0>;
-	if (sdepth == 8) k = k_batch_closest<false, 8>;
-	else if (sdepth == 16) k = k_batch_closest<false, 16>;
-	else if (sdepth == 32) k = k_batch_closest<false, 32>;
+	BatchKernel k = binary_batch_kernel(sdepth);
 	rrg::note_launch(), k<<<grid, kTraceThreads, smem, s>>>(nodes, nnodes, nullptr, 0, tris, ntris, rays, n, ray_off,
 	                                                      c->d_tri_off, nmesh, fetch, hits, c->d_counter);
 	RRG_CUDA(cudaGetLastError());

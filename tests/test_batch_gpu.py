@@ -161,6 +161,32 @@ def test_stack_depths_agree(small_batch):
     b.set_stack_smem(0)
 
 
+def test_root_queue_agrees(small_batch):
+    """The batch kernel's root-box queue (rays entering neither child box of
+    their mesh's root answered at once, the rest traced 32 to a warp) gives
+    the same records, bit for bit, for every stack depth and rays-per-warp
+    setting, in plain launches and in the graph rebuild."""
+    import torch
+    mb, counts, rays, off, off_d, b = small_batch
+    b.set_root_queue(False)
+    b.set_stack_smem(0)
+    base = run(b, rays, off_d, 32)
+    b.set_root_queue(True)
+    for sd in (0, 16):
+        b.set_stack_smem(sd)
+        for k in (32, 128):
+            np.testing.assert_array_equal(run(b, rays, off_d, k).view(np.uint32), base.view(np.uint32),
+                                          err_msg=f"queue, stack {sd} rays per warp {k}")
+    b.set_stack_smem(0)
+    n = rays.shape[0]
+    hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    b.rebuild_intersect_device(rays.data_ptr(), off_d.data_ptr(), n, hits.data_ptr())
+    torch.cuda.synchronize()
+    assert b.status() == 0
+    np.testing.assert_array_equal(hits.cpu().numpy().view(np.uint32), base.view(np.uint32))
+    b.set_root_queue(False)
+
+
 def test_rebuild_in_graph_equals_per_mesh_colliders(small_batch):
     """One graph replay rebuilds every mesh's tree from the batch's vertex
     positions and traces all the rays (rrg_batch_rebuild_intersect_device):

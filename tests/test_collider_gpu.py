@@ -266,15 +266,16 @@ def test_out_of_range_index_is_invalid():
 
 
 def test_traversal_variants_agree(c0):
-    """The while-while kernel (default) and the if-if kernel return the same
-    hits (ties broken by triangle index, so bit-identical)."""
+    """The if-if, while-while and default (root-box queue) kernels return
+    the same hits (ties broken by triangle index, so bit-identical)."""
     v, t, rays, _, c = c0
     c.set_traversal(1)
     a = c.intersect_batch(rays)
-    c.set_traversal(2)
-    b = c.intersect_batch(rays)
-    for f in ("hit", "tri", "dist", "uv", "side"):
-        np.testing.assert_array_equal(a[f], b[f])
+    for trav in (2, 0):
+        c.set_traversal(trav)
+        b = c.intersect_batch(rays)
+        for f in ("hit", "tri", "dist", "uv", "side"):
+            np.testing.assert_array_equal(a[f], b[f])
 
 
 def test_launch_count_counts_device_calls(c0):
