@@ -176,12 +176,15 @@ RRG_API int rrg_intersect_device(rrg_collider* c, const float* rays_dev, uint32_
 RRG_API int rrg_occluded_device(rrg_collider* c, const float* rays_dev, uint32_t n, uint8_t* occluded_dev,
                         void* stream);
 
-/* Host buffers in, host buffers out: copies the rays to the device, traces,
- * copies the hit records back and synchronises.  Uses device staging buffers
- * owned by the collider (grown on demand); host threads that call this or
- * rrg_intersect_rrray on one collider at once take turns.  Batches above 4,194,304 rays go
- * through in chunks whose copies overlap the tracing of the neighbouring
- * chunks (the overlap needs page-locked host buffers). */
+/* Host buffers in, host buffers out; synchronous.  Up to 4,194,304 rays in
+ * page-locked host memory (cudaHostAlloc / cudaHostRegister, both buffers
+ * 16-byte aligned): the kernel reads the rays and writes the hit records in
+ * host memory directly over the host link.  Otherwise the rays are copied to
+ * device staging buffers owned by the collider (grown on demand), traced and
+ * copied back: batches above 262,144 rays in chunks whose copies overlap the
+ * tracing of the neighbouring chunks (the overlap needs page-locked host
+ * buffers).  Host threads that call this or rrg_intersect_rrray on one
+ * collider at once take turns. */
 RRG_API int rrg_intersect_host(rrg_collider* c, const float* rays_host, uint32_t n, float* hits_host, void* stream);
 
 /* rr::RRRay array on the host (128-byte stride): reads rayOrigin, rayDir,

@@ -165,6 +165,14 @@ RRG_API int rrg_lightmap_bake_host(rrg_lightmapper* lm, const rrg_gather_params*
  * nonzero.  Synchronises the device. */
 RRG_API int rrg_lightmapper_count_rays(rrg_lightmapper* lm, int enable, uint64_t* closest, uint64_t* shadow);
 
+/* Order in which the wavefront gather traces each bounce's closest-hit rays
+ * (and the learned gather its first segments): RRG_RAY_ORDER_DEFAULT and
+ * RRG_RAY_ORDER_BINNED sort the live paths by their rays' origin and
+ * direction cell first (one counting-sort pass, rrg_binning.cu),
+ * RRG_RAY_ORDER_AS_GIVEN traces them in path order.  Results do not depend
+ * on it. */
+RRG_API int rrg_lightmapper_set_ray_order(rrg_lightmapper* lm, uint32_t order);
+
 /* Number of unwrap seams found (0 before the first filter call with seams). */
 RRG_API uint64_t rrg_lightmapper_seams(const rrg_lightmapper* lm);
 /* Runs of samples over all seams (a run: consecutive samples of a seam that

@@ -313,6 +313,19 @@ int rrg_occluded_device(rrg_collider* h, const float* rays_dev, uint32_t n, uint
 	return launch_occluded(c, reinterpret_cast<const float4*>(rays_dev), n, occ_dev, (cudaStream_t)stream);
 }
 
+// The device address of page-locked (registered or cudaHostAlloc'ed) host
+// memory, which kernels can read and write in place over the host link; null
+// for pageable memory or on any error (the caller then copies).
+static const void* mapped_host(const void* p) {
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return nullptr;
+	}
+	if (a.type != cudaMemoryTypeHost || !a.devicePointer || ((uintptr_t)a.devicePointer & 15)) return nullptr;
+	return a.devicePointer;
+}
+
 int rrg_intersect_host(rrg_collider* h, const float* rays_host, uint32_t n, float* hits_host, void* stream) {
 	Collider* c = reinterpret_cast<Collider*>(h);
 	if (!c) return RRG_ERR_INVALID;
@@ -321,6 +334,20 @@ int rrg_intersect_host(rrg_collider* h, const float* rays_host, uint32_t n, floa
 	std::lock_guard<std::mutex> lk(c->host_mu);
 	RRG_CUDA(cudaSetDevice(c->device));
 	cudaStream_t s = (cudaStream_t)stream;
+	if (n <= kHostChunk) {
+		// page-locked rays and hits up to one chunk: the kernel reads the
+		// rays and writes the hits in host memory itself (no staging copies,
+		// no chunk bookkeeping)
+		const void* rd = mapped_host(rays_host);
+		void* hd = rd ? const_cast<void*>(mapped_host(hits_host)) : nullptr;
+		if (rd && hd) {
+			int st = launch_closest(c, reinterpret_cast<const float4*>(rd), n, reinterpret_cast<float4*>(hd), nullptr,
+			                        nullptr, s);
+			if (st) return st;
+			RRG_CUDA(cudaStreamSynchronize(s));
+			return RRG_OK;
+		}
+	}
 	if (n <= kHostSingle) {
 		int st = ensure_stage(c, 32 * (size_t)n, 16 * (size_t)n);
 		if (st) return st;
@@ -336,7 +363,10 @@ int rrg_intersect_host(rrg_collider* h, const float* rays_host, uint32_t n, floa
 	// copied in on s_in, traced alternately on the caller's stream and s_comp
 	// (each slot with its own work counter, so a chunk's kernel can start in
 	// the previous one's tail), hits copied out on s_out: the copies of one
-	// chunk overlap the tracing of its neighbours.
+	// chunk overlap the tracing of its neighbours.  (Writing the hit records
+	// of binned chunks straight into page-locked host memory instead measured
+	// 25-50 % slower on GB300: the binned order scatters them in 16-byte
+	// pieces over the host link.)
 	const uint32_t chunk = n > kHostChunk ? kHostChunk : ((n + 3) / 4 + 255) / 256 * 256;
 	int st = ensure_stage(c, 3 * 32 * (size_t)chunk, 3 * 16 * (size_t)chunk);
 	if (!st) st = ensure_pipeline(c);

@@ -27,9 +27,8 @@ __device__ __forceinline__ uint32_t spread3(uint32_t x) {   // 3 bits -> positio
 	return (x & 1u) | ((x & 2u) << 2) | ((x & 4u) << 4);
 }
 
-__device__ __forceinline__ uint32_t ray_key(const float4* __restrict__ rays, uint32_t i, float lo0, float lo1,
-                                            float lo2, float s0, float s1, float s2) {
-	const float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
+__device__ __forceinline__ uint32_t key_od(float4 a, float4 b, float lo0, float lo1, float lo2, float s0, float s1,
+                                           float s2) {
 	auto cell = [](float v, float lo, float s, int n) {
 		float q = (v - lo) * s;
 		int c = (int)q;
@@ -41,6 +40,11 @@ __device__ __forceinline__ uint32_t ray_key(const float4* __restrict__ rays, uin
 	const uint32_t kd = (dx & 1u) | ((dy & 1u) << 1) | ((dz & 1u) << 2) | ((dx & 2u) << 2) |
 	                    ((dy & 2u) << 3) | ((dz & 2u) << 4);                                   // 6 bits
 	return (ko << 6) | kd;
+}
+
+__device__ __forceinline__ uint32_t ray_key(const float4* __restrict__ rays, uint32_t i, float lo0, float lo1,
+                                            float lo2, float s0, float s1, float s2) {
+	return key_od(__ldg(rays + 2 * (size_t)i), __ldg(rays + 2 * (size_t)i + 1), lo0, lo1, lo2, s0, s1, s2);
 }
 
 __global__ void __launch_bounds__(kBinThreads) k_bin_hist(const float4* __restrict__ rays, uint32_t n, uint32_t chunk,
@@ -165,7 +169,121 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply_exclusive(uint32_t*
 	if (i < n) v[i] = bsum[blockIdx.x] + (w ? wsum[w - 1] : 0u) + incl - x;
 }
 
+// The same two passes over a list of path ids whose count stays on the
+// device (the wavefront gather's live paths): path p's ray is (eye[p],
+// dir[p]); the scatter writes the path ids themselves in key order.
+__global__ void __launch_bounds__(kBinThreads) k_bin_hist_paths(const float4* __restrict__ eye,
+                                                                const float4* __restrict__ dir,
+                                                                const uint32_t* __restrict__ list,
+                                                                const uint32_t* __restrict__ n_dev, float lo0,
+                                                                float lo1, float lo2, float s0, float s1, float s2,
+                                                                uint16_t* __restrict__ keys,
+                                                                uint32_t* __restrict__ hist, uint32_t nblocks) {
+	extern __shared__ uint32_t sh[];
+	for (int b = threadIdx.x; b < kBins; b += blockDim.x) sh[b] = 0;
+	__syncthreads();
+	const uint32_t n = *n_dev;
+	const uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
+	const uint32_t begin = min(n, blockIdx.x * chunk);
+	const uint32_t end = min(n, begin + chunk);
+	for (uint32_t base = begin; base < end; base += blockDim.x) {
+		const uint32_t i = base + threadIdx.x;
+		const bool ok = i < end;
+		uint32_t k = 0xFFFFFFFFu;
+		if (ok) {
+			const uint32_t p = list[i];
+			k = key_od(eye[p], dir[p], lo0, lo1, lo2, s0, s1, s2);
+			keys[i] = (uint16_t)k;
+		}
+		const uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+		if (ok && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&sh[k], (uint32_t)__popc(peers));
+	}
+	__syncthreads();
+	for (int b = threadIdx.x; b < kBins; b += blockDim.x) hist[(size_t)b * nblocks + blockIdx.x] = sh[b];
+}
+
+__global__ void __launch_bounds__(kBinThreads) k_bin_scatter_paths(const uint16_t* __restrict__ keys,
+                                                                   const uint32_t* __restrict__ list,
+                                                                   const uint32_t* __restrict__ n_dev,
+                                                                   const uint32_t* __restrict__ offs, uint32_t nblocks,
+                                                                   uint32_t* __restrict__ out) {
+	extern __shared__ uint32_t cur[];
+	for (int b = threadIdx.x; b < kBins; b += blockDim.x) cur[b] = offs[(size_t)b * nblocks + blockIdx.x];
+	__syncthreads();
+	const uint32_t n = *n_dev;
+	const uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
+	const uint32_t begin = min(n, blockIdx.x * chunk);
+	const uint32_t end = min(n, begin + chunk);
+	const int lane = threadIdx.x & 31;
+	for (uint32_t base = begin; base < end; base += blockDim.x) {
+		const uint32_t i = base + threadIdx.x;
+		const bool ok = i < end;
+		const uint32_t k = ok ? (uint32_t)keys[i] : 0xFFFFFFFFu;
+		const uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+		const int leader = __ffs(peers) - 1;
+		uint32_t pos = 0;
+		if (ok && lane == leader) pos = atomicAdd(&cur[k], (uint32_t)__popc(peers));
+		pos = __shfl_sync(0xFFFFFFFFu, pos, leader);
+		if (ok) out[pos + __popc(peers & ((1u << lane) - 1u))] = list[i];
+	}
+}
+
 }  // namespace
+
+// Bytes of scratch bin_paths needs for lists of up to cap paths.
+size_t bin_paths_bytes(const Collider* c, uint32_t cap) {
+	const uint64_t nh = (uint64_t)kBins * (uint32_t)c->num_sms;
+	const uint64_t nsum = (nh + kScanThreads - 1) / kScanThreads;
+	return sizeof(uint32_t) * (size_t)cap + sizeof(uint32_t) * nh + sizeof(uint32_t) * nsum + 256 +
+	       sizeof(uint16_t) * (size_t)cap;
+}
+
+// Sorts the *n_dev path ids of list by the key of their rays (eye, dir)
+// into out (cap entries), with scratch of bin_paths_bytes(c, cap) bytes.
+int bin_paths(Collider* c, const float4* eye, const float4* dir, const uint32_t* list, const uint32_t* n_dev,
+              uint32_t cap, void* scratch, uint32_t* out, cudaStream_t s) {
+	const uint32_t nblocks = (uint32_t)c->num_sms;
+	const uint64_t nh = (uint64_t)kBins * nblocks;
+	const uint64_t nsum = (nh + kScanThreads - 1) / kScanThreads;
+	if (!c->bin_attr) {
+		RRG_CUDA(cudaFuncSetAttribute(k_bin_hist, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                              (int)(kBins * sizeof(uint32_t))));
+		RRG_CUDA(cudaFuncSetAttribute(k_bin_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                              (int)(kBins * sizeof(uint32_t))));
+		c->bin_attr = true;
+	}
+	static bool path_attr = false;
+	if (!path_attr) {
+		RRG_CUDA(cudaFuncSetAttribute(k_bin_hist_paths, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                              (int)(kBins * sizeof(uint32_t))));
+		RRG_CUDA(cudaFuncSetAttribute(k_bin_scatter_paths, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                              (int)(kBins * sizeof(uint32_t))));
+		path_attr = true;
+	}
+	uint8_t* p = reinterpret_cast<uint8_t*>(scratch);
+	p += sizeof(uint32_t) * (size_t)cap;   // (unused: keeps the layout of bin_rays)
+	uint32_t* hist = reinterpret_cast<uint32_t*>(p);
+	p += sizeof(uint32_t) * nh;
+	uint32_t* bsum = reinterpret_cast<uint32_t*>(p);
+	p += sizeof(uint32_t) * nsum;
+	p = reinterpret_cast<uint8_t*>(((uintptr_t)p + 255) & ~(uintptr_t)255);
+	uint16_t* keys = reinterpret_cast<uint16_t*>(p);
+	float s3[3];
+	for (int k = 0; k < 3; k++) {
+		const float ext = c->aabb_hi[k] - c->aabb_lo[k];
+		s3[k] = ext > 0.f ? 8.f / ext : 0.f;
+	}
+	const size_t smem = kBins * sizeof(uint32_t);
+	rrg::note_launch(), k_bin_hist_paths<<<nblocks, kBinThreads, smem, s>>>(eye, dir, list, n_dev, c->aabb_lo[0],
+	                                                                        c->aabb_lo[1], c->aabb_lo[2], s3[0], s3[1],
+	                                                                        s3[2], keys, hist, nblocks);
+	rrg::note_launch(), k_scan_block_sums<<<(unsigned)nsum, kScanThreads, 0, s>>>(hist, nh, bsum);
+	rrg::note_launch(), k_scan_sums_exclusive<<<1, kScanThreads, 0, s>>>(bsum, (uint32_t)nsum);
+	rrg::note_launch(), k_scan_apply_exclusive<<<(unsigned)nsum, kScanThreads, 0, s>>>(hist, nh, bsum);
+	rrg::note_launch(), k_bin_scatter_paths<<<nblocks, kBinThreads, smem, s>>>(keys, list, n_dev, hist, nblocks, out);
+	RRG_CUDA(cudaGetLastError());
+	return RRG_OK;
+}
 
 int bin_rays(Collider* c, const float4* rays, uint32_t n, cudaStream_t s, int slot, const uint32_t** perm_out) {
 	*perm_out = nullptr;

@@ -942,10 +942,13 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
 }
 
-// Closest hit of every live path (trace_path's traversal and hit fields).
-__global__ void __launch_bounds__(128, 8) k_wf_closest(GatherScene g, WfState w, int cur, uint32_t* status) {
+// Closest hit of every live path (trace_path's traversal and hit fields),
+// in the order of `order` (the live paths sorted by their rays' key) or of
+// the live list.
+__global__ void __launch_bounds__(128, 8) k_wf_closest(GatherScene g, WfState w, int cur, const uint32_t* order,
+                                                     uint32_t* status) {
 	const uint32_t n = w.counts[cur];
-	const uint32_t* live = w.live + (size_t)cur * w.cap;
+	const uint32_t* live = order ? order : w.live + (size_t)cur * w.cap;
 	bool overflow = false;
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		const uint32_t p = live[i];
@@ -976,12 +979,13 @@ __global__ void __launch_bounds__(128, 8) k_wf_closest(GatherScene g, WfState w,
 // query record (first_hit, as the warp-per-texel learned kernel writes it),
 // record of path p = ti * Q + k at recs[p] (recs = the batch's first texel's
 // records).
-__global__ void __launch_bounds__(128, 8) k_wf_first_hit(GatherScene g, WfState w, CacheRec* __restrict__ recs,
-                                                       uint32_t* status) {
+__global__ void __launch_bounds__(128, 8) k_wf_first_hit(GatherScene g, WfState w, const uint32_t* order,
+                                                       CacheRec* __restrict__ recs, uint32_t* status) {
 	const uint32_t n = w.counts[0];
+	const uint32_t* live = order ? order : w.live;
 	bool overflow = false;
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		const uint32_t p = w.live[i];
+		const uint32_t p = live[i];
 		const float4 e = w.eye[p], d = w.dir[p];
 		recs[p] = first_hit(g, mk(e.x, e.y, e.z), mk(d.x, d.y, d.z), __float_as_uint(e.w), overflow);
 	}
@@ -1280,6 +1284,7 @@ struct Lightmapper {
 	// 1 id per texel of a batch, 3 path lists, 3 counters
 	void* d_wf = nullptr;
 	size_t wf_bytes = 0;
+	uint32_t ray_order = RRG_RAY_ORDER_DEFAULT;   // wavefront rays traced in key order (rrg_binning.cu) or as given
 	uint64_t ncovered = 0;
 	// learned-gather work buffers (grown on demand)
 	CacheRec* d_recs = nullptr;
@@ -1426,8 +1431,13 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 	const uint32_t N = Q > rounds ? Q : rounds;
 	const uint64_t B = std::min<uint64_t>(count, kWfMaxPaths / Q);   // texels per batch
 	const uint64_t cap = B * Q;                                       // paths per batch
-	const size_t bytes = 9 * 16 * cap + 2 * 16 * B + 8 * B + 5 * 4 * cap + 16;
-	if (int st = grow_scratch(L, bytes)) return st;
+	const size_t state_bytes = (9 * 16 * cap + 2 * 16 * B + 8 * B + 5 * 4 * cap + 16 + 255) / 256 * 256;
+	// binned order (the default): the live paths sorted by their rays' key
+	// before each closest-hit pass, with the sort's scratch after the state
+	const bool binned = L->ray_order != RRG_RAY_ORDER_AS_GIVEN;
+	const size_t order_bytes = binned ? (4 * cap + 255) / 256 * 256 : 0;
+	const size_t bin_bytes = binned ? bin_paths_bytes(L->c, (uint32_t)cap) : 0;
+	if (int st = grow_scratch(L, state_bytes + order_bytes + bin_bytes)) return st;
 	WfState w;
 	float4* f4 = reinterpret_cast<float4*>(L->d_wf);
 	w.eye = f4;
@@ -1449,6 +1459,8 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 	w.Q = Q;
 	w.N = N;
 	w.rays = L->count_rays ? L->d_rays : nullptr;
+	uint32_t* order = binned ? reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(L->d_wf) + state_bytes) : nullptr;
+	void* bin_scratch = binned ? reinterpret_cast<uint8_t*>(L->d_wf) + state_bytes + order_bytes : nullptr;
 	int per_sm = 0;
 	RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather<false, false, true>, kGatherWarps * 32, 0));
 	int per_sm_c = 0;
@@ -1466,7 +1478,11 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 		    L->d_status, nullptr, DirOut{}, w);
 		RRG_CUDA(cudaGetLastError());
 		if (recs) {
-			rrg::note_launch(), k_wf_first_hit<<<grid_c, 128, 0, s>>>(g, w, recs + b0 * Q, L->d_status);
+			if (binned) {
+				if (int st = bin_paths(L->c, w.eye, w.dir, w.live, w.counts, (uint32_t)cap, bin_scratch, order, s))
+					return st;
+			}
+			rrg::note_launch(), k_wf_first_hit<<<grid_c, 128, 0, s>>>(g, w, order, recs + b0 * Q, L->d_status);
 			rrg::note_launch(), k_wf_learned_out<<<(int)((nb + 127) / 128), 128, 0, s>>>(g, w, (uint32_t)nb, first, out);
 			RRG_CUDA(cudaGetLastError());
 			continue;
@@ -1475,7 +1491,12 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 		for (uint32_t depth = 0; depth <= g.max_depth; depth++) {
 			RRG_CUDA(cudaMemsetAsync(w.counts + 2, 0, 2 * sizeof(uint32_t), s));
 			RRG_CUDA(cudaMemsetAsync(w.counts + (cur ^ 1), 0, sizeof(uint32_t), s));
-			rrg::note_launch(), k_wf_closest<<<grid_c, 128, 0, s>>>(g, w, cur, L->d_status);
+			if (binned) {
+				if (int st = bin_paths(L->c, w.eye, w.dir, w.live + (size_t)cur * cap, w.counts + cur, (uint32_t)cap,
+				                       bin_scratch, order, s))
+					return st;
+			}
+			rrg::note_launch(), k_wf_closest<<<grid_c, 128, 0, s>>>(g, w, cur, order, L->d_status);
 			rrg::note_launch(), k_wf_nee<<<grid_c, 128, 0, s>>>(g, w);
 			rrg::note_launch(), k_wf_shadow<<<grid_c, 128, 0, s>>>(g, w, L->d_status);
 			rrg::note_launch(), k_wf_shade<<<grid_c, 128, 0, s>>>(g, w, cur);
@@ -2146,6 +2167,13 @@ int rrg_lightmap_bake_host(rrg_lightmapper* h, const rrg_gather_params* p, const
 	RRG_CUDA(cudaMemcpyAsync(out_host, L->d_stage, bytes, cudaMemcpyDeviceToHost, s));
 	RRG_CUDA(cudaStreamSynchronize(s));
 	return rrg_lightmapper_status(h, s);
+}
+
+int rrg_lightmapper_set_ray_order(rrg_lightmapper* h, uint32_t order) {
+	Lightmapper* L = reinterpret_cast<Lightmapper*>(h);
+	if (!L || order > RRG_RAY_ORDER_BINNED) return RRG_ERR_INVALID;
+	L->ray_order = order;
+	return RRG_OK;
 }
 
 int rrg_lightmapper_count_rays(rrg_lightmapper* h, int enable, uint64_t* closest, uint64_t* shadow) {

@@ -156,6 +156,10 @@ int launch_closest_on(Collider* c, const float4* rays, uint32_t n, float4* hits,
 // binning (rrg_binning.cu): permutation of the n rays into binned order in
 // scratch slot bin_slot (0..3) of the collider
 int bin_rays(Collider* c, const float4* rays, uint32_t n, cudaStream_t s, int bin_slot, const uint32_t** perm_out);
+// the wavefront gather's live paths sorted by their rays' key (device count)
+size_t bin_paths_bytes(const Collider* c, uint32_t cap);
+int bin_paths(Collider* c, const float4* eye, const float4* dir, const uint32_t* list, const uint32_t* n_dev,
+              uint32_t cap, void* scratch, uint32_t* out, cudaStream_t s);
 int launch_occluded(Collider* c, const float4* rays, uint32_t n, uint8_t* occ, cudaStream_t s);
 int launch_rrray(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, cudaStream_t s);
 int launch_rrray_scratch(Collider* c, void* rrrays_dev, uint32_t n, uint8_t* hit_dev, uint32_t* words,

@@ -247,6 +247,13 @@ class RRLightmapper:
     def seam_runs(self) -> int:
         return int(_lib().rrg_lightmapper_seam_runs(self._h))
 
+    def set_ray_order(self, order: int) -> None:
+        """col.RAY_ORDER_DEFAULT / _BINNED (live paths sorted by their rays'
+        key before each closest-hit pass) or col.RAY_ORDER_AS_GIVEN."""
+        L = _lib()
+        L.rrg_lightmapper_set_ray_order.argtypes = [C.c_void_p, C.c_uint32]
+        col._check(L.rrg_lightmapper_set_ray_order(self._h, int(order)), "rrg_lightmapper_set_ray_order")
+
     def count_rays(self, enable: bool = True) -> tuple[int, int]:
         """(closest-hit rays, shadow rays) the wavefront gather traced since
         the previous call; counting continues while enable."""

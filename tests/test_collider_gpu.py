@@ -323,8 +323,9 @@ def test_ray_orders_agree():
 def test_host_pipeline_matches_device(n):
     """rrg_intersect_host returns what rrg_intersect_device returns: above
     one 4 Mi-ray chunk (pipelined, binned chunks, three staging slots
-    reused), between 256 Ki and 4 Mi rays (four pipelined chunks) and in one
-    piece."""
+    reused); up to one chunk from page-locked buffers (traced in place in
+    host memory) and from pageable ones (between 256 Ki and 4 Mi rays in
+    four pipelined chunks, below in one piece)."""
     import torch
     v, t = scenes.icosphere_c0()
     c = col.RRCollider.create(v, t)
@@ -345,6 +346,10 @@ def test_host_pipeline_matches_device(n):
         c.intersect_device(d_rays.data_ptr(), n, d_hits.data_ptr())
         torch.cuda.synchronize()
         assert torch.equal(h_hits.view(torch.int32), d_hits.cpu().view(torch.int32))
+    if n <= 1 << 22:   # pageable buffers: the staged copy paths
+        p_hits = np.full((n, 4), 3.0, np.float32)
+        assert col._lib().rrg_intersect_host(c.handle, rays.ctypes.data, n, p_hits.ctypes.data, None) == 0
+        assert np.array_equal(p_hits.view(np.int32), d_hits.cpu().numpy().view(np.int32))
     assert c.status() == 0
 
 

@@ -215,9 +215,10 @@ def test_directional_lightmaps_match_oracle(setup):
 def test_wavefront_equals_warp_per_texel(setup, ao):
     """The two schedules of the plain gather (RRG_GATHER_WARP: a warp per
     texel; RRG_GATHER_WAVEFRONT: the paths of a batch advance bounce by
-    bounce) give every texel bit for bit the same value and bent normal: a
-    range over an atlas boundary, covered and uncovered texels, with and
-    without ambient occlusion."""
+    bounce, their closest-hit rays in key order or in path order) give every
+    texel bit for bit the same value and bent normal: a range over an atlas
+    boundary, covered and uncovered texels, with and without ambient
+    occlusion."""
     gs, c, L, G = setup
     S = gs.size * gs.size
     first, count = 255 * S - 3000, 9000   # the last atlas is sparsely covered
@@ -225,10 +226,14 @@ def test_wavefront_equals_warp_per_texel(setup, ao):
     pw = lm.make_params(gs.lights, quality=32, mode=lm.GATHER_WARP, **kw)
     pf = lm.make_params(gs.lights, quality=32, mode=lm.GATHER_WAVEFRONT, **kw)
     a, ab = L.gather_bent(pw, first, count)
-    b, bb = L.gather_bent(pf, first, count)
     assert (a[:, 3] > 0).sum() > 1000 and (a[:, 3] == 0).sum() > 100
-    np.testing.assert_array_equal(a, b)
-    np.testing.assert_array_equal(ab, bb)
+    # the wavefront's closest-hit rays traced in key order (default) and in path order
+    for order in (col.RAY_ORDER_DEFAULT, col.RAY_ORDER_AS_GIVEN):
+        L.set_ray_order(order)
+        b, bb = L.gather_bent(pf, first, count)
+        np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(ab, bb)
+    L.set_ray_order(col.RAY_ORDER_DEFAULT)
 
 
 def test_wavefront_large_call_matches_oracle(setup):
