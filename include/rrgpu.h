@@ -181,9 +181,9 @@ RRG_API int rrg_occluded_device(rrg_collider* c, const float* rays_dev, uint32_t
  * 16-byte aligned): the kernel reads the rays and writes the hit records in
  * host memory directly over the host link.  Otherwise the rays are copied to
  * device staging buffers owned by the collider (grown on demand), traced and
- * copied back: batches above 262,144 rays in chunks whose copies overlap the
- * tracing of the neighbouring chunks (the overlap needs page-locked host
- * buffers).  Host threads that call this or rrg_intersect_rrray on one
+ * copied back: batches above 262,144 rays in chunks (of 4 Mi rays, or four
+ * below that) whose copies overlap the tracing of the neighbouring chunks
+ * (the overlap needs page-locked host buffers).  Host threads that call this or rrg_intersect_rrray on one
  * collider at once take turns. */
 RRG_API int rrg_intersect_host(rrg_collider* c, const float* rays_host, uint32_t n, float* hits_host, void* stream);
 

@@ -166,11 +166,12 @@ RRG_API int rrg_lightmap_bake_host(rrg_lightmapper* lm, const rrg_gather_params*
 RRG_API int rrg_lightmapper_count_rays(rrg_lightmapper* lm, int enable, uint64_t* closest, uint64_t* shadow);
 
 /* Order in which the wavefront gather traces each bounce's closest-hit rays
- * (and the learned gather its first segments): RRG_RAY_ORDER_DEFAULT and
- * RRG_RAY_ORDER_BINNED sort the live paths by their rays' origin and
- * direction cell first (one counting-sort pass, rrg_binning.cu),
- * RRG_RAY_ORDER_AS_GIVEN traces them in path order.  Results do not depend
- * on it. */
+ * (and the learned gather its first segments): RRG_RAY_ORDER_BINNED sorts
+ * the live paths by their rays' origin and direction cell first (one
+ * counting-sort pass, rrg_binning.cu); RRG_RAY_ORDER_DEFAULT and
+ * RRG_RAY_ORDER_AS_GIVEN trace them in path order, where a warp's rays are
+ * one texel's samples (measured 4-6 % faster than binned on GB300).
+ * Results do not depend on it. */
 RRG_API int rrg_lightmapper_set_ray_order(rrg_lightmapper* lm, uint32_t order);
 
 /* Number of unwrap seams found (0 before the first filter call with seams). */

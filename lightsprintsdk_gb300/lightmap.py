@@ -248,8 +248,9 @@ class RRLightmapper:
         return int(_lib().rrg_lightmapper_seam_runs(self._h))
 
     def set_ray_order(self, order: int) -> None:
-        """col.RAY_ORDER_DEFAULT / _BINNED (live paths sorted by their rays'
-        key before each closest-hit pass) or col.RAY_ORDER_AS_GIVEN."""
+        """col.RAY_ORDER_BINNED (live paths sorted by their rays' key before
+        each closest-hit pass) or col.RAY_ORDER_DEFAULT / _AS_GIVEN (path
+        order)."""
         L = _lib()
         L.rrg_lightmapper_set_ray_order.argtypes = [C.c_void_p, C.c_uint32]
         col._check(L.rrg_lightmapper_set_ray_order(self._h, int(order)), "rrg_lightmapper_set_ray_order")

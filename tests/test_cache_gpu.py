@@ -213,15 +213,19 @@ def test_learned_gather_schedules_agree(gather_setup):
     tmp = torch.empty((2 * S, 4), dtype=torch.float32, device="cuda")
     rc.bake_learned(L, cache, p, 0, 2 * S, tmp.data_ptr(), steps=50, batch=16384)
     outs = {}
-    for mode in (lm.GATHER_WARP, lm.GATHER_WAVEFRONT):
+    for mode, order in ((lm.GATHER_WARP, col.RAY_ORDER_DEFAULT), (lm.GATHER_WAVEFRONT, col.RAY_ORDER_DEFAULT),
+                        (lm.GATHER_WAVEFRONT, col.RAY_ORDER_BINNED)):
+        L.set_ray_order(order)
         pm = lm.make_params(gs.lights, quality=64, max_depth=8, seed=0xC2, mode=mode)
         for frac in (2.0, 0.25):
             out = torch.full((2 * S, 4), 7.0, dtype=torch.float32, device="cuda")
             nf = rc.gather_learned(L, cache, pm, 9 * S, 2 * S, out.data_ptr(), fallback_frac=frac)
             torch.cuda.synchronize()
-            outs[(mode, frac)] = (out.cpu().numpy(), nf)
+            outs[(mode, order, frac)] = (out.cpu().numpy(), nf)
+    L.set_ray_order(col.RAY_ORDER_DEFAULT)
     for frac in (2.0, 0.25):
-        a, na = outs[(lm.GATHER_WARP, frac)]
-        b, nb = outs[(lm.GATHER_WAVEFRONT, frac)]
-        assert na == nb
-        np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+        a, na = outs[(lm.GATHER_WARP, col.RAY_ORDER_DEFAULT, frac)]
+        for order in (col.RAY_ORDER_DEFAULT, col.RAY_ORDER_BINNED):
+            b, nb = outs[(lm.GATHER_WAVEFRONT, order, frac)]
+            assert na == nb
+            np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))

@@ -322,10 +322,10 @@ def test_ray_orders_agree():
 @pytest.mark.parametrize("n", [3 * (1 << 22) + 12345, 1000003, 70001])
 def test_host_pipeline_matches_device(n):
     """rrg_intersect_host returns what rrg_intersect_device returns: above
-    one 4 Mi-ray chunk (pipelined, binned chunks, three staging slots
-    reused); up to one chunk from page-locked buffers (traced in place in
-    host memory) and from pageable ones (between 256 Ki and 4 Mi rays in
-    four pipelined chunks, below in one piece)."""
+    4 Mi rays (pipelined, binned chunks of 4 Mi rays, three staging slots
+    reused); up to 4 Mi rays from page-locked
+    buffers (traced in place in host memory) and from pageable ones (staged
+    chunks above 256 Ki rays, below in one piece)."""
     import torch
     v, t = scenes.icosphere_c0()
     c = col.RRCollider.create(v, t)

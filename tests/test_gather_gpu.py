@@ -227,8 +227,8 @@ def test_wavefront_equals_warp_per_texel(setup, ao):
     pf = lm.make_params(gs.lights, quality=32, mode=lm.GATHER_WAVEFRONT, **kw)
     a, ab = L.gather_bent(pw, first, count)
     assert (a[:, 3] > 0).sum() > 1000 and (a[:, 3] == 0).sum() > 100
-    # the wavefront's closest-hit rays traced in key order (default) and in path order
-    for order in (col.RAY_ORDER_DEFAULT, col.RAY_ORDER_AS_GIVEN):
+    # the wavefront's closest-hit rays traced in key order and in path order (default)
+    for order in (col.RAY_ORDER_BINNED, col.RAY_ORDER_DEFAULT):
         L.set_ray_order(order)
         b, bb = L.gather_bent(pf, first, count)
         np.testing.assert_array_equal(a, b)
