@@ -45,7 +45,7 @@ BYTES_PER_RAY = 48          # 32 B ray in (two float4) + 16 B hit record out
 # dram__bytes_write.sum of one launch / its rays): config 1 from a cold-cache
 # capture of 2 Mi rays, config 0 from a capture of the full 1 Mi-ray launch;
 # the bench scales them to its launch
-MEASURED_DRAM_BYTES_PER_RAY = {"c1": 113.5, "c0": 41.2}
+MEASURED_DRAM_BYTES_PER_RAY = {"c1": 113.5, "c0": 44.1}
 # L2 -> L1 read bytes per ray of k_closest (ncu l1tex__m_xbar2l1tex_read_bytes.sum / rays, config-1 capture
 # of 2 Mi rays)
 L2_READ_BYTES_PER_RAY = {"c1": 445.0}

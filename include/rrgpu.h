@@ -179,7 +179,9 @@ RRG_API int rrg_occluded_device(rrg_collider* c, const float* rays_dev, uint32_t
 /* Host buffers in, host buffers out; synchronous.  Up to 4,194,304 rays in
  * page-locked host memory (cudaHostAlloc / cudaHostRegister, both buffers
  * 16-byte aligned): the kernel reads the rays and writes the hit records in
- * host memory directly over the host link.  Otherwise the rays are copied to
+ * host memory directly over the host link (the if-if kernel in the given
+ * order, whatever the collider's traversal setting, so that each warp
+ * writes one contiguous run of records).  Otherwise the rays are copied to
  * device staging buffers owned by the collider (grown on demand), traced and
  * copied back: batches above 262,144 rays in chunks (of 4 Mi rays, or four
  * below that) whose copies overlap the tracing of the neighbouring chunks

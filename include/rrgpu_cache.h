@@ -1,7 +1,7 @@
 /* rrgpu_cache.h -- C ABI of the learned radiance cache used by the lightmap
  * gather.  The cache has no counterpart in the reference: it replaces the
  * bounces past the first of the plain gather (rrgpu_gather.h), whose output
- * stays its fallback and the judge of its error.
+ * stays its fallback and the yardstick of its error.
  *
  * Network: 64 encoded inputs (a frequency or multiresolution hash encoding
  * of the position in the scene box, normal, albedo), four hidden layers of

@@ -3,7 +3,7 @@ the learned lightmap gather (rrg_lightmap_train_samples /
 rrg_lightmap_gather_learned in include/rrgpu_gather.h).
 
 The cache has no counterpart in the reference: it replaces the bounces past
-the first of the plain gather, which remains its fallback and the judge of
+the first of the plain gather, which remains its fallback and the yardstick of
 its error."""
 from __future__ import annotations
 

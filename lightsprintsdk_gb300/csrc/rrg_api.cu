@@ -353,8 +353,7 @@ int rrg_intersect_host(rrg_collider* h, const float* rays_host, uint32_t n, floa
 		const void* rd = mapped_host(rays_host);
 		void* hd = rd ? const_cast<void*>(mapped_host(hits_host)) : nullptr;
 		if (rd && hd) {
-			int st = launch_closest(c, reinterpret_cast<const float4*>(rd), n, reinterpret_cast<float4*>(hd), nullptr,
-			                        nullptr, s);
+			int st = launch_closest_mapped(c, reinterpret_cast<const float4*>(rd), n, reinterpret_cast<float4*>(hd), s);
 			if (st) return st;
 			RRG_CUDA(cudaStreamSynchronize(s));
 			return RRG_OK;

@@ -187,6 +187,8 @@ uint32_t graph_build_max_nodes(const GraphBuild* g);
 // or-ed with kBatchRootQueue for the root-box queue
 constexpr uint32_t kBatchRootQueue = 0x10000u;
 int batch_trace_blocks(Collider* c, uint32_t nmesh, uint32_t sdepth, int* blocks);
+// closest hit with rays and hits in page-locked host memory (rrg_intersect_host)
+int launch_closest_mapped(Collider* c, const float4* rays, uint32_t n, float4* hits, cudaStream_t s);
 // launch_batch_closest on explicit binary-tree buffers (a graph build's)
 int launch_batch_closest_on(Collider* c, const TNode* nodes, int nnodes, const float4* tris, int ntris,
                             const float4* rays, uint32_t n, const uint32_t* ray_off, uint32_t nmesh, int fetch,

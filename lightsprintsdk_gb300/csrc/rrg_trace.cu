@@ -680,6 +680,26 @@ int trace_event(Collider* c, cudaStream_t s, bool end) {
 	return RRG_OK;
 }
 
+// Rays and hit records in page-locked host memory, read and written by the
+// kernel over the host link: the if-if kernel in the given order, so that a
+// warp writes its 32 hit records as one contiguous 512-byte run (the
+// root-box queue's and the binned order's scattered 16-byte writes cost
+// more over the link than they save: 3.3 against 4.0 Grays/s on config 0).
+int launch_closest_mapped(Collider* c, const float4* rays, uint32_t n, float4* hits, cudaStream_t s) {
+	if (!n) return RRG_OK;
+	if (c->width == 8 && c->d_wnodes) return launch_closest(c, rays, n, hits, nullptr, nullptr, s);
+	uint32_t* words = c->d_counter;
+	RRG_CUDA(cudaMemsetAsync(words, 0, 4, s));
+	const uint32_t want = (n + 31) / 32 * 32 / kTraceThreads + 1;
+	const int grid = (int)(want < (uint32_t)c->trace_blocks ? want : (uint32_t)c->trace_blocks);
+	int st = trace_event(c, s, false);
+	if (st) return st;
+	rrg::note_launch(), k_closest<false, false><<<grid, kTraceThreads, 0, s>>>(
+	    c->d_nodes, (int)c->nnodes, c->d_tris, (int)c->nvalid, rays, n, hits, nullptr, nullptr, words, nullptr);
+	RRG_CUDA(cudaGetLastError());
+	return trace_event(c, s, true);
+}
+
 int launch_closest(Collider* c, const float4* rays, uint32_t n, float4* hits, float4* planes, float* points,
                    cudaStream_t s) {
 	return launch_closest_on(c, rays, n, hits, planes, points, c->d_counter, s, 3);
