@@ -268,7 +268,8 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_occluded_w(const uint4* __
 // QUEUE: the rays of a claimed block pass through the root-box queue
 // (next_queued's scheme, with each ray's own mesh root): rays entering
 // neither child box of their mesh's root are answered at once, the others
-// traced 32 at a time.
+// traced 32 at a time.  Capped at 9 blocks per SM (56 registers; the
+// queue variant spills 16 bytes): 2 % faster on config 3 than 8 blocks.
 template <bool WIDE, int SDEPTH>
 __device__ __forceinline__ void batch_trace_ray(const TNode* __restrict__ nodes, int nnodes,
                                                 const uint4* __restrict__ wn, int nwnodes,
@@ -301,7 +302,7 @@ __device__ __forceinline__ void batch_trace_ray(const TNode* __restrict__ nodes,
 }
 
 template <bool WIDE, int SDEPTH, bool QUEUE>
-__global__ void __launch_bounds__(kTraceThreads) k_batch_closest(const TNode* __restrict__ nodes, int nnodes,
+__global__ void __launch_bounds__(kTraceThreads, 9) k_batch_closest(const TNode* __restrict__ nodes, int nnodes,
                                                                  const uint4* __restrict__ wn, int nwnodes,
                                                                  const float4* __restrict__ tris, int ntris,
                                                                  const float4* __restrict__ rays, uint32_t n,
