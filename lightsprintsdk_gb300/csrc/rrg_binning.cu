@@ -230,6 +230,19 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_scatter_paths(const uint16_
 
 }  // namespace
 
+// The binning kernels' shared-memory allowance (128 KB of bins), set on the
+// collider's device the first time it bins.
+static int bin_attrs(Collider* c) {
+	if (c->bin_attr) return RRG_OK;
+	const int smem = (int)(kBins * sizeof(uint32_t));
+	RRG_CUDA(cudaFuncSetAttribute(k_bin_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+	RRG_CUDA(cudaFuncSetAttribute(k_bin_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+	RRG_CUDA(cudaFuncSetAttribute(k_bin_hist_paths, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+	RRG_CUDA(cudaFuncSetAttribute(k_bin_scatter_paths, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+	c->bin_attr = true;
+	return RRG_OK;
+}
+
 // Bytes of scratch bin_paths needs for lists of up to cap paths.
 size_t bin_paths_bytes(const Collider* c, uint32_t cap) {
 	const uint64_t nh = (uint64_t)kBins * (uint32_t)c->num_sms;
@@ -245,21 +258,7 @@ int bin_paths(Collider* c, const float4* eye, const float4* dir, const uint32_t*
 	const uint32_t nblocks = (uint32_t)c->num_sms;
 	const uint64_t nh = (uint64_t)kBins * nblocks;
 	const uint64_t nsum = (nh + kScanThreads - 1) / kScanThreads;
-	if (!c->bin_attr) {
-		RRG_CUDA(cudaFuncSetAttribute(k_bin_hist, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                              (int)(kBins * sizeof(uint32_t))));
-		RRG_CUDA(cudaFuncSetAttribute(k_bin_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                              (int)(kBins * sizeof(uint32_t))));
-		c->bin_attr = true;
-	}
-	static bool path_attr = false;
-	if (!path_attr) {
-		RRG_CUDA(cudaFuncSetAttribute(k_bin_hist_paths, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                              (int)(kBins * sizeof(uint32_t))));
-		RRG_CUDA(cudaFuncSetAttribute(k_bin_scatter_paths, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                              (int)(kBins * sizeof(uint32_t))));
-		path_attr = true;
-	}
+	if (int st = bin_attrs(c)) return st;
 	uint8_t* p = reinterpret_cast<uint8_t*>(scratch);
 	p += sizeof(uint32_t) * (size_t)cap;   // (unused: keeps the layout of bin_rays)
 	uint32_t* hist = reinterpret_cast<uint32_t*>(p);
@@ -303,13 +302,7 @@ int bin_rays(Collider* c, const float4* rays, uint32_t n, cudaStream_t s, int sl
 		c->bin_bytes[slot] = need;
 		account_collider(c);
 	}
-	if (!c->bin_attr) {
-		RRG_CUDA(cudaFuncSetAttribute(k_bin_hist, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                              (int)(kBins * sizeof(uint32_t))));
-		RRG_CUDA(cudaFuncSetAttribute(k_bin_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                              (int)(kBins * sizeof(uint32_t))));
-		c->bin_attr = true;
-	}
+	if (int st = bin_attrs(c)) return st;
 	uint8_t* p = reinterpret_cast<uint8_t*>(c->d_bin[slot]);
 	uint32_t* perm = reinterpret_cast<uint32_t*>(p);
 	p += sizeof(uint32_t) * (size_t)n;

@@ -422,6 +422,7 @@ struct RadianceCache {
 	float* tv = nullptr;
 	float* tgrad = nullptr;
 	uint64_t table_floats = 0;
+	int infer_per_sm = 0;          // resident k_mlp_infer blocks per SM (0: not yet known)
 };
 
 static void free_cache(RadianceCache* C) {
@@ -536,12 +537,13 @@ static int infer_impl(RadianceCache* C, const void* recs_dev, uint64_t n, float*
 	if (!C || !recs_dev || !out_dev || ((uintptr_t)out_dev & 15)) return RRG_ERR_INVALID;
 	if (!n) return RRG_OK;
 	const size_t smem = sizeof(uint32_t) * (kMlpFragWords + kInferWarps * 16 * 32);
-	static int per_sm = 0;
-	if (!per_sm) {
+	if (!C->infer_per_sm) {   // on the cache's device, once
+		int per_sm = 0;
 		RRG_CUDA(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 		RRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_infer, kInferWarps * 32, smem));
-		if (per_sm < 1) per_sm = 1;
+		C->infer_per_sm = per_sm < 1 ? 1 : per_sm;
 	}
+	const int per_sm = C->infer_per_sm;
 	uint64_t ntiles = (n + 15) / 16;
 	uint64_t blocks = (ntiles + kInferWarps - 1) / kInferWarps;
 	uint64_t cap = (uint64_t)C->num_sms * per_sm;   // one wave of resident blocks, grid-stride over the tiles
