@@ -416,7 +416,8 @@ def run_reference(args, rank: int):
                              "sample": ("every ray of the step" if whole else
                                         f"{len(sub)} of {len(rays)} rays per step (evenly spaced); ms_per_step is "
                                         f"the sample's own time"),
-                             "build_s": R.build_s, "memory_bytes": R.memory},
+                             "build_s": R.build_s, "memory_bytes": R.memory,
+                             "fits_in_driver_run": whole},
             "port": {"value": port, "unit": "Grays/s", "cores": threads,
                      "sample": f"oracle/rr_oracle.c over its own BVH, {len(psub)} rays"},
             "e2e": {"value": val, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
