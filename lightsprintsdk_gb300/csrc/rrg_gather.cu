@@ -654,9 +654,9 @@ struct WarpSmem {
 // advance bounce by bounce, one thread per live path, instead of one warp per
 // texel following its lanes' paths to the end (where the warp waits for its
 // longest path: about 5 of 32 lanes busy).  Each bounce is trace_path's loop
-// body split into kernels: k_wf_closest (the closest hit and its fields),
-// k_wf_nee (the contributions toward the lights), k_wf_shadow (one thread per
-// shadow ray), k_wf_shade (the unoccluded contributions added in light order,
+// body split into kernels: k_wf_closest (the closest hit and its fields,
+// then the contributions toward the lights, wf_nee), k_wf_shadow (one thread
+// per shadow ray), k_wf_shade (the unoccluded contributions added in light order,
 // roulette, next direction), with the same arithmetic in the same order, so
 // every path's radiance is bit-identical to trace_path's; k_wf_reduce sums
 // each texel's samples in the order the warp-per-texel kernel does.  Path
@@ -942,6 +942,35 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
 }
 
+// Next event estimation of path p at its hit (trace_path's loop body after
+// the closest hit): the contribution toward each light, and a shadow ray
+// where the light is above the surface and the contribution is not zero.
+// Called by k_wf_closest right after the hit, with the hit in registers.
+__device__ __forceinline__ void wf_nee(const GatherScene& g, const WfState& w, uint32_t p, V3 pnt, V3 nrm,
+                                       uint32_t tri) {
+	const V3 alb = ld3(g.albedo + 3 * (size_t)tri);
+	for (int li = 0; li < 2; li++) {
+		float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+		V3 sdir;
+		if (li == 0) {
+			sdir = neg(g.dir_direction);
+		} else {
+			V3 dd = sub(g.point_position, pnt);
+			sdir = normalized(dd);
+		}
+		if (dot(nrm, sdir) > 0.f) {
+			V3 unob = li == 0 ? g.dir_color : point_irr(g, pnt);
+			float dif = clampf(-dot(neg(sdir), nrm), 0.f, 1.f);
+			V3 contrib = mulv(unob, mul(alb, dif));
+			if (!(contrib.x == 0.f && contrib.y == 0.f && contrib.z == 0.f)) {
+				e = make_float4(contrib.x, contrib.y, contrib.z, 1.f);
+				w.shadow[atomicAdd(&w.counts[3], 1u)] = 2 * p + (uint32_t)li;
+			}
+		}
+		w.nee[2 * (size_t)p + li] = e;
+	}
+}
+
 // (The wavefront's traversal kernels are capped at 7 blocks of 128 per SM:
 // 72 registers, no spills in k_wf_closest; measured 1 % faster over the
 // config-2 bake than 8 blocks with 64 registers and spills.)
@@ -973,6 +1002,7 @@ __global__ void __launch_bounds__(128, 7) k_wf_closest(GatherScene g, WfState w,
 		w.hitp[p] = make_float4(hp.x, hp.y, hp.z, __uint_as_float(tri));
 		w.hitn[p] = make_float4(fs.n[0], fs.n[1], fs.n[2], 0.f);
 		w.hits[atomicAdd(&w.counts[2], 1u)] = p;
+		wf_nee(g, w, p, hp, mk(fs.n[0], fs.n[1], fs.n[2]), tri);
 	}
 	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
 }
@@ -1004,40 +1034,6 @@ __global__ void k_wf_learned_out(GatherScene g, WfState w, uint32_t nb, uint64_t
 	if (tid == ~0ull) return;
 	const float4 l = w.slot_lights[ti];
 	out[tid - out_base] = make_float4(l.x, l.y, l.z, texel_alpha(g, tid));
-}
-
-// Next event estimation of every path that hit (trace_path's loop body after
-// the closest hit): the contribution toward each light, and a shadow ray
-// where the light is above the surface and the contribution is not zero.
-__global__ void __launch_bounds__(128) k_wf_nee(GatherScene g, WfState w) {
-	const uint32_t n = w.counts[2];
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		const uint32_t p = w.hits[i];
-		const float4 hp4 = w.hitp[p], hn4 = w.hitn[p];
-		const V3 pnt = mk(hp4.x, hp4.y, hp4.z), nrm = mk(hn4.x, hn4.y, hn4.z);
-		const uint32_t tri = __float_as_uint(hp4.w);
-		const V3 alb = ld3(g.albedo + 3 * (size_t)tri);
-		for (int li = 0; li < 2; li++) {
-			float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
-			V3 sdir;
-			if (li == 0) {
-				sdir = neg(g.dir_direction);
-			} else {
-				V3 dd = sub(g.point_position, pnt);
-				sdir = normalized(dd);
-			}
-			if (dot(nrm, sdir) > 0.f) {
-				V3 unob = li == 0 ? g.dir_color : point_irr(g, pnt);
-				float dif = clampf(-dot(neg(sdir), nrm), 0.f, 1.f);
-				V3 contrib = mulv(unob, mul(alb, dif));
-				if (!(contrib.x == 0.f && contrib.y == 0.f && contrib.z == 0.f)) {
-					e = make_float4(contrib.x, contrib.y, contrib.z, 1.f);
-					w.shadow[atomicAdd(&w.counts[3], 1u)] = 2 * p + (uint32_t)li;
-				}
-			}
-			w.nee[2 * (size_t)p + li] = e;
-		}
-	}
 }
 
 // The shadow rays of this bounce, one thread each (the same ray and test as
@@ -1407,7 +1403,8 @@ static int launch_gather_kernel(Lightmapper* L, const GatherScene& g, uint64_t f
 
 // The wavefront gather of texels [first, first + count): batches of texels,
 // each set up by k_gather<0, 0, 1> (first rays and light rounds), advanced
-// bounce by bounce (k_wf_closest, k_wf_nee, k_wf_shadow, k_wf_shade; the
+// bounce by bounce (k_wf_closest with each hit's next-event estimation,
+// k_wf_shadow, k_wf_shade; the
 // path counts stay on the device) and summed (k_wf_reduce).
 // The lightmapper's device scratch (the wavefront's path state; the bake's
 // triangle-major form-factor hits between k_bake_factors and the transpose),
@@ -1505,7 +1502,6 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 					return st;
 			}
 			rrg::note_launch(), k_wf_closest<<<grid_c, 128, 0, s>>>(g, w, cur, order, L->d_status);
-			rrg::note_launch(), k_wf_nee<<<grid_c, 128, 0, s>>>(g, w);
 			rrg::note_launch(), k_wf_shadow<<<grid_c, 128, 0, s>>>(g, w, L->d_status);
 			rrg::note_launch(), k_wf_shade<<<grid_c, 128, 0, s>>>(g, w, cur);
 			cur ^= 1;
