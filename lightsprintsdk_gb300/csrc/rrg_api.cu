@@ -122,10 +122,11 @@ constexpr uint32_t kHostChunk = 1u << 22;
 constexpr uint32_t kHostSingle = 1u << 18;
 
 // Chunk sizes of a pipelined call: kHostChunk rays each (128 MiB of rays in,
-// 64 MiB of hits out, binned), or four equal chunks below that.  (A ramp of
-// 1, 2, 4, 8 ... 8, 4, 2, 1 Mi rays, which shortens the unhidden first
-// copy-in and last copy-out and bins larger chunks, measured 3 % slower end
-// to end on config 1 on GB300: 3.31 against 3.41 Grays/s.)
+// 64 MiB of hits out, binned), or four equal chunks below that.  (On config
+// 1 on GB300 both a ramp of 1, 2, 4, 8 ... 8, 4, 2, 1 Mi rays, which
+// shortens the unhidden first copy-in and last copy-out, and 4, 8, 8, 8, 4
+// Mi rays, which bins larger chunks, measured slower end to end: 3.31 and
+// 3.35 against 3.43 Grays/s.)
 static void chunk_schedule(uint32_t n, std::vector<uint32_t>& sizes) {
 	const uint32_t chunk = n > kHostChunk ? kHostChunk : ((n + 3) / 4 + 255) / 256 * 256;
 	sizes.clear();
