@@ -677,9 +677,16 @@ struct WfState {
 	uint32_t* live;        // 2 x cap: live path lists, ping-pong
 	uint32_t* hits;        // cap: paths that hit in this bounce
 	uint32_t* shadow;      // 2 x cap: shadow rays of this bounce (2p + li)
-	uint32_t* counts;      // [0], [1]: live counts (ping-pong), [2]: hits, [3]: shadow rays
+	uint32_t* counts;      // [0], [1]: live counts (ping-pong), [2]: hits, [3]: shadow rays,
+	                       // [4]: the light rounds' shadow rays
 	uint32_t cap;          // paths
 	uint32_t Q, N;
+	// the light rounds of a batch's texels: slot (ti x shot + round) x 2 + light
+	float4* lr_light;      // the round's contribution (xyz); w = 1 once its shadow ray found the light
+	float4* lr_bent;       // its bent-normal term (xyz)
+	float4* lr_ray;        // 2 per shadow ray: (origin, shooter triangle bits), (direction, length)
+	uint32_t* lr_slot;     // the slot of each shadow ray
+	uint32_t shot;         // light rounds per texel
 	unsigned long long* rays = nullptr;   // optional counts of traced rays: [0] closest, [1] shadow
 };
 
@@ -749,6 +756,9 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 		}
 		const Sub* S = st + b;
 		for (int q = lane; q < kMaxRounds * 2; q += 32) sm.lit[q >> 1][q & 1] = 0;
+		if (WF)   // the wavefront traces the light rounds' shadow rays later (k_wf_light_trace)
+			for (uint32_t q = lane; q < 2 * wf.shot; q += 32)
+				wf.lr_light[(size_t)ti * 2 * wf.shot + q] = make_float4(0.f, 0.f, 0.f, 0.f);
 		// HomogenousFiller2 points: candidate num = reset + j, the k-th accepted one
 		// serves hemisphere ray k (gather.cpp:88-93)
 		const unsigned reset = (unsigned)(hash64(g.seed, S_FILLER, tid) & 0xffffu);
@@ -853,7 +863,26 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 					}
 				}
 			}
-			if (fires && round < (uint32_t)kMaxRounds) {
+			if (WF && fires && round < wf.shot) {
+				// the round's contributions, and its shadow rays for k_wf_light_trace
+				for (int li = 0; li < 2; li++) {
+					const size_t slot = ((size_t)ti * wf.shot + round) * 2 + li;
+					V3 d = li == 0 ? neg(g.dir_direction) : sub(g.point_position, origin);
+					float dsize = len(d);
+					d = divf(d, dsize);
+					if (li == 0) dsize = __fmul_rn(dsize, g.locality);
+					float ni = dot(d, nrm);
+					if (ni <= 0.f || !isfinite(ni)) continue;
+					V3 irr = li == 0 ? g.dir_color : point_irr(g, origin);
+					const V3 lc = mul(irr, ni), lb = mul(d, __fmul_rn(absavg3(irr), ni));   // gather.cpp:488
+					wf.lr_light[slot] = make_float4(lc.x, lc.y, lc.z, 0.f);
+					wf.lr_bent[slot] = make_float4(lb.x, lb.y, lb.z, 0.f);
+					const uint32_t j = atomicAdd(&wf.counts[4], 1u);
+					wf.lr_ray[2 * (size_t)j] = make_float4(origin.x, origin.y, origin.z, __uint_as_float(s.tri));
+					wf.lr_ray[2 * (size_t)j + 1] = make_float4(d.x, d.y, d.z, dsize);
+					wf.lr_slot[j] = (uint32_t)slot;
+				}
+			} else if (fires && round < (uint32_t)kMaxRounds) {
 				for (int li = 0; li < 2; li++) {
 					sm.lit[round][li] = 0;
 					V3 d = li == 0 ? neg(g.dir_direction) : sub(g.point_position, origin);
@@ -889,13 +918,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 6) k_gather(GatherScene g, 
 					if (sm.lit[r][li]) lights = add(lights, sm.light[r][li]);
 			lights = divf(lights, (float)shot);
 			if (WF) {
-				V3 bl = mk(0.f, 0.f, 0.f);
-				for (uint32_t r = 0; r < shot; r++)
-					for (int li = 0; li < 2; li++)
-						if (sm.lit[r][li]) bl = add(bl, sm.lbent[r][li]);
-				wf.slot_tid[ti] = tid;
-				wf.slot_lights[ti] = make_float4(lights.x, lights.y, lights.z, 0.f);
-				wf.slot_bl[ti] = make_float4(bl.x, bl.y, bl.z, 0.f);
+				wf.slot_tid[ti] = tid;   // the light rounds are summed by k_wf_light_sum
 			} else if (LEARNED) {
 				out[oi] = make_float4(lights.x, lights.y, lights.z, texel_alpha(g, tid));
 			} else {
@@ -1059,6 +1082,44 @@ __global__ void __launch_bounds__(128, 7) k_wf_shadow(GatherScene g, WfState w, 
 		if (!occluded(g, pnt, sdir, g.tmin, smax, tri, overflow)) w.nee[q].w = 2.f;
 	}
 	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// The light rounds' shadow rays of a batch, one thread each (the set-up
+// made them: processTexel's light rounds, gather.cpp:421-559 via
+// GatheredIrradianceLights::shotRay): a ray that reaches its light marks the
+// round's contribution.
+__global__ void __launch_bounds__(128, 7) k_wf_light_trace(GatherScene g, WfState w, uint32_t* status) {
+	const uint32_t n = w.counts[4];
+	bool overflow = false;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const float4 o4 = w.lr_ray[2 * (size_t)i], d4 = w.lr_ray[2 * (size_t)i + 1];
+		if (w.rays) count_ray(w.rays + 1);
+		if (!occluded(g, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), g.tmin, d4.w, __float_as_uint(o4.w), overflow))
+			w.lr_light[w.lr_slot[i]].w = 1.f;
+	}
+	if (overflow) atomicOr(status, (uint32_t)RRG_ERR_STACK);
+}
+
+// Each texel's light rounds, averaged in round and light order as the
+// warp-per-texel kernel sums them (gather.cpp:541-559), and their
+// bent-normal terms.
+__global__ void k_wf_light_sum(WfState w, uint32_t nb) {
+	const uint32_t ti = blockIdx.x * blockDim.x + threadIdx.x;
+	if (ti >= nb || w.slot_tid[ti] == ~0ull) return;
+	V3 lights = mk(0.f, 0.f, 0.f), bl = mk(0.f, 0.f, 0.f);
+	for (uint32_t r = 0; r < w.shot; r++)
+		for (int li = 0; li < 2; li++) {
+			const size_t slot = ((size_t)ti * w.shot + r) * 2 + li;
+			const float4 l = w.lr_light[slot];
+			if (l.w > 0.f) {
+				lights = add(lights, mk(l.x, l.y, l.z));
+				const float4 b = w.lr_bent[slot];
+				bl = add(bl, mk(b.x, b.y, b.z));
+			}
+		}
+	lights = divf(lights, (float)w.shot);
+	w.slot_lights[ti] = make_float4(lights.x, lights.y, lights.z, 0.f);
+	w.slot_bl[ti] = make_float4(bl.x, bl.y, bl.z, 0.f);
 }
 
 // The rest of trace_path's loop body for every path that hit: the unoccluded
@@ -1434,7 +1495,10 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 	const uint32_t N = Q > rounds ? Q : rounds;
 	const uint64_t B = std::min<uint64_t>(count, kWfMaxPaths / Q);   // texels per batch
 	const uint64_t cap = B * Q;                                       // paths per batch
-	const size_t state_bytes = (9 * 16 * cap + 2 * 16 * B + 8 * B + 5 * 4 * cap + 16 + 255) / 256 * 256;
+	const uint32_t shot = rounds < (uint32_t)kMaxRounds ? rounds : (uint32_t)kMaxRounds;
+	const uint64_t nslot = B * shot * 2;   // light rounds of a batch
+	const size_t base_bytes = (9 * 16 * cap + 2 * 16 * B + 8 * B + 5 * 4 * cap + 32 + 255) / 256 * 256;
+	const size_t state_bytes = base_bytes + (4 * 16 * nslot + 4 * nslot + 255) / 256 * 256;
 	// binned order (RRG_RAY_ORDER_BINNED): the live paths sorted by their
 	// rays' key before each closest-hit pass, with the sort's scratch after
 	// the state.  Not the default: on the config-2 scene it measured 4-6 %
@@ -1460,6 +1524,12 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 	w.hits = w.live + 2 * cap;
 	w.shadow = w.hits + cap;
 	w.counts = w.shadow + 2 * cap;
+	float4* lr = reinterpret_cast<float4*>(reinterpret_cast<uint8_t*>(L->d_wf) + base_bytes);
+	w.lr_light = lr;
+	w.lr_bent = lr + nslot;
+	w.lr_ray = lr + 2 * nslot;
+	w.lr_slot = reinterpret_cast<uint32_t*>(lr + 4 * nslot);
+	w.shot = shot;
 	w.cap = (uint32_t)cap;
 	w.Q = Q;
 	w.N = N;
@@ -1474,13 +1544,15 @@ static int gather_wavefront(Lightmapper* L, const GatherScene& g, uint64_t first
 	for (uint64_t b0 = 0; b0 < count; b0 += B) {
 		const uint64_t nb = std::min<uint64_t>(B, count - b0);
 		RRG_CUDA(cudaMemsetAsync(L->d_counter, 0, 8, s));
-		RRG_CUDA(cudaMemsetAsync(w.counts, 0, 4 * sizeof(uint32_t), s));
+		RRG_CUDA(cudaMemsetAsync(w.counts, 0, 5 * sizeof(uint32_t), s));
 		const uint64_t want = (nb + kGatherWarps - 1) / kGatherWarps;
 		const uint64_t capb = (uint64_t)(per_sm > 0 ? per_sm : 1) * L->c->num_sms;
 		const int grid = (int)(want < capb ? want : capb);
 		rrg::note_launch(), k_gather<false, false, true><<<grid, kGatherWarps * 32, 0, s>>>(
 		    g, L->d_off, L->d_sub, first + b0, nb, nullptr, first, out, nullptr, reinterpret_cast<uint32_t*>(L->d_counter),
 		    L->d_status, nullptr, DirOut{}, w);
+		rrg::note_launch(), k_wf_light_trace<<<grid_c, 128, 0, s>>>(g, w, L->d_status);
+		rrg::note_launch(), k_wf_light_sum<<<(int)((nb + 127) / 128), 128, 0, s>>>(w, (uint32_t)nb);
 		RRG_CUDA(cudaGetLastError());
 		if (recs) {
 			if (binned) {
