@@ -1481,7 +1481,7 @@ static int grow_scratch(Lightmapper* L, size_t bytes) {
 }
 
 constexpr uint64_t kWfMinTexels = 16384;
-// paths per batch: 2^25 (4.8 GB of path state at 144 B a path) keeps the
+// paths per batch: 2^25 (6 GB of path state at about 180 B a path) keeps the
 // deep bounces' launches full; on the config-2 scene 2^23 measured 4 %
 // slower and 2^24 1 % slower
 constexpr uint64_t kWfMaxPaths = 1ull << 25;
