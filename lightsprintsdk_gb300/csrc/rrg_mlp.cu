@@ -253,11 +253,10 @@ __device__ void wgrad_chunk(const uint32_t* __restrict__ In, const uint32_t* __r
 	}
 #pragma unroll
 	for (int nt = 0; nt < NT; nt++) {
+		// columns n and n + 1 are adjacent (n even): one 8-byte atomic per row
 		int n = 8 * nt + 2 * q;
-		atomicAdd(&grad[(m0 + g) * NO + n], acc[nt][0]);
-		atomicAdd(&grad[(m0 + g) * NO + n + 1], acc[nt][1]);
-		atomicAdd(&grad[(m0 + g + 8) * NO + n], acc[nt][2]);
-		atomicAdd(&grad[(m0 + g + 8) * NO + n + 1], acc[nt][3]);
+		atomicAdd(reinterpret_cast<float2*>(&grad[(m0 + g) * NO + n]), make_float2(acc[nt][0], acc[nt][1]));
+		atomicAdd(reinterpret_cast<float2*>(&grad[(m0 + g + 8) * NO + n]), make_float2(acc[nt][2], acc[nt][3]));
 	}
 }
 

@@ -255,13 +255,13 @@ __device__ __forceinline__ void mlp_encode_half_hash(const float* p, const float
 __device__ __forceinline__ void hash_backward(const float* p, const float* lo, const float* ie, const HashGrid& g,
                                               int l, float d0, float d1) {
 	const HashCorners h = hash_cell(p, lo, ie, g.res[l]);
-	float* tl = g.tgrad + (size_t)l * g.T * 2;
+	// the entry's two features are adjacent: one 8-byte atomic for both
+	float2* tl = reinterpret_cast<float2*>(g.tgrad + (size_t)l * g.T * 2);
 #pragma unroll
 	for (int c = 0; c < 8; c++) {
 		const uint32_t idx = hash_index(g, l, h.x0[0] + (c & 1), h.x0[1] + ((c >> 1) & 1), h.x0[2] + ((c >> 2) & 1));
 		const float wc = hash_weight(h, c);
-		atomicAdd(tl + 2 * idx, wc * d0);
-		atomicAdd(tl + 2 * idx + 1, wc * d1);
+		atomicAdd(tl + idx, make_float2(wc * d0, wc * d1));
 	}
 }
 
