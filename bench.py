@@ -898,13 +898,14 @@ def main():
     L = col._lib()
     for _ in range(2):
         L.rrg_intersect_host(c.handle, h_rays.data_ptr(), n, h_hits.data_ptr(), sp)
-    # nine rounds of calls; the median round's time per call (the host link
-    # and cores are shared, so single rounds vary)
-    e2e_steps = max(9, args.steps // 2)
-    per_round = max(1, e2e_steps // 9)
+    # fifteen rounds of calls; the median round's time per call (the host
+    # link and cores are shared, so single rounds vary)
+    rounds = 15
+    e2e_steps = max(rounds, args.steps // 2)
+    per_round = max(1, e2e_steps // rounds)
     torch.cuda.synchronize()
     round_s = []
-    for _ in range(9):
+    for _ in range(rounds):
         t0 = time.perf_counter()
         for _ in range(per_round):
             st = L.rrg_intersect_host(c.handle, h_rays.data_ptr(), n, h_hits.data_ptr(), sp)
@@ -941,8 +942,9 @@ def main():
                                  f"ncu capture x rays; the kernel is issue-bound (69 % issue-active, 13.4 of 32 lanes), "
                                  f"so the HBM fraction is low by design"},
             "e2e": {"value": world * n / e2e_s / 1e9, "unit": "Grays/s", "h2d_bytes_per_step": 32 * n,
-                    "d2h_bytes_per_step": 16 * n, "calls": 9 * per_round,
-                    "statistic": f"median of 9 rounds of {per_round} calls (rrg_intersect_host, page-locked buffers)",
+                    "d2h_bytes_per_step": 16 * n, "calls": rounds * per_round,
+                    "statistic": f"median of {rounds} rounds of {per_round} calls (rrg_intersect_host, "
+                                 f"page-locked buffers)",
                     "rounds": [round(n / t / 1e9, 4) for t in round_s]},
             "gpu_launches": launches,
             "clocks": clk.summary(),
