@@ -19,10 +19,13 @@
 // the one before).  So it runs as one warp per atlas over the atlas's seams,
 // and each seam is made cheap: its runs of samples in one texel pair are
 // found once, from the geometry; the used flags of the atlas sit in shared
-// memory; a seam's texel values are loaded in one round trip; lanes 0..7
-// each carry one float component of the two accumulators, adding in the
-// reference's order, so the sums are its sequential float sums, bit for bit.
+// memory, with a flag per texel for this seam's own writes; a seam's texel
+// values are loaded in one round trip; lanes 0..7 each carry one float
+// component of the two accumulators and add a run's repeated value in closed
+// form per binade, so the sums are the reference's sequential float sums,
+// bit for bit.
 #include "rrg_internal.cuh"
+#include "rrg_add_repeat.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -216,11 +219,14 @@ __global__ void k_seam_runs(const Seam* __restrict__ seams, uint64_t nseams, uin
 // component of its two accumulators (lane l: component l & 3 of accumulator
 // l >> 2): where a texel's run ends, the texel gets its accumulator's
 // average; a run of c samples adds its texels' sum c times, in the
-// reference's order, so every value is the reference's sequential float
-// result, bit for bit.  A texel this seam wrote and reads
-// again is taken from a log of its writes.
+// reference's order (a run's c additions in closed form, add_repeat), so
+// every value is the reference's sequential float result, bit for bit.  A
+// texel this seam wrote and reads again is read back from memory where the
+// atlas's flags sit in shared memory (a flag per texel marks this seam's
+// writes, cleared when the seam ends), else taken from a log of its writes.
 constexpr int kSeamLog = 2048;                 // >= the writes of one seam (2 per run)
 constexpr uint32_t kUsedSmemMax = 128 * 1024;  // used flags of atlases up to 362^2 texels in shared memory
+constexpr uint8_t kUsed = 1, kWritten = 2;     // per-texel flags in shared memory: used; written by this seam
 
 struct SeamLog {
 	uint32_t key[kSeamLog];
@@ -270,7 +276,7 @@ __global__ void __launch_bounds__(32) k_smooth_seams(float4* __restrict__ work, 
 	const bool carrier = lane < 8;
 	const bool first_acc = lane < 4;
 	if (used_in_smem)
-		for (uint64_t k = lane; k < S; k += 32) used[k] = img[k].w != 0.f;
+		for (uint64_t k = lane; k < S; k += 32) used[k] = img[k].w != 0.f ? kUsed : 0;
 	__syncwarp();
 	for (uint32_t s = seam_off[a]; s < seam_off[a + 1]; s++) {
 		const uint64_t r0 = run_off[s];
@@ -288,7 +294,7 @@ __global__ void __launch_bounds__(32) k_smooth_seams(float4* __restrict__ work, 
 				i1 = r[0];
 				i2 = r[1];
 				cnt = r[2];
-				ok = used_in_smem ? (used[i1] && used[i2]) : (img[i1].w != 0.f && img[i2].w != 0.f);
+				ok = used_in_smem ? (used[i1] & used[i2] & kUsed) != 0 : (img[i1].w != 0.f && img[i2].w != 0.f);
 				if (ok) {
 					x1 = img[i1];
 					x2 = img[i2];
@@ -308,9 +314,12 @@ __global__ void __launch_bounds__(32) k_smooth_seams(float4* __restrict__ work, 
 						if (first_acc) {
 							const float q = __fdiv_rn(acc, w1);
 							imgf[4 * (size_t)last1 + comp] = q;
-							reinterpret_cast<float*>(&lg.val[nlog])[comp] = q;
+							if (!used_in_smem) reinterpret_cast<float*>(&lg.val[nlog])[comp] = q;
 						}
-						if (lane == 0) lg.key[nlog] = last1;
+						if (lane == 0) {
+							lg.key[nlog] = last1;
+							if (used_in_smem) used[last1] |= kWritten;
+						}
 						nlog++;
 					}
 					last1 = k1;
@@ -323,9 +332,12 @@ __global__ void __launch_bounds__(32) k_smooth_seams(float4* __restrict__ work, 
 						if (carrier && !first_acc) {
 							const float q = __fdiv_rn(acc, w2);
 							imgf[4 * (size_t)last2 + comp] = q;
-							reinterpret_cast<float*>(&lg.val[nlog])[comp] = q;
+							if (!used_in_smem) reinterpret_cast<float*>(&lg.val[nlog])[comp] = q;
 						}
-						if (lane == 0) lg.key[nlog] = last2;
+						if (lane == 0) {
+							lg.key[nlog] = last2;
+							if (used_in_smem) used[last2] |= kWritten;
+						}
 						nlog++;
 					}
 					last2 = k2;
@@ -336,18 +348,24 @@ __global__ void __launch_bounds__(32) k_smooth_seams(float4* __restrict__ work, 
 				if (changed) {
 					// the pair's values: this seam's writes, else as loaded
 					float4 z1 = y1, z2 = y2, l;
-					if (seam_log_find(lg, nlog, k1, lane, l)) z1 = l;
-					if (seam_log_find(lg, nlog, k2, lane, l)) z2 = l;
+					if (used_in_smem) {
+						if (used[k1] & kWritten) z1 = img[k1];
+						if (used[k2] & kWritten) z2 = img[k2];
+					} else {
+						if (seam_log_find(lg, nlog, k1, lane, l)) z1 = l;
+						if (seam_log_find(lg, nlog, k2, lane, l)) z2 = l;
+					}
 					v = __fadd_rn(comp4(z1, comp), comp4(z2, comp));
 				}
-				if (carrier)
-					for (uint32_t q = 0; q < kc; q++) acc = __fadd_rn(acc, v);
+				if (carrier) acc = add_repeat(acc, v, kc);
 			}
 		}
 		const float w1 = __shfl_sync(kFull, acc, 3), w2 = __shfl_sync(kFull, acc, 7);
 		if (last1 != kNoTexel && first_acc) imgf[4 * (size_t)last1 + comp] = __fdiv_rn(acc, w1);
 		__syncwarp();
 		if (last2 != kNoTexel && carrier && !first_acc) imgf[4 * (size_t)last2 + comp] = __fdiv_rn(acc, w2);
+		if (used_in_smem)
+			for (unsigned j = (unsigned)lane; j < nlog; j += 32) used[lg.key[j]] &= kUsed;
 		__syncwarp();
 	}
 }

@@ -6,7 +6,9 @@
    GPU against the reference itself, bit-exact.
 2. On the config-2 interior (several atlases per call, an offset first
    atlas): gathered lightmaps filtered on the GPU equal the oracle's filters
-   applied atlas by atlas, bit-exact."""
+   applied atlas by atlas, bit-exact.
+3. On a 400 x 400 sphere atlas, whose used flags exceed the seam kernel's
+   shared memory: the same against the oracle."""
 import numpy as np
 import pytest
 
@@ -92,3 +94,22 @@ def test_interior_filters_match_oracle(interior, first, count, wrap):
         got = after[a * S:(a + 1) * S].reshape(gs.size, gs.size, 4)
         bad = np.nonzero((got != want).any(-1).reshape(-1))[0]
         assert bad.size == 0, (a, bad[:10], got.reshape(-1, 4)[bad[:3]], want.reshape(-1, 4)[bad[:3]])
+
+
+def test_large_atlas_seams_match_oracle():
+    """Above 362^2 texels the seam kernel keeps the atlas's used flags in
+    global memory and finds a seam's own earlier writes in its log instead of
+    by per-texel flags: all filters with seams, bit-exact against the oracle."""
+    import torch
+    size = 400
+    v, nrm, t, uv = G.lightmap_case(4, size)
+    c = col.RRCollider.create(v, t)
+    L = lm.RRLightmapper(c, np.full((len(t), 3), 0.5, np.float32), np.zeros(len(t), np.int32), uv, 1, size)
+    img = G.lightmap_image(L.flags(), size, seed=11)
+    d = torch.from_numpy(img.reshape(-1, 4).copy()).cuda()
+    L.filter_device(lm.filter_params(), 0, 1, d.data_ptr())
+    torch.cuda.synchronize()
+    got = d.cpu().numpy().reshape(size, size, 4)
+    want = orc.lightmap_filter(img, 1.0, 1000, (0, 0, 0, 0), False, orc.unwrap_seams(t, uv), 15)
+    bad = np.nonzero((got != want).any(-1).reshape(-1))[0]
+    assert bad.size == 0, (bad[:10], got.reshape(-1, 4)[bad[:3]], want.reshape(-1, 4)[bad[:3]])
