@@ -63,9 +63,11 @@ constexpr uint32_t kPlainSteps = 64;
 // binade.  Zero and subnormal binades take the real steps.  The loop has no
 // branch but its exit, as the 8 lanes that carry components run it together:
 // the quotient room / d comes from a float division within one of the true
-// one (RRG_AR_DIV) and is corrected with exact products.
-RRG_AR_FN float add_repeat(float x, float v, uint32_t k) {
-	const uint32_t p = k < kPlainSteps ? k : kPlainSteps;
+// one (RRG_AR_DIV) and is corrected with exact products.  `plain` sets how
+// many of the k steps are plain additions first (an accumulator that already
+// holds many additions of a like value needs none).
+RRG_AR_FN float add_repeat(float x, float v, uint32_t k, uint32_t plain = kPlainSteps) {
+	const uint32_t p = k < plain ? k : plain;
 	for (uint32_t q = 0; q < p; q++) x = RRG_AR_ADD(x, v);
 	k -= p;
 	while (k >= 4u) {

@@ -18,12 +18,14 @@
 // ones wrote (on the finely tessellated atlases nearly every seam depends on
 // the one before).  So it runs as one warp per atlas over the atlas's seams,
 // and each seam is made cheap: its runs of samples in one texel pair are
-// found once, from the geometry; the used flags of the atlas sit in shared
-// memory, with a flag per texel for this seam's own writes; a seam's texel
-// values are loaded in one round trip; lanes 0..7 each carry one float
-// component of the two accumulators and add a run's repeated value in closed
-// form per binade, so the sums are the reference's sequential float sums,
-// bit for bit.
+// found once, from the geometry, and loaded a seam ahead; the used flags of
+// the atlas sit in shared memory; a seam's texel values are loaded in one
+// round trip; a seam of at most 8 runs (nearly all on finely tessellated
+// atlases) sums each texel group's runs on its own four lanes at once
+// (seam_parallel), a longer one walks its runs with lanes 0..7 carrying the
+// components of the two accumulators; a run's repeated value is added in
+// closed form per binade, so the sums are the reference's sequential float
+// sums, bit for bit.
 #include "rrg_internal.cuh"
 #include "rrg_add_repeat.cuh"
 
@@ -228,9 +230,16 @@ constexpr int kSeamLog = 2048;                 // >= the writes of one seam (2 p
 constexpr uint32_t kUsedSmemMax = 128 * 1024;  // used flags of atlases up to 362^2 texels in shared memory
 constexpr uint8_t kUsed = 1, kWritten = 2;     // per-texel flags in shared memory: used; written by this seam
 
+constexpr int kChains = 8;   // texel groups of one seam on the parallel path (4 lanes each)
+
 struct SeamLog {
 	uint32_t key[kSeamLog];
 	float4 val[kSeamLog];
+	// the parallel path: per run (at most kChains runs) its texel sum and
+	// samples; per chain the run that ends it, its texel and its write order
+	float4 run_v[kChains];
+	uint32_t run_cnt[kChains];
+	uint32_t chain_end[kChains], chain_tex[kChains], chain_key[kChains];
 };
 
 // Latest value this seam wrote to `key`, if any (the last of the log's n
@@ -258,6 +267,99 @@ __device__ __forceinline__ float comp4(const float4& x, int c) {
 	return c == 0 ? x.x : (c == 1 ? x.y : (c == 2 ? x.z : x.w));
 }
 
+// One seam on the parallel path, when it has at most kChains runs; false
+// (nothing written) where the seam needs the sequential walk.  In the
+// reference's walk (RRBuffer.cpp:764-781) an accumulator restarts when its
+// edge's texel changes, and the texel it leaves gets its average; so each
+// accumulator's sums split into groups of consecutive counting runs with
+// one texel, whose sums are independent of one another as long as no run
+// reads a texel that this seam wrote before it.  Then every group is one
+// chain of additions from zero over its runs (four lanes: one component
+// each), and every group's texel is written at once, a texel that two groups
+// write taking the later group's value, as in the reference's order (at a
+// run boundary edge 1's texel before edge 2's).  A seam with a run that
+// reads a texel written before it in the seam, or with more than kChains
+// groups, goes to the sequential walk.
+// Lane j < m holds run j (texels i1, i2, samples cnt).
+__device__ __forceinline__ bool seam_parallel(const float4* __restrict__ img, float* __restrict__ imgf,
+                                              const uint8_t* __restrict__ used, int used_in_smem, uint32_t i1,
+                                              uint32_t i2, uint32_t cnt, uint32_t m, SeamLog& lg, int lane) {
+	const unsigned kFull = 0xFFFFFFFFu;
+	bool ok = false;
+	float4 x1 = make_float4(0.f, 0.f, 0.f, 0.f), x2 = x1;
+	if ((uint32_t)lane < m) {
+		ok = used_in_smem ? (used[i1] & used[i2] & kUsed) != 0 : (img[i1].w != 0.f && img[i2].w != 0.f);
+		if (ok) {
+			x1 = img[i1];
+			x2 = img[i2];
+		}
+	}
+	const unsigned O = __ballot_sync(kFull, ok);   // counting runs
+	if (!O) return true;                            // nothing is written
+	// groups: a counting run starts one where its texel differs from the
+	// previous counting run's, and ends one where the next counting run starts
+	// one (or none follows)
+	const unsigned below = O & ((1u << lane) - 1u);
+	const int prev = below ? 31 - __clz(below) : lane;
+	const uint32_t p1 = __shfl_sync(kFull, i1, prev), p2 = __shfl_sync(kFull, i2, prev);
+	const unsigned S1 = __ballot_sync(kFull, ok && (!below || i1 != p1));
+	const unsigned S2 = __ballot_sync(kFull, ok && (!below || i2 != p2));
+	const unsigned above = lane < 31 ? O & ~((2u << lane) - 1u) : 0u;
+	const int next = above ? __ffs(above) - 1 : -1;
+	const unsigned E1 = __ballot_sync(kFull, ok && (next < 0 || ((S1 >> next) & 1u)));
+	const unsigned E2 = __ballot_sync(kFull, ok && (next < 0 || ((S2 >> next) & 1u)));
+	const int n1 = __popc(E1), nch = n1 + __popc(E2);
+	if (nch > kChains) return false;
+	if (ok)
+		lg.run_v[lane] = make_float4(__fadd_rn(x1.x, x2.x), __fadd_rn(x1.y, x2.y), __fadd_rn(x1.z, x2.z),
+		                             __fadd_rn(x1.w, x2.w));
+	if ((uint32_t)lane < m) lg.run_cnt[lane] = cnt;
+	// this lane's chain: group k (edge 1's groups first, in run order), component c
+	const int k = lane >> 2, c = lane & 3;
+	const bool mine = k < nch;
+	const bool edge1 = k < n1;
+	int end = 0, start = 0;
+	if (mine) {
+		unsigned E = edge1 ? E1 : E2;
+		for (int t = edge1 ? k : k - n1; t > 0; t--) E &= E - 1u;
+		end = __ffs(E) - 1;
+		const unsigned starts = (edge1 ? S1 : S2) & ((2u << end) - 1u);   // end < kChains
+		start = 31 - __clz(starts);
+	}
+	const uint32_t end_i1 = __shfl_sync(kFull, i1, end), end_i2 = __shfl_sync(kFull, i2, end);
+	const uint32_t tex = mine ? (edge1 ? end_i1 : end_i2) : kNoTexel;
+	// writes in the reference's order: group ending at run q, edge e -> 2q + e
+	const uint32_t key = 2u * (uint32_t)end + (edge1 ? 0u : 1u);
+	if (mine && c == 0) {
+		lg.chain_end[k] = (uint32_t)end;
+		lg.chain_tex[k] = tex;
+		lg.chain_key[k] = key;
+	}
+	__syncwarp();
+	// a counting run that reads a texel written before it: sequential walk
+	bool dirty = false, later = false;
+	for (int t = 0; t < nch; t++) {
+		const uint32_t te = lg.chain_tex[t];
+		if (ok && (int)lg.chain_end[t] < lane && (te == i1 || te == i2)) dirty = true;
+		if (mine && lg.chain_key[t] > key && te == tex) later = true;
+	}
+	if (__any_sync(kFull, dirty)) return false;
+	float acc = 0.f;
+	if (mine) {
+		uint32_t done = 0;   // additions so far: the first kPlainSteps are plain
+		for (int r = start; r <= end; r++) {
+			if (!((O >> r) & 1u)) continue;
+			const uint32_t n = lg.run_cnt[r];
+			const float v = comp4(lg.run_v[r], c);
+			acc = add_repeat(acc, v, n, done < kPlainSteps ? kPlainSteps - done : 0u);
+			done += n;
+		}
+	}
+	const float w = __shfl_sync(kFull, acc, lane | 3);
+	if (mine && !later) imgf[4 * (size_t)tex + c] = __fdiv_rn(acc, w);
+	return true;
+}
+
 __global__ void __launch_bounds__(32) k_smooth_seams(float4* __restrict__ work, const uint32_t* __restrict__ runs,
                                                      const uint32_t* __restrict__ run_off,
                                                      const uint32_t* __restrict__ seam_off, uint32_t first_atlas,
@@ -278,9 +380,42 @@ __global__ void __launch_bounds__(32) k_smooth_seams(float4* __restrict__ work, 
 	if (used_in_smem)
 		for (uint64_t k = lane; k < S; k += 32) used[k] = img[k].w != 0.f ? kUsed : 0;
 	__syncwarp();
-	for (uint32_t s = seam_off[a]; s < seam_off[a + 1]; s++) {
-		const uint64_t r0 = run_off[s];
-		const uint32_t m = (uint32_t)(run_off[s + 1] - r0);
+	// A seam's run offsets and runs do not depend on texel values, so they are
+	// loaded one seam ahead (the offsets two): q0..q1 are the runs of the seam
+	// about to start, q2 the end of the one after, and lane j holds run j of
+	// the seam about to start (the first 32).
+	const uint32_t s_begin = seam_off[a], s_end = seam_off[a + 1];
+	uint32_t q0 = 0, q1 = 0, q2 = 0, n1 = 0, n2 = 0, nc = 0;
+	if (s_begin < s_end) {
+		q0 = run_off[s_begin];
+		q1 = run_off[s_begin + 1];
+		q2 = s_begin + 1 < s_end ? run_off[s_begin + 2] : q1;
+	}
+	if (q0 + (uint32_t)lane < q1) {
+		const uint32_t* r = runs + 3 * ((uint64_t)q0 + (uint32_t)lane);
+		n1 = r[0];
+		n2 = r[1];
+		nc = r[2];
+	}
+	for (uint32_t s = s_begin; s < s_end; s++) {
+		const uint64_t r0 = q0;
+		const uint32_t m = q1 - q0;
+		const uint32_t f1 = n1, f2 = n2, fc = nc;   // run `lane` of this seam
+		q0 = q1;
+		q1 = q2;
+		if (s + 2 < s_end) q2 = run_off[s + 3];
+		n1 = n2 = nc = 0;
+		if (q0 + (uint32_t)lane < q1) {
+			const uint32_t* r = runs + 3 * ((uint64_t)q0 + (uint32_t)lane);
+			n1 = r[0];
+			n2 = r[1];
+			nc = r[2];
+		}
+		if (m <= (uint32_t)kChains) {
+			const bool done = seam_parallel(img, imgf, used, used_in_smem, f1, f2, fc, m, lg, lane);
+			__syncwarp();
+			if (done) continue;
+		}
 		uint32_t last1 = kNoTexel, last2 = kNoTexel;
 		unsigned nlog = 0;   // the same in every lane
 		float acc = 0.f, v = 0.f;
@@ -290,10 +425,16 @@ __global__ void __launch_bounds__(32) k_smooth_seams(float4* __restrict__ work, 
 			uint32_t i1 = 0, i2 = 0, cnt = 0;
 			float4 x1 = make_float4(0.f, 0.f, 0.f, 0.f), x2 = x1;
 			if (j < m) {
-				const uint32_t* r = runs + 3 * (r0 + j);
-				i1 = r[0];
-				i2 = r[1];
-				cnt = r[2];
+				if (c0 == 0) {
+					i1 = f1;
+					i2 = f2;
+					cnt = fc;
+				} else {
+					const uint32_t* r = runs + 3 * (r0 + j);
+					i1 = r[0];
+					i2 = r[1];
+					cnt = r[2];
+				}
 				ok = used_in_smem ? (used[i1] & used[i2] & kUsed) != 0 : (img[i1].w != 0.f && img[i2].w != 0.f);
 				if (ok) {
 					x1 = img[i1];

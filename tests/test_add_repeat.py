@@ -3,7 +3,8 @@
 run's texel sum once per edge sample): the same header compiled as C++ on
 the CPU, against the loop of single float additions, bit for bit, over
 random accumulators and values (ties to even, sums crossing many binades,
-negative values, zeros, subnormals, infinities and NaN), once with the exact
+negative values, zeros, subnormals, infinities and NaN; the default and
+random numbers of leading plain additions), once with the exact
 quotient and once with a quotient perturbed by up to one (the kernel's
 approximate division), which the correction must absorb."""
 import os
@@ -55,7 +56,8 @@ int main(int argc, char** argv) {
 		else if (mode == 6) { x = -bf(fb(v) + ((uint32_t)(rnd() % 5) << 23)); if (rnd() & 1) v = -v; }
 		else { v = bf((uint32_t)(rnd() % 0x7F800000u)); x = bf((uint32_t)(rnd() % 0x7F800000u)); }
 		const uint32_t k = (uint32_t)(rnd() % 1200);
-		const float a = add_loop(x, v, k), b = rrg::add_repeat(x, v, k);
+		const uint32_t plain = (it & 1) ? rrg::kPlainSteps : (uint32_t)(rnd() % 80);   // leading plain additions
+		const float a = add_loop(x, v, k), b = rrg::add_repeat(x, v, k, plain);
 		n++;
 		if (fb(a) != fb(b)) {
 			if (bad < 5) printf("mismatch x=%a v=%a k=%u loop=%a closed=%a\n", x, v, k, a, b);
