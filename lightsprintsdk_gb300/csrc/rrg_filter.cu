@@ -20,10 +20,11 @@
 // and each seam is made cheap: its runs of samples in one texel pair are
 // found once, from the geometry, and loaded a seam ahead; the used flags of
 // the atlas sit in shared memory; a seam's texel values are loaded in one
-// round trip; a seam of at most 8 runs (nearly all on finely tessellated
-// atlases) sums each texel group's runs on its own four lanes at once
-// (seam_parallel), a longer one walks its runs with lanes 0..7 carrying the
-// components of the two accumulators; a run's repeated value is added in
+// round trip; a seam of at most 32 runs whose runs read no texel it wrote
+// before them sums each texel group's runs on its own four lanes, eight
+// groups at a time (seam_parallel, seam_parallel_runs); any other walks its
+// runs with lanes 0..7 carrying the components of the two accumulators; a
+// run's repeated value is added in
 // closed form per binade, so the sums are the reference's sequential float
 // sums, bit for bit.
 #include "rrg_internal.cuh"
@@ -230,15 +231,16 @@ constexpr int kSeamLog = 2048;                 // >= the writes of one seam (2 p
 constexpr uint32_t kUsedSmemMax = 128 * 1024;  // used flags of atlases up to 362^2 texels in shared memory
 constexpr uint8_t kUsed = 1, kWritten = 2;     // per-texel flags in shared memory: used; written by this seam
 
-constexpr int kChains = 8;   // texel groups of one seam on the parallel path (4 lanes each)
+constexpr int kChains = 8;               // texel groups summed at once on the parallel path (4 lanes each)
+constexpr uint32_t kParallelRuns = 32;   // runs of a seam on the parallel path (one lane each)
 
 struct SeamLog {
 	uint32_t key[kSeamLog];
 	float4 val[kSeamLog];
-	// the parallel path: per run (at most kChains runs) its texel sum and
-	// samples; per chain the run that ends it, its texel and its write order
-	float4 run_v[kChains];
-	uint32_t run_cnt[kChains];
+	// the parallel path: per run its texel sum and samples; per group (seams
+	// of at most kChains runs) the run that ends it, its texel and write order
+	float4 run_v[kParallelRuns];
+	uint32_t run_cnt[kParallelRuns];
 	uint32_t chain_end[kChains], chain_tex[kChains], chain_key[kChains];
 };
 
@@ -360,6 +362,95 @@ __device__ __forceinline__ bool seam_parallel(const float4* __restrict__ img, fl
 	return true;
 }
 
+// seam_parallel for seams of kChains + 1 .. kParallelRuns runs: the same
+// texel groups, summed kChains groups at a time, with the checks (a run that
+// reads a texel written before it; a group's texel written again by a later
+// group) made in one pass over the runs rather than over the groups, which
+// is cheaper for many groups and dearer for few (seams of up to 8 runs took
+// 15 % longer this way on the config-2 atlases).  False (nothing written)
+// where the seam needs the sequential walk.  Lane j < m holds run j.
+__device__ __forceinline__ bool seam_parallel_runs(const float4* __restrict__ img, float* __restrict__ imgf,
+                                              const uint8_t* __restrict__ used, int used_in_smem, uint32_t i1,
+                                              uint32_t i2, uint32_t cnt, uint32_t m, SeamLog& lg, int lane) {
+	const unsigned kFull = 0xFFFFFFFFu;
+	bool ok = false;
+	float4 x1 = make_float4(0.f, 0.f, 0.f, 0.f), x2 = x1;
+	if ((uint32_t)lane < m) {
+		ok = used_in_smem ? (used[i1] & used[i2] & kUsed) != 0 : (img[i1].w != 0.f && img[i2].w != 0.f);
+		if (ok) {
+			x1 = img[i1];
+			x2 = img[i2];
+		}
+	}
+	const unsigned O = __ballot_sync(kFull, ok);   // counting runs
+	if (!O) return true;                            // nothing is written
+	// groups: a counting run starts one where its texel differs from the
+	// previous counting run's, and ends one where the next counting run starts
+	// one (or none follows)
+	const unsigned below = O & ((1u << lane) - 1u);
+	const int prev = below ? 31 - __clz(below) : lane;
+	const uint32_t p1 = __shfl_sync(kFull, i1, prev), p2 = __shfl_sync(kFull, i2, prev);
+	const unsigned S1 = __ballot_sync(kFull, ok && (!below || i1 != p1));
+	const unsigned S2 = __ballot_sync(kFull, ok && (!below || i2 != p2));
+	const unsigned above = lane < 31 ? O & ~((2u << lane) - 1u) : 0u;
+	const int next = above ? __ffs(above) - 1 : -1;
+	const unsigned E1 = __ballot_sync(kFull, ok && (next < 0 || ((S1 >> next) & 1u)));
+	const unsigned E2 = __ballot_sync(kFull, ok && (next < 0 || ((S2 >> next) & 1u)));
+	// over the runs q: whether this lane's run reads a texel that a group
+	// ending before it writes (dirty), and whether the texel its edge-1 /
+	// edge-2 group writes is written again by a later group (key 2q + edge)
+	const bool my_e1 = (E1 >> lane) & 1u, my_e2 = (E2 >> lane) & 1u;
+	bool dirty = false, later1 = false, later2 = false;
+	for (uint32_t q = 0; q < m; q++) {
+		const uint32_t t1 = __shfl_sync(kFull, i1, (int)q), t2 = __shfl_sync(kFull, i2, (int)q);
+		const bool e1 = (E1 >> q) & 1u, e2 = (E2 >> q) & 1u;
+		if ((int)q < lane)
+			dirty |= ok && ((e1 && (t1 == i1 || t1 == i2)) || (e2 && (t2 == i1 || t2 == i2)));
+		else if ((int)q > lane) {
+			later1 |= my_e1 && ((e1 && t1 == i1) || (e2 && t2 == i1));
+			later2 |= my_e2 && ((e1 && t1 == i2) || (e2 && t2 == i2));
+		} else
+			later1 |= my_e1 && e2 && t2 == i1;
+	}
+	if (__any_sync(kFull, dirty)) return false;
+	const unsigned L1 = __ballot_sync(kFull, later1), L2 = __ballot_sync(kFull, later2);
+	if (ok)
+		lg.run_v[lane] = make_float4(__fadd_rn(x1.x, x2.x), __fadd_rn(x1.y, x2.y), __fadd_rn(x1.z, x2.z),
+		                             __fadd_rn(x1.w, x2.w));
+	if ((uint32_t)lane < m) lg.run_cnt[lane] = cnt;
+	__syncwarp();
+	const int n1 = __popc(E1), nch = n1 + __popc(E2);
+	for (int base = 0; base < nch; base += kChains) {
+		// this lane's group: k (edge 1's groups first, in run order), component c
+		const int k = base + (lane >> 2), c = lane & 3;
+		const bool mine = k < nch;
+		const bool edge1 = k < n1;
+		int end = 0, start = 0;
+		if (mine) {
+			unsigned E = edge1 ? E1 : E2;
+			for (int t = edge1 ? k : k - n1; t > 0; t--) E &= E - 1u;
+			end = __ffs(E) - 1;
+			start = 31 - __clz((edge1 ? S1 : S2) & ((2u << end) - 1u));
+		}
+		const uint32_t end_i1 = __shfl_sync(kFull, i1, end), end_i2 = __shfl_sync(kFull, i2, end);
+		const bool write = mine && !(((edge1 ? L1 : L2) >> end) & 1u);
+		float acc = 0.f;
+		if (mine) {
+			uint32_t done = 0;   // additions so far: the first kPlainSteps are plain
+			for (int r = start; r <= end; r++) {
+				if (!((O >> r) & 1u)) continue;
+				const uint32_t n = lg.run_cnt[r];
+				const float v = comp4(lg.run_v[r], c);
+				acc = add_repeat(acc, v, n, done < kPlainSteps ? kPlainSteps - done : 0u);
+				done += n;
+			}
+		}
+		const float w = __shfl_sync(kFull, acc, lane | 3);
+		if (write) imgf[4 * (size_t)(edge1 ? end_i1 : end_i2) + c] = __fdiv_rn(acc, w);
+	}
+	return true;
+}
+
 __global__ void __launch_bounds__(32) k_smooth_seams(float4* __restrict__ work, const uint32_t* __restrict__ runs,
                                                      const uint32_t* __restrict__ run_off,
                                                      const uint32_t* __restrict__ seam_off, uint32_t first_atlas,
@@ -411,8 +502,10 @@ __global__ void __launch_bounds__(32) k_smooth_seams(float4* __restrict__ work, 
 			n2 = r[1];
 			nc = r[2];
 		}
-		if (m <= (uint32_t)kChains) {
-			const bool done = seam_parallel(img, imgf, used, used_in_smem, f1, f2, fc, m, lg, lane);
+		if (m <= kParallelRuns) {
+			const bool done = m <= (uint32_t)kChains
+			                      ? seam_parallel(img, imgf, used, used_in_smem, f1, f2, fc, m, lg, lane)
+			                      : seam_parallel_runs(img, imgf, used, used_in_smem, f1, f2, fc, m, lg, lane);
 			__syncwarp();
 			if (done) continue;
 		}
